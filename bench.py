@@ -1,0 +1,359 @@
+"""Benchmark: forward solve + adjoint gradient, seconds per 1M DOF.
+
+Workload (the headline configuration): Hexa1 cube of 70 x 70 x 70 elements
+(357,911 nodes, 1,073,733 DOF), interior nodes jittered by U(-0.1h, 0.1h)
+(seed 0), IsotropicElasticity3D(E=1000, nu=0.3), x=0 face clamped, z-force
+-1/n_nodes per node on the x=1 face.  One step = `solve()` to relative
+residual 1e-10 plus the gradient of sum(u) with respect to the nodal forces
+through the hand-written adjoint (the reference benchmark's loss,
+benchmarks/cubes.py:31-37).  Synthetic seeded data; no dataset.
+
+value      mixed precision (FP32 K + FP32 CG with FP64 residual replacement),
+           inputs resident in HBM, CUDA events on the launching stream.
+e2e        the same through the public API from host tensors: the model is
+           built from CPU tensors, so every step copies its inputs to the
+           device and its results (u, f, sigma, F, grad) back.
+plain_fp64 the FP64 Jacobi-CG path (scalar CSR in the reference pattern).
+
+`--impl reference` times the CPU oracle (a restatement of torch-fem's CPU
+path: numpy assembly + scipy Jacobi-CG) on a bounded sample of the same
+workload, because torch-fem itself is Python that cannot be run where the
+GPU is.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "torch-fem_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+METRIC = "solve+grad s per 1M DOF: FP32-CG+FP64-refine+adjoint vs plain FP64 @ rel err 1e-8"
+UNIT = "s/1M DOF"
+
+
+def cube_workload(n: int, device):
+    from torchfem_gb300 import Solid, mesh
+    from torchfem_gb300.materials import IsotropicElasticity3D
+
+    nodes, el = mesh.cube_hexa(n + 1, n + 1, n + 1)
+    gen = torch.Generator().manual_seed(0)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen, dtype=torch.float64) * 2 - 1) * (0.1 / n)
+    x0 = nodes[:, 0] == 0.0
+    x1 = nodes[:, 0] == 1.0
+    nodes, el = nodes.to(device), el.to(device)
+    m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+    con = torch.zeros(nodes.shape, dtype=torch.bool, device=device)
+    con[x0.to(device), :] = True
+    m.constraints = con
+    forces = torch.zeros(nodes.shape, dtype=torch.float64, device=device)
+    forces[x1.to(device), 2] = -1.0 / len(nodes)
+    return m, forces
+
+
+def step(m, forces, precision, stol):
+    f = forces.detach().requires_grad_(True)
+    m.forces = f
+    u, fi, s, gr, st = m.solve(stol=stol, precision=precision, differentiable_parameters=f)
+    (g,) = torch.autograd.grad(u.sum(), f)
+    return u, fi, s, gr, st, g
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def spmv_bytes(dm) -> float:
+    """Algorithmic bytes of one FP32 block-CSR SpMV: values 4*9 per block,
+    one int32 column per block, int64 row pointers, x read once, y written."""
+    d = dm.d
+    return dm.n_blocks * (4 * d * d + 4) + 8 * (dm.n_nod + 1) + 2 * 4 * dm.n_dofs
+
+
+def cpu_baseline(n_sample: int, steps: int = 1):
+    """The oracle's CPU solve + adjoint on a smaller cube of the same kind."""
+    from oracle import fem_oracle as O
+
+    nodes, el = O.cube_hexa(n_sample + 1, n_sample + 1, n_sample + 1)
+    rng = torch.Generator().manual_seed(0)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    jit = (torch.rand(nodes.shape, generator=rng, dtype=torch.float64).numpy() * 2 - 1) * (0.1 / n_sample)
+    nodes = nodes + inner[:, None] * jit
+    con = np.zeros(nodes.shape, dtype=bool)
+    con[nodes[:, 0] == 0.0, :] = True
+    F = np.zeros(nodes.shape)
+    F[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        m = O.LinearModel(nodes, el, O.elastic_c("3d", 1000.0, 0.3, len(el)))
+        m.solve(F, con, method="cg", rtol=1e-10)
+        m.adjoint(np.ones(m.n_dofs), method="cg", rtol=1e-10)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    dofs = nodes.size
+    return {"value": t / (dofs / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"oracle (numpy assembly + scipy Jacobi-CG, rtol 1e-10, solve + adjoint) on the "
+                      f"{n_sample}^3 jittered Hexa1 cube ({dofs} DOF), best of {steps}, "
+                      f"scaled linearly to 1M DOF; numpy/BLAS may use every host thread, scipy SpMV runs on one"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+        return dist, rank, world, local
+    return None, rank, world, local
+
+
+def reduce_max(dist, x: float, device) -> float:
+    if dist is None:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    dist, rank, world, _ = dist_setup()
+    if rank != 0:
+        return
+    times = []
+    for _ in range(args.warmup + args.steps):
+        times.append(cpu_baseline(args.cpu_n)["value"])
+    timed = times[args.warmup:] or times
+    v = sum(timed) / len(timed)
+    cb = cpu_baseline(args.cpu_n)
+    cb["value"] = v
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"hexa1_cube_{args.n}^3_jittered (CPU sample {args.cpu_n}^3)",
+                   "parallelism": "replicas"},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=70, help="elements per cube edge")
+    ap.add_argument("--stol", type=float, default=1e-10)
+    ap.add_argument("--cpu-n", type=int, default=24, help="cube size of the CPU baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    args = ap.parse_args()
+    torch.set_default_dtype(torch.float64)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    dist, rank, world, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from torchfem_gb300 import _lib
+
+    lib = _lib.load()
+    m, forces = cube_workload(args.n, dev)
+    dm = m.device_mesh
+    n_dofs = m.n_dofs
+    stream = torch.cuda.current_stream(dev)
+
+    # warm-up (W untimed steps), then K timed steps of the mixed path
+    for _ in range(max(args.warmup, 0)):
+        out = step(m, forces, "mixed", args.stol)
+    torch.cuda.synchronize()
+    lib.fem_set_timing(1)
+    spmv_ms, spmv_n, iters = 0.0, 0, []
+    launches0 = lib.fem_launch_count()
+    if dist is not None:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            out = step(m, forces, "mixed", args.stol)
+            st = m.last_solve
+            iters.append(st.iterations)
+            spmv_ms += st.system.stats.spmv_ms
+            spmv_n += st.system.stats.spmv_timed
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.fem_launch_count() - launches0
+    lib.fem_set_timing(0)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = reduce_max(dist, ms, dev)
+    u_mixed, g_mixed = out[0], out[5]
+
+    # end to end through the public API from host tensors
+    m_host, forces_host = cube_workload(args.n, torch.device("cpu"))
+    forces_host = forces_host.pin_memory()
+    _ = m_host.device_mesh  # setup (pattern, geometry) outside the timed region
+    e2e_out = step(m_host, forces_host, "mixed", args.stol)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_out = step(m_host, forces_host, "mixed", args.stol)
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms = reduce_max(dist, e2e_ms, dev)
+    n_elem = m.n_elem
+    h2d = 8 * n_dofs * 2 + n_dofs + 16 * n_elem  # forces, prescribed displacements, constraints, (lambda, G)
+    d2h = sum(t.numel() * t.element_size() for t in e2e_out[:5]) + 8 * n_dofs  # outputs + gradient
+
+    result = {}
+    if not args.no_plain:
+        out_p = step(m, forces, "fp64", args.stol)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        out_p = step(m, forces, "fp64", args.stol)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = reduce_max(dist, p0.elapsed_time(p1), dev)
+        u_p, g_p = out_p[0], out_p[5]
+        err_u = float((u_mixed - u_p).abs().max() / u_p.abs().max())
+        err_g = float((g_mixed - g_p).abs().max() / g_p.abs().max())
+        err_s = float((out[2] - out_p[2]).abs().max() / out_p[2].abs().max())
+        result = {"plain_fp64": {"value": plain_ms / 1e3 / (n_dofs / 1e6), "ms_per_step": plain_ms,
+                                 "cg_iterations": m.last_solve.iterations},
+                  "mixed_speedup_vs_plain": plain_ms / ms,
+                  "rel_err_mixed_vs_fp64": {"u": err_u, "sigma": err_s, "grad": err_g}}
+
+    peak, peak_kind = measured_peak_hbm()
+    avg_spmv_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
+    sb = spmv_bytes(dm)
+    achieved = sb / avg_spmv_s / 1e9 if avg_spmv_s else None
+    traffic_file = ROOT / "profiles" / "spmv_bsr_traffic.json"
+    traffic = None
+    if traffic_file.exists():
+        try:
+            tj = json.loads(traffic_file.read_text())
+            traffic = tj["bytes_per_block"] * dm.n_blocks
+        except (KeyError, ValueError):
+            traffic = None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": ms / 1e3 / (n_dofs / 1e6),
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms,
+            "higher_is_better": False,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32+f64",
+            "data": "synthetic (seeded jittered cube)",
+            "config": {"workload": f"hexa1_cube_{args.n}^3_jittered_linear_elastic_solve+adjoint",
+                       "dofs": n_dofs, "nnz": dm.nnz, "n_elem": n_elem, "stol": args.stol,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (FP32 K = %.0f MB)" % (dm.n_blocks * 40 / 1e6)},
+            "cg_iterations": iters,
+            "gpu_launches": launches,
+            "e2e": {"value": e2e_ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "roofline": {"bound": "hbm", "kernel": "k_spmv_bsr<3,8>", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                         "traffic": traffic, "algorithmic_bytes": sb, "avg_launch_us": avg_spmv_s * 1e6 if avg_spmv_s else None,
+                         "peak_source": peak_kind},
+            "clocks": clocks.summary(),
+            **result,
+        }
+        if world == 1:
+            line["cpu_baseline"] = cpu_baseline(args.cpu_n)
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,316 @@
+/*
+ * torchfem_gb300.h — C ABI of the GB300 forward + adjoint finite-element path.
+ *
+ * The library replaces the compute underneath torch-fem's `FEM.solve`
+ * (src/torchfem/base.py:597-923): sparsity precompute, Gauss-point element
+ * integration, element-to-CSR assembly with Dirichlet condensation, the
+ * linear solve behind `sparse_solve` (src/torchfem/sparse.py:271-347) and the
+ * adjoint pieces behind `NewtonRaphsonAdjoint.backward`
+ * (src/torchfem/sparse.py:641-724).  torch-fem itself is pure Python and has
+ * no FFI; each entry point below cites the Python function whose arithmetic it
+ * takes over, which is the seam a binding (ctypes, cffi, pybind) attaches to.
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers into caller-owned memory unless a
+ *    comment says "host".  The library never allocates device memory; entry
+ *    points that need scratch take (ws, ws_bytes) sized by the matching
+ *    *_workspace_bytes query.
+ *  - `stream` is a cudaStream_t passed as void*; all work is ordered on it.
+ *    Entry points that return a size to the host synchronise that stream.
+ *  - Index types: node ids, column indices and element-contributor codes are
+ *    int32; row pointers and slot maps are int64.
+ *  - `status` (nullable) is a device int32 word into which kernels OR
+ *    (1 << FEM_*) bits for device-detected conditions.
+ *  - Degree-of-freedom numbering is node-major, dof = node * dim + component
+ *    (src/torchfem/base.py:73-76).
+ */
+#ifndef TORCHFEM_GB300_H
+#define TORCHFEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FEM_ABI_VERSION 1
+
+/* Return codes.  The Python host maps them to the reference's exceptions:
+ * FEM_NOT_CONVERGED / FEM_NONFINITE / FEM_BREAKDOWN -> RuntimeError
+ * (src/torchfem/sparse.py:412-421, :500-512, :622-623), FEM_BAD_JACOBIAN ->
+ * ValueError (src/torchfem/base.py:311-312), FEM_INVALID -> ValueError. */
+enum {
+  FEM_OK = 0,
+  FEM_NOT_CONVERGED = 1,
+  FEM_NONFINITE = 2,
+  FEM_BAD_JACOBIAN = 3,
+  FEM_BOUNDS = 4,
+  FEM_INVALID = 5,
+  FEM_CUDA_ERROR = 6,
+  FEM_BREAKDOWN = 7
+};
+
+/* Element types (src/torchfem/elements.py).  Shape-function gradient tables
+ * and weights are supplied by the caller, so the library does not fix the
+ * quadrature; it only fixes (nodes, dim, integration points). */
+enum {
+  FEM_QUAD1 = 1,  /* 4 nodes, 2D, 4 points   (elements.py:491-567)  */
+  FEM_HEXA1 = 2,  /* 8 nodes, 3D, 8 points   (elements.py:936-1075) */
+  FEM_TETRA2 = 3, /* 10 nodes, 3D, 4 points  (elements.py:793-933)  */
+  FEM_TETRA1 = 4, /* 4 nodes, 3D, 1 point    (elements.py:727-790)  */
+  FEM_TRIA1 = 5,  /* 3 nodes, 2D, 1 point    (elements.py:309-382)  */
+  FEM_QUAD2 = 6,  /* 8 nodes, 2D, 4 points   (elements.py:570-724)  */
+  FEM_TRIA2 = 7   /* 6 nodes, 2D, 3 points   (elements.py:385-488)  */
+};
+
+/* Material data layouts consumed by the element kernels. */
+enum {
+  FEM_MAT_ISO = 1,        /* [n_elem][2] = (lambda, G): C = lambda I(x)I + G (I4 sym sum).
+                             Covers IsotropicElasticity3D / PlaneStrain and, with effective
+                             constants, PlaneStress (materials/elasticity.py:44-241). */
+  FEM_MAT_GENERAL = 2,    /* [n_elem][dim^4] full tangent C_iJkL per element. */
+  FEM_MAT_TANGENT_IP = 3  /* [nip][n_elem][dim^4] tangent per integration point. */
+};
+
+enum { FEM_F64 = 0, FEM_F32 = 1 };
+enum { FEM_FMT_CSR_F64 = 1, FEM_FMT_BSR_F32 = 2 };
+
+/* Last error message of the calling thread (host string). */
+const char* fem_last_error(void);
+int fem_abi_version(void);
+/* Number of kernels the library has launched in this process (host counter). */
+int64_t fem_launch_count(void);
+
+/* ------------------------------------------------------------------------ */
+/* Sparsity pattern: FEM.__init__ (src/torchfem/base.py:72-122).            */
+/* The reference builds packed 64-bit (row, col) keys, `torch.unique`s them  */
+/* and `searchsorted`s every element entry.  Here the pattern is derived     */
+/* from the node graph: the DOF pattern is the node adjacency with a dense   */
+/* dim x dim block per node pair, plus the diagonal of nodes that belong to  */
+/* no element — the same set the reference's keys produce.                   */
+/* ------------------------------------------------------------------------ */
+
+size_t fem_pattern_workspace_bytes(int64_t n_nod, int64_t n_elem, int n_e);
+
+/* Node->element incidence (inc: codes e*n_e + local node, ascending per
+ * node) and node-neighbour counts scanned into nbr_ptr [n_nod+1].  Writes the
+ * number of node-pair blocks to *n_blocks (host). */
+int fem_pattern_graph_count(const int32_t* elements, int64_t n_elem, int n_e, int64_t n_nod,
+                            int64_t* inc_ptr, int32_t* inc, int64_t* nbr_ptr,
+                            int64_t* n_blocks, void* ws, size_t ws_bytes, int32_t* status,
+                            void* stream);
+
+/* Sorted node neighbour lists nbr [n_blocks] (each node lists itself). */
+int fem_pattern_graph_fill(const int32_t* elements, int64_t n_elem, int n_e, int64_t n_nod,
+                           const int64_t* inc_ptr, const int32_t* inc, const int64_t* nbr_ptr,
+                           int32_t* nbr, int32_t* status, void* stream);
+
+/* Scalar CSR row pointers [n_dofs+1] of the reference pattern; *nnz (host). */
+int fem_pattern_csr_rows(const int64_t* nbr_ptr, int64_t n_nod, int dof_per_node,
+                         const int64_t* inc_ptr, int64_t* row_ptr, int64_t* nnz, void* ws,
+                         size_t ws_bytes, void* stream);
+
+/* Column indices [nnz] (== glob_idx[1], base.py:112-117) and the slot of
+ * each diagonal entry [n_dofs] (== diag_map, base.py:106-108). */
+int fem_pattern_csr_cols(const int64_t* nbr_ptr, const int32_t* nbr, int64_t n_nod,
+                         int dof_per_node, const int64_t* inc_ptr, const int64_t* row_ptr,
+                         int32_t* col, int64_t* diag_map, void* stream);
+
+/* Slot of every element-matrix entry, row-major over (e, p, q) — the
+ * reference's k_map (base.py:93-104) — for parity checks and for callers that
+ * assemble with it. */
+int fem_pattern_kmap(const int32_t* elements, int64_t n_elem, int n_e, int dof_per_node,
+                     const int64_t* nbr_ptr, const int32_t* nbr, const int64_t* row_ptr,
+                     int64_t* k_map, int32_t* status, void* stream);
+
+/* Block-level contributor lists used by the atomic-free assembly: for block b
+ * (a node pair), contrib[blk_ptr[b] .. blk_ptr[b+1]) are codes
+ * (e*n_e + la)*n_e + lb in ascending element order, which is the order in
+ * which CPU index_add_ visits them (base.py:410-411).  blk_row [n_blocks]
+ * is the row node of each block, diag_blk [n_nod] the block (a, a). */
+int fem_pattern_blocks(const int32_t* elements, int64_t n_elem, int n_e, int64_t n_nod,
+                       const int64_t* inc_ptr, const int32_t* inc, const int64_t* nbr_ptr,
+                       const int32_t* nbr, int64_t n_blocks, int64_t* blk_ptr,
+                       int32_t* contrib, int32_t* blk_row, int64_t* diag_blk, void* ws,
+                       size_t ws_bytes, int32_t* status, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Element integration: eval_shape_functions (base.py:293-314) and           */
+/* Mechanics.integrate_material (base.py:982-1092).                          */
+/* ------------------------------------------------------------------------ */
+
+typedef struct fem_mesh {
+  int etype;               /* FEM_* element type */
+  int64_t n_nod;
+  int64_t n_elem;
+  const double* nodes;     /* [n_nod][dim] */
+  const int32_t* elements; /* [n_elem][n_e] */
+  const double* weights;   /* [nip] integration weights */
+  const double* bt;        /* [nip][n_elem][n_e][dim] dN/dx (fem_geometry output) */
+  const double* detj;      /* [nip][n_elem] */
+  const int64_t* inc_ptr;  /* [n_nod+1] node->element incidence */
+  const int32_t* inc;      /* [n_elem*n_e] */
+  const double* thickness; /* [n_elem] planar thickness, NULL for solids */
+} fem_mesh;
+
+typedef struct fem_material {
+  int kind;                /* FEM_MAT_* */
+  const double* data;
+} fem_material;
+
+/* Jacobian, its determinant and the physical shape-function gradients at
+ * every integration point (base.py:306-313).  dndxi is [nip][dim][n_e].
+ * detJ <= 0 flags FEM_BAD_JACOBIAN in *status. */
+int fem_geometry(const fem_mesh* mesh, const double* dndxi, double* bt, double* detj,
+                 int32_t* status, void* stream);
+
+/* Element stiffness Ke = sum_ip w detJ t B^T C B (base.py:1085-1090,
+ * solid.py:52-54, planar.py:86-88), stored [n_elem][n_e*dim][n_e*dim] in
+ * out_dtype (FEM_F64 or FEM_F32). */
+int fem_element_stiffness(const fem_mesh* mesh, const fem_material* mat, int out_dtype,
+                          void* ke, int32_t* status, void* stream);
+
+/* Element internal forces f_e = sum_ip w detJ t B^T sigma with the linear
+ * stress update sigma = sigma_prev + C:(sym grad v - de0) (base.py:1050-1083,
+ * elasticity.py:119-127).  con_mode: 0 use v as is, 1 replace v at
+ * constrained DOFs by con_values (du_bc, base.py:710-711), 2 zero v there.
+ * sigma_prev [nip][n_elem][dim][dim] and de0 [n_elem][dim][dim] are
+ * nullable.  fe [n_elem][n_e][dim]; flux [nip][n_elem][dim][dim] and the
+ * increment gradient hgrad = H_inc [nip][n_elem][dim][dim] (base.py:1052)
+ * are nullable outputs. */
+int fem_element_force(const fem_mesh* mesh, const fem_material* mat, const double* v,
+                      const uint8_t* con_mask, const double* con_values, int con_mode,
+                      const double* sigma_prev, const double* de0, double* fe, double* flux,
+                      double* hgrad, int32_t* status, void* stream);
+
+/* Deterministic nodal assembly of element vectors (assemble_rhs,
+ * base.py:428-445): out[dof] = sum over the node's incident elements in
+ * ascending order, starting from +0.0 — the serial order of CPU index_add_.
+ * If sub != NULL, out = gathered - sub.  con_mode: 0 none, 1 zero at
+ * constrained DOFs (res[con] = 0, base.py:738-739), 2 copy con_src there.
+ * Optional *sumsq (device, nullable) receives ||out||^2 and then needs a
+ * workspace of fem_gather_workspace_bytes(n_nod*dim). */
+size_t fem_gather_workspace_bytes(int64_t n);
+int fem_gather_nodal(const fem_mesh* mesh, const double* fe, const double* sub,
+                     const uint8_t* con_mask, int con_mode, const double* con_src, double* out,
+                     double* sumsq, void* ws, size_t ws_bytes, void* stream);
+
+/* Vector-Jacobian product of fem_element_force for the hand-written adjoint
+ * (replaces torch.autograd.grad at sparse.py:698-705).  Given the cotangent
+ * g of the assembled forces (nodal, [n_nod*dim]), of the flux output
+ * (gflux, nullable) and of the hgrad output (ghgrad, nullable), writes the
+ * nullable cotangents of: sigma_prev
+ * (gsig [nip][n_elem][dim][dim]), material data (gmat, layout of mat->data),
+ * thickness (gthick [n_elem]), de0 (gde0 [n_elem][dim][dim]) and of the
+ * per-element input field (gve [n_elem][n_e][dim], gather with
+ * fem_gather_nodal).  v/con_* as in fem_element_force. */
+int fem_element_vjp(const fem_mesh* mesh, const fem_material* mat, const double* v,
+                    const uint8_t* con_mask, const double* con_values, int con_mode,
+                    const double* sigma_prev, const double* de0, const double* g,
+                    const double* gflux, const double* ghgrad, double* gsig, double* gmat,
+                    double* gthick, double* gde0, double* gve, int32_t* status, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Assembly: FEM.assemble_matrix (base.py:398-426).                         */
+/* ------------------------------------------------------------------------ */
+
+typedef struct fem_blocks {
+  int n_e;                 /* nodes per element */
+  int dim;                 /* DOFs per node */
+  int64_t n_nod;
+  int64_t n_blocks;
+  const int64_t* nbr_ptr;  /* [n_nod+1] */
+  const int32_t* nbr;      /* [n_blocks] */
+  const int64_t* blk_ptr;  /* [n_blocks+1] */
+  const int32_t* contrib;  /* [n_elem*n_e*n_e] */
+  const int32_t* blk_row;  /* [n_blocks] */
+  const int64_t* diag_blk; /* [n_nod] */
+  const int64_t* inc_ptr;  /* [n_nod+1] (orphan-node detection) */
+} fem_blocks;
+
+/* Scalar CSR values in the reference pattern from Ke (ke_dtype FP64/FP32),
+ * summed per slot in ascending element order from +0.0, then constrained
+ * rows/columns zeroed and their diagonal set to 1.0 (base.py:410-419). */
+int fem_assemble_csr(const fem_blocks* blocks, int ke_dtype, const void* ke,
+                     const int64_t* row_ptr, const uint8_t* con_mask, double* val,
+                     void* stream);
+
+/* The same sums into a block-CSR (dim x dim blocks, FP32) over the node graph. */
+int fem_assemble_bsr(const fem_blocks* blocks, int ke_dtype, const void* ke,
+                     const uint8_t* con_mask, float* bval, void* stream);
+
+/* Jacobi: inv_diag[r] = 1 / val[diag_map[r]] (sparse.py:406-407). */
+int fem_jacobi(const double* val, const int64_t* diag_map, int64_t n, double* inv_diag,
+               int32_t* status, void* stream);
+
+/* Block Jacobi: FP32 inverses of the dim x dim diagonal blocks. */
+int fem_block_jacobi(const fem_blocks* blocks, const float* bval, float* inv_blocks,
+                     int32_t* status, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Linear solve: sparse_solve (sparse.py:271-347), Jacobi-CG branch          */
+/* (sparse.py:414-421) and the mixed-precision variant.                      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct fem_matrix {
+  int format;              /* FEM_FMT_CSR_F64 or FEM_FMT_BSR_F32 */
+  int block;               /* 1 for CSR, dim for BSR */
+  int64_t n;               /* unknowns */
+  int64_t n_rows;          /* scalar rows (CSR) or block rows (BSR) */
+  const int64_t* row_ptr;  /* [n_rows+1] */
+  const int32_t* col;      /* scalar or block column ids */
+  const void* val;         /* FP64 [nnz] or FP32 [n_blocks][block][block] */
+  const void* precond;     /* FP64 inverse diagonal [n] or FP32 inverse blocks */
+} fem_matrix;
+
+typedef struct fem_solve_info {
+  int64_t iterations;      /* CG iterations */
+  int64_t replacements;    /* FP64 residual replacements (mixed) */
+  double rel_residual;     /* ||b - A x|| / ||b|| as tracked by the solver */
+  int32_t status;          /* FEM_* */
+  double spmv_ms;          /* summed CUDA-event time of the SpMV launches (timing on) */
+  int64_t spmv_timed;      /* number of SpMV launches in spmv_ms */
+} fem_solve_info;
+
+/* Turns CUDA-event timing of every CG SpMV launch on (1) or off (0). */
+void fem_set_timing(int enable);
+
+size_t fem_pcg_workspace_bytes(const fem_matrix* A);
+
+/* Preconditioned CG on A x = b from x = 0, stopping at ||r|| <= rtol ||b||
+ * (the criterion of cupyx/scipy cg used at sparse.py:417, :508).  FP64 CSR
+ * with Jacobi reproduces the reference GPU branch; an FP32 BSR matrix runs
+ * the same iteration in single precision. */
+int fem_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter,
+            void* ws, size_t ws_bytes, fem_solve_info* info, void* stream);
+
+/* FP64 matrix-free operator y = A x of the condensed system: the element
+ * kernels apply K to x with constrained entries zeroed, and y = x at
+ * constrained DOFs (the matrix assemble_matrix builds, base.py:410-419). */
+typedef struct fem_operator64 {
+  const fem_mesh* mesh;
+  const fem_material* mat;
+  const uint8_t* con_mask; /* [n_nod*dim] */
+} fem_operator64;
+
+size_t fem_apply64_workspace_bytes(const fem_operator64* op);
+int fem_apply64(const fem_operator64* op, const double* x, double* y, void* ws, size_t ws_bytes,
+                void* stream);
+
+size_t fem_pcg_mixed_workspace_bytes(const fem_matrix* A32, const fem_operator64* op);
+
+/* Mixed precision: FP32 BSR K and FP32 block-Jacobi CG, with the solution
+ * accumulated in FP64 and the recursive residual replaced by the FP64
+ * matrix-free residual b - A x whenever it has dropped by `delta` since the
+ * last replacement (reliable updates; Sleijpen & van der Vorst 1996).  Stops
+ * when the FP64 residual satisfies ||b - A x|| <= rtol ||b||. */
+int fem_pcg_mixed(const fem_matrix* A32, const fem_operator64* op, const double* b, double* x,
+                  double rtol, double delta, int64_t max_iter, void* ws, size_t ws_bytes,
+                  fem_solve_info* info, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TORCHFEM_GB300_H */

@@ -1,0 +1,305 @@
+"""CPU oracle of torch-fem's forward + adjoint path — TEST INFRASTRUCTURE ONLY.
+
+This module restates, in numpy/scipy, the arithmetic of the reference's hot
+path so that the GPU library can be checked against it.  Only `tests/`,
+`__graft_entry__.smoke()` and the `cpu_baseline` leg of `bench.py` may import
+it; the product (`torch-fem_gb300/`) never does.
+
+Parity pin: every function here is checked against golden vectors generated
+by running the reference itself (tests/golden/make_golden.py, committed with
+its outputs) — pattern, k_map, element matrices, assembled values, solutions
+and adjoint gradients.
+
+Restated reference code (paths relative to the torch-fem repository):
+  pattern              src/torchfem/base.py:72-122
+  shape gradients      src/torchfem/base.py:293-314, elements.py (tables)
+  integrate_material   src/torchfem/base.py:982-1092 (+ solid.py:52-58,
+                       planar.py:86-92, materials/elasticity.py:44-241)
+  assemble_matrix      src/torchfem/base.py:398-426 (serial index_add_ order)
+  assemble_rhs         src/torchfem/base.py:428-445
+  solve (linear)       src/torchfem/base.py:597-923 with sparse.py:271-514
+  adjoint              src/torchfem/sparse.py:641-724
+"""
+
+from __future__ import annotations
+
+from math import sqrt
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+# --------------------------------------------------------------- elements ---
+_HEX_SIGNS = np.array(
+    [(-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1)],
+    dtype=np.float64,
+)
+_QUAD_SIGNS = np.array([(-1, -1), (1, -1), (1, 1), (-1, 1)], dtype=np.float64)
+
+
+def _hexa1_dn(xi):
+    x = xi[:, None, :]  # [nip, 1, 3]
+    s = _HEX_SIGNS[None]  # [1, 8, 3]
+    f = 1.0 + s * x  # [nip, 8, 3]
+    d0 = s[..., 0] * f[..., 1] * f[..., 2]
+    d1 = s[..., 1] * f[..., 0] * f[..., 2]
+    d2 = s[..., 2] * f[..., 0] * f[..., 1]
+    return 0.125 * np.stack([d0, d1, d2], axis=1)  # [nip, 3, 8]
+
+
+def _quad1_dn(xi):
+    x = xi[:, None, :]
+    s = _QUAD_SIGNS[None]
+    f = 1.0 + s * x
+    return 0.25 * np.stack([s[..., 0] * f[..., 1], s[..., 1] * f[..., 0]], axis=1)  # [nip, 2, 4]
+
+
+def _tetra2_dn(xi):
+    x, y, z = xi[:, 0], xi[:, 1], xi[:, 2]
+    o = np.zeros_like(x)
+    c = 4 * (x + y + z) - 3
+    dx = [c, 4 * x - 1, o, o, -4 * (2 * x + y + z - 1), 4 * y, -4 * y, -4 * z, 4 * z, o]
+    dy = [c, o, 4 * y - 1, o, -4 * x, 4 * x, -4 * (x + 2 * y + z - 1), -4 * z, o, 4 * z]
+    dz = [c, o, o, 4 * z - 1, -4 * x, o, -4 * y, -4 * (x + y + 2 * z - 1), 4 * x, 4 * y]
+    return np.stack([np.stack(dx, -1), np.stack(dy, -1), np.stack(dz, -1)], axis=1)
+
+
+def _tetra1_dn(xi):
+    b = np.array([[-1.0, 1.0, 0.0, 0.0], [-1.0, 0.0, 1.0, 0.0], [-1.0, 0.0, 0.0, 1.0]])
+    return np.broadcast_to(b, (xi.shape[0], 3, 4)).copy()
+
+
+def _tria1_dn(xi):
+    b = np.array([[-1.0, 1.0, 0.0], [-1.0, 0.0, 1.0]])
+    return np.broadcast_to(b, (xi.shape[0], 2, 3)).copy()
+
+
+_S3 = 1.0 / sqrt(3.0)
+ELEMENTS = {
+    # name: (nodes, dim, ipoints, weights, dN/dxi)
+    "Hexa1": (8, 3, np.array([[a * _S3, b * _S3, c * _S3] for c in (-1.0, 1.0) for b in (-1.0, 1.0) for a in (-1.0, 1.0)]),
+              np.ones(8), _hexa1_dn),
+    "Quad1": (4, 2, np.array([[a * _S3, b * _S3] for b in (-1, 1) for a in (-1, 1)]), np.ones(4), _quad1_dn),
+    "Tetra2": (10, 3, np.array([[0.58541020, 0.13819660, 0.13819660], [0.13819660, 0.58541020, 0.13819660],
+                                [0.13819660, 0.13819660, 0.58541020], [0.13819660, 0.13819660, 0.13819660]]),
+               np.full(4, 0.041666667), _tetra2_dn),
+    "Tetra1": (4, 3, np.array([[0.25, 0.25, 0.25]]), np.array([1.0 / 6.0]), _tetra1_dn),
+    "Tria1": (3, 2, np.array([[1.0 / 3.0, 1.0 / 3.0]]), np.array([0.5]), _tria1_dn),
+}
+
+
+def element_name(n_e: int, dim: int) -> str:
+    table = {(8, 3): "Hexa1", (10, 3): "Tetra2", (4, 3): "Tetra1", (4, 2): "Quad1", (3, 2): "Tria1"}
+    return table[(n_e, dim)]
+
+
+# ---------------------------------------------------------------- pattern ---
+def pattern(elements: np.ndarray, n_nod: int, d: int):
+    """glob_idx [2, nnz], k_map [n_elem (n_e d)^2], diag_map [n_dofs] of the
+    reference's precompute (base.py:72-122): unique packed (row << 32 | col)
+    keys of all element entries plus the diagonal, then searchsorted."""
+    elements = np.asarray(elements, dtype=np.int64)
+    n_elem = elements.shape[0]
+    idx = (d * elements[..., None] + np.arange(d)).reshape(n_elem, -1)
+    keys = ((idx[:, :, None] << 32) | idx[:, None, :]).reshape(-1)
+    diag = np.arange(n_nod * d, dtype=np.int64)
+    packed = np.unique(np.concatenate([keys, (diag << 32) | diag]))
+    k_map = np.searchsorted(packed, keys)
+    diag_map = np.searchsorted(packed, (diag << 32) | diag)
+    glob_idx = np.stack([packed >> 32, packed & 0xFFFFFFFF])
+    return glob_idx, k_map, diag_map, idx
+
+
+# ----------------------------------------------------------- integration ---
+def shape_gradients(nodes: np.ndarray, elements: np.ndarray, etype: str):
+    """B [nip, n_elem, dim, n_e] (dN/dx) and detJ [nip, n_elem] (base.py:306-313)."""
+    n_e, dim, ip, w, dn = ELEMENTS[etype]
+    b = dn(ip)  # [nip, dim, n_e]
+    X = nodes[elements]  # [n_elem, n_e, dim]
+    J = np.einsum("iaN,ANj->iAaj", b, X)
+    detJ = np.linalg.det(J)
+    if np.any(detJ <= 0.0):
+        raise ValueError("Negative Jacobian. Check element numbering.")
+    B = np.einsum("iAaj,ijN->iAaN", np.linalg.inv(J), b)
+    return B, detJ, w
+
+
+def iso_c(lam: np.ndarray, G: np.ndarray, d: int) -> np.ndarray:
+    """C = lam I(x)I + G (I4 + I4^T) per element (elasticity.py:58-70)."""
+    I = np.eye(d)
+    i4 = np.einsum("ij,kl->ijkl", I, I)
+    i4s = np.einsum("ik,jl->ijkl", I, I) + np.einsum("il,jk->ijkl", I, I)
+    return lam[:, None, None, None, None] * i4 + G[:, None, None, None, None] * i4s
+
+
+def elastic_c(kind: str, E, nu, n_elem: int) -> np.ndarray:
+    """Tangent of IsotropicElasticity3D / PlaneStress / PlaneStrain (elasticity.py:44-241)."""
+    E = np.broadcast_to(np.asarray(E, dtype=np.float64), (n_elem,))
+    nu = np.broadcast_to(np.asarray(nu, dtype=np.float64), (n_elem,))
+    lbd = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    G = E / (2.0 * (1.0 + nu))
+    if kind == "3d":
+        return iso_c(lbd, G, 3)
+    C = np.zeros((n_elem, 2, 2, 2, 2))
+    if kind == "plane_stress":
+        fac = E / (1.0 - nu**2)
+        a, b, s = fac, fac * nu, fac * 0.5 * (1.0 - nu)
+    elif kind == "plane_strain":
+        a, b, s = 2.0 * G + lbd, lbd, G
+    else:
+        raise ValueError(kind)
+    C[:, 0, 0, 0, 0] = a
+    C[:, 1, 1, 1, 1] = a
+    C[:, 0, 0, 1, 1] = b
+    C[:, 1, 1, 0, 0] = b
+    for i, j, k, l in ((0, 1, 0, 1), (0, 1, 1, 0), (1, 0, 0, 1), (1, 0, 1, 0)):
+        C[:, i, j, k, l] = s
+    return C
+
+
+def integrate(B, detJ, w, C, du_e, sigma_prev=None, de0=None, thickness=None, need_k=True):
+    """Linear-elastic integrate_material (base.py:1020-1092): element forces,
+    stiffness, stress and increment gradient.  du_e [n_elem, n_e, d]."""
+    nip, n_elem, d, n_e = B.shape
+    t = np.ones(n_elem) if thickness is None else thickness
+    du = du_e.transpose(0, 2, 1)  # [n_elem, d, n_e]
+    f = np.zeros((n_elem, n_e * d))
+    k = np.zeros((n_elem, n_e * d, n_e * d)) if need_k else None
+    sig = np.zeros((nip, n_elem, d, d))
+    H_all = np.zeros((nip, n_elem, d, d))
+    e0 = np.zeros((n_elem, d, d)) if de0 is None else de0
+    for i in range(nip):
+        H = du @ B[i].transpose(0, 2, 1)
+        de = 0.5 * (H.transpose(0, 2, 1) + H)
+        s = np.einsum("eijkl,ekl->eij", C, de - e0)
+        if sigma_prev is not None:
+            s = s + sigma_prev[i]
+        sig[i] = s
+        H_all[i] = H
+        fc = np.einsum("e,eiI,eAi->eIA", t * detJ[i], B[i], s)
+        f += w[i] * fc.reshape(n_elem, -1)
+        if need_k:
+            BCB = np.einsum("eJp,eiJkL,eLq->epiqk", B[i], C, B[i]).reshape(n_elem, n_e * d, n_e * d)
+            k += (t * detJ[i])[:, None, None] * BCB * w[i]
+    return f, k, sig, H_all
+
+
+def assemble_matrix(k, k_map, nnz, glob_idx, diag_map, con):
+    """Serial ascending-order sums (CPU index_add_ order), then condensation."""
+    val = np.zeros(nnz)
+    np.add.at(val, k_map, k.ravel())
+    is_con = np.zeros(diag_map.shape[0], dtype=bool)
+    is_con[con] = True
+    val[is_con[glob_idx[0]] | is_con[glob_idx[1]]] = 0.0
+    val[diag_map[con]] = 1.0
+    return val
+
+
+def assemble_rhs(f, idx, n_dofs):
+    F = np.zeros(n_dofs)
+    np.add.at(F, idx.ravel(), f.ravel())
+    return F
+
+
+# ------------------------------------------------------------------ model ---
+class LinearModel:
+    """Linear-elastic model: the reference's single-increment solve
+    (increments [0, 1]) and its adjoint, on the CPU."""
+
+    def __init__(self, nodes, elements, C, thickness=None):
+        self.nodes = np.asarray(nodes, dtype=np.float64)
+        self.elements = np.asarray(elements, dtype=np.int64)
+        self.n_nod, self.d = self.nodes.shape
+        self.n_elem, self.n_e = self.elements.shape
+        self.n_dofs = self.n_nod * self.d
+        self.etype = element_name(self.n_e, self.d)
+        self.C = np.asarray(C, dtype=np.float64)
+        self.thickness = None if thickness is None else np.asarray(thickness, dtype=np.float64)
+        self.glob_idx, self.k_map, self.diag_map, self.idx = pattern(self.elements, self.n_nod, self.d)
+        self.B, self.detJ, self.w = shape_gradients(self.nodes, self.elements, self.etype)
+
+    def stiffness(self):
+        du0 = np.zeros((self.n_elem, self.n_e, self.d))
+        _, k, _, _ = integrate(self.B, self.detJ, self.w, self.C, du0, thickness=self.thickness)
+        return k
+
+    def matrix(self, con, k=None):
+        k = self.stiffness() if k is None else k
+        val = assemble_matrix(k, self.k_map, self.glob_idx.shape[1], self.glob_idx, self.diag_map, con)
+        return sp.csr_matrix((val, (self.glob_idx[0], self.glob_idx[1])), shape=(self.n_dofs, self.n_dofs))
+
+    def forces_of(self, u):
+        du_e = u.reshape(self.n_nod, self.d)[self.elements]
+        f, _, sig, H = integrate(self.B, self.detJ, self.w, self.C, du_e, thickness=self.thickness, need_k=False)
+        return assemble_rhs(f, self.idx, self.n_dofs), sig, H
+
+    def solve(self, forces, constraints, displacements=None, method="spsolve", rtol=1e-12):
+        """u, f, sigma (mean over points) of one linear increment (base.py:704-857)."""
+        F_ext = np.asarray(forces, dtype=np.float64).ravel()
+        con = np.nonzero(np.asarray(constraints).ravel())[0]
+        DU = np.zeros(self.n_dofs) if displacements is None else np.asarray(displacements, dtype=np.float64).ravel()
+        du = np.zeros(self.n_dofs)
+        du[con] = DU[con]
+        F_int, _, _ = self.forces_of(du)
+        res = F_int - F_ext
+        res[con] = 0.0
+        K = self.matrix(con)
+        du = du - self.linear_solve(K, res, method, rtol)
+        du[con] = DU[con]
+        F_int, sig, H = self.forces_of(du)
+        self.K, self.con = K, con
+        return du.reshape(self.n_nod, self.d), F_int.reshape(self.n_nod, self.d), sig.mean(axis=0)
+
+    @staticmethod
+    def linear_solve(K, b, method="spsolve", rtol=1e-12):
+        if method == "spsolve":
+            return spla.spsolve(K.tocsc(), b)
+        M = sp.diags(1.0 / K.diagonal())
+        x, info = spla.cg(K, b, rtol=rtol, atol=0.0, M=M, maxiter=20 * K.shape[0])
+        if info != 0:
+            raise RuntimeError(f"CG failed with exit code {info}")
+        return x
+
+    def adjoint(self, g_u, method="spsolve", rtol=1e-12):
+        """lambda = K^-1 g on free DOFs (sparse.py:671-680); 0 on constrained."""
+        g = np.asarray(g_u, dtype=np.float64).ravel().copy()
+        g[self.con] = 0.0
+        return self.linear_solve(self.K, g, method, rtol)
+
+    def grad_forces(self, g_u, method="spsolve"):
+        """d(L)/d(forces) for a loss with dL/du = g_u: equals lambda."""
+        return self.adjoint(g_u, method).reshape(self.n_nod, self.d)
+
+    def compliance_grad_c(self, u):
+        """dL/dC_e for L = f.u at equilibrium: -sum_ip w detJ t eps(u):dC:eps(u)
+        expressed per entry of C_e: -sum_ip w detJ t eps_ij eps_kl."""
+        du_e = u.reshape(self.n_nod, self.d)[self.elements].transpose(0, 2, 1)
+        t = np.ones(self.n_elem) if self.thickness is None else self.thickness
+        g = np.zeros_like(self.C)
+        for i in range(self.B.shape[0]):
+            H = du_e @ self.B[i].transpose(0, 2, 1)
+            eps = 0.5 * (H + H.transpose(0, 2, 1))
+            g -= (self.w[i] * self.detJ[i] * t)[:, None, None, None, None] * np.einsum("eij,ekl->eijkl", eps, eps)
+        return g
+
+
+# ------------------------------------------------------------- workloads ---
+def cube_hexa(Nx, Ny, Nz, Lx=1.0, Ly=1.0, Lz=1.0):
+    """Node/element numbering of the reference's cube_hexa (mesh.py:8-46)."""
+    X, Y, Z = np.linspace(0, Lx, Nx), np.linspace(0, Ly, Ny), np.linspace(0, Lz, Nz)
+    x, y, z = np.meshgrid(X, Y, Z, indexing="ij")
+    nodes = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    ids = np.arange(Nx * Ny * Nz).reshape(Nx, Ny, Nz)
+    c = lambda i, j, k: ids[i : Nx - 1 + i, j : Ny - 1 + j, k : Nz - 1 + k].ravel()  # noqa: E731
+    el = np.stack([c(0, 0, 0), c(1, 0, 0), c(1, 1, 0), c(0, 1, 0), c(0, 0, 1), c(1, 0, 1), c(1, 1, 1), c(0, 1, 1)], 1)
+    return nodes, el
+
+
+def rect_quad(Nx, Ny, Lx=1.0, Ly=1.0):
+    """Node/element numbering of the reference's rect_quad (mesh.py:103-135)."""
+    X, Y = np.linspace(0, Lx, Nx), np.linspace(0, Ly, Ny)
+    x, y = np.meshgrid(X, Y, indexing="ij")
+    nodes = np.stack([x.ravel(), y.ravel()], axis=1)
+    ids = np.arange(Nx * Ny).reshape(Nx, Ny)
+    c = lambda i, j: ids[i : Nx - 1 + i, j : Ny - 1 + j].ravel()  # noqa: E731
+    return nodes, np.stack([c(0, 0), c(1, 0), c(1, 1), c(0, 1)], 1)

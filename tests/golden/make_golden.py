@@ -1,0 +1,219 @@
+"""Generates the golden fixtures in this folder by running torch-fem itself.
+
+Run in a container that has the reference checkout at /root/reference:
+
+    python tests/golden/make_golden.py
+
+The reference's optional plotting / AMG / IO dependencies (pyvista,
+matplotlib, meshio, pyamg) are replaced by inert stub modules so that
+`import torchfem` succeeds; the hot path (FEM.__init__, integrate_material,
+assemble_matrix, solve with method="spsolve", NewtonRaphsonAdjoint) runs
+unmodified.  Outputs are small .npz files; nothing here runs on the GPU machine.
+"""
+
+from __future__ import annotations
+
+import importlib.abc
+import importlib.machinery
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+import torch
+
+REFERENCE_SRC = "/root/reference/src"
+OUT = Path(__file__).resolve().parent
+STUB_ROOTS = ("pyamg", "pyvista", "meshio", "matplotlib", "mpl_toolkits")
+
+
+class _Any:
+    def __init__(self, *a, **k):
+        pass
+
+    def __call__(self, *a, **k):
+        return _Any()
+
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        return _Any()
+
+    def __mro_entries__(self, bases):
+        return (object,)
+
+    def __iter__(self):
+        return iter(())
+
+
+for _op in ("add", "radd", "sub", "rsub", "mul", "rmul", "truediv", "rtruediv", "or", "ror", "and", "getitem"):
+    setattr(_Any, f"__{_op}__", lambda self, *a: _Any())
+
+
+class _StubLoader(importlib.abc.Loader):
+    def create_module(self, spec):
+        m = types.ModuleType(spec.name)
+        m.__path__ = []
+
+        def _getattr(attr):
+            if attr.startswith("__"):
+                raise AttributeError(attr)
+            return _Any()
+
+        m.__getattr__ = _getattr
+        return m
+
+    def exec_module(self, module):
+        pass
+
+
+class _StubFinder(importlib.abc.MetaPathFinder):
+    def find_spec(self, fullname, path, target=None):
+        if fullname.split(".")[0] in STUB_ROOTS:
+            return importlib.machinery.ModuleSpec(fullname, _StubLoader(), is_package=True)
+        return None
+
+
+def import_reference():
+    sys.meta_path.insert(0, _StubFinder())
+    sys.path.insert(0, REFERENCE_SRC)
+    import torchfem  # noqa: F401
+
+    return torchfem
+
+
+def jitter(nodes: torch.Tensor, h: float, seed: int = 0) -> torch.Tensor:
+    """Interior nodes moved by U(-0.1h, 0.1h) per coordinate (seeded)."""
+    g = torch.Generator().manual_seed(seed)
+    lo, hi = nodes.min(0).values, nodes.max(0).values
+    inner = ((nodes > lo) & (nodes < hi)).all(1)
+    delta = (torch.rand(nodes.shape, generator=g, dtype=torch.float64) * 2.0 - 1.0) * 0.1 * h
+    return nodes + inner[:, None] * delta
+
+
+def cube_problem(tf, N: int, jit: bool):
+    from torchfem import Solid
+    from torchfem.materials import IsotropicElasticity3D
+    from torchfem.mesh import cube_hexa
+
+    nodes, elements = cube_hexa(N + 1, N + 1, N + 1)
+    if jit:
+        nodes = jitter(nodes, 1.0 / N)
+    model = Solid(nodes, elements, IsotropicElasticity3D(1000.0, 0.3))
+    model.constraints[nodes[:, 0] == 0.0, :] = True
+    model.forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    return model
+
+
+def make_c1(tf):
+    """10^3 Hexa1 cube: u, f, sigma and d(sum u)/d(forces)."""
+    model = cube_problem(tf, 10, jit=False)
+    forces = model.forces.clone().requires_grad_(True)
+    model.forces = forces
+    u, f, s, _, _ = model.solve(method="spsolve", differentiable_parameters=forces)
+    (g,) = torch.autograd.grad(u.sum(), forces)
+    np.savez_compressed(
+        OUT / "c1_cube10.npz", u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(),
+        grad_forces=g.numpy(), torch_version=torch.__version__,
+    )
+
+
+def make_hexa_jitter3(tf):
+    """3^3 jittered Hexa1: pattern, element matrices, assembled values,
+    solution and gradients w.r.t. forces and per-element E."""
+    from torchfem import Solid
+    from torchfem.materials import IsotropicElasticity3D
+
+    base = cube_problem(tf, 3, jit=True)
+    nodes, elements = base.nodes, base.elements
+    con = torch.nonzero(base.constraints.ravel()).ravel()
+    ke = base.k0()
+    kval = base.assemble_matrix(ke, con)._values()
+    E = torch.full((len(elements),), 1000.0)
+    E = E * (1.0 + 0.2 * torch.rand(len(elements), generator=torch.Generator().manual_seed(1)))
+    E.requires_grad_(True)
+    model = Solid(nodes, elements, IsotropicElasticity3D(E, 0.3))
+    model.constraints = base.constraints.clone()
+    forces = base.forces.clone().requires_grad_(True)
+    model.forces = forces
+    u, f, s, gr, _ = model.solve(method="spsolve", differentiable_parameters=(forces, E))
+    (g_f,) = torch.autograd.grad(u.sum(), forces, retain_graph=True)
+    compliance = torch.inner(f.ravel(), u.ravel())
+    (g_E,) = torch.autograd.grad(compliance, E)
+    np.savez_compressed(
+        OUT / "hexa_jitter3.npz", nodes=nodes.numpy(), elements=elements.numpy(),
+        constraints=base.constraints.numpy(), forces=base.forces.detach().numpy(), E=E.detach().numpy(),
+        glob_idx=base.glob_idx.numpy(), k_map=base.k_map.numpy(), diag_map=base.diag_map.numpy(),
+        ke=ke.numpy(), kval=kval.numpy(), u=u.detach().numpy(), f=f.detach().numpy(),
+        sigma=s.detach().numpy(), grad=gr.detach().numpy(), grad_forces=g_f.numpy(), grad_E=g_E.numpy(),
+        compliance=compliance.detach().numpy(),
+    )
+
+
+def simp_problem(Nx: int, Ny: int, seed: int = 0):
+    from torchfem import Planar
+    from torchfem.materials import IsotropicElasticityPlaneStress
+    from torchfem.mesh import rect_quad
+
+    nodes, elements = rect_quad(Nx + 1, Ny + 1, 2.0, 1.0)
+    rho = 0.2 + 0.8 * torch.rand(len(elements), generator=torch.Generator().manual_seed(seed), dtype=torch.float64)
+    rho.requires_grad_(True)
+    model = Planar(nodes, elements, IsotropicElasticityPlaneStress(rho**3 * 1.0, 0.3))
+    model.constraints[nodes[:, 0] == 0.0, :] = True
+    tip = torch.argmin(((nodes - torch.tensor([2.0, 0.5])) ** 2).sum(1))
+    model.forces[tip, 1] = -1.0
+    return model, rho, tip
+
+
+def make_simp(tf, Nx, Ny, name, sample=None):
+    """Compliance L = f.u of the SIMP cantilever and dL/drho (reference autograd)."""
+    model, rho, tip = simp_problem(Nx, Ny)
+    u, f, s, _, _ = model.solve(method="spsolve", differentiable_parameters=rho)
+    L = torch.inner(f.ravel(), u.ravel())
+    (g,) = torch.autograd.grad(L, rho)
+    out = dict(compliance=L.detach().numpy(), tip=int(tip), u_tip=u[tip].detach().numpy(),
+               grad_norm=float(g.norm()), grad_sum=float(g.sum()))
+    if sample is None:
+        out.update(u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(), grad_rho=g.numpy(),
+                   rho=rho.detach().numpy())
+    else:
+        idx = torch.randperm(len(rho), generator=torch.Generator().manual_seed(2))[:sample]
+        out.update(sample_idx=idx.numpy(), grad_rho_sample=g[idx].numpy())
+    np.savez_compressed(OUT / name, **out)
+
+
+def make_patterns(tf):
+    """Patterns of a Tetra2 mesh (reference cube_tetra + linear_to_quadratic)
+    and of a quad mesh with one node that belongs to no element."""
+    from torchfem import Planar, Solid
+    from torchfem.elements import linear_to_quadratic
+    from torchfem.materials import IsotropicElasticity3D, IsotropicElasticityPlaneStress
+    from torchfem.mesh import cube_tetra, rect_quad
+
+    n_t, e_t = linear_to_quadratic(*cube_tetra(3, 3, 3))
+    mt = Solid(n_t, e_t, IsotropicElasticity3D(1000.0, 0.3))
+    n_q, e_q = rect_quad(4, 3)
+    n_q = torch.cat([n_q, torch.tensor([[5.0, 5.0]])])
+    mq = Planar(n_q, e_q, IsotropicElasticityPlaneStress(1000.0, 0.3))
+    np.savez_compressed(
+        OUT / "patterns.npz",
+        tet2_nodes=n_t.numpy(), tet2_elements=e_t.numpy(), tet2_glob_idx=mt.glob_idx.numpy(),
+        tet2_k_map=mt.k_map.numpy(), tet2_diag_map=mt.diag_map.numpy(),
+        orphan_nodes=n_q.numpy(), orphan_elements=e_q.numpy(), orphan_glob_idx=mq.glob_idx.numpy(),
+        orphan_k_map=mq.k_map.numpy(), orphan_diag_map=mq.diag_map.numpy(),
+    )
+
+
+def main():
+    torch.set_default_dtype(torch.float64)
+    tf = import_reference()
+    make_c1(tf)
+    make_hexa_jitter3(tf)
+    make_patterns(tf)
+    make_simp(tf, 20, 10, "simp_20x10.npz")
+    make_simp(tf, 400, 200, "simp_400x200.npz", sample=20)
+    print("fixtures written to", OUT)
+
+
+if __name__ == "__main__":
+    main()

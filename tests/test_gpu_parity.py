@@ -1,0 +1,252 @@
+"""GPU parity of the C-ABI kernels against the reference's golden vectors and
+the CPU oracle.
+
+Tolerances: integer pattern data and assembly given the reference's element
+matrices are compared bit for bit; element matrices to 1e-13 relative (the
+GPU sums Gauss points in a different floating-point order than the
+reference's batched einsum); solutions and gradients to 1e-8 relative, the
+accuracy target of the forward + adjoint path, with the CG run to 1e-12.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fem_oracle as O
+from torchfem_gb300 import Planar, Solid, mesh
+from torchfem_gb300.materials import IsotropicElasticity3D, IsotropicElasticityPlaneStress
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-8
+
+
+def rel(a, b):
+    a = a.detach().cpu().double().numpy() if torch.is_tensor(a) else np.asarray(a)
+    b = b.detach().cpu().double().numpy() if torch.is_tensor(b) else np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def cube_model(g, E=None):
+    nodes = torch.tensor(g["nodes"])
+    el = torch.tensor(g["elements"])
+    m = Solid(nodes, el, IsotropicElasticity3D(1000.0 if E is None else E, 0.3))
+    m.constraints = torch.tensor(g["constraints"])
+    m.forces = torch.tensor(g["forces"])
+    return m
+
+
+def test_pattern_parity_hexa(cuda, golden):
+    g = golden("hexa_jitter3.npz")
+    m = cube_model(g)
+    assert np.array_equal(m.glob_idx.cpu().numpy(), g["glob_idx"])
+    assert np.array_equal(m.k_map.cpu().numpy(), g["k_map"])
+    assert np.array_equal(m.diag_map.cpu().numpy(), g["diag_map"])
+
+
+@pytest.mark.parametrize("which", ["tet2", "orphan"])
+def test_pattern_parity_tet2_orphan(cuda, golden, which):
+    g = golden("patterns.npz")
+    nodes = torch.tensor(g[f"{which}_nodes"])
+    el = torch.tensor(g[f"{which}_elements"])
+    if nodes.shape[1] == 3:
+        m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+    else:
+        m = Planar(nodes, el, IsotropicElasticityPlaneStress(1000.0, 0.3))
+    assert np.array_equal(m.glob_idx.cpu().numpy(), g[f"{which}_glob_idx"])
+    assert np.array_equal(m.k_map.cpu().numpy(), g[f"{which}_k_map"])
+    assert np.array_equal(m.diag_map.cpu().numpy(), g[f"{which}_diag_map"])
+
+
+def test_assembly_bit_exact_given_reference_ke(cuda, golden):
+    g = golden("hexa_jitter3.npz")
+    m = cube_model(g)
+    dm = m.device_mesh
+    ke = torch.tensor(g["ke"], device=cuda).contiguous()
+    con = m.constraints.reshape(-1).to(cuda, torch.uint8).contiguous()
+    val = dm.assemble_csr(ke, con).cpu().numpy()
+    assert np.array_equal(val, g["kval"])  # bit for bit
+
+
+def test_element_stiffness_vs_reference(cuda, golden):
+    g = golden("hexa_jitter3.npz")
+    m = cube_model(g)
+    dm = m.device_mesh
+    kind, data = m.material.kernel_data(m.n_elem)
+    data = data.to(cuda).contiguous()
+    from torchfem_gb300 import _lib
+
+    ke = dm.element_stiffness(dm.make_mesh(None), _lib.FemMaterial(kind, data.data_ptr()))
+    assert rel(ke, torch.tensor(g["ke"])) <= 1e-13
+
+
+def test_c1_forward_and_adjoint(cuda, golden):
+    g = golden("c1_cube10.npz")
+    nodes, el = mesh.cube_hexa(11, 11, 11)
+    m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    forces = torch.zeros_like(nodes)
+    forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    forces.requires_grad_(True)
+    m.forces = forces
+    u, f, s, _, _ = m.solve(stol=1e-12, differentiable_parameters=forces)
+    assert rel(u, g["u"]) <= RTOL
+    assert rel(f, g["f"]) <= RTOL
+    assert rel(s, g["sigma"]) <= RTOL
+    (gf,) = torch.autograd.grad(u.sum(), forces)
+    assert rel(gf, g["grad_forces"]) <= RTOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_jittered_cube_gradients(cuda, golden, precision):
+    g = golden("hexa_jitter3.npz")
+    E = torch.tensor(g["E"], requires_grad=True)
+    m = cube_model(g, E)
+    forces = m.forces.clone().requires_grad_(True)
+    m.forces = forces
+    u, f, s, gr, _ = m.solve(stol=1e-12, precision=precision, differentiable_parameters=(forces, E))
+    assert rel(u, g["u"]) <= RTOL
+    assert rel(f, g["f"]) <= RTOL
+    assert rel(s, g["sigma"]) <= RTOL
+    assert rel(gr, g["grad"]) <= RTOL
+    (gf,) = torch.autograd.grad(u.sum(), forces, retain_graph=True)
+    assert rel(gf, g["grad_forces"]) <= RTOL
+    L = torch.inner(f.ravel(), u.ravel())
+    assert abs(float(L) - float(g["compliance"])) <= RTOL * abs(float(g["compliance"]))
+    (gE,) = torch.autograd.grad(L, E)
+    assert rel(gE, g["grad_E"]) <= RTOL
+
+
+def simp(Nx, Ny, rho):
+    nodes, el = mesh.rect_quad(Nx + 1, Ny + 1, 2.0, 1.0)
+    m = Planar(nodes, el, IsotropicElasticityPlaneStress(rho**3 * 1.0, 0.3))
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    tip = torch.argmin(((nodes - torch.tensor([2.0, 0.5])) ** 2).sum(1))
+    m.forces[tip, 1] = -1.0
+    return m
+
+
+def compliance(m, rho, **kw):
+    u, f, _, _, _ = m.solve(differentiable_parameters=rho, **kw)
+    return torch.inner(f.ravel(), u.ravel())
+
+
+def test_simp_small_vs_reference(cuda, golden):
+    g = golden("simp_20x10.npz")
+    rho = torch.tensor(g["rho"], requires_grad=True)
+    m = simp(20, 10, rho)
+    L = compliance(m, rho, stol=1e-12)
+    assert abs(float(L) - float(g["compliance"])) <= RTOL * abs(float(g["compliance"]))
+    (gr,) = torch.autograd.grad(L, rho)
+    assert rel(gr, g["grad_rho"]) <= RTOL
+
+
+def test_simp_central_differences(cuda, golden):
+    g = golden("simp_20x10.npz")
+    rho0 = torch.tensor(g["rho"])
+    rho = rho0.clone().requires_grad_(True)
+    L = compliance(simp(20, 10, rho), rho, stol=1e-13)
+    (gr,) = torch.autograd.grad(L, rho)
+    idx = torch.randperm(len(rho0), generator=torch.Generator().manual_seed(3))[:5]
+    h = 1e-6
+    for i in idx.tolist():
+        rp, rm = rho0.clone(), rho0.clone()
+        rp[i] += h
+        rm[i] -= h
+        with torch.no_grad():
+            Lp = float(compliance(simp(20, 10, rp), rp, stol=1e-13))
+            Lm = float(compliance(simp(20, 10, rm), rm, stol=1e-13))
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(fd - float(gr[i])) <= 1e-5 * abs(float(gr[i])) + 1e-9
+
+
+PATCH_2D = torch.tensor([[1.0e-3, 2.0e-4], [3.0e-4, -1.0e-3]])
+PATCH_3D = torch.tensor([[1.0e-3, 2.0e-4, -1.0e-4], [3.0e-4, -1.0e-3, 5.0e-5], [1.0e-4, 2.0e-4, 7.0e-4]])
+
+
+@pytest.mark.parametrize("etype", ["Quad1", "Hexa1", "Tetra1", "Tetra2", "Tria1", "Tria2", "Quad2"])
+def test_patch(cuda, etype):
+    """A linear displacement field prescribed on the boundary is reproduced
+    inside, with uniform stress (reference tests/test_models.py:54-71)."""
+    if etype in ("Quad1", "Quad2"):
+        nodes, el = mesh.rect_quad(4, 4)
+    elif etype in ("Tria1", "Tria2"):
+        nodes, q = mesh.rect_quad(4, 4)
+        el = torch.cat([q[:, [0, 1, 2]], q[:, [0, 2, 3]]])
+    elif etype == "Hexa1":
+        nodes, el = mesh.cube_hexa(3, 3, 3)
+    else:
+        nodes, el = mesh.cube_tetra(3, 3, 3)
+    if etype in ("Quad2", "Tria2", "Tetra2"):
+        nodes, el = mesh.linear_to_quadratic(nodes, el)
+    dim = nodes.shape[1]
+    if dim == 2:
+        m = Planar(nodes, el, IsotropicElasticityPlaneStress(1000.0, 0.3))
+        G = PATCH_2D
+    else:
+        m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+        G = PATCH_3D
+    assert m.etype.__name__ == etype
+    u_exact = nodes @ G.T
+    bnd = torch.zeros(len(nodes), dtype=torch.bool)
+    for k in range(dim):
+        c = nodes[:, k]
+        bnd |= torch.isclose(c, c.min()) | torch.isclose(c, c.max())
+    m.constraints = bnd[:, None].repeat(1, dim)
+    m.displacements = u_exact
+    u, _, sigma, _, _ = m.solve(stol=1e-14)
+    assert torch.allclose(u, u_exact, atol=1e-12)
+    assert torch.allclose(sigma, sigma[0].expand_as(sigma), atol=1e-10)
+
+
+def test_plain_and_mixed_agree_on_jittered_cube(cuda):
+    nodes, el = mesh.cube_hexa(13, 13, 13)
+    gen = torch.Generator().manual_seed(0)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen) * 2 - 1) * 0.1 / 12
+    res = {}
+    for p in ("fp64", "mixed"):
+        m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+        m.constraints[nodes[:, 0] == 0.0, :] = True
+        m.forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+        res[p] = m.solve(precision=p, stol=1e-10)
+        if p == "mixed":
+            assert m.last_solve.iterations[0] > 0
+    assert rel(res["mixed"][0], res["fp64"][0]) <= RTOL
+    assert rel(res["mixed"][2], res["fp64"][2]) <= RTOL
+    # oracle at the same size
+    om = O.LinearModel(nodes.numpy(), el.numpy(), O.elastic_c("3d", 1000.0, 0.3, len(el)))
+    con = np.zeros(nodes.shape, dtype=bool)
+    con[nodes[:, 0].numpy() == 0.0, :] = True
+    F = np.zeros(nodes.shape)
+    F[nodes[:, 0].numpy() == 1.0, 2] = -1.0 / len(nodes)
+    u, f, s = om.solve(F, con)
+    assert rel(res["fp64"][0], u) <= RTOL
+    assert rel(res["mixed"][0], u) <= RTOL
+
+
+def test_assembly_and_solve_deterministic(cuda, golden):
+    g = golden("hexa_jitter3.npz")
+    outs = []
+    for _ in range(3):
+        m = cube_model(g)
+        outs.append(m.solve()[0].cpu().numpy())
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+
+
+def test_negative_jacobian_raises(cuda):
+    nodes, el = mesh.cube_hexa(3, 3, 3)
+    el = el[:, [1, 0, 3, 2, 5, 4, 7, 6]]  # mirrored numbering: detJ < 0
+    m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    with pytest.raises(ValueError, match="Jacobian"):
+        m.solve()
+
+
+def test_cg_iteration_cap_cuts_back_then_raises(cuda):
+    nodes, el = mesh.cube_hexa(5, 5, 5)
+    m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    m.forces[nodes[:, 0] == 1.0, 2] = -1.0
+    with pytest.raises(RuntimeError, match="did not converge"):
+        m.solve(cg_max_iter=2, max_cutbacks=2)

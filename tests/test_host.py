@@ -1,0 +1,113 @@
+"""Host-side logic that needs no GPU: API validation, element tables, mesh
+numbering against the reference, method resolution, failure without CUDA."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fem_oracle as O
+from torchfem_gb300 import Planar, Solid
+from torchfem_gb300 import elements as E
+from torchfem_gb300 import mesh
+from torchfem_gb300.base import resolve_precision
+from torchfem_gb300.materials import (
+    IsotropicElasticity3D,
+    IsotropicElasticityPlaneStrain,
+    IsotropicElasticityPlaneStress,
+)
+
+
+def test_element_tables_match_oracle():
+    for cls, name in ((E.Hexa1, "Hexa1"), (E.Quad1, "Quad1"), (E.Tetra2, "Tetra2"), (E.Tetra1, "Tetra1"),
+                      (E.Tria1, "Tria1")):
+        n_e, dim, ip, w, dn = O.ELEMENTS[name]
+        assert np.array_equal(cls.gradient_table().numpy(), dn(ip))
+        assert np.array_equal(cls.iweights().numpy().astype(np.float64), w)
+
+
+def test_shape_functions_partition_of_unity():
+    for cls in (E.Hexa1, E.Quad1, E.Quad2, E.Tria1, E.Tria2, E.Tetra1, E.Tetra2):
+        xi = cls.ipoints()
+        assert torch.allclose(cls.N(xi).sum(-1), torch.ones(len(xi), dtype=torch.float64))
+        assert torch.allclose(cls.B(xi).sum(-1), torch.zeros(len(xi), cls.iso_dim, dtype=torch.float64), atol=1e-14)
+
+
+def test_mesh_numbering_matches_reference(golden):
+    # numpy and torch linspace may differ in the last bit: coordinates to 1 ulp,
+    # connectivity exactly
+    n, e = mesh.cube_hexa(11, 11, 11)
+    on, oe = O.cube_hexa(11, 11, 11)
+    assert np.allclose(n.numpy(), on, rtol=0, atol=1e-15) and np.array_equal(e.numpy(), oe)
+    n, e = mesh.rect_quad(21, 11, 2.0, 1.0)
+    on, oe = O.rect_quad(21, 11, 2.0, 1.0)
+    assert np.allclose(n.numpy(), on, rtol=0, atol=1e-15) and np.array_equal(e.numpy(), oe)
+    g = golden("patterns.npz")
+    n, e = mesh.linear_to_quadratic(*mesh.cube_tetra(3, 3, 3))
+    assert np.array_equal(e.numpy(), g["tet2_elements"])
+    assert np.array_equal(n.numpy(), g["tet2_nodes"])
+
+
+def test_box_tetra6_and_ogrid_positive_volumes():
+    n, e = mesh.box_tetra6(4, 3, 3, 3.0, 1.0, 1.0)
+    x = n[e]
+    vol = torch.linalg.det(torch.stack([x[:, 1] - x[:, 0], x[:, 2] - x[:, 0], x[:, 3] - x[:, 0]], 1))
+    assert (vol > 0).all() and torch.isclose(vol.sum() / 6.0, torch.tensor(3.0, dtype=torch.float64))
+    n, e = mesh.plate_hole_ogrid(32, 8)
+    assert n.shape == (32 * 9, 2) and e.shape == (32 * 8, 4)
+    x = n[e]
+    a = (x[:, 1, 0] - x[:, 0, 0]) * (x[:, 3, 1] - x[:, 0, 1]) - (x[:, 1, 1] - x[:, 0, 1]) * (x[:, 3, 0] - x[:, 0, 0])
+    assert (a > 0).all()
+    assert torch.isclose(n[:, 0].min(), torch.tensor(0.0, dtype=torch.float64))
+    assert torch.isclose(n[:, 0].max(), torch.tensor(2.0, dtype=torch.float64))
+
+
+def test_setters_validate_like_reference():
+    n, e = mesh.cube_hexa(3, 3, 3)
+    m = Solid(n, e, IsotropicElasticity3D(1000.0, 0.3))
+    with pytest.raises(ValueError):
+        m.forces = torch.zeros(3, 3)
+    with pytest.raises(TypeError):
+        m.forces = torch.zeros(len(n), 3, dtype=torch.int64)
+    with pytest.raises(TypeError):
+        m.constraints = torch.zeros(len(n), 3)
+    with pytest.raises(ValueError):
+        m.displacements = torch.zeros(2, 3)
+    assert m.n_dofs == 81 and m.n_int == 8 and m.idx.dtype == torch.int32
+    q = Planar(*mesh.rect_quad(3, 3), IsotropicElasticityPlaneStress(1.0, 0.3))
+    assert q.thickness.shape == (4,) and q.n_int == 4
+
+
+def test_method_resolution():
+    assert resolve_precision(None, None) == "fp64"
+    assert resolve_precision("cg", None) == "fp64"
+    assert resolve_precision("gb300-mixed", None) == "mixed"
+    assert resolve_precision(None, "mixed") == "mixed"
+    with pytest.raises(ValueError):
+        resolve_precision("foo", None)
+    with pytest.raises(RuntimeError):
+        resolve_precision("spsolve", None)
+
+
+def test_material_kernel_data_and_step():
+    n_elem = 5
+    for mat, d in ((IsotropicElasticity3D(1000.0, 0.3), 3), (IsotropicElasticityPlaneStress(2.0, 0.25), 2),
+                   (IsotropicElasticityPlaneStrain(3.0, 0.2), 2)):
+        kind, data = mat.vectorize(n_elem).kernel_data(n_elem)
+        assert kind == 1 and data.shape == (n_elem, 2)
+        lam, G = data[0]
+        I = torch.eye(d, dtype=torch.float64)
+        rec = lam * torch.einsum("ij,kl->ijkl", I, I) + G * (
+            torch.einsum("ik,jl->ijkl", I, I) + torch.einsum("il,jk->ijkl", I, I))
+        assert torch.allclose(rec, mat.C.to(torch.float64), rtol=1e-14)
+        H = torch.randn(4, d, d, dtype=torch.float64)
+        s, _, C = mat.step(H, None, torch.zeros(4, d, d, dtype=torch.float64), None, torch.zeros(d, d), None, 0)
+        assert torch.allclose(s, torch.einsum("ijkl,nkl->nij", mat.C.to(torch.float64), 0.5 * (H + H.transpose(1, 2))))
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU failure path")
+def test_solve_without_cuda_fails_loudly():
+    n, e = mesh.cube_hexa(3, 3, 3)
+    m = Solid(n, e, IsotropicElasticity3D(1000.0, 0.3))
+    m.constraints[n[:, 0] == 0, :] = True
+    with pytest.raises(RuntimeError, match="CUDA"):
+        m.solve()

@@ -1,0 +1,80 @@
+"""The CPU oracle against golden vectors produced by the reference itself."""
+
+import numpy as np
+import pytest
+
+from oracle import fem_oracle as O
+
+
+def test_pattern_hexa(golden):
+    g = golden("hexa_jitter3.npz")
+    gi, km, dm, _ = O.pattern(g["elements"], len(g["nodes"]), 3)
+    assert np.array_equal(gi, g["glob_idx"])
+    assert np.array_equal(km, g["k_map"])
+    assert np.array_equal(dm, g["diag_map"])
+
+
+@pytest.mark.parametrize("which", ["tet2", "orphan"])
+def test_pattern_tet2_and_orphan(golden, which):
+    g = golden("patterns.npz")
+    nodes, el = g[f"{which}_nodes"], g[f"{which}_elements"]
+    gi, km, dm, _ = O.pattern(el, len(nodes), nodes.shape[1])
+    assert np.array_equal(gi, g[f"{which}_glob_idx"])
+    assert np.array_equal(km, g[f"{which}_k_map"])
+    assert np.array_equal(dm, g[f"{which}_diag_map"])
+
+
+def test_element_matrices_and_assembly(golden):
+    g = golden("hexa_jitter3.npz")
+    m = O.LinearModel(g["nodes"], g["elements"], O.elastic_c("3d", 1000.0, 0.3, len(g["elements"])))
+    k = m.stiffness()
+    assert np.abs(k - g["ke"]).max() <= 1e-13 * np.abs(g["ke"]).max()
+    con = np.nonzero(g["constraints"].ravel())[0]
+    val = O.assemble_matrix(g["ke"], m.k_map, m.glob_idx.shape[1], m.glob_idx, m.diag_map, con)
+    assert np.array_equal(val, g["kval"])  # serial order: bit-identical
+
+
+def test_c1_solution(golden):
+    g = golden("c1_cube10.npz")
+    nodes, el = O.cube_hexa(11, 11, 11)
+    m = O.LinearModel(nodes, el, O.elastic_c("3d", 1000.0, 0.3, len(el)))
+    con = np.zeros_like(nodes, dtype=bool)
+    con[nodes[:, 0] == 0.0, :] = True
+    F = np.zeros_like(nodes)
+    F[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    u, f, s = m.solve(F, con)
+    for a, b in ((u, g["u"]), (f, g["f"]), (s, g["sigma"])):
+        assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max()
+    gf = m.grad_forces(np.ones(m.n_dofs))
+    assert np.abs(gf - g["grad_forces"]).max() <= 1e-10 * np.abs(g["grad_forces"]).max()
+
+
+def test_hexa_jitter_gradients(golden):
+    g = golden("hexa_jitter3.npz")
+    el = g["elements"]
+    C = O.elastic_c("3d", g["E"], 0.3, len(el))
+    m = O.LinearModel(g["nodes"], el, C)
+    u, f, s = m.solve(g["forces"], g["constraints"])
+    assert np.abs(u - g["u"]).max() <= 1e-10 * np.abs(g["u"]).max()
+    # dL/dE for L = f.u: C is linear in E, dC/dE = C/E
+    gC = m.compliance_grad_c(u.ravel())
+    gE = (gC * C).sum(axis=(1, 2, 3, 4)) / g["E"]
+    assert np.abs(gE - g["grad_E"]).max() <= 1e-9 * np.abs(g["grad_E"]).max()
+
+
+def test_simp_small(golden):
+    g = golden("simp_20x10.npz")
+    nodes, el = O.rect_quad(21, 11, 2.0, 1.0)
+    rho = g["rho"]
+    C = O.elastic_c("plane_stress", rho**3, 0.3, len(el))
+    m = O.LinearModel(nodes, el, C, thickness=np.ones(len(el)))
+    con = np.zeros_like(nodes, dtype=bool)
+    con[nodes[:, 0] == 0.0, :] = True
+    F = np.zeros_like(nodes)
+    F[int(g["tip"]), 1] = -1.0
+    u, f, s = m.solve(F, con)
+    L = float(np.dot(f.ravel(), u.ravel()))
+    assert abs(L - float(g["compliance"])) <= 1e-10 * abs(float(g["compliance"]))
+    gC = m.compliance_grad_c(u.ravel())
+    grho = (gC * C).sum(axis=(1, 2, 3, 4)) * 3.0 / rho  # E = rho^3
+    assert np.abs(grho - g["grad_rho"]).max() <= 1e-9 * np.abs(g["grad_rho"]).max()

@@ -1,0 +1,71 @@
+// Shared device/host helpers for the torch-fem GB300 kernels.
+//
+// Every entry point of the C-ABI (include/torchfem_gb300.h) returns an int
+// status.  Device-side conditions (negative Jacobian, exceeded size limits,
+// non-finite values) are OR-ed as bit flags into a caller-owned int32 status
+// word, which the host reads after the stream has drained.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/torchfem_gb300.h"
+
+namespace tfg {
+
+// Device status bits (mirrors the FEM_* status codes: bit = 1 << code).
+constexpr int kStatNonFinite = 1 << FEM_NONFINITE;
+constexpr int kStatBadJacobian = 1 << FEM_BAD_JACOBIAN;
+constexpr int kStatBounds = 1 << FEM_BOUNDS;
+
+void set_last_error(const char* fmt, ...);
+
+// Host-side count of kernel launches issued by this library (all threads).
+void note_launch();
+
+// Converts a pending CUDA error into FEM_CUDA_ERROR with a message.
+int check_cuda(const char* where);
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned int grid_for(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  return static_cast<unsigned int>(g);
+}
+
+__device__ __forceinline__ void flag_status(int32_t* status, int bits) {
+  if (status) atomicOr(reinterpret_cast<int*>(status), bits);
+}
+
+// Warp-level sum (fixed butterfly order: deterministic).
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-level sum of a double; blockDim.x must be a multiple of 32 and
+// <= 1024.  The result is valid in thread 0.  Fixed order: deterministic.
+__device__ __forceinline__ double block_sum(double v, double* smem32) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) smem32[wid] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  double t = (threadIdx.x < nw) ? smem32[threadIdx.x] : 0.0;
+  if (wid == 0) t = warp_sum(t);
+  __syncthreads();
+  return t;
+}
+
+}  // namespace tfg
+
+#define TFG_CHECK_LAUNCH(where)                      \
+  do {                                               \
+    int _rc = ::tfg::check_cuda(where);              \
+    if (_rc != FEM_OK) return _rc;                   \
+  } while (0)

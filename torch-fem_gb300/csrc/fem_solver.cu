@@ -1,0 +1,913 @@
+// Assembly (FEM.assemble_matrix, src/torchfem/base.py:398-426), Jacobi and
+// block-Jacobi preconditioners, and the preconditioned CG solvers that replace
+// the sparse_solve backends (src/torchfem/sparse.py:271-514).
+//
+// Determinism: every sum runs in a fixed order.  Assembly sums a slot's
+// contributions in ascending element order from +0.0 (the order CPU
+// index_add_ visits them), and all CG reductions are two-stage: per-CTA
+// partials in a fixed tree, then a fixed-order sum by whichever CTA arrives
+// last.  No floating-point atomics are used anywhere.
+#include <algorithm>
+#include <vector>
+
+#include "fem_common.cuh"
+
+namespace tfg {
+
+int etype_info(int etype, int* ne, int* d, int* nip);
+
+// ---------------------------------------------------------------- assembly --
+// Thread per node-pair block (a, b): gathers the d x d sub-blocks of every
+// contributing element matrix, sums them in ascending element order and
+// writes them with the Dirichlet condensation of base.py:414-419.
+template <typename KT, typename AT, bool kBSR>
+__global__ void k_assemble(int n_e, int D, int64_t n_blocks, const int64_t* __restrict__ nbr_ptr,
+                           const int32_t* __restrict__ nbr, const int64_t* __restrict__ blk_ptr,
+                           const int32_t* __restrict__ contrib, const int32_t* __restrict__ blk_row,
+                           const int64_t* __restrict__ inc_ptr, const KT* __restrict__ ke,
+                           const int64_t* __restrict__ row_ptr, const uint8_t* __restrict__ con,
+                           double* __restrict__ val, float* __restrict__ bval) {
+  const int64_t blk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (blk >= n_blocks) return;
+  const int64_t a = blk_row[blk];
+  const int64_t b = nbr[blk];
+  const int64_t k = blk - nbr_ptr[a];
+  const int ND = n_e * D;
+  const int nn = n_e * n_e;
+  AT acc[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) acc[i][j] = AT(0);
+  for (int64_t q = blk_ptr[blk]; q < blk_ptr[blk + 1]; ++q) {
+    const int32_t c = contrib[q];
+    const int64_t e = c / nn;
+    const int la = (c / n_e) % n_e, lb = c % n_e;
+    const KT* src = ke + e * (int64_t)ND * ND + (int64_t)(la * D) * ND + lb * D;
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j < D; ++j) acc[i][j] += (AT)src[i * ND + j];
+  }
+  const bool orphan = inc_ptr[a + 1] == inc_ptr[a];
+  for (int i = 0; i < D; ++i) {
+    const int64_t r = a * D + i;
+    const bool rc = con[r] != 0;
+    for (int j = 0; j < D; ++j) {
+      const int64_t cdof = b * D + j;
+      double v = (double)acc[i][j];
+      if (rc || con[cdof]) v = 0.0;
+      if (r == cdof && rc) v = 1.0;
+      if (kBSR) {
+        bval[blk * D * D + i * D + j] = (float)v;
+      } else {
+        if (orphan) {
+          if (i == j) val[row_ptr[r]] = v;
+        } else {
+          val[row_ptr[r] + k * D + j] = v;
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_jacobi(const double* __restrict__ val, const int64_t* __restrict__ diag_map, int64_t n,
+                         double* __restrict__ inv, int32_t* status) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const double d = val[diag_map[r]];
+  const double v = 1.0 / d;
+  if (!isfinite(v)) flag_status(status, kStatNonFinite);
+  inv[r] = v;
+}
+
+__global__ void k_block_jacobi(const float* __restrict__ bval, const int64_t* __restrict__ diag_blk,
+                               int64_t n_nod, int D, float* __restrict__ inv, int32_t* status) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n_nod) return;
+  const float* m = bval + diag_blk[a] * D * D;
+  double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j) M[i][j] = m[i * D + j];
+  double R[3][3];
+  double det;
+  if (D == 2) {
+    det = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+    R[0][0] = M[1][1] / det;
+    R[0][1] = -M[0][1] / det;
+    R[1][0] = -M[1][0] / det;
+    R[1][1] = M[0][0] / det;
+  } else if (D == 3) {
+    const double c00 = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+    const double c01 = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+    const double c02 = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+    det = M[0][0] * c00 + M[0][1] * c01 + M[0][2] * c02;
+    R[0][0] = c00 / det;
+    R[1][0] = c01 / det;
+    R[2][0] = c02 / det;
+    R[0][1] = (M[0][2] * M[2][1] - M[0][1] * M[2][2]) / det;
+    R[1][1] = (M[0][0] * M[2][2] - M[0][2] * M[2][0]) / det;
+    R[2][1] = (M[0][1] * M[2][0] - M[0][0] * M[2][1]) / det;
+    R[0][2] = (M[0][1] * M[1][2] - M[0][2] * M[1][1]) / det;
+    R[1][2] = (M[0][2] * M[1][0] - M[0][0] * M[1][2]) / det;
+    R[2][2] = (M[0][0] * M[1][1] - M[0][1] * M[1][0]) / det;
+  } else {
+    det = M[0][0];
+    R[0][0] = 1.0 / det;
+  }
+  bool ok = isfinite(det) && det != 0.0;
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j) {
+      inv[a * D * D + i * D + j] = (float)R[i][j];
+      ok = ok && isfinite(R[i][j]);
+    }
+  if (!ok) flag_status(status, kStatNonFinite);
+}
+
+// --------------------------------------------------------------------- CG ---
+enum { kDoneNo = 0, kDoneConverged = 1, kDoneMaxIter = 2, kDoneNonFinite = 3, kDoneBreakdown = 4 };
+
+struct Ctrl {
+  double rz;       // r.z of the current iterate
+  double rz_new;   // r.z after the last update (held while a replacement is pending)
+  double alpha;
+  double beta;
+  double rr;       // ||r||^2 of the working residual
+  double rr_ref;   // ||r||^2 at the last FP64 replacement (mixed)
+  double rr_true;  // ||b - A x||^2 from the last FP64 replacement (mixed)
+  double bb;       // ||b||^2
+  double tol2bb;   // rtol^2 ||b||^2
+  double delta2;   // replacement threshold (mixed)
+  long long iters;
+  long long max_iter;
+  long long replacements;
+  int done;
+  int replace;
+  int mixed;
+  unsigned int counter;
+};
+
+__device__ __forceinline__ bool arrive_last(unsigned int* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  return last;
+}
+
+// Sum of partial[0..n)*stride+k in a fixed order (single CTA).
+__device__ __forceinline__ double sum_partials(const double* partial, int n, int stride, int k,
+                                               double* red) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(partial + (int64_t)i * stride + k);
+  return block_sum(s, red);
+}
+
+__device__ __forceinline__ bool ctrl_idle(const Ctrl* c) {
+  return (*(volatile const int*)&c->done) != 0 || (*(volatile const int*)&c->replace) != 0;
+}
+
+// Scalar CSR FP64 SpMV q = A p with TPR threads per row, fused p.q partial;
+// the last CTA forms alpha = rz / p.q.
+template <int TPR>
+__global__ void __launch_bounds__(256)
+k_spmv_csr(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+           const double* __restrict__ val, const double* __restrict__ p, double* __restrict__ q,
+           double* __restrict__ partial, Ctrl* ctrl) {
+  __shared__ double red[32];
+  if (ctrl_idle(ctrl)) return;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = t / TPR;
+  const int sub = (int)(t % TPR);
+  double pq = 0.0;
+  double s = 0.0;
+  if (row < n) {
+    const int64_t rs = row_ptr[row], re = row_ptr[row + 1];
+    for (int64_t j = rs + sub; j < re; j += TPR) s += val[j] * p[col[j]];
+  }
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
+  if (row < n && sub == 0) {
+    q[row] = s;
+    pq = p[row] * s;
+  }
+  const double bsum = block_sum(pq, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = bsum;
+  if (arrive_last(&ctrl->counter)) {
+    const double tot = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      if (!(tot > 0.0) || !isfinite(tot)) {
+        ctrl->done = isfinite(tot) ? kDoneBreakdown : kDoneNonFinite;
+      } else {
+        ctrl->alpha = ctrl->rz / tot;
+      }
+    }
+  }
+}
+
+// Block-CSR FP32 SpMV with TPB threads per block row, FP32 products and
+// accumulation, p.q partial in FP64.
+template <int D, int TPB>
+__global__ void __launch_bounds__(256)
+k_spmv_bsr(int64_t n_rows, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+           const float* __restrict__ bval, const float* __restrict__ p, float* __restrict__ q,
+           double* __restrict__ partial, Ctrl* ctrl) {
+  __shared__ double red[32];
+  if (ctrl_idle(ctrl)) return;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = t / TPB;
+  const int sub = (int)(t % TPB);
+  float y[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) y[i] = 0.f;
+  if (row < n_rows) {
+    const int64_t rs = row_ptr[row], re = row_ptr[row + 1];
+    for (int64_t k = rs + sub; k < re; k += TPB) {
+      const int64_t c = col[k];
+      const float* m = bval + k * (D * D);
+      float x[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) x[j] = p[c * D + j];
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) y[i] = fmaf(m[i * D + j], x[j], y[i]);
+    }
+  }
+#pragma unroll
+  for (int o = TPB / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < D; ++i) y[i] += __shfl_down_sync(0xffffffffu, y[i], o, TPB);
+  double pq = 0.0;
+  if (row < n_rows && sub == 0) {
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      q[row * D + i] = y[i];
+      pq += (double)p[row * D + i] * (double)y[i];
+    }
+  }
+  const double bsum = block_sum(pq, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = bsum;
+  if (arrive_last(&ctrl->counter)) {
+    const double tot = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      if (!(tot > 0.0) || !isfinite(tot)) {
+        ctrl->done = isfinite(tot) ? kDoneBreakdown : kDoneNonFinite;
+      } else {
+        ctrl->alpha = ctrl->rz / tot;
+      }
+    }
+  }
+}
+
+// z = M r for one group of G DOFs: Jacobi (G = 1, FP64 inverse diagonal) or
+// block Jacobi (G = dim, FP32 inverse blocks).
+template <int G, typename VT>
+__device__ __forceinline__ void apply_prec(const void* prec, int64_t i, const VT (&r)[G], VT (&z)[G]) {
+  if constexpr (G == 1) {
+    z[0] = (VT)(((const double*)prec)[i] * (double)r[0]);
+  } else {
+    const float* m = (const float*)prec + i * G * G;
+#pragma unroll
+    for (int a = 0; a < G; ++a) {
+      float s = 0.f;
+#pragma unroll
+      for (int b = 0; b < G; ++b) s = fmaf(m[a * G + b], (float)r[b], s);
+      z[a] = (VT)s;
+    }
+  }
+}
+
+// Finalisation shared by the update and replacement kernels.
+__device__ void finish_update(Ctrl* c, double rz_new, double rr, bool count_iter) {
+  if (count_iter) c->iters += 1;
+  c->rr = rr;
+  if (!isfinite(rr) || !isfinite(rz_new)) {
+    c->done = kDoneNonFinite;
+    return;
+  }
+  bool stop = false;
+  if (c->mixed) {
+    if (rr <= c->tol2bb || rr <= c->delta2 * c->rr_ref) {
+      c->replace = 1;
+      c->rz_new = rz_new;
+      stop = true;
+    }
+  } else if (rr <= c->tol2bb) {
+    c->done = kDoneConverged;
+    stop = true;
+  }
+  if (!stop && c->iters >= c->max_iter) {
+    c->done = kDoneMaxIter;
+    c->rz_new = rz_new;
+    return;
+  }
+  if (!stop) {
+    c->beta = rz_new / c->rz;
+    c->rz = rz_new;
+  }
+}
+
+// x += alpha p; r -= alpha q; z = M r; partial r.z and r.r.
+template <int G, typename VT>
+__global__ void __launch_bounds__(256)
+k_update(int64_t n_groups, VT* __restrict__ x, VT* __restrict__ r, const VT* __restrict__ p,
+         const VT* __restrict__ q, VT* __restrict__ z, const void* __restrict__ prec,
+         double* __restrict__ partial, Ctrl* ctrl) {
+  __shared__ double red[32];
+  if (ctrl_idle(ctrl)) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rz = 0.0, rr = 0.0;
+  if (i < n_groups) {
+    const VT alpha = (VT)ctrl->alpha;
+    VT rv[G], zv[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int64_t k = i * G + g;
+      x[k] += alpha * p[k];
+      rv[g] = r[k] - alpha * q[k];
+      r[k] = rv[g];
+    }
+    apply_prec<G, VT>(prec, i, rv, zv);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      z[i * G + g] = zv[g];
+      rz += (double)rv[g] * (double)zv[g];
+      rr += (double)rv[g] * (double)rv[g];
+    }
+  }
+  const double s1 = block_sum(rz, red);
+  const double s2 = block_sum(rr, red);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = s1;
+    partial[2 * blockIdx.x + 1] = s2;
+  }
+  if (arrive_last(&ctrl->counter)) {
+    const double t1 = sum_partials(partial, gridDim.x, 2, 0, red);
+    const double t2 = sum_partials(partial, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      finish_update(ctrl, t1, t2, true);
+    }
+  }
+}
+
+template <typename VT>
+__global__ void k_pupdate(int64_t n, const VT* __restrict__ z, VT* __restrict__ p, Ctrl* ctrl) {
+  if (ctrl_idle(ctrl)) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const VT beta = (VT)ctrl->beta;
+  p[i] = z[i] + beta * p[i];
+}
+
+// Start (x = 0): r = b, z = M r, p = z; rz, rr, bb; tolerances.
+template <int G, typename VT>
+__global__ void __launch_bounds__(256)
+k_init(int64_t n_groups, const double* __restrict__ b, VT* __restrict__ x, VT* __restrict__ r,
+       VT* __restrict__ z, VT* __restrict__ p, const void* __restrict__ prec,
+       double* __restrict__ partial, Ctrl* ctrl, double rtol2) {
+  __shared__ double red[32];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rz = 0.0, rr = 0.0, bb = 0.0;
+  if (i < n_groups) {
+    VT rv[G], zv[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const double bv = b[i * G + g];
+      bb += bv * bv;
+      rv[g] = (VT)bv;
+      r[i * G + g] = rv[g];
+      x[i * G + g] = VT(0);
+    }
+    apply_prec<G, VT>(prec, i, rv, zv);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      z[i * G + g] = zv[g];
+      p[i * G + g] = zv[g];
+      rz += (double)rv[g] * (double)zv[g];
+      rr += (double)rv[g] * (double)rv[g];
+    }
+  }
+  const double s1 = block_sum(rz, red);
+  const double s2 = block_sum(rr, red);
+  const double s3 = block_sum(bb, red);
+  if (threadIdx.x == 0) {
+    partial[3 * blockIdx.x] = s1;
+    partial[3 * blockIdx.x + 1] = s2;
+    partial[3 * blockIdx.x + 2] = s3;
+  }
+  if (arrive_last(&ctrl->counter)) {
+    const double t1 = sum_partials(partial, gridDim.x, 3, 0, red);
+    const double t2 = sum_partials(partial, gridDim.x, 3, 1, red);
+    const double t3 = sum_partials(partial, gridDim.x, 3, 2, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      ctrl->rz = t1;
+      ctrl->rr = t2;
+      ctrl->rr_ref = t2;
+      ctrl->rr_true = t3;
+      ctrl->bb = t3;
+      ctrl->tol2bb = rtol2 * t3;
+      ctrl->iters = 0;
+      ctrl->replacements = 0;
+      ctrl->replace = 0;
+      if (!isfinite(t1) || !isfinite(t3)) ctrl->done = kDoneNonFinite;
+      else if (t3 == 0.0 || t2 <= ctrl->tol2bb) ctrl->done = kDoneConverged;
+      else ctrl->done = kDoneNo;
+    }
+  }
+}
+
+// Mixed precision: fold the FP32 correction into the FP64 solution.
+__global__ void k_fold(int64_t n, double* __restrict__ x64, float* __restrict__ xlo) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x64[i] += (double)xlo[i];
+  xlo[i] = 0.f;
+}
+
+// Mixed precision replacement: r = b - y (FP64), r_lo = (float) r, z = M r_lo,
+// new r.z / r.r; convergence is decided on the FP64 residual.
+template <int G>
+__global__ void __launch_bounds__(256)
+k_replace(int64_t n_groups, const double* __restrict__ b, const double* __restrict__ y,
+          float* __restrict__ rlo, float* __restrict__ z, const void* __restrict__ prec,
+          double* __restrict__ partial, Ctrl* ctrl) {
+  __shared__ double red[32];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rz = 0.0, rr = 0.0, r64 = 0.0;
+  if (i < n_groups) {
+    float rv[G], zv[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int64_t k = i * G + g;
+      const double rd = b[k] - y[k];
+      r64 += rd * rd;
+      rv[g] = (float)rd;
+      rlo[k] = rv[g];
+    }
+    apply_prec<G, float>(prec, i, rv, zv);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      z[i * G + g] = zv[g];
+      rz += (double)rv[g] * (double)zv[g];
+      rr += (double)rv[g] * (double)rv[g];
+    }
+  }
+  const double s1 = block_sum(rz, red);
+  const double s2 = block_sum(rr, red);
+  const double s3 = block_sum(r64, red);
+  if (threadIdx.x == 0) {
+    partial[3 * blockIdx.x] = s1;
+    partial[3 * blockIdx.x + 1] = s2;
+    partial[3 * blockIdx.x + 2] = s3;
+  }
+  if (arrive_last(&ctrl->counter)) {
+    const double t1 = sum_partials(partial, gridDim.x, 3, 0, red);
+    const double t2 = sum_partials(partial, gridDim.x, 3, 1, red);
+    const double t3 = sum_partials(partial, gridDim.x, 3, 2, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      ctrl->rr_true = t3;
+      ctrl->replacements += 1;
+      ctrl->replace = 0;
+      if (!isfinite(t3) || !isfinite(t1)) {
+        ctrl->done = kDoneNonFinite;
+      } else if (t3 <= ctrl->tol2bb) {
+        ctrl->done = kDoneConverged;
+      } else if (ctrl->done == kDoneNo) {
+        ctrl->rr = t2;
+        ctrl->rr_ref = t2;
+        ctrl->beta = t1 / ctrl->rz;
+        ctrl->rz = t1;
+      }
+    }
+  }
+}
+
+__global__ void k_copy_cast(int64_t n, const float* __restrict__ in, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+
+// ------------------------------------------------------------- host driver --
+constexpr int kThreads = 256;
+constexpr int kCsrTpr = 8;
+constexpr int kBsrTpb = 8;
+
+static int read_ctrl(Ctrl* d, Ctrl* h, cudaStream_t st) {
+  if (cudaMemcpyAsync(h, d, sizeof(Ctrl), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return check_cuda("read_ctrl");
+  if (cudaStreamSynchronize(st) != cudaSuccess) return check_cuda("read_ctrl sync");
+  return FEM_OK;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+static int64_t spmv_grid(const fem_matrix* A) {
+  if (A->format == FEM_FMT_CSR_F64) return grid_for(A->n_rows * kCsrTpr, kThreads);
+  return grid_for(A->n_rows * kBsrTpb, kThreads);
+}
+
+static int64_t max_grid(const fem_matrix* A) {
+  return std::max<int64_t>(spmv_grid(A), grid_for(A->n, kThreads));
+}
+
+static int status_of(int done) {
+  switch (done) {
+    case kDoneConverged: return FEM_OK;
+    case kDoneMaxIter: return FEM_NOT_CONVERGED;
+    case kDoneNonFinite: return FEM_NONFINITE;
+    case kDoneBreakdown: return FEM_BREAKDOWN;
+    default: return FEM_NOT_CONVERGED;
+  }
+}
+
+static int validate_matrix(const fem_matrix* A) {
+  if (!A || A->n <= 0) {
+    set_last_error("fem_pcg: empty matrix");
+    return FEM_INVALID;
+  }
+  if (A->format == FEM_FMT_CSR_F64) {
+    if (A->block != 1 || A->n_rows != A->n) {
+      set_last_error("fem_pcg: CSR needs block 1 and n_rows == n");
+      return FEM_INVALID;
+    }
+  } else if (A->format == FEM_FMT_BSR_F32) {
+    if (A->block < 2 || A->block > 3 || A->n_rows * A->block != A->n) {
+      set_last_error("fem_pcg: BSR needs block 2 or 3 and n_rows * block == n");
+      return FEM_INVALID;
+    }
+  } else {
+    set_last_error("fem_pcg: unknown matrix format %d", A->format);
+    return FEM_INVALID;
+  }
+  return FEM_OK;
+}
+
+// Optional CUDA-event timing of the SpMV launches (fem_set_timing).
+constexpr int kMaxChunk = 64;
+static int g_timing = 0;
+
+struct SpmvTimer {
+  cudaEvent_t ev[2 * kMaxChunk];
+  bool ready = false;
+  double ms = 0.0;
+  long long timed = 0;
+  int init() {
+    if (ready) return FEM_OK;
+    for (int i = 0; i < 2 * kMaxChunk; ++i)
+      if (cudaEventCreate(&ev[i]) != cudaSuccess) return check_cuda("event create");
+    ready = true;
+    return FEM_OK;
+  }
+  // Sums the durations of the first `active` SpMV launches of a chunk.
+  void collect(int active) {
+    for (int c = 0; c < active && c < kMaxChunk; ++c) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, ev[2 * c], ev[2 * c + 1]) == cudaSuccess) {
+        ms += t;
+        timed += 1;
+      }
+    }
+  }
+  ~SpmvTimer() {
+    if (ready)
+      for (int i = 0; i < 2 * kMaxChunk; ++i) cudaEventDestroy(ev[i]);
+  }
+};
+
+static thread_local SpmvTimer g_timer;
+
+// One CG iteration (SpMV, update, direction) on the working precision;
+// slot >= 0 brackets the SpMV with the timer's events.
+template <int G, typename VT>
+static void launch_iteration(const fem_matrix* A, VT* x, VT* r, VT* z, VT* p, VT* q, double* partial,
+                             Ctrl* ctrl, cudaStream_t st, int slot = -1) {
+  if (slot >= 0) cudaEventRecord(g_timer.ev[2 * slot], st);
+  if constexpr (G == 1) {
+    k_spmv_csr<kCsrTpr><<<grid_for(A->n_rows * kCsrTpr, kThreads), kThreads, 0, st>>>(
+        A->n_rows, A->row_ptr, A->col, (const double*)A->val, (const double*)p, (double*)q,
+        partial, ctrl);
+  } else {
+    k_spmv_bsr<G, kBsrTpb><<<grid_for(A->n_rows * kBsrTpb, kThreads), kThreads, 0, st>>>(
+        A->n_rows, A->row_ptr, A->col, (const float*)A->val, (const float*)p, (float*)q, partial,
+        ctrl);
+  }
+  ::tfg::note_launch();
+  if (slot >= 0) cudaEventRecord(g_timer.ev[2 * slot + 1], st);
+  const int64_t ng = A->n / G;
+  k_update<G, VT><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, x, r, p, q, z, A->precond,
+                                                               partial, ctrl);
+  ::tfg::note_launch();
+  k_pupdate<VT><<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, z, p, ctrl);
+  ::tfg::note_launch();
+}
+
+struct Vecs {
+  Ctrl* ctrl;
+  void *x, *r, *z, *p, *q;
+  double* partial;
+  double* y64;
+  double* fe;
+  void* gather_ws;
+};
+
+static size_t layout(const fem_matrix* A, int64_t fe_len, Vecs* v, void* ws) {
+  const size_t vt = (A->format == FEM_FMT_CSR_F64) ? sizeof(double) : sizeof(float);
+  const int64_t n = A->n;
+  char* base = reinterpret_cast<char*>(ws);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* ptr = base ? base + off : nullptr;
+    off += align256(bytes);
+    return ptr;
+  };
+  Vecs t;
+  t.ctrl = reinterpret_cast<Ctrl*>(take(sizeof(Ctrl)));
+  t.x = take(n * vt);
+  t.r = take(n * vt);
+  t.z = take(n * vt);
+  t.p = take(n * vt);
+  t.q = take(n * vt);
+  t.partial = reinterpret_cast<double*>(take(sizeof(double) * 3 * (max_grid(A) + 1)));
+  t.y64 = fe_len > 0 ? reinterpret_cast<double*>(take(sizeof(double) * n)) : nullptr;
+  t.fe = fe_len > 0 ? reinterpret_cast<double*>(take(sizeof(double) * fe_len)) : nullptr;
+  t.gather_ws = nullptr;
+  if (v) *v = t;
+  return off;
+}
+
+template <int G, typename VT>
+static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter,
+                   const Vecs& v, fem_solve_info* info, cudaStream_t st) {
+  Ctrl h;
+  memset(&h, 0, sizeof(h));
+  h.max_iter = max_iter;
+  h.mixed = 0;
+  if (cudaMemcpyAsync(v.ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return check_cuda("fem_pcg ctrl");
+  VT* xv = (G == 1) ? reinterpret_cast<VT*>(x) : reinterpret_cast<VT*>(v.x);
+  const int64_t ng = A->n / G;
+  k_init<G, VT><<<grid_for(ng, kThreads), kThreads, 0, st>>>(
+      ng, b, xv, (VT*)v.r, (VT*)v.z, (VT*)v.p, A->precond, v.partial, v.ctrl, rtol * rtol);
+      ::tfg::note_launch();
+  TFG_CHECK_LAUNCH("fem_pcg init");
+  int rc = read_ctrl(v.ctrl, &h, st);
+  if (rc) return rc;
+  const bool timing = g_timing && g_timer.init() == FEM_OK;
+  g_timer.ms = 0.0;
+  g_timer.timed = 0;
+  int chunk = 8;
+  while (h.done == kDoneNo) {
+    const long long before = h.iters;
+    for (int c = 0; c < chunk; ++c)
+      launch_iteration<G, VT>(A, xv, (VT*)v.r, (VT*)v.z, (VT*)v.p, (VT*)v.q, v.partial, v.ctrl, st,
+                              timing ? c : -1);
+    TFG_CHECK_LAUNCH("fem_pcg iterate");
+    rc = read_ctrl(v.ctrl, &h, st);
+    if (rc) return rc;
+    if (timing) g_timer.collect((int)(h.iters - before));
+    chunk = std::min(chunk * 2, kMaxChunk);
+  }
+  if (G != 1) k_copy_cast<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, (const float*)v.x, x);
+  ::tfg::note_launch();
+  TFG_CHECK_LAUNCH("fem_pcg finish");
+  if (info) {
+    info->iterations = h.iters;
+    info->replacements = 0;
+    info->rel_residual = h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0;
+    info->status = status_of(h.done);
+    info->spmv_ms = g_timer.ms;
+    info->spmv_timed = g_timer.timed;
+  }
+  if (h.done != kDoneConverged)
+    set_last_error("CG did not converge: %lld iterations, relative residual %.3e, code %d", h.iters,
+                   h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0, h.done);
+  return status_of(h.done);
+}
+
+}  // namespace tfg
+
+using namespace tfg;
+
+extern "C" {
+
+void fem_set_timing(int enable) { g_timing = enable; }
+
+int fem_assemble_csr(const fem_blocks* B, int ke_dtype, const void* ke, const int64_t* row_ptr,
+                     const uint8_t* con_mask, double* val, void* stream) {
+  cudaStream_t st = as_stream(stream);
+  if (B->dim < 1 || B->dim > 3) {
+    set_last_error("fem_assemble_csr: dim must be 1..3");
+    return FEM_INVALID;
+  }
+  if (B->n_blocks == 0) return FEM_OK;
+  const unsigned g = grid_for(B->n_blocks, 128);
+  if (ke_dtype == FEM_F64)
+    k_assemble<double, double, false><<<g, 128, 0, st>>>(
+        B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
+        B->inc_ptr, (const double*)ke, row_ptr, con_mask, val, nullptr);
+  else
+    k_assemble<float, double, false><<<g, 128, 0, st>>>(
+        B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
+        B->inc_ptr, (const float*)ke, row_ptr, con_mask, val, nullptr);
+        ::tfg::note_launch();
+  return check_cuda("fem_assemble_csr");
+}
+
+int fem_assemble_bsr(const fem_blocks* B, int ke_dtype, const void* ke, const uint8_t* con_mask,
+                     float* bval, void* stream) {
+  cudaStream_t st = as_stream(stream);
+  if (B->dim < 1 || B->dim > 3) {
+    set_last_error("fem_assemble_bsr: dim must be 1..3");
+    return FEM_INVALID;
+  }
+  if (B->n_blocks == 0) return FEM_OK;
+  const unsigned g = grid_for(B->n_blocks, 128);
+  if (ke_dtype == FEM_F64)
+    k_assemble<double, double, true><<<g, 128, 0, st>>>(
+        B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
+        B->inc_ptr, (const double*)ke, nullptr, con_mask, nullptr, bval);
+  else
+    k_assemble<float, float, true><<<g, 128, 0, st>>>(
+        B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
+        B->inc_ptr, (const float*)ke, nullptr, con_mask, nullptr, bval);
+        ::tfg::note_launch();
+  return check_cuda("fem_assemble_bsr");
+}
+
+int fem_jacobi(const double* val, const int64_t* diag_map, int64_t n, double* inv_diag,
+               int32_t* status, void* stream) {
+  cudaStream_t st = as_stream(stream);
+  k_jacobi<<<grid_for(n, kThreads), kThreads, 0, st>>>(val, diag_map, n, inv_diag, status);
+  ::tfg::note_launch();
+  return check_cuda("fem_jacobi");
+}
+
+int fem_block_jacobi(const fem_blocks* B, const float* bval, float* inv_blocks, int32_t* status,
+                     void* stream) {
+  cudaStream_t st = as_stream(stream);
+  k_block_jacobi<<<grid_for(B->n_nod, kThreads), kThreads, 0, st>>>(bval, B->diag_blk, B->n_nod,
+                                                                    B->dim, inv_blocks, status);
+                                                                    ::tfg::note_launch();
+  return check_cuda("fem_block_jacobi");
+}
+
+size_t fem_pcg_workspace_bytes(const fem_matrix* A) {
+  if (validate_matrix(A) != FEM_OK) return 0;
+  return layout(A, 0, nullptr, nullptr);
+}
+
+int fem_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter, void* ws,
+            size_t ws_bytes, fem_solve_info* info, void* stream) {
+  int rc = validate_matrix(A);
+  if (rc) return rc;
+  if (ws_bytes < fem_pcg_workspace_bytes(A)) {
+    set_last_error("fem_pcg: workspace too small");
+    return FEM_INVALID;
+  }
+  cudaStream_t st = as_stream(stream);
+  Vecs v;
+  layout(A, 0, &v, ws);
+  if (A->format == FEM_FMT_CSR_F64) return run_pcg<1, double>(A, b, x, rtol, max_iter, v, info, st);
+  if (A->block == 2) return run_pcg<2, float>(A, b, x, rtol, max_iter, v, info, st);
+  return run_pcg<3, float>(A, b, x, rtol, max_iter, v, info, st);
+}
+
+static int64_t op_fe_len(const fem_operator64* op) {
+  int ne, d, nip;
+  if (etype_info(op->mesh->etype, &ne, &d, &nip) != FEM_OK) return -1;
+  return op->mesh->n_elem * ne * d;
+}
+
+size_t fem_apply64_workspace_bytes(const fem_operator64* op) {
+  const int64_t fl = op_fe_len(op);
+  if (fl < 0) return 0;
+  return align256(sizeof(double) * (fl > 0 ? fl : 1));
+}
+
+int fem_apply64(const fem_operator64* op, const double* x, double* y, void* ws, size_t ws_bytes,
+                void* stream) {
+  if (ws_bytes < fem_apply64_workspace_bytes(op)) {
+    set_last_error("fem_apply64: workspace too small");
+    return FEM_INVALID;
+  }
+  double* fe = reinterpret_cast<double*>(ws);
+  int rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, fe,
+                             nullptr, nullptr, nullptr, stream);
+  if (rc) return rc;
+  return fem_gather_nodal(op->mesh, fe, nullptr, op->con_mask, 2, x, y, nullptr, nullptr, 0, stream);
+}
+
+size_t fem_pcg_mixed_workspace_bytes(const fem_matrix* A32, const fem_operator64* op) {
+  if (validate_matrix(A32) != FEM_OK || A32->format != FEM_FMT_BSR_F32) return 0;
+  const int64_t fl = op_fe_len(op);
+  if (fl < 0) return 0;
+  return layout(A32, fl > 0 ? fl : 1, nullptr, nullptr);
+}
+
+int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b, double* x,
+                  double rtol, double delta, int64_t max_iter, void* ws, size_t ws_bytes,
+                  fem_solve_info* info, void* stream) {
+  int rc = validate_matrix(A);
+  if (rc) return rc;
+  if (A->format != FEM_FMT_BSR_F32) {
+    set_last_error("fem_pcg_mixed: needs an FP32 BSR matrix");
+    return FEM_INVALID;
+  }
+  const size_t need = fem_pcg_mixed_workspace_bytes(A, op);
+  if (need == 0 || ws_bytes < need) {
+    set_last_error("fem_pcg_mixed: workspace too small");
+    return FEM_INVALID;
+  }
+  cudaStream_t st = as_stream(stream);
+  Vecs v;
+  layout(A, op_fe_len(op), &v, ws);
+  Ctrl h;
+  memset(&h, 0, sizeof(h));
+  h.max_iter = max_iter;
+  h.mixed = 1;
+  h.delta2 = delta * delta;
+  if (cudaMemcpyAsync(v.ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return check_cuda("fem_pcg_mixed ctrl");
+  const int G = A->block;
+  const int64_t ng = A->n / G;
+  float *xl = (float*)v.x, *r = (float*)v.r, *z = (float*)v.z, *p = (float*)v.p, *q = (float*)v.q;
+  cudaMemsetAsync(x, 0, sizeof(double) * A->n, st);
+  if (G == 2)
+    k_init<2, float><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, b, xl, r, z, p, A->precond,
+                                                                  v.partial, v.ctrl, rtol * rtol);
+  else
+    k_init<3, float><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, b, xl, r, z, p, A->precond,
+                                                                  v.partial, v.ctrl, rtol * rtol);
+                                                                  ::tfg::note_launch();
+  TFG_CHECK_LAUNCH("fem_pcg_mixed init");
+  rc = read_ctrl(v.ctrl, &h, st);
+  if (rc) return rc;
+  const bool timing = g_timing && g_timer.init() == FEM_OK;
+  g_timer.ms = 0.0;
+  g_timer.timed = 0;
+  int chunk = 8;
+  while (h.done == kDoneNo) {
+    if (h.replace) {
+      // FP64 reliable update: x += x_lo; r = b - A x (matrix-free FP64).
+      k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl);
+      ::tfg::note_launch();
+      rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, v.fe,
+                             nullptr, nullptr, nullptr, stream);
+      if (rc) return rc;
+      rc = fem_gather_nodal(op->mesh, v.fe, nullptr, op->con_mask, 2, x, v.y64, nullptr, nullptr, 0,
+                            stream);
+      if (rc) return rc;
+      if (G == 2)
+        k_replace<2><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, b, v.y64, r, z, A->precond,
+                                                                  v.partial, v.ctrl);
+      else
+        k_replace<3><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, b, v.y64, r, z, A->precond,
+                                                                  v.partial, v.ctrl);
+                                                                  ::tfg::note_launch();
+      k_pupdate<float><<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, z, p, v.ctrl);
+      ::tfg::note_launch();
+      TFG_CHECK_LAUNCH("fem_pcg_mixed replace");
+      rc = read_ctrl(v.ctrl, &h, st);
+      if (rc) return rc;
+      continue;
+    }
+    const long long before = h.iters;
+    for (int c = 0; c < chunk; ++c) {
+      if (G == 2) launch_iteration<2, float>(A, xl, r, z, p, q, v.partial, v.ctrl, st, timing ? c : -1);
+      else launch_iteration<3, float>(A, xl, r, z, p, q, v.partial, v.ctrl, st, timing ? c : -1);
+    }
+    TFG_CHECK_LAUNCH("fem_pcg_mixed iterate");
+    rc = read_ctrl(v.ctrl, &h, st);
+    if (rc) return rc;
+    if (timing) g_timer.collect((int)(h.iters - before));
+    chunk = std::min(chunk * 2, kMaxChunk);
+  }
+  // fold whatever correction is left (max-iter exit) into x
+  k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl);
+  ::tfg::note_launch();
+  TFG_CHECK_LAUNCH("fem_pcg_mixed finish");
+  rc = read_ctrl(v.ctrl, &h, st);
+  if (rc) return rc;
+  if (info) {
+    info->iterations = h.iters;
+    info->replacements = h.replacements;
+    info->rel_residual = h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0;
+    info->status = status_of(h.done);
+    info->spmv_ms = g_timer.ms;
+    info->spmv_timed = g_timer.timed;
+  }
+  if (h.done != kDoneConverged)
+    set_last_error("mixed CG did not converge: %lld iterations, relative residual %.3e, code %d",
+                   h.iters, h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0, h.done);
+  return status_of(h.done);
+}
+
+}  // extern "C"

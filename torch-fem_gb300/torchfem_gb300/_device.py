@@ -1,0 +1,375 @@
+"""Device-resident state of one finite-element mesh and the C-ABI calls on it.
+
+`DeviceMesh` owns everything the kernels need in HBM for a mesh: the
+connectivity (int32), the node graph and CSR pattern (FEM.__init__,
+src/torchfem/base.py:72-122), the block contributor lists of the
+atomic-free assembly, and the geometry cache (shape-function gradients and
+Jacobian determinants at every integration point, base.py:293-314), which
+the reference recomputes on every integration pass.  All buffers are torch
+tensors; the library only borrows their pointers.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import torch
+from torch import Tensor
+
+from . import _lib
+from ._lib import check, ptr
+
+
+def _i(x) -> int:
+    return int(x)
+
+
+@dataclass
+class SolveStats:
+    """Iteration record of the last linear solve."""
+
+    iterations: int = 0
+    replacements: int = 0
+    rel_residual: float = 0.0
+    spmv_ms: float = 0.0
+    spmv_timed: int = 0
+
+
+class LinearSystem:
+    """Assembled, condensed stiffness matrix plus preconditioner on the device.
+
+    precision "fp64": scalar CSR in the reference pattern, FP64 values,
+    Jacobi preconditioner (the CuPy branch of sparse.py:406-421).
+    precision "mixed": FP32 block-CSR over the node graph, FP32 block-Jacobi,
+    with FP64 matrix-free residual replacement.
+    """
+
+    def __init__(self, dm: "DeviceMesh", precision: str):
+        self.dm = dm
+        self.precision = precision
+        self.val: Tensor | None = None
+        self.bval: Tensor | None = None
+        self.precond: Tensor | None = None
+        self.matrix = _lib.FemMatrix()
+        self.ws: Tensor | None = None
+        self.stats = SolveStats()
+        self._op_refs = None
+
+
+class DeviceMesh:
+    """Pattern, geometry and kernels for one mesh on one CUDA device."""
+
+    def __init__(self, nodes: Tensor, elements: Tensor, etype, dof_per_node: int):
+        self.device = _lib.require_cuda()
+        self.lib = _lib.load()
+        self.etype = etype
+        self.n_e = etype.nodes
+        self.dim = nodes.shape[1]
+        self.d = dof_per_node
+        if self.d != self.dim:
+            raise NotImplementedError("only mechanics with one DOF per spatial dimension")
+        self.n_nod = nodes.shape[0]
+        self.n_elem = elements.shape[0]
+        self.n_dofs = self.n_nod * self.d
+        dev = self.device
+        self.nodes = nodes.detach().to(dev, torch.float64).contiguous()
+        self.elements = elements.detach().to(dev, torch.int32).contiguous()
+        table = etype.gradient_table()
+        self.nip = table.shape[0]
+        self.dndxi = table.to(dev).contiguous()
+        self.weights = etype.iweights().to(dev, torch.float64).contiguous()
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._build_pattern()
+        self._build_geometry()
+
+    # ------------------------------------------------------------ plumbing --
+    @property
+    def stream(self) -> int:
+        return _lib.stream_handle(self.device)
+
+    def _empty(self, n, dtype) -> Tensor:
+        return torch.empty(int(n), dtype=dtype, device=self.device)
+
+    def _ws(self, nbytes: int) -> Tensor:
+        return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=self.device)
+
+    def check_status(self, what: str) -> None:
+        """Reads the device status word (synchronises) and raises on a flag."""
+        s = int(self.status.item())
+        if s == 0:
+            return
+        self.status.zero_()
+        if s & (1 << _lib.FEM_BAD_JACOBIAN):
+            raise ValueError("Negative Jacobian. Check element numbering.")
+        if s & (1 << _lib.FEM_BOUNDS):
+            raise _lib.FemError(_lib.FEM_BOUNDS, f"{what}: index or size limit exceeded")
+        if s & (1 << _lib.FEM_NONFINITE):
+            raise _lib.FemError(_lib.FEM_NONFINITE, f"{what}: non-finite value")
+        raise _lib.FemError(s, f"{what}: device status {s:#x}")
+
+    # ------------------------------------------------------------- pattern --
+    def _build_pattern(self) -> None:
+        L, st = self.lib, self.stream
+        n_nod, n_elem, n_e = self.n_nod, self.n_elem, self.n_e
+        ws = self._ws(L.fem_pattern_workspace_bytes(n_nod, n_elem, n_e))
+        self.inc_ptr = self._empty(n_nod + 1, torch.int64)
+        self.inc = self._empty(max(n_elem * n_e, 1), torch.int32)
+        self.nbr_ptr = self._empty(n_nod + 1, torch.int64)
+        nb = C.c_int64(0)
+        check(
+            L.fem_pattern_graph_count(
+                ptr(self.elements), n_elem, n_e, n_nod, ptr(self.inc_ptr), ptr(self.inc),
+                ptr(self.nbr_ptr), C.byref(nb), ptr(ws), ws.numel(), ptr(self.status), st,
+            ),
+            "fem_pattern_graph_count",
+        )
+        self.check_status("pattern")
+        self.n_blocks = nb.value
+        self.nbr = self._empty(self.n_blocks, torch.int32)
+        check(
+            L.fem_pattern_graph_fill(
+                ptr(self.elements), n_elem, n_e, n_nod, ptr(self.inc_ptr), ptr(self.inc),
+                ptr(self.nbr_ptr), ptr(self.nbr), ptr(self.status), st,
+            ),
+            "fem_pattern_graph_fill",
+        )
+        self.row_ptr = self._empty(self.n_dofs + 1, torch.int64)
+        nnz = C.c_int64(0)
+        check(
+            L.fem_pattern_csr_rows(
+                ptr(self.nbr_ptr), n_nod, self.d, ptr(self.inc_ptr), ptr(self.row_ptr),
+                C.byref(nnz), ptr(ws), ws.numel(), st,
+            ),
+            "fem_pattern_csr_rows",
+        )
+        self.nnz = nnz.value
+        self.col = self._empty(self.nnz, torch.int32)
+        self.diag_map = self._empty(self.n_dofs, torch.int64)
+        check(
+            L.fem_pattern_csr_cols(
+                ptr(self.nbr_ptr), ptr(self.nbr), n_nod, self.d, ptr(self.inc_ptr),
+                ptr(self.row_ptr), ptr(self.col), ptr(self.diag_map), st,
+            ),
+            "fem_pattern_csr_cols",
+        )
+        self.blk_ptr = self._empty(self.n_blocks + 1, torch.int64)
+        self.contrib = self._empty(max(n_elem * n_e * n_e, 1), torch.int32)
+        self.blk_row = self._empty(self.n_blocks, torch.int32)
+        self.diag_blk = self._empty(n_nod, torch.int64)
+        check(
+            L.fem_pattern_blocks(
+                ptr(self.elements), n_elem, n_e, n_nod, ptr(self.inc_ptr), ptr(self.inc),
+                ptr(self.nbr_ptr), ptr(self.nbr), self.n_blocks, ptr(self.blk_ptr),
+                ptr(self.contrib), ptr(self.blk_row), ptr(self.diag_blk), ptr(ws), ws.numel(),
+                ptr(self.status), st,
+            ),
+            "fem_pattern_blocks",
+        )
+        self.check_status("pattern")
+        del ws
+        self.blocks = _lib.FemBlocks(
+            n_e, self.d, n_nod, self.n_blocks, ptr(self.nbr_ptr), ptr(self.nbr), ptr(self.blk_ptr),
+            ptr(self.contrib), ptr(self.blk_row), ptr(self.diag_blk), ptr(self.inc_ptr),
+        )
+
+    def kmap(self) -> Tensor:
+        """The reference's k_map (int64 here) for parity checks."""
+        out = self._empty(self.n_elem * (self.n_e * self.d) ** 2, torch.int64)
+        check(
+            self.lib.fem_pattern_kmap(
+                ptr(self.elements), self.n_elem, self.n_e, self.d, ptr(self.nbr_ptr), ptr(self.nbr),
+                ptr(self.row_ptr), ptr(out), ptr(self.status), self.stream,
+            ),
+            "fem_pattern_kmap",
+        )
+        self.check_status("kmap")
+        return out
+
+    def glob_idx(self) -> Tensor:
+        """[2, nnz] (row, col) of the CSR pattern, int64 (base.py:112-117)."""
+        rows = torch.repeat_interleave(
+            torch.arange(self.n_dofs, device=self.device), self.row_ptr.diff()
+        )
+        return torch.stack([rows, self.col.to(torch.int64)])
+
+    # ------------------------------------------------------------ geometry --
+    def _build_geometry(self) -> None:
+        self.bt = self._empty(self.nip * self.n_elem * self.n_e * self.dim, torch.float64)
+        self.detj = self._empty(self.nip * self.n_elem, torch.float64)
+        self.mesh = self.make_mesh(None)
+        check(
+            self.lib.fem_geometry(
+                C.byref(self.mesh), ptr(self.dndxi), ptr(self.bt), ptr(self.detj), ptr(self.status),
+                self.stream,
+            ),
+            "fem_geometry",
+        )
+        self.check_status("geometry")
+        self.mesh = self.make_mesh(None)
+
+    def make_mesh(self, thickness: Tensor | None) -> _lib.FemMesh:
+        return _lib.FemMesh(
+            self.etype.etype_id, self.n_nod, self.n_elem, ptr(self.nodes), ptr(self.elements),
+            ptr(self.weights), ptr(getattr(self, "bt", None)), ptr(getattr(self, "detj", None)),
+            ptr(self.inc_ptr), ptr(self.inc), ptr(thickness),
+        )
+
+    # ------------------------------------------------------------ elements --
+    def element_stiffness(self, mesh, mat, dtype=torch.float64) -> Tensor:
+        nd = self.n_e * self.d
+        ke = self._empty(self.n_elem * nd * nd, dtype)
+        code = _lib.FEM_F64 if dtype == torch.float64 else _lib.FEM_F32
+        check(
+            self.lib.fem_element_stiffness(
+                C.byref(mesh), C.byref(mat), code, ptr(ke), ptr(self.status), self.stream
+            ),
+            "fem_element_stiffness",
+        )
+        return ke.view(self.n_elem, nd, nd)
+
+    def element_force(self, mesh, mat, v, con_mask=None, con_values=None, con_mode=0,
+                      sigma_prev=None, de0=None, want_flux=False, want_h=False):
+        fe = self._empty(self.n_elem * self.n_e * self.d, torch.float64)
+        flux = self._empty(self.nip * self.n_elem * self.d * self.d, torch.float64) if want_flux else None
+        hg = self._empty(self.nip * self.n_elem * self.d * self.d, torch.float64) if want_h else None
+        check(
+            self.lib.fem_element_force(
+                C.byref(mesh), C.byref(mat), ptr(v), ptr(con_mask), ptr(con_values), con_mode,
+                ptr(sigma_prev), ptr(de0), ptr(fe), ptr(flux), ptr(hg), ptr(self.status), self.stream,
+            ),
+            "fem_element_force",
+        )
+        return fe, flux, hg
+
+    def gather(self, fe, sub=None, con_mask=None, con_mode=0, con_src=None, want_norm=False):
+        out = self._empty(self.n_dofs, torch.float64)
+        sumsq = None
+        ws = None
+        if want_norm:
+            sumsq = self._empty(1, torch.float64)
+            ws = self._ws(self.lib.fem_gather_workspace_bytes(self.n_dofs))
+        check(
+            self.lib.fem_gather_nodal(
+                C.byref(self.mesh), ptr(fe), ptr(sub), ptr(con_mask), con_mode, ptr(con_src),
+                ptr(out), ptr(sumsq), ptr(ws), 0 if ws is None else ws.numel(), self.stream,
+            ),
+            "fem_gather_nodal",
+        )
+        return out, sumsq
+
+    def vjp(self, mesh, mat, v, g, con_mask=None, con_values=None, con_mode=0, sigma_prev=None,
+            de0=None, gflux=None, gh=None, want_sig=False, want_mat=False, want_thick=False,
+            want_de0=False, want_v=False, mat_numel=0):
+        n_ip_e = self.nip * self.n_elem * self.d * self.d
+        gsig = self._empty(n_ip_e, torch.float64) if want_sig else None
+        gmat = self._empty(mat_numel, torch.float64) if want_mat else None
+        gthick = self._empty(self.n_elem, torch.float64) if want_thick else None
+        gde0 = self._empty(self.n_elem * self.d * self.d, torch.float64) if want_de0 else None
+        gve = self._empty(self.n_elem * self.n_e * self.d, torch.float64) if want_v else None
+        check(
+            self.lib.fem_element_vjp(
+                C.byref(mesh), C.byref(mat), ptr(v), ptr(con_mask), ptr(con_values), con_mode,
+                ptr(sigma_prev), ptr(de0), ptr(g), ptr(gflux), ptr(gh), ptr(gsig), ptr(gmat),
+                ptr(gthick), ptr(gde0), ptr(gve), ptr(self.status), self.stream,
+            ),
+            "fem_element_vjp",
+        )
+        gv = None
+        if want_v:
+            gv, _ = self.gather(gve)
+        return gsig, gmat, gthick, gde0, gv
+
+    # ------------------------------------------------------------ assembly --
+    def assemble_csr(self, ke: Tensor, con_mask: Tensor) -> Tensor:
+        val = self._empty(self.nnz, torch.float64)
+        code = _lib.FEM_F64 if ke.dtype == torch.float64 else _lib.FEM_F32
+        check(
+            self.lib.fem_assemble_csr(
+                C.byref(self.blocks), code, ptr(ke), ptr(self.row_ptr), ptr(con_mask), ptr(val),
+                self.stream,
+            ),
+            "fem_assemble_csr",
+        )
+        return val
+
+    def assemble_bsr(self, ke: Tensor, con_mask: Tensor) -> Tensor:
+        bval = self._empty(self.n_blocks * self.d * self.d, torch.float32)
+        code = _lib.FEM_F64 if ke.dtype == torch.float64 else _lib.FEM_F32
+        check(
+            self.lib.fem_assemble_bsr(
+                C.byref(self.blocks), code, ptr(ke), ptr(con_mask), ptr(bval), self.stream
+            ),
+            "fem_assemble_bsr",
+        )
+        return bval
+
+    def build_system(self, mesh, mat, con_mask: Tensor, precision: str, keep_refs=()) -> LinearSystem:
+        """Element stiffness, assembly and preconditioner for one tangent."""
+        sysm = LinearSystem(self, precision)
+        L, st = self.lib, self.stream
+        if precision == "fp64":
+            ke = self.element_stiffness(mesh, mat, torch.float64)
+            sysm.val = self.assemble_csr(ke, con_mask)
+            del ke
+            sysm.precond = self._empty(self.n_dofs, torch.float64)
+            check(
+                L.fem_jacobi(ptr(sysm.val), ptr(self.diag_map), self.n_dofs, ptr(sysm.precond),
+                             ptr(self.status), st),
+                "fem_jacobi",
+            )
+            sysm.matrix = _lib.FemMatrix(
+                _lib.FEM_FMT_CSR_F64, 1, self.n_dofs, self.n_dofs, ptr(self.row_ptr), ptr(self.col),
+                ptr(sysm.val), ptr(sysm.precond),
+            )
+            ws_bytes = L.fem_pcg_workspace_bytes(C.byref(sysm.matrix))
+        elif precision == "mixed":
+            ke = self.element_stiffness(mesh, mat, torch.float32)
+            sysm.bval = self.assemble_bsr(ke, con_mask)
+            del ke
+            sysm.precond = self._empty(self.n_nod * self.d * self.d, torch.float32)
+            check(
+                L.fem_block_jacobi(C.byref(self.blocks), ptr(sysm.bval), ptr(sysm.precond),
+                                   ptr(self.status), st),
+                "fem_block_jacobi",
+            )
+            sysm.matrix = _lib.FemMatrix(
+                _lib.FEM_FMT_BSR_F32, self.d, self.n_dofs, self.n_nod, ptr(self.nbr_ptr),
+                ptr(self.nbr), ptr(sysm.bval), ptr(sysm.precond),
+            )
+            sysm.op_mesh = mesh
+            sysm.op_mat = mat
+            sysm.op = _lib.FemOperator64(C.pointer(mesh), C.pointer(mat), ptr(con_mask))
+            ws_bytes = L.fem_pcg_mixed_workspace_bytes(C.byref(sysm.matrix), C.byref(sysm.op))
+        else:
+            raise ValueError(f"unknown precision {precision!r}")
+        sysm.con_mask = con_mask
+        sysm._op_refs = keep_refs
+        sysm.ws = self._ws(ws_bytes)
+        self.check_status("assembly")
+        return sysm
+
+    def solve(self, sysm: LinearSystem, b: Tensor, rtol: float, max_iter: int | None = None,
+              delta: float = 0.1) -> Tensor:
+        """x with A x = b (A the condensed system), from x = 0."""
+        x = self._empty(self.n_dofs, torch.float64)
+        info = _lib.FemSolveInfo()
+        if max_iter is None:
+            max_iter = 10 * self.n_dofs
+        b = b.contiguous()
+        if sysm.precision == "fp64":
+            rc = self.lib.fem_pcg(
+                C.byref(sysm.matrix), ptr(b), ptr(x), rtol, max_iter, ptr(sysm.ws), sysm.ws.numel(),
+                C.byref(info), self.stream,
+            )
+        else:
+            rc = self.lib.fem_pcg_mixed(
+                C.byref(sysm.matrix), C.byref(sysm.op), ptr(b), ptr(x), rtol, delta, max_iter,
+                ptr(sysm.ws), sysm.ws.numel(), C.byref(info), self.stream,
+            )
+        sysm.stats = SolveStats(info.iterations, info.replacements, info.rel_residual, info.spmv_ms,
+                                info.spmv_timed)
+        if rc == _lib.FEM_NOT_CONVERGED:
+            raise RuntimeError(f"CG failed with exit code {info.iterations}")
+        check(rc, "linear solve")
+        return x

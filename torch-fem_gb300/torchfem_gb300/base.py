@@ -1,0 +1,339 @@
+"""Finite-element model base classes with the reference's API
+(src/torchfem/base.py:23-1092): constructor, load/BC attributes with the same
+validation, and `solve(...)` with the reference signature.  The compute
+behind `solve` runs on the GPU through the C ABI; there is no CPU path.
+"""
+
+from __future__ import annotations
+
+import math
+from collections.abc import Iterable
+
+import torch
+from torch import Tensor
+
+from . import _lib
+from ._device import DeviceMesh
+from .elements import Element
+from .materials import Material
+from .sparse import IntegrateMaterial, NewtonLinear, SolveContext
+
+_REFERENCE_METHODS = ("spsolve", "minres", "cg", "pardiso", "amgx")
+_GPU_METHODS = {None: "fp64", "cg": "fp64", "gb300": "fp64", "gb300-mixed": "mixed"}
+
+
+def resolve_precision(method: str | None, precision: str | None) -> str:
+    """Maps `method` / `precision` to the solver variant.
+
+    "cg" (and None) is the Jacobi-preconditioned CG of the reference's CUDA
+    branch in FP64; "gb300-mixed" or precision="mixed" selects FP32 storage
+    and CG inside FP64 residual replacement.  The reference's direct and
+    third-party backends are not part of this library.
+    """
+    if method is not None and method not in _REFERENCE_METHODS and method not in _GPU_METHODS:
+        raise ValueError(
+            f"Method {method} is not supported. Choose from 'cg', 'gb300' or 'gb300-mixed'."
+        )
+    if method in ("spsolve", "minres", "pardiso", "amgx"):
+        raise RuntimeError(
+            f"Method '{method}' is a CPU/third-party backend of torch-fem; torchfem_gb300 "
+            "solves with its own GPU CG ('cg', 'gb300', 'gb300-mixed')."
+        )
+    p = _GPU_METHODS[method]
+    if precision is not None:
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        p = precision
+    return p
+
+
+class FEM:
+    """Abstract finite-element model (base.py:23-132)."""
+
+    etype: type[Element]
+
+    def __init__(self, nodes: Tensor, elements: Tensor, material: Material | None):
+        self.nodes = nodes
+        self.elements = elements
+        self.n_dofs = self.n_dof_per_node * nodes.shape[0]
+        self.n_nod = nodes.shape[0]
+        self.n_dim = nodes.shape[1]
+        self.n_elem = len(self.elements)
+        self.n_int = len(self.etype.iweights())
+        dev, dt = nodes.device, nodes.dtype
+        self._neumann = torch.zeros(self.n_nod, self.n_dof_per_node, dtype=dt, device=dev)
+        self._dirichlet = torch.zeros(self.n_nod, self.n_dof_per_node, dtype=dt, device=dev)
+        self._constraints = torch.zeros(self.n_nod, self.n_dof_per_node, dtype=torch.bool, device=dev)
+        self._external_gradient = torch.zeros(self.n_elem, *self.n_flux, dtype=dt, device=dev)
+        # an external strain that was never set is zero: the kernels then skip it
+        self._external_gradient_set = False
+        idx = (self.n_dof_per_node * self.elements).unsqueeze(-1) + torch.arange(
+            self.n_dof_per_node, device=elements.device
+        )
+        self.idx = idx.reshape(self.n_elem, -1).to(torch.int32)
+        if material is None or material.is_vectorized:
+            self.material = material
+        else:
+            self.material = material.vectorize(self.n_elem)
+        self._dm: DeviceMesh | None = None
+        self.last_solve: SolveContext | None = None
+
+    # ---------------------------------------------------------- interface --
+    @property
+    def n_dof_per_node(self) -> int:
+        raise NotImplementedError
+
+    @property
+    def n_flux(self) -> list[int]:
+        raise NotImplementedError
+
+    @property
+    def n_state(self) -> int:
+        assert self.material is not None
+        return self.material.n_state
+
+    @property
+    def volume_scale(self) -> Tensor:
+        return torch.ones(self.n_elem, device=self.nodes.device)
+
+    def _thickness(self) -> Tensor | None:
+        return None
+
+    # ------------------------------------------------------- device state --
+    @property
+    def device_mesh(self) -> DeviceMesh:
+        """Pattern and geometry on the GPU, built on first use."""
+        if self._dm is None:
+            self._dm = DeviceMesh(self.nodes, self.elements, self.etype, self.n_dof_per_node)
+        return self._dm
+
+    @property
+    def k_map(self) -> Tensor:
+        """Slot of every element-matrix entry (base.py:93-104), int32."""
+        return self.device_mesh.kmap().to(torch.int32)
+
+    @property
+    def glob_idx(self) -> Tensor:
+        """(row, col) of every stored entry, int64 [2, nnz] (base.py:112-117)."""
+        return self.device_mesh.glob_idx()
+
+    @property
+    def diag_map(self) -> Tensor:
+        """Slot of each diagonal entry, int32 (base.py:106-108)."""
+        return self.device_mesh.diag_map.to(torch.int32)
+
+    # ------------------------------------------------------------ setters --
+    @property
+    def constraints(self) -> Tensor:
+        return self._constraints
+
+    @constraints.setter
+    def constraints(self, value: Tensor):
+        if not value.shape == (self.n_nod, self.n_dof_per_node):
+            raise ValueError("Constraints must have the same shape as nodes.")
+        if value.dtype != torch.bool:
+            raise TypeError("Constraints must be a boolean tensor.")
+        self._constraints = value.to(self.nodes.device)
+
+    # -------------------------------------------------------------- solve --
+    def solve(
+        self,
+        increments: Tensor | None = None,
+        max_iter: int = 10,
+        rtol: float = 1e-8,
+        atol: float = 1e-6,
+        stol: float = 1e-10,
+        cutback_factor: float = 0.5,
+        growth_factor: float = 1.1,
+        max_cutbacks: int = 10,
+        verbose: bool = False,
+        method: str | None = None,
+        device: str | None = None,
+        return_intermediate: bool = False,
+        aggregate_integration_points: bool = True,
+        use_cached_solve: bool = False,
+        nlgeom: bool = False,
+        alpha: float = 0.0,
+        differentiable_parameters: Tensor | Iterable[Tensor] | None = None,
+        precision: str | None = None,
+        cg_max_iter: int | None = None,
+    ) -> tuple[Tensor, Tensor, Tensor, Tensor, Tensor]:
+        """Quasi-static solve by load increments (base.py:597-923).
+
+        Same arguments and results as the reference.  `method` selects the
+        GPU solver ("cg"/None: FP64 Jacobi-CG; "gb300-mixed": FP32 CG with
+        FP64 residual replacement) and `precision` may override it.  `stol` is
+        the relative residual of each linear solve.  `use_cached_solve` and
+        `verbose` are accepted; the CG always starts from zero and nothing is
+        printed.
+        """
+        prec = resolve_precision(method, precision)
+        if device is not None and torch.device(device).type != "cuda":
+            raise RuntimeError("torchfem_gb300 solves on a CUDA device only")
+        if alpha > 0.0:
+            raise NotImplementedError("viscous stabilization (alpha > 0) is not implemented")
+        if nlgeom or self.n_state != 0:
+            raise NotImplementedError(
+                "nonlinear materials / nlgeom are not implemented on the GPU path yet"
+            )
+        increments = torch.tensor([0.0, 1.0]) if increments is None else increments
+        N = len(increments)
+
+        if differentiable_parameters is None:
+            differentiable_parameters = ()
+        elif isinstance(differentiable_parameters, torch.Tensor):
+            differentiable_parameters = (differentiable_parameters,)
+        else:
+            differentiable_parameters = tuple(differentiable_parameters)
+        track = any(p.requires_grad for p in differentiable_parameters)
+
+        dm = self.device_mesh
+        dev = dm.device
+        out_dev = self.nodes.device
+        d = self.n_dof_per_node
+        con_bool = self._constraints.reshape(-1).to(dev)
+        con_mask = con_bool.to(torch.uint8).contiguous()
+        assert self.material is not None
+        mat_kind, mat_data = self.material.kernel_data(self.n_elem)
+
+        with torch.set_grad_enabled(track):
+            mat_data = mat_data.to(dev, torch.float64)
+            thickness = self._thickness()
+            if thickness is not None:
+                thickness = thickness.to(dev, torch.float64).contiguous()
+            F_neu = self._neumann.reshape(-1).to(dev, torch.float64)
+            DU_dir = self._dirichlet.reshape(-1).to(dev, torch.float64)
+            de0_full = (
+                self._external_gradient.to(dev, torch.float64) if self._external_gradient_set else None
+            )
+
+        sc = SolveContext(dm, con_mask, mat_kind, prec, max_iter, rtol, atol, stol, cg_max_iter)
+        self.last_solve = sc
+
+        shape_ip = (dm.nip, self.n_elem, *self.n_flux)
+        u_cur = torch.zeros(self.n_dofs, dtype=torch.float64, device=dev)
+        f_cur = torch.zeros(self.n_dofs, dtype=torch.float64, device=dev)
+        flux_cur = torch.zeros(shape_ip, dtype=torch.float64, device=dev)
+        grad_cur = torch.eye(self.n_flux[0], dtype=torch.float64, device=dev).expand(shape_ip).clone()
+        state_cur = torch.zeros(dm.nip, self.n_elem, self.n_state, dtype=torch.float64, device=dev)
+        du = torch.zeros(self.n_dofs, dtype=torch.float64, device=dev)
+
+        outs_u, outs_f, outs_flux, outs_grad, outs_state = [u_cur], [f_cur], [flux_cur], [grad_cur], [state_cur]
+
+        lam = float(increments[0])
+        step_frac = 1.0
+        with torch.set_grad_enabled(track):
+            for n in range(1, N):
+                target = float(increments[n])
+                span = target - lam
+                direction = math.copysign(1.0, span)
+                step_size = step_frac * abs(span)
+                min_step = abs(span) * cutback_factor**max_cutbacks
+                while abs(target - lam) > 1e-12 * max(1.0, abs(target)):
+                    step = direction * min(step_size, abs(target - lam))
+                    F_ext = (lam + step) * F_neu
+                    DU = step * DU_dir
+                    de0 = None if de0_full is None else (step * de0_full).contiguous()
+                    sigma_prev = flux_cur if track else flux_cur.detach()
+                    try:
+                        du = NewtonLinear.apply(
+                            sc, du.detach(), F_ext.contiguous(), DU.contiguous(),
+                            sigma_prev.contiguous(), de0, mat_data, thickness,
+                        )
+                    except RuntimeError as err:
+                        if isinstance(err, _lib.FemError) and err.code not in (
+                            _lib.FEM_NOT_CONVERGED, _lib.FEM_NONFINITE, _lib.FEM_BREAKDOWN
+                        ):
+                            raise
+                        step_size = cutback_factor * abs(step)
+                        if step_size < min_step:
+                            raise RuntimeError(
+                                f"Newton-Raphson did not converge in increment {n} "
+                                f"after {max_cutbacks} cutbacks."
+                            ) from err
+                        continue
+                    du_eval = torch.where(con_bool, DU, du)
+                    f_int, flux_new, h_inc = IntegrateMaterial.apply(
+                        sc, du_eval.contiguous(), sigma_prev.contiguous(), de0, mat_data, thickness
+                    )
+                    f_cur = f_int
+                    u_cur = u_cur + du_eval
+                    flux_cur = flux_new
+                    grad_cur = grad_cur + h_inc
+                    du = du_eval
+                    lam += step
+                    step_size = min(growth_factor * step_size, abs(span))
+                step_frac = min(step_size / abs(span), 1.0) if span != 0.0 else 1.0
+                outs_u.append(u_cur)
+                outs_f.append(f_cur)
+                outs_flux.append(flux_cur)
+                outs_grad.append(grad_cur)
+                outs_state.append(state_cur)
+
+            u = torch.stack(outs_u).reshape(N, self.n_nod, d)
+            f = torch.stack(outs_f).reshape(N, self.n_nod, d)
+            flux = torch.stack(outs_flux)
+            grad = torch.stack(outs_grad)
+            state = torch.stack(outs_state)
+            if aggregate_integration_points:
+                grad = grad.mean(dim=1)
+                flux = flux.mean(dim=1)
+                state = state.mean(dim=1)
+            flux = flux.squeeze((-2, -1))
+            grad = grad.squeeze((-2, -1))
+            if not track:
+                u, f, flux, grad, state = (t.detach() for t in (u, f, flux, grad, state))
+            dt = self.nodes.dtype
+            u, f, flux, grad, state = (t.to(out_dev, dt) for t in (u, f, flux, grad, state))
+        if return_intermediate:
+            return u, f, flux, grad, state
+        return u[-1], f[-1], flux[-1], grad[-1], state[-1]
+
+
+class Mechanics(FEM):
+    """Solid and structural mechanics (base.py:926-1092)."""
+
+    @property
+    def n_dof_per_node(self) -> int:
+        return self.nodes.shape[1]
+
+    @property
+    def initial_grad(self) -> Tensor:
+        return torch.eye(self.n_flux[0])
+
+    @property
+    def forces(self) -> Tensor:
+        return self._neumann
+
+    @forces.setter
+    def forces(self, value: Tensor):
+        if not value.shape == (self.n_nod, self.n_dof_per_node):
+            raise ValueError("Forces must have the same shape as nodes.")
+        if not torch.is_floating_point(value):
+            raise TypeError("Forces must be a floating-point tensor.")
+        self._neumann = value.to(self.nodes.device)
+
+    @property
+    def displacements(self) -> Tensor:
+        return self._dirichlet
+
+    @displacements.setter
+    def displacements(self, value: Tensor):
+        if not value.shape == (self.n_nod, self.n_dof_per_node):
+            raise ValueError("Displacements must have the same shape as nodes.")
+        if not torch.is_floating_point(value):
+            raise TypeError("Displacements must be a floating-point tensor.")
+        self._dirichlet = value.to(self.nodes.device)
+
+    @property
+    def ext_strain(self) -> Tensor:
+        return self._external_gradient
+
+    @ext_strain.setter
+    def ext_strain(self, value: Tensor):
+        if not value.shape == (self.n_elem, self.n_dof_per_node, self.n_dim):
+            raise ValueError("External strain must have the same shape as strains.")
+        if not torch.is_floating_point(value):
+            raise TypeError("External strain must be a floating-point tensor.")
+        self._external_gradient = value.to(self.nodes.device)
+        self._external_gradient_set = True

@@ -1,0 +1,180 @@
+"""Newton solve with a hand-written adjoint, on the GPU kernels.
+
+Mirrors `newton_solve` / `NewtonRaphsonAdjoint` (src/torchfem/sparse.py:517-795)
+for small-strain materials with a constant tangent (linear elasticity):
+
+forward   Newton iterations on res(du) = F_int(du_bc; sigma_prev, de0, C, t) - F_ext,
+          res[con] = 0 (base.py:704-743), each linear step solved by the GPU CG.
+backward  the adjoint solve K lambda = grad_du on the same CG and
+          preconditioner (sparse.py:671-680), then the residual's
+          vector-Jacobian product with cotangent -lambda computed by one element
+          kernel (fem_element_vjp) instead of an autograd replay of the
+          assembly (sparse.py:690-705).
+
+`IntegrateMaterial` is the converged-state evaluation (base.py:843-857):
+nodal internal forces, stress and increment gradient of a displacement
+increment, with its own kernel-based backward.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+from torch import Tensor
+
+from ._device import DeviceMesh, LinearSystem
+
+
+class SolveContext:
+    """What one solve() call shares between its Newton steps and backward."""
+
+    def __init__(self, dm: DeviceMesh, con_mask: Tensor, mat_kind: int, precision: str,
+                 max_iter: int, rtol: float, atol: float, stol: float, cg_max_iter: int | None,
+                 delta: float = 0.1):
+        self.dm = dm
+        self.con_mask = con_mask  # uint8 [n_dofs] on the device
+        self.con_bool = con_mask.bool()
+        self.mat_kind = mat_kind
+        self.precision = precision
+        self.max_iter = max_iter
+        self.rtol = rtol
+        self.atol = atol
+        self.stol = stol
+        self.cg_max_iter = cg_max_iter
+        self.delta = delta
+        self.system: LinearSystem | None = None
+        self.system_key = None
+        self.iterations: list[int] = []
+        self.newton_iterations: list[int] = []
+
+    def structs(self, mat_data: Tensor, thickness: Tensor | None):
+        from . import _lib
+
+        mesh = self.dm.make_mesh(thickness)
+        mat = _lib.FemMaterial(self.mat_kind, mat_data.data_ptr())
+        return mesh, mat
+
+    def get_system(self, mat_data: Tensor, thickness: Tensor | None) -> LinearSystem:
+        """The condensed tangent for these material data (built once per solve,
+        as the reference keeps self.K for a constant-tangent material)."""
+        key = (mat_data.data_ptr(), None if thickness is None else thickness.data_ptr())
+        if self.system is None or self.system_key != key:
+            mesh, mat = self.structs(mat_data, thickness)
+            self.system = self.dm.build_system(
+                mesh, mat, self.con_mask, self.precision, keep_refs=(mat_data, thickness, mesh, mat)
+            )
+            self.system_key = key
+        return self.system
+
+    def solve(self, b: Tensor) -> Tensor:
+        assert self.system is not None
+        x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, self.delta)
+        self.iterations.append(self.system.stats.iterations)
+        return x
+
+
+def _residual(sc: SolveContext, du, F_ext, DU, sigma_prev, de0, mat_data, thickness):
+    """res = F_int(du_bc) - F_ext with res[con] = 0, and ||res|| (device)."""
+    mesh, mat = sc.structs(mat_data, thickness)
+    fe, _, _ = sc.dm.element_force(
+        mesh, mat, du, sc.con_mask, DU, 1, sigma_prev, de0
+    )
+    res, sumsq = sc.dm.gather(fe, sub=F_ext, con_mask=sc.con_mask, con_mode=1, want_norm=True)
+    return res, sumsq
+
+
+class NewtonLinear(torch.autograd.Function):
+    """Newton solve of one load (sub)step for a constant-tangent material."""
+
+    @staticmethod
+    def forward(ctx, sc: SolveContext, du, F_ext, DU, sigma_prev, de0, mat_data, thickness):
+        du = du.detach().clone()
+        res0 = None
+        converged = False
+        for i in range(sc.max_iter):
+            res, sumsq = _residual(sc, du, F_ext, DU, sigma_prev, de0, mat_data, thickness)
+            res_norm = float(sumsq.sqrt().item())
+            if i == 0:
+                res0 = res_norm
+            if res_norm < sc.rtol * res0 or res_norm < sc.atol:
+                converged = True
+                sc.newton_iterations.append(i)
+                break
+            if res_norm != res_norm or res_norm in (float("inf"), float("-inf")):
+                break
+            sc.get_system(mat_data, thickness)
+            du = du - sc.solve(res)
+        if not converged:
+            raise RuntimeError("Newton-Raphson iteration did not converge.")
+        ctx.sc = sc
+        ctx.save_for_backward(du, DU, sigma_prev, de0, mat_data, thickness)
+        return du
+
+    @staticmethod
+    def backward(ctx, grad_du):
+        sc: SolveContext = ctx.sc
+        du, DU, sigma_prev, de0, mat_data, thickness = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        g = torch.where(sc.con_bool, torch.zeros_like(grad_du), grad_du).contiguous()
+        sc.get_system(mat_data, thickness)
+        lam = sc.solve(g)
+        mesh, mat = sc.structs(mat_data, thickness)
+        neg = (-lam).contiguous()
+        gsig, gmat, gthick, gde0, gv = sc.dm.vjp(
+            mesh, mat, du, neg, sc.con_mask, DU, 1, sigma_prev, de0,
+            want_sig=need[4], want_mat=need[6], want_thick=need[7] and thickness is not None,
+            want_de0=need[5] and de0 is not None, want_v=need[3], mat_numel=mat_data.numel(),
+        )
+        g_F = lam if need[2] else None
+        g_DU = torch.where(sc.con_bool, gv, torch.zeros_like(gv)) if need[3] else None
+        return (
+            None,
+            None,
+            g_F,
+            g_DU,
+            None if gsig is None else gsig.view_as(sigma_prev),
+            None if gde0 is None else gde0.view_as(de0),
+            None if gmat is None else gmat.view_as(mat_data),
+            gthick,
+        )
+
+
+class IntegrateMaterial(torch.autograd.Function):
+    """Converged-state evaluation: (F_int, flux, H_inc) of an increment."""
+
+    @staticmethod
+    def forward(ctx, sc: SolveContext, du_eval, sigma_prev, de0, mat_data, thickness):
+        mesh, mat = sc.structs(mat_data, thickness)
+        dm = sc.dm
+        fe, flux, hg = dm.element_force(
+            mesh, mat, du_eval, None, None, 0, sigma_prev, de0, want_flux=True, want_h=True
+        )
+        f_int, _ = dm.gather(fe)
+        shape = (dm.nip, dm.n_elem, dm.d, dm.d)
+        ctx.sc = sc
+        ctx.save_for_backward(du_eval, sigma_prev, de0, mat_data, thickness)
+        return f_int, flux.view(shape), hg.view(shape)
+
+    @staticmethod
+    def backward(ctx, g_f, g_flux, g_h):
+        sc: SolveContext = ctx.sc
+        du_eval, sigma_prev, de0, mat_data, thickness = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        mesh, mat = sc.structs(mat_data, thickness)
+        gsig, gmat, gthick, gde0, gv = sc.dm.vjp(
+            mesh, mat, du_eval, None if g_f is None else g_f.contiguous(), None, None, 0,
+            sigma_prev, de0,
+            gflux=None if g_flux is None else g_flux.contiguous(),
+            gh=None if g_h is None else g_h.contiguous(),
+            want_sig=need[2], want_mat=need[4], want_thick=need[5] and thickness is not None,
+            want_de0=need[3] and de0 is not None, want_v=need[1], mat_numel=mat_data.numel(),
+        )
+        return (
+            None,
+            gv,
+            None if gsig is None else gsig.view_as(sigma_prev),
+            None if gde0 is None else gde0.view_as(de0),
+            None if gmat is None else gmat.view_as(mat_data),
+            gthick,
+        )
