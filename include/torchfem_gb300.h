@@ -74,7 +74,7 @@ enum {
 };
 
 enum { FEM_F64 = 0, FEM_F32 = 1 };
-enum { FEM_FMT_CSR_F64 = 1, FEM_FMT_BSR_F32 = 2 };
+enum { FEM_FMT_CSR_F64 = 1, FEM_FMT_SELL_F32 = 2 };
 
 /* Last error message of the calling thread (host string). */
 const char* fem_last_error(void);
@@ -236,17 +236,33 @@ int fem_assemble_csr(const fem_blocks* blocks, int ke_dtype, const void* ke,
                      const int64_t* row_ptr, const uint8_t* con_mask, double* val,
                      void* stream);
 
-/* The same sums into a block-CSR (dim x dim blocks, FP32) over the node graph. */
-int fem_assemble_bsr(const fem_blocks* blocks, int ke_dtype, const void* ke,
-                     const uint8_t* con_mask, float* bval, void* stream);
+/* Sliced block layout of the node graph for the FP32 matrix: rows (nodes)
+ * in slices of 32, each slice padded to its longest row; block slot k of row
+ * a lives at slot sell_base[a/32] + 32 k + a%32 and component c of its
+ * dim x dim block at value index sell_base[a/32]*dim^2 + (k dim^2 + c)*32 +
+ * a%32.  fem_sell_layout writes sell_base [n_slices+1] and the slot count
+ * (*n_slots, host); fem_sell_columns the column of every slot (padding slots
+ * point at their own row and hold zeros). */
+size_t fem_sell_workspace_bytes(int64_t n_nod);
+int fem_sell_layout(const fem_blocks* blocks, int64_t* sell_base, int64_t* n_slots, void* ws,
+                    size_t ws_bytes, void* stream);
+int fem_sell_columns(const fem_blocks* blocks, const int64_t* sell_base, int32_t* col,
+                     void* stream);
+
+/* The same per-slot sums and condensation as fem_assemble_csr, written as
+ * FP32 dim x dim blocks into the sliced layout (sval [n_slots * dim^2]). */
+int fem_assemble_sell(const fem_blocks* blocks, int ke_dtype, const void* ke,
+                      const uint8_t* con_mask, const int64_t* sell_base, int64_t n_slots,
+                      float* sval, void* stream);
 
 /* Jacobi: inv_diag[r] = 1 / val[diag_map[r]] (sparse.py:406-407). */
 int fem_jacobi(const double* val, const int64_t* diag_map, int64_t n, double* inv_diag,
                int32_t* status, void* stream);
 
-/* Block Jacobi: FP32 inverses of the dim x dim diagonal blocks. */
-int fem_block_jacobi(const fem_blocks* blocks, const float* bval, float* inv_blocks,
-                     int32_t* status, void* stream);
+/* Block Jacobi: FP32 inverses [n_nod][dim][dim] of the diagonal blocks of
+ * the sliced FP32 matrix. */
+int fem_block_jacobi(const fem_blocks* blocks, const float* sval, const int64_t* sell_base,
+                     float* inv_blocks, int32_t* status, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Linear solve: sparse_solve (sparse.py:271-347), Jacobi-CG branch          */
@@ -254,13 +270,13 @@ int fem_block_jacobi(const fem_blocks* blocks, const float* bval, float* inv_blo
 /* ------------------------------------------------------------------------ */
 
 typedef struct fem_matrix {
-  int format;              /* FEM_FMT_CSR_F64 or FEM_FMT_BSR_F32 */
-  int block;               /* 1 for CSR, dim for BSR */
+  int format;              /* FEM_FMT_CSR_F64 or FEM_FMT_SELL_F32 */
+  int block;               /* 1 for CSR, dim for the sliced block layout */
   int64_t n;               /* unknowns */
-  int64_t n_rows;          /* scalar rows (CSR) or block rows (BSR) */
-  const int64_t* row_ptr;  /* [n_rows+1] */
-  const int32_t* col;      /* scalar or block column ids */
-  const void* val;         /* FP64 [nnz] or FP32 [n_blocks][block][block] */
+  int64_t n_rows;          /* scalar rows (CSR) or node rows (sliced) */
+  const int64_t* row_ptr;  /* CSR row pointers [n_rows+1] or sell_base [n_slices+1] */
+  const int32_t* col;      /* scalar column ids or slot columns */
+  const void* val;         /* FP64 [nnz] or FP32 sliced block values */
   const void* precond;     /* FP64 inverse diagonal [n] or FP32 inverse blocks */
 } fem_matrix;
 
@@ -280,7 +296,7 @@ size_t fem_pcg_workspace_bytes(const fem_matrix* A);
 
 /* Preconditioned CG on A x = b from x = 0, stopping at ||r|| <= rtol ||b||
  * (the criterion of cupyx/scipy cg used at sparse.py:417, :508).  FP64 CSR
- * with Jacobi reproduces the reference GPU branch; an FP32 BSR matrix runs
+ * with Jacobi reproduces the reference GPU branch; an FP32 sliced matrix runs
  * the same iteration in single precision. */
 int fem_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter,
             void* ws, size_t ws_bytes, fem_solve_info* info, void* stream);
@@ -300,7 +316,7 @@ int fem_apply64(const fem_operator64* op, const double* x, double* y, void* ws, 
 
 size_t fem_pcg_mixed_workspace_bytes(const fem_matrix* A32, const fem_operator64* op);
 
-/* Mixed precision: FP32 BSR K and FP32 block-Jacobi CG, with the solution
+/* Mixed precision: FP32 sliced-block K and FP32 block-Jacobi CG, with the solution
  * accumulated in FP64 and the recursive residual replaced by the FP64
  * matrix-free residual b - A x whenever it has dropped by `delta` since the
  * last replacement (reliable updates; Sleijpen & van der Vorst 1996).  Stops

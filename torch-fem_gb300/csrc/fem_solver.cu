@@ -15,18 +15,31 @@
 namespace tfg {
 
 int etype_info(int etype, int* ne, int* d, int* nip);
+size_t scan_workspace_bytes(int64_t n);
+int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
+
 
 // ---------------------------------------------------------------- assembly --
 // Thread per node-pair block (a, b): gathers the d x d sub-blocks of every
 // contributing element matrix, sums them in ascending element order and
 // writes them with the Dirichlet condensation of base.py:414-419.
-template <typename KT, typename AT, bool kBSR>
+// Position of component c of block slot k of row a in the sliced layout:
+// slices of 32 rows, slot-major, each component contiguous over the 32 rows.
+__device__ __forceinline__ int64_t sell_index(const int64_t* __restrict__ sell_base, int64_t a, int64_t k,
+                                              int c, int DD) {
+  const int64_t s = a >> 5;
+  const int lane = (int)(a & 31);
+  return sell_base[s] * DD + (k * DD + c) * 32 + lane;
+}
+
+template <typename KT, typename AT, bool kSELL>
 __global__ void k_assemble(int n_e, int D, int64_t n_blocks, const int64_t* __restrict__ nbr_ptr,
                            const int32_t* __restrict__ nbr, const int64_t* __restrict__ blk_ptr,
                            const int32_t* __restrict__ contrib, const int32_t* __restrict__ blk_row,
                            const int64_t* __restrict__ inc_ptr, const KT* __restrict__ ke,
                            const int64_t* __restrict__ row_ptr, const uint8_t* __restrict__ con,
-                           double* __restrict__ val, float* __restrict__ bval) {
+                           double* __restrict__ val, const int64_t* __restrict__ sell_base,
+                           float* __restrict__ sval) {
   const int64_t blk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (blk >= n_blocks) return;
   const int64_t a = blk_row[blk];
@@ -56,8 +69,8 @@ __global__ void k_assemble(int n_e, int D, int64_t n_blocks, const int64_t* __re
       double v = (double)acc[i][j];
       if (rc || con[cdof]) v = 0.0;
       if (r == cdof && rc) v = 1.0;
-      if (kBSR) {
-        bval[blk * D * D + i * D + j] = (float)v;
+      if (kSELL) {
+        sval[sell_index(sell_base, a, k, i * D + j, D * D)] = (float)v;
       } else {
         if (orphan) {
           if (i == j) val[row_ptr[r]] = v;
@@ -79,14 +92,15 @@ __global__ void k_jacobi(const double* __restrict__ val, const int64_t* __restri
   inv[r] = v;
 }
 
-__global__ void k_block_jacobi(const float* __restrict__ bval, const int64_t* __restrict__ diag_blk,
+__global__ void k_block_jacobi(const float* __restrict__ sval, const int64_t* __restrict__ sell_base,
+                               const int64_t* __restrict__ nbr_ptr, const int64_t* __restrict__ diag_blk,
                                int64_t n_nod, int D, float* __restrict__ inv, int32_t* status) {
   const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n_nod) return;
-  const float* m = bval + diag_blk[a] * D * D;
+  const int64_t k = diag_blk[a] - nbr_ptr[a];
   double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   for (int i = 0; i < D; ++i)
-    for (int j = 0; j < D; ++j) M[i][j] = m[i * D + j];
+    for (int j = 0; j < D; ++j) M[i][j] = sval[sell_index(sell_base, a, k, i * D + j, D * D)];
   double R[3][3];
   double det;
   if (D == 2) {
@@ -165,6 +179,52 @@ __device__ __forceinline__ double sum_partials(const double* partial, int n, int
   return block_sum(s, red);
 }
 
+// L2 eviction-priority hints (PTX createpolicy / ld.L2::cache_hint): the part
+// of the matrix that should stay resident in L2 across CG iterations is read
+// evict_last, the streamed remainder evict_first.
+__device__ __forceinline__ uint64_t l2_policy(bool keep) {
+  uint64_t pol;
+  if (keep) asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  else asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ float ld_l2(const float* ptr, uint64_t pol) {
+  float v;
+  asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+__device__ __forceinline__ double ld_l2(const double* ptr, uint64_t pol) {
+  double v;
+  asm("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+__device__ __forceinline__ int32_t ld_l2(const int32_t* ptr, uint64_t pol) {
+  int32_t v;
+  asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+// Two block sums in one pass (fixed order).  Valid in thread 0.
+__device__ __forceinline__ void block_sum2(double& a, double& b, double2* smem32) {
+  a = warp_sum(a);
+  b = warp_sum(b);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) smem32[wid] = make_double2(a, b);
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  double2 t = (threadIdx.x < nw) ? smem32[threadIdx.x] : make_double2(0.0, 0.0);
+  if (wid == 0) {
+    t.x = warp_sum(t.x);
+    t.y = warp_sum(t.y);
+  }
+  a = t.x;
+  b = t.y;
+  __syncthreads();
+}
+
 __device__ __forceinline__ bool ctrl_idle(const Ctrl* c) {
   return (*(volatile const int*)&c->done) != 0 || (*(volatile const int*)&c->replace) != 0;
 }
@@ -175,7 +235,7 @@ template <int TPR>
 __global__ void __launch_bounds__(256)
 k_spmv_csr(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
            const double* __restrict__ val, const double* __restrict__ p, double* __restrict__ q,
-           double* __restrict__ partial, Ctrl* ctrl) {
+           double* __restrict__ partial, Ctrl* ctrl, int64_t keep_nnz) {
   __shared__ double red[32];
   if (ctrl_idle(ctrl)) return;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -185,7 +245,8 @@ k_spmv_csr(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __rest
   double s = 0.0;
   if (row < n) {
     const int64_t rs = row_ptr[row], re = row_ptr[row + 1];
-    for (int64_t j = rs + sub; j < re; j += TPR) s += val[j] * p[col[j]];
+    const uint64_t pol = l2_policy(rs < keep_nnz);
+    for (int64_t j = rs + sub; j < re; j += TPR) s += ld_l2(val + j, pol) * p[ld_l2(col + j, pol)];
   }
 #pragma unroll
   for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
@@ -208,26 +269,40 @@ k_spmv_csr(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __rest
   }
 }
 
-// Block-CSR FP32 SpMV with TPB threads per block row, FP32 products and
-// accumulation, p.q partial in FP64.
-template <int D, int TPB>
-__global__ void __launch_bounds__(256)
-k_spmv_bsr(int64_t n_rows, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-           const float* __restrict__ bval, const float* __restrict__ p, float* __restrict__ q,
-           double* __restrict__ partial, Ctrl* ctrl) {
+// Sliced block SpMV, FP32: thread per node row, slices of 32 rows stored
+// slot-major with every block component contiguous over the slice, so each
+// load instruction of a warp reads one full 128-byte line.  FP32 products and
+// accumulation; the p.q partial is formed in FP64.
+constexpr int kSellWarps = 4;  // warps sharing one slice's slots
+
+template <int D>
+__global__ void __launch_bounds__(kSellWarps * 32)
+k_spmv_sell(int64_t n_rows, const int64_t* __restrict__ sell_base, const int32_t* __restrict__ col,
+            const float* __restrict__ sval, const float* __restrict__ p, float* __restrict__ q,
+            double* __restrict__ partial, Ctrl* ctrl, int64_t keep_slots) {
+  constexpr int DD = D * D;
+  __shared__ float ys[kSellWarps][D][32];
   __shared__ double red[32];
   if (ctrl_idle(ctrl)) return;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t row = t / TPB;
-  const int sub = (int)(t % TPB);
-  float y[D];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t n_slices = (n_rows + 31) >> 5;
+  double pq = 0.0;
+  for (int64_t s = blockIdx.x; s < n_slices; s += gridDim.x) {
+    const int64_t b0 = sell_base[s];
+    const int len = (int)((sell_base[s + 1] - b0) >> 5);
+    const uint64_t pol = l2_policy(b0 < keep_slots);
+    const int32_t* cp = col + b0 + lane;
+    const float* vp = sval + b0 * DD + lane;
+    float y[D];
 #pragma unroll
-  for (int i = 0; i < D; ++i) y[i] = 0.f;
-  if (row < n_rows) {
-    const int64_t rs = row_ptr[row], re = row_ptr[row + 1];
-    for (int64_t k = rs + sub; k < re; k += TPB) {
-      const int64_t c = col[k];
-      const float* m = bval + k * (D * D);
+    for (int i = 0; i < D; ++i) y[i] = 0.f;
+#pragma unroll 2
+    for (int k = w; k < len; k += kSellWarps) {
+      const int64_t c = ld_l2(cp + (int64_t)k * 32, pol);
+      const float* vk = vp + (int64_t)k * DD * 32;
+      float m[DD];
+#pragma unroll
+      for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, pol);
       float x[D];
 #pragma unroll
       for (int j = 0; j < D; ++j) x[j] = p[c * D + j];
@@ -236,18 +311,23 @@ k_spmv_bsr(int64_t n_rows, const int64_t* __restrict__ row_ptr, const int32_t* _
 #pragma unroll
         for (int j = 0; j < D; ++j) y[i] = fmaf(m[i * D + j], x[j], y[i]);
     }
-  }
 #pragma unroll
-  for (int o = TPB / 2; o > 0; o >>= 1)
+    for (int i = 0; i < D; ++i) ys[w][i][lane] = y[i];
+    __syncthreads();
+    if (w == 0) {
+      const int64_t a = s * 32 + lane;
+      if (a < n_rows) {
 #pragma unroll
-    for (int i = 0; i < D; ++i) y[i] += __shfl_down_sync(0xffffffffu, y[i], o, TPB);
-  double pq = 0.0;
-  if (row < n_rows && sub == 0) {
+        for (int i = 0; i < D; ++i) {
+          float t = ys[0][i][lane];
 #pragma unroll
-    for (int i = 0; i < D; ++i) {
-      q[row * D + i] = y[i];
-      pq += (double)p[row * D + i] * (double)y[i];
+          for (int v = 1; v < kSellWarps; ++v) t += ys[v][i][lane];
+          q[a * D + i] = t;
+          pq += (double)p[a * D + i] * (double)t;
+        }
+      }
     }
+    __syncthreads();
   }
   const double bsum = block_sum(pq, red);
   if (threadIdx.x == 0) partial[blockIdx.x] = bsum;
@@ -262,6 +342,34 @@ k_spmv_bsr(int64_t n_rows, const int64_t* __restrict__ row_ptr, const int32_t* _
       }
     }
   }
+}
+
+// Slice lengths: 32 x (largest degree among the slice's rows).
+__global__ void k_sell_len(const int64_t* __restrict__ nbr_ptr, int64_t n_nod, int64_t* __restrict__ len) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n_slices = (n_nod + 31) >> 5;
+  if (s >= n_slices) return;
+  int64_t m = 0;
+  for (int l = 0; l < 32; ++l) {
+    const int64_t a = s * 32 + l;
+    if (a < n_nod) m = max(m, nbr_ptr[a + 1] - nbr_ptr[a]);
+  }
+  len[s] = 32 * m;
+}
+
+// Column of every slot; padding slots point at the row itself (value 0).
+__global__ void k_sell_cols(const int64_t* __restrict__ nbr_ptr, const int32_t* __restrict__ nbr,
+                            int64_t n_nod, const int64_t* __restrict__ sell_base, int32_t* __restrict__ col) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n_slices = (n_nod + 31) >> 5;
+  if (a >= n_slices * 32) return;
+  const int64_t s = a >> 5;
+  const int lane = (int)(a & 31);
+  const int64_t b0 = sell_base[s];
+  const int64_t len = (sell_base[s + 1] - b0) >> 5;
+  const int64_t deg = a < n_nod ? nbr_ptr[a + 1] - nbr_ptr[a] : 0;
+  const int32_t pad = a < n_nod ? (int32_t)a : 0;
+  for (int64_t k = 0; k < len; ++k) col[b0 + k * 32 + lane] = k < deg ? nbr[nbr_ptr[a] + k] : pad;
 }
 
 // z = M r for one group of G DOFs: Jacobi (G = 1, FP64 inverse diagonal) or
@@ -312,18 +420,20 @@ __device__ void finish_update(Ctrl* c, double rz_new, double rr, bool count_iter
   }
 }
 
-// x += alpha p; r -= alpha q; z = M r; partial r.z and r.r.
+// x += alpha p; r -= alpha q; z = M r; partial r.z and r.r.  Grid-stride
+// over groups of G DOFs (a node for block Jacobi).
 template <int G, typename VT>
 __global__ void __launch_bounds__(256)
 k_update(int64_t n_groups, VT* __restrict__ x, VT* __restrict__ r, const VT* __restrict__ p,
          const VT* __restrict__ q, VT* __restrict__ z, const void* __restrict__ prec,
          double* __restrict__ partial, Ctrl* ctrl) {
+  __shared__ double2 red2[32];
   __shared__ double red[32];
   if (ctrl_idle(ctrl)) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rz = 0.0, rr = 0.0;
-  if (i < n_groups) {
-    const VT alpha = (VT)ctrl->alpha;
+  const VT alpha = (VT)ctrl->alpha;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_groups;
+       i += (int64_t)gridDim.x * blockDim.x) {
     VT rv[G], zv[G];
 #pragma unroll
     for (int g = 0; g < G; ++g) {
@@ -340,11 +450,10 @@ k_update(int64_t n_groups, VT* __restrict__ x, VT* __restrict__ r, const VT* __r
       rr += (double)rv[g] * (double)rv[g];
     }
   }
-  const double s1 = block_sum(rz, red);
-  const double s2 = block_sum(rr, red);
+  block_sum2(rz, rr, red2);
   if (threadIdx.x == 0) {
-    partial[2 * blockIdx.x] = s1;
-    partial[2 * blockIdx.x + 1] = s2;
+    partial[2 * blockIdx.x] = rz;
+    partial[2 * blockIdx.x + 1] = rr;
   }
   if (arrive_last(&ctrl->counter)) {
     const double t1 = sum_partials(partial, gridDim.x, 2, 0, red);
@@ -357,12 +466,11 @@ k_update(int64_t n_groups, VT* __restrict__ x, VT* __restrict__ r, const VT* __r
 }
 
 template <typename VT>
-__global__ void k_pupdate(int64_t n, const VT* __restrict__ z, VT* __restrict__ p, Ctrl* ctrl) {
+__global__ void __launch_bounds__(256) k_pupdate(int64_t n, const VT* __restrict__ z, VT* __restrict__ p, Ctrl* ctrl) {
   if (ctrl_idle(ctrl)) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
   const VT beta = (VT)ctrl->beta;
-  p[i] = z[i] + beta * p[i];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
 }
 
 // Start (x = 0): r = b, z = M r, p = z; rz, rr, bb; tolerances.
@@ -498,7 +606,42 @@ __global__ void k_copy_cast(int64_t n, const float* __restrict__ in, double* __r
 // ------------------------------------------------------------- host driver --
 constexpr int kThreads = 256;
 constexpr int kCsrTpr = 8;
-constexpr int kBsrTpb = 8;
+
+// SM count of the current device (cached per host thread).
+static int sm_count() {
+  static thread_local int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
+  }
+  return n;
+}
+
+// Bytes of matrix data kept resident in L2 across CG iterations (read with
+// evict_last); the rest streams with evict_first.  TORCHFEM_GB300_L2_KEEP_MB
+// overrides the default for experiments.
+static int64_t l2_keep_bytes() {
+  static int64_t keep = -1;
+  if (keep < 0) {
+    const char* e = getenv("TORCHFEM_GB300_L2_KEEP_MB");
+    keep = (int64_t)((e ? atof(e) : 0.0) * 1e6);
+    if (keep < 0) keep = 0;
+  }
+  return keep;
+}
+
+static unsigned vec_grid(int64_t n) {
+  const int64_t cap = (int64_t)sm_count() * 4;
+  const int64_t need = (n + kThreads - 1) / kThreads;
+  return (unsigned)std::max<int64_t>(1, std::min(cap, need));
+}
+
+static unsigned sell_grid(int64_t n_rows) {
+  const int64_t ns = (n_rows + 31) / 32;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  return (unsigned)std::max<int64_t>(1, std::min(cap, ns));
+}
 
 static int read_ctrl(Ctrl* d, Ctrl* h, cudaStream_t st) {
   if (cudaMemcpyAsync(h, d, sizeof(Ctrl), cudaMemcpyDeviceToHost, st) != cudaSuccess)
@@ -511,7 +654,7 @@ static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 static int64_t spmv_grid(const fem_matrix* A) {
   if (A->format == FEM_FMT_CSR_F64) return grid_for(A->n_rows * kCsrTpr, kThreads);
-  return grid_for(A->n_rows * kBsrTpb, kThreads);
+  return sell_grid(A->n_rows);
 }
 
 static int64_t max_grid(const fem_matrix* A) {
@@ -538,9 +681,9 @@ static int validate_matrix(const fem_matrix* A) {
       set_last_error("fem_pcg: CSR needs block 1 and n_rows == n");
       return FEM_INVALID;
     }
-  } else if (A->format == FEM_FMT_BSR_F32) {
+  } else if (A->format == FEM_FMT_SELL_F32) {
     if (A->block < 2 || A->block > 3 || A->n_rows * A->block != A->n) {
-      set_last_error("fem_pcg: BSR needs block 2 or 3 and n_rows * block == n");
+      set_last_error("fem_pcg: sliced blocks need block 2 or 3 and n_rows * block == n");
       return FEM_INVALID;
     }
   } else {
@@ -576,10 +719,8 @@ struct SpmvTimer {
       }
     }
   }
-  ~SpmvTimer() {
-    if (ready)
-      for (int i = 0; i < 2 * kMaxChunk; ++i) cudaEventDestroy(ev[i]);
-  }
+  // no destructor: the events live until the process exits, when the CUDA
+  // runtime may already be gone
 };
 
 static thread_local SpmvTimer g_timer;
@@ -593,19 +734,18 @@ static void launch_iteration(const fem_matrix* A, VT* x, VT* r, VT* z, VT* p, VT
   if constexpr (G == 1) {
     k_spmv_csr<kCsrTpr><<<grid_for(A->n_rows * kCsrTpr, kThreads), kThreads, 0, st>>>(
         A->n_rows, A->row_ptr, A->col, (const double*)A->val, (const double*)p, (double*)q,
-        partial, ctrl);
+        partial, ctrl, l2_keep_bytes() / 12);
   } else {
-    k_spmv_bsr<G, kBsrTpb><<<grid_for(A->n_rows * kBsrTpb, kThreads), kThreads, 0, st>>>(
+    k_spmv_sell<G><<<sell_grid(A->n_rows), kSellWarps * 32, 0, st>>>(
         A->n_rows, A->row_ptr, A->col, (const float*)A->val, (const float*)p, (float*)q, partial,
-        ctrl);
+        ctrl, l2_keep_bytes() / (4 * G * G + 4));
   }
   ::tfg::note_launch();
   if (slot >= 0) cudaEventRecord(g_timer.ev[2 * slot + 1], st);
   const int64_t ng = A->n / G;
-  k_update<G, VT><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, x, r, p, q, z, A->precond,
-                                                               partial, ctrl);
+  k_update<G, VT><<<vec_grid(ng), kThreads, 0, st>>>(ng, x, r, p, q, z, A->precond, partial, ctrl);
   ::tfg::note_launch();
-  k_pupdate<VT><<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, z, p, ctrl);
+  k_pupdate<VT><<<vec_grid(A->n), kThreads, 0, st>>>(A->n, z, p, ctrl);
   ::tfg::note_launch();
 }
 
@@ -712,34 +852,67 @@ int fem_assemble_csr(const fem_blocks* B, int ke_dtype, const void* ke, const in
   if (ke_dtype == FEM_F64)
     k_assemble<double, double, false><<<g, 128, 0, st>>>(
         B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
-        B->inc_ptr, (const double*)ke, row_ptr, con_mask, val, nullptr);
+        B->inc_ptr, (const double*)ke, row_ptr, con_mask, val, nullptr, nullptr);
   else
     k_assemble<float, double, false><<<g, 128, 0, st>>>(
         B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
-        B->inc_ptr, (const float*)ke, row_ptr, con_mask, val, nullptr);
+        B->inc_ptr, (const float*)ke, row_ptr, con_mask, val, nullptr, nullptr);
         ::tfg::note_launch();
   return check_cuda("fem_assemble_csr");
 }
 
-int fem_assemble_bsr(const fem_blocks* B, int ke_dtype, const void* ke, const uint8_t* con_mask,
-                     float* bval, void* stream) {
+size_t fem_sell_workspace_bytes(int64_t n_nod) {
+  const int64_t ns = (n_nod + 31) / 32;
+  return (size_t)(ns + 1) * sizeof(int64_t) + scan_workspace_bytes(ns);
+}
+
+int fem_sell_layout(const fem_blocks* B, int64_t* sell_base, int64_t* n_slots, void* ws,
+                    size_t ws_bytes, void* stream) {
   cudaStream_t st = as_stream(stream);
-  if (B->dim < 1 || B->dim > 3) {
-    set_last_error("fem_assemble_bsr: dim must be 1..3");
+  if (ws_bytes < fem_sell_workspace_bytes(B->n_nod)) {
+    set_last_error("fem_sell_layout: workspace too small");
     return FEM_INVALID;
   }
-  if (B->n_blocks == 0) return FEM_OK;
+  const int64_t ns = (B->n_nod + 31) / 32;
+  int64_t* len = reinterpret_cast<int64_t*>(ws);
+  k_sell_len<<<grid_for(ns, kThreads), kThreads, 0, st>>>(B->nbr_ptr, B->n_nod, len);
+  ::tfg::note_launch();
+  int rc = scan_exclusive(len, sell_base, ns, len + ns + 1, st);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(n_slots, sell_base + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda("fem_sell_layout sync");
+  return check_cuda("fem_sell_layout");
+}
+
+int fem_sell_columns(const fem_blocks* B, const int64_t* sell_base, int32_t* col, void* stream) {
+  cudaStream_t st = as_stream(stream);
+  const int64_t ns = (B->n_nod + 31) / 32;
+  k_sell_cols<<<grid_for(ns * 32, kThreads), kThreads, 0, st>>>(B->nbr_ptr, B->nbr, B->n_nod, sell_base, col);
+  ::tfg::note_launch();
+  return check_cuda("fem_sell_columns");
+}
+
+int fem_assemble_sell(const fem_blocks* B, int ke_dtype, const void* ke, const uint8_t* con_mask,
+                      const int64_t* sell_base, int64_t n_slots, float* sval, void* stream) {
+  cudaStream_t st = as_stream(stream);
+  if (B->dim < 1 || B->dim > 3) {
+    set_last_error("fem_assemble_sell: dim must be 1..3");
+    return FEM_INVALID;
+  }
+  cudaMemsetAsync(sval, 0, sizeof(float) * n_slots * B->dim * B->dim, st);
+  if (B->n_blocks == 0) return check_cuda("fem_assemble_sell");
   const unsigned g = grid_for(B->n_blocks, 128);
   if (ke_dtype == FEM_F64)
     k_assemble<double, double, true><<<g, 128, 0, st>>>(
         B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
-        B->inc_ptr, (const double*)ke, nullptr, con_mask, nullptr, bval);
+        B->inc_ptr, (const double*)ke, nullptr, con_mask, nullptr, sell_base, sval);
   else
     k_assemble<float, float, true><<<g, 128, 0, st>>>(
         B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
-        B->inc_ptr, (const float*)ke, nullptr, con_mask, nullptr, bval);
-        ::tfg::note_launch();
-  return check_cuda("fem_assemble_bsr");
+        B->inc_ptr, (const float*)ke, nullptr, con_mask, nullptr, sell_base, sval);
+  ::tfg::note_launch();
+  return check_cuda("fem_assemble_sell");
 }
 
 int fem_jacobi(const double* val, const int64_t* diag_map, int64_t n, double* inv_diag,
@@ -750,11 +923,11 @@ int fem_jacobi(const double* val, const int64_t* diag_map, int64_t n, double* in
   return check_cuda("fem_jacobi");
 }
 
-int fem_block_jacobi(const fem_blocks* B, const float* bval, float* inv_blocks, int32_t* status,
-                     void* stream) {
+int fem_block_jacobi(const fem_blocks* B, const float* sval, const int64_t* sell_base,
+                     float* inv_blocks, int32_t* status, void* stream) {
   cudaStream_t st = as_stream(stream);
-  k_block_jacobi<<<grid_for(B->n_nod, kThreads), kThreads, 0, st>>>(bval, B->diag_blk, B->n_nod,
-                                                                    B->dim, inv_blocks, status);
+  k_block_jacobi<<<grid_for(B->n_nod, kThreads), kThreads, 0, st>>>(
+      sval, sell_base, B->nbr_ptr, B->diag_blk, B->n_nod, B->dim, inv_blocks, status);
                                                                     ::tfg::note_launch();
   return check_cuda("fem_block_jacobi");
 }
@@ -806,7 +979,7 @@ int fem_apply64(const fem_operator64* op, const double* x, double* y, void* ws, 
 }
 
 size_t fem_pcg_mixed_workspace_bytes(const fem_matrix* A32, const fem_operator64* op) {
-  if (validate_matrix(A32) != FEM_OK || A32->format != FEM_FMT_BSR_F32) return 0;
+  if (validate_matrix(A32) != FEM_OK || A32->format != FEM_FMT_SELL_F32) return 0;
   const int64_t fl = op_fe_len(op);
   if (fl < 0) return 0;
   return layout(A32, fl > 0 ? fl : 1, nullptr, nullptr);
@@ -817,8 +990,8 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
                   fem_solve_info* info, void* stream) {
   int rc = validate_matrix(A);
   if (rc) return rc;
-  if (A->format != FEM_FMT_BSR_F32) {
-    set_last_error("fem_pcg_mixed: needs an FP32 BSR matrix");
+  if (A->format != FEM_FMT_SELL_F32) {
+    set_last_error("fem_pcg_mixed: needs an FP32 sliced-block matrix");
     return FEM_INVALID;
   }
   const size_t need = fem_pcg_mixed_workspace_bytes(A, op);
@@ -872,7 +1045,7 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
         k_replace<3><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, b, v.y64, r, z, A->precond,
                                                                   v.partial, v.ctrl);
                                                                   ::tfg::note_launch();
-      k_pupdate<float><<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, z, p, v.ctrl);
+      k_pupdate<float><<<vec_grid(A->n), kThreads, 0, st>>>(A->n, z, p, v.ctrl);
       ::tfg::note_launch();
       TFG_CHECK_LAUNCH("fem_pcg_mixed replace");
       rc = read_ctrl(v.ctrl, &h, st);

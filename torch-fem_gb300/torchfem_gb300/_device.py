@@ -172,6 +172,22 @@ class DeviceMesh:
             n_e, self.d, n_nod, self.n_blocks, ptr(self.nbr_ptr), ptr(self.nbr), ptr(self.blk_ptr),
             ptr(self.contrib), ptr(self.blk_row), ptr(self.diag_blk), ptr(self.inc_ptr),
         )
+        self._sell = None
+
+    def sell(self):
+        """Sliced block layout of the node graph (built on first use)."""
+        if self._sell is None:
+            L, st = self.lib, self.stream
+            n_slices = (self.n_nod + 31) // 32
+            base = self._empty(n_slices + 1, torch.int64)
+            ws = self._ws(L.fem_sell_workspace_bytes(self.n_nod))
+            n_slots = C.c_int64(0)
+            check(L.fem_sell_layout(C.byref(self.blocks), ptr(base), C.byref(n_slots), ptr(ws), ws.numel(), st),
+                  "fem_sell_layout")
+            col = self._empty(max(n_slots.value, 1), torch.int32)
+            check(L.fem_sell_columns(C.byref(self.blocks), ptr(base), ptr(col), st), "fem_sell_columns")
+            self._sell = (base, col, n_slots.value)
+        return self._sell
 
     def kmap(self) -> Tensor:
         """The reference's k_map (int64 here) for parity checks."""
@@ -293,16 +309,18 @@ class DeviceMesh:
         )
         return val
 
-    def assemble_bsr(self, ke: Tensor, con_mask: Tensor) -> Tensor:
-        bval = self._empty(self.n_blocks * self.d * self.d, torch.float32)
+    def assemble_sell(self, ke: Tensor, con_mask: Tensor) -> Tensor:
+        base, _, n_slots = self.sell()
+        sval = self._empty(max(n_slots, 1) * self.d * self.d, torch.float32)
         code = _lib.FEM_F64 if ke.dtype == torch.float64 else _lib.FEM_F32
         check(
-            self.lib.fem_assemble_bsr(
-                C.byref(self.blocks), code, ptr(ke), ptr(con_mask), ptr(bval), self.stream
+            self.lib.fem_assemble_sell(
+                C.byref(self.blocks), code, ptr(ke), ptr(con_mask), ptr(base), n_slots, ptr(sval),
+                self.stream,
             ),
-            "fem_assemble_bsr",
+            "fem_assemble_sell",
         )
-        return bval
+        return sval
 
     def build_system(self, mesh, mat, con_mask: Tensor, precision: str, keep_refs=()) -> LinearSystem:
         """Element stiffness, assembly and preconditioner for one tangent."""
@@ -325,17 +343,18 @@ class DeviceMesh:
             ws_bytes = L.fem_pcg_workspace_bytes(C.byref(sysm.matrix))
         elif precision == "mixed":
             ke = self.element_stiffness(mesh, mat, torch.float32)
-            sysm.bval = self.assemble_bsr(ke, con_mask)
+            sysm.bval = self.assemble_sell(ke, con_mask)
             del ke
+            base, col, _ = self.sell()
             sysm.precond = self._empty(self.n_nod * self.d * self.d, torch.float32)
             check(
-                L.fem_block_jacobi(C.byref(self.blocks), ptr(sysm.bval), ptr(sysm.precond),
+                L.fem_block_jacobi(C.byref(self.blocks), ptr(sysm.bval), ptr(base), ptr(sysm.precond),
                                    ptr(self.status), st),
                 "fem_block_jacobi",
             )
             sysm.matrix = _lib.FemMatrix(
-                _lib.FEM_FMT_BSR_F32, self.d, self.n_dofs, self.n_nod, ptr(self.nbr_ptr),
-                ptr(self.nbr), ptr(sysm.bval), ptr(sysm.precond),
+                _lib.FEM_FMT_SELL_F32, self.d, self.n_dofs, self.n_nod, ptr(base), ptr(col),
+                ptr(sysm.bval), ptr(sysm.precond),
             )
             sysm.op_mesh = mesh
             sysm.op_mat = mat

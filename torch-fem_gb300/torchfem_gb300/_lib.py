@@ -25,7 +25,7 @@ FEM_BREAKDOWN = 7
 FEM_QUAD1, FEM_HEXA1, FEM_TETRA2, FEM_TETRA1, FEM_TRIA1, FEM_QUAD2, FEM_TRIA2 = range(1, 8)
 FEM_MAT_ISO, FEM_MAT_GENERAL, FEM_MAT_TANGENT_IP = 1, 2, 3
 FEM_F64, FEM_F32 = 0, 1
-FEM_FMT_CSR_F64, FEM_FMT_BSR_F32 = 1, 2
+FEM_FMT_CSR_F64, FEM_FMT_SELL_F32 = 1, 2
 
 vp = C.c_void_p
 i64 = C.c_int64
@@ -137,9 +137,12 @@ _SIGNATURES = {
          vp, vp],
     ),
     "fem_assemble_csr": (C.c_int, [_P(FemBlocks), C.c_int, vp, vp, vp, vp, vp]),
-    "fem_assemble_bsr": (C.c_int, [_P(FemBlocks), C.c_int, vp, vp, vp, vp]),
+    "fem_sell_workspace_bytes": (C.c_size_t, [i64]),
+    "fem_sell_layout": (C.c_int, [_P(FemBlocks), vp, _P(i64), vp, C.c_size_t, vp]),
+    "fem_sell_columns": (C.c_int, [_P(FemBlocks), vp, vp, vp]),
+    "fem_assemble_sell": (C.c_int, [_P(FemBlocks), C.c_int, vp, vp, vp, i64, vp, vp]),
     "fem_jacobi": (C.c_int, [vp, vp, i64, vp, vp, vp]),
-    "fem_block_jacobi": (C.c_int, [_P(FemBlocks), vp, vp, vp, vp]),
+    "fem_block_jacobi": (C.c_int, [_P(FemBlocks), vp, vp, vp, vp, vp]),
     "fem_set_timing": (None, [C.c_int]),
     "fem_pcg_workspace_bytes": (C.c_size_t, [_P(FemMatrix)]),
     "fem_pcg": (
