@@ -301,6 +301,23 @@ size_t fem_pcg_workspace_bytes(const fem_matrix* A);
 int fem_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter,
             void* ws, size_t ws_bytes, fem_solve_info* info, void* stream);
 
+/* Allocation-free variant of fem_pcg (no counterpart in the reference).
+ * For callers that cannot allocate device memory where they solve — a host
+ * reaching this library through an FFI with no CUDA allocator binding, or a
+ * control loop that cannot accept cudaMalloc's implicit synchronisation or
+ * its failure under memory pressure.  Same arguments and results as
+ * fem_pcg without (ws, ws_bytes): the scratch is one static 6 MiB device
+ * array per GPU, held by every GPU that loads the library until the process
+ * exits, so A->n may be at most fem_pcg_static_max_unknowns() (131072);
+ * larger systems return FEM_BOUNDS with a message.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and
+ * should come before any stream capture on that device.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by
+ * the caller.  Nothing from a previous call is reused. */
+int64_t fem_pcg_static_max_unknowns(void);
+int fem_pcg_static(const fem_matrix* A, const double* b, double* x, double rtol,
+                   int64_t max_iter, fem_solve_info* info, void* stream);
+
 /* FP64 matrix-free operator y = A x of the condensed system: the element
  * kernels apply K to x with constrained entries zeroed, and y = x at
  * constrained DOFs (the matrix assemble_matrix builds, base.py:410-419). */

@@ -8,6 +8,7 @@
 // partials in a fixed tree, then a fixed-order sum by whichever CTA arrives
 // last.  No floating-point atomics are used anywhere.
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "fem_common.cuh"
@@ -1081,6 +1082,88 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
     set_last_error("mixed CG did not converge: %lld iterations, relative residual %.3e, code %d",
                    h.iters, h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0, h.done);
   return status_of(h.done);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------- allocation-free CG solve --
+// fem_pcg_static: the same preconditioned CG as fem_pcg, for callers that
+// cannot allocate device memory at the point where they solve — an embedding
+// host behind an FFI that has no binding to a CUDA allocator, or a control
+// loop where cudaMalloc's implicit synchronisation, or its failure under
+// memory pressure, is not acceptable.  Its scratch (CG vectors, reduction
+// partials, control block) lives in one file-scope device array that every
+// GPU loading this library holds until the process exits.  All calls share
+// that array: calls that overlap on the GPU (different streams or host
+// threads on the same device) race on it and must be serialised by the
+// caller.  Everything the solve reads from the array is rewritten at the
+// start of each call, so the contents left by a previous call do not matter.
+namespace tfg {
+
+constexpr size_t kStaticScratchBytes = size_t(6) << 20;  // 6 MiB per device
+constexpr int64_t kStaticMaxUnknowns = 131072;
+
+static __device__ __align__(256) unsigned char g_pcg_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static void* g_scratch_ptr[kMaxDevices] = {nullptr};
+static std::mutex g_scratch_mutex;
+
+// Device address of the scratch array on the current device.  The array's
+// name is a host-side stand-in, so the address is looked up once per device
+// with that device current.
+static int static_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return check_cuda("fem_pcg_static: cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_last_error("fem_pcg_static: device id %d beyond %d", dev, kMaxDevices);
+    return FEM_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (g_scratch_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_pcg_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_last_error("fem_pcg_static: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return FEM_CUDA_ERROR;
+    }
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return FEM_OK;
+}
+
+}  // namespace tfg
+
+extern "C" {
+
+int64_t fem_pcg_static_max_unknowns(void) { return tfg::kStaticMaxUnknowns; }
+
+int fem_pcg_static(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter,
+                   fem_solve_info* info, void* stream) {
+  int rc = validate_matrix(A);
+  if (rc) return rc;
+  const size_t need = fem_pcg_workspace_bytes(A);
+  if (A->n > kStaticMaxUnknowns || need > kStaticScratchBytes) {
+    set_last_error("fem_pcg_static: %lld unknowns exceed the static workspace limit of %lld "
+                   "(%zu bytes needed, %zu available); use fem_pcg with a caller workspace",
+                   (long long)A->n, (long long)kStaticMaxUnknowns, need, kStaticScratchBytes);
+    return FEM_BOUNDS;
+  }
+  void* ws = nullptr;
+  rc = static_scratch(&ws);
+  if (rc) return rc;
+  cudaStream_t st = as_stream(stream);
+  Vecs v;
+  layout(A, 0, &v, ws);
+  // The SpMV event timer creates CUDA events on first use; keep it off here.
+  const int timing = g_timing;
+  g_timing = 0;
+  if (A->format == FEM_FMT_CSR_F64) rc = run_pcg<1, double>(A, b, x, rtol, max_iter, v, info, st);
+  else if (A->block == 2) rc = run_pcg<2, float>(A, b, x, rtol, max_iter, v, info, st);
+  else rc = run_pcg<3, float>(A, b, x, rtol, max_iter, v, info, st);
+  g_timing = timing;
+  return rc;
 }
 
 }  // extern "C"

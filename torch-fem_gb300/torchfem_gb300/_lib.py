@@ -149,6 +149,10 @@ _SIGNATURES = {
         C.c_int,
         [_P(FemMatrix), vp, vp, C.c_double, i64, vp, C.c_size_t, _P(FemSolveInfo), vp],
     ),
+    "fem_pcg_static_max_unknowns": (i64, []),
+    "fem_pcg_static": (
+        C.c_int, [_P(FemMatrix), vp, vp, C.c_double, i64, _P(FemSolveInfo), vp]
+    ),
     "fem_apply64_workspace_bytes": (C.c_size_t, [_P(FemOperator64)]),
     "fem_apply64": (C.c_int, [_P(FemOperator64), vp, vp, vp, C.c_size_t, vp]),
     "fem_pcg_mixed_workspace_bytes": (C.c_size_t, [_P(FemMatrix), _P(FemOperator64)]),
