@@ -137,6 +137,16 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
+def cg_iteration_bytes(dm) -> float:
+    """Algorithmic bytes of one mixed-precision CG iteration: the FP32 block
+    matrix (36 value bytes and one int32 column per stored block, int64 slice
+    pointers) and twelve FP32 vector streams (SpMV: p, q; update: x, r read and
+    written, p, q read, z written; direction: z, p read, p written) plus the
+    3x3 block-Jacobi inverse (12 bytes per DOF)."""
+    n_slices = (dm.n_nod + 31) // 32
+    return dm.n_blocks * 40 + 8 * (n_slices + 1) + 48 * dm.n_dofs + 12 * dm.n_dofs
+
+
 def spmv_bytes(dm) -> float:
     """Algorithmic bytes of one FP32 block SpMV: 4*9 value bytes and one
     int32 column per stored block, x read once, y written once (the padding
@@ -217,6 +227,31 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_profile(args):
+    """A short, fixed launch sequence for ncu: setup, one assembly, then
+    exactly --profile-iters CG iterations of the chosen precision."""
+    from torchfem_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    _lib.load().fem_set_cg_path(1 if args.cg_path == "persistent" else 0)
+    m, forces = cube_workload(args.n, dev)
+    dm = m.device_mesh
+    kind, data = m.material.kernel_data(m.n_elem)
+    data = data.to(dev).contiguous()
+    mesh_s = dm.make_mesh(None)
+    mat = _lib.FemMaterial(kind, data.data_ptr())
+    con = m.constraints.reshape(-1).to(dev, torch.uint8).contiguous()
+    sysm = dm.build_system(mesh_s, mat, con, args.profile, keep_refs=(data, mesh_s, mat))
+    b = torch.where(con.bool(), torch.zeros_like(forces.reshape(-1)), forces.reshape(-1)).contiguous()
+    try:
+        dm.solve(sysm, b, 1e-30, max_iter=args.profile_iters)
+    except RuntimeError:
+        pass  # stopped by the iteration cap, as intended
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "n": args.n, "iterations": sysm.stats.iterations,
+                      "n_blocks": dm.n_blocks, "nnz": dm.nnz, "n_dofs": dm.n_dofs}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -227,10 +262,17 @@ def main():
     ap.add_argument("--stol", type=float, default=1e-10)
     ap.add_argument("--cpu-n", type=int, default=24, help="cube size of the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+                    help="profiling mode: assemble one system and run --profile-iters CG iterations")
+    ap.add_argument("--profile-iters", type=int, default=20)
+    ap.add_argument("--cg-path", choices=["persistent", "kernels"], default="persistent")
     args = ap.parse_args()
     torch.set_default_dtype(torch.float64)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile:
+        run_profile(args)
         return
 
     dist, rank, world, local = dist_setup()
@@ -239,6 +281,7 @@ def main():
     from torchfem_gb300 import _lib
 
     lib = _lib.load()
+    lib.fem_set_cg_path(1 if args.cg_path == "persistent" else 0)
     m, forces = cube_workload(args.n, dev)
     dm = m.device_mesh
     n_dofs = m.n_dofs
@@ -307,10 +350,20 @@ def main():
                   "rel_err_mixed_vs_fp64": {"u": err_u, "sigma": err_s, "grad": err_g}}
 
     peak, peak_kind = measured_peak_hbm()
-    avg_spmv_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
-    sb = spmv_bytes(dm)
-    achieved = sb / avg_spmv_s / 1e9 if avg_spmv_s else None
-    traffic_file = ROOT / "profiles" / "spmv_bsr_traffic.json"
+    persistent = lib.fem_get_cg_path() == 1
+    if persistent:
+        # CUDA events around each persistent CG launch; spmv_n counts the
+        # iterations those launches ran
+        unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
+        sb = cg_iteration_bytes(dm)
+        kernel_name = "k_pcg_persistent<3,float> (one CG iteration)"
+    else:
+        unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
+        sb = spmv_bytes(dm)
+        kernel_name = "k_spmv_sell<3>"
+    avg_spmv_s = unit_s
+    achieved = sb / unit_s / 1e9 if unit_s else None
+    traffic_file = ROOT / "profiles" / "spmv_sell_traffic.json"
     traffic = None
     if traffic_file.exists():
         try:
@@ -341,9 +394,9 @@ def main():
             "gpu_launches": launches,
             "e2e": {"value": e2e_ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-            "roofline": {"bound": "hbm", "kernel": "k_spmv_sell<3>", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                         "traffic": traffic, "algorithmic_bytes": sb, "avg_launch_us": avg_spmv_s * 1e6 if avg_spmv_s else None,
+                         "traffic": traffic, "algorithmic_bytes": sb, "avg_unit_us": avg_spmv_s * 1e6 if avg_spmv_s else None,
                          "peak_source": peak_kind},
             "clocks": clocks.summary(),
             **result,

@@ -289,8 +289,16 @@ typedef struct fem_solve_info {
   int64_t spmv_timed;      /* number of SpMV launches in spmv_ms */
 } fem_solve_info;
 
-/* Turns CUDA-event timing of every CG SpMV launch on (1) or off (0). */
+/* Turns CUDA-event timing of the CG on (1) or off (0).  With the persistent
+ * CG (default) spmv_ms covers whole iterations and spmv_timed counts them;
+ * with per-iteration kernels it covers the SpMV launches only. */
 void fem_set_timing(int enable);
+
+/* CG iteration path: 1 (default) one persistent cooperative kernel per run
+ * of iterations; 0 three kernels per iteration.  Also selectable with the
+ * environment variable TORCHFEM_GB300_CG=kernels. */
+void fem_set_cg_path(int persistent);
+int fem_get_cg_path(void);
 
 size_t fem_pcg_workspace_bytes(const fem_matrix* A);
 

@@ -250,3 +250,30 @@ def test_cg_iteration_cap_cuts_back_then_raises(cuda):
     m.forces[nodes[:, 0] == 1.0, 2] = -1.0
     with pytest.raises(RuntimeError, match="did not converge"):
         m.solve(cg_max_iter=2, max_cutbacks=2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_persistent_and_kernel_cg_paths_agree(cuda, precision):
+    """The persistent cooperative CG and the three-kernels-per-iteration CG
+    run the same iteration: same solution to 1e-10, same iteration counts."""
+    from torchfem_gb300 import _lib
+
+    lib = _lib.load()
+    nodes, el = mesh.cube_hexa(11, 11, 11)
+    gen = torch.Generator().manual_seed(0)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen) * 2 - 1) * 0.01
+    out, iters = {}, {}
+    try:
+        for path in (1, 0):
+            lib.fem_set_cg_path(path)
+            m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+            m.constraints[nodes[:, 0] == 0.0, :] = True
+            m.forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+            out[path] = m.solve(precision=precision, stol=1e-12)[0]
+            iters[path] = m.last_solve.iterations
+    finally:
+        lib.fem_set_cg_path(1)
+    assert rel(out[1], out[0]) <= 1e-10
+    for a, b in zip(iters[1], iters[0]):
+        assert abs(a - b) <= max(2, 0.02 * b)

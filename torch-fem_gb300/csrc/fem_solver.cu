@@ -138,7 +138,14 @@ __global__ void k_block_jacobi(const float* __restrict__ sval, const int64_t* __
 }
 
 // --------------------------------------------------------------------- CG ---
-enum { kDoneNo = 0, kDoneConverged = 1, kDoneMaxIter = 2, kDoneNonFinite = 3, kDoneBreakdown = 4 };
+enum {
+  kDoneNo = 0,
+  kDoneConverged = 1,
+  kDoneMaxIter = 2,
+  kDoneNonFinite = 3,
+  kDoneBreakdown = 4,
+  kDoneBarrierTimeout = 5
+};
 
 struct Ctrl {
   double rz;       // r.z of the current iterate
@@ -158,6 +165,9 @@ struct Ctrl {
   int replace;
   int mixed;
   unsigned int counter;
+  unsigned int bar_count;  // persistent kernel: grid-barrier arrivals
+  unsigned int bar_gen;    // persistent kernel: grid-barrier generation
+  int bar_error;           // persistent kernel: a barrier wait ran out
 };
 
 __device__ __forceinline__ bool arrive_last(unsigned int* counter) {
@@ -604,9 +614,273 @@ __global__ void k_copy_cast(int64_t n, const float* __restrict__ in, double* __r
   if (i < n) out[i] = (double)in[i];
 }
 
+
+// ------------------------------------------------------- persistent CG ------
+// One cooperative launch runs CG iterations until convergence, a pending FP64
+// replacement (mixed) or the iteration cap.  Each CTA owns a contiguous range
+// of rows (slices for the sliced layout): it computes q = A p for them, then
+// updates x, r, z and p for the same rows, so the only data crossing CTAs are
+// the gathered p values and three scalars per iteration.  Three grid barriers
+// per iteration; every CTA sums the per-CTA partials itself in one fixed
+// order, so all CTAs take identical decisions and results are deterministic.
+// The matrix is streamed with L2 evict_first; the CG vectors stay in L2.
+constexpr int kCsrTpr = 8;  // lanes per scalar CSR row
+constexpr int kPThreads = 512;
+constexpr int kPKS = 4;  // warps sharing one slice (sliced layout)
+
+struct PersistParams {
+  int64_t n;
+  int64_t n_rows;
+  const int64_t* row_ptr;  // CSR row pointers or sell_base
+  const int32_t* col;
+  const void* val;
+  const void* prec;
+  void* x;
+  void* r;
+  void* z;
+  void* p;
+  void* q;
+  double* partial;  // [3 * gridDim.x]
+  Ctrl* ctrl;
+  long long spin_limit;  // clock cycles a barrier wait may last
+};
+
+// Grid barrier with a bounded wait.  Returns false (on every thread) once
+// any CTA's wait has run out; the kernel then stops.
+__device__ __forceinline__ bool grid_barrier(Ctrl* c, long long spin_limit) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &c->bar_gen;
+    const unsigned int g0 = *gen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&c->bar_count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*gen == g0) {
+        if (*(volatile int*)&c->bar_error) break;
+        if (clock64() - t0 > spin_limit) {
+          atomicExch(&c->bar_error, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok = (*(volatile int*)&c->bar_error) == 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Sum over CTAs of partial[3*i + k], same fixed order in every CTA; the
+// result is returned to every thread.
+__device__ __forceinline__ double all_partials(const double* partial, int k, double* red) {
+  __shared__ double out;
+  double v = 0.0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v += __ldcg(partial + 3 * i + k);
+  v = block_sum(v, red);
+  if (threadIdx.x == 0) out = v;
+  __syncthreads();
+  const double r = out;
+  __syncthreads();
+  return r;
+}
+
+template <int G, typename VT>
+__global__ void __launch_bounds__(kPThreads, 2) k_pcg_persistent(PersistParams P) {
+  __shared__ double red[32];
+  __shared__ double2 red2[32];
+  __shared__ float ys[kPThreads / 32][G][32];
+  Ctrl* c = P.ctrl;
+  if (ctrl_idle(c)) return;
+  const int cta = blockIdx.x, NC = gridDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
+  VT* __restrict__ x = (VT*)P.x;
+  VT* __restrict__ r = (VT*)P.r;
+  VT* __restrict__ z = (VT*)P.z;
+  VT* __restrict__ p = (VT*)P.p;
+  VT* __restrict__ q = (VT*)P.q;
+  const uint64_t stream = l2_policy(false);
+  // rows owned by this CTA
+  int64_t row_lo, row_hi, s_lo = 0, s_hi = 0;
+  if constexpr (G == 1) {
+    row_lo = P.n_rows * cta / NC;
+    row_hi = P.n_rows * (cta + 1) / NC;
+  } else {
+    const int64_t ns = (P.n_rows + 31) >> 5;
+    s_lo = ns * cta / NC;
+    s_hi = ns * (cta + 1) / NC;
+    row_lo = min(s_lo * 32, P.n_rows);
+    row_hi = min(s_hi * 32, P.n_rows);
+  }
+  double rz = c->rz;
+  long long iters = c->iters;
+  const long long max_iter = c->max_iter;
+  const double tol2bb = c->tol2bb, delta2 = c->delta2, rr_ref = c->rr_ref;
+  const int mixed = c->mixed;
+  while (true) {
+    // ---- phase A: q = A p on own rows, partial p.q
+    double pq = 0.0;
+    if constexpr (G == 1) {
+      // groups of kCsrTpr lanes per scalar row, 32 / kCsrTpr rows per warp
+      constexpr int TPR = kCsrTpr;
+      const double* val = (const double*)P.val;
+      const int sub = lane % TPR;
+      const int64_t gid = (int64_t)warp * (32 / TPR) + lane / TPR;
+      const int64_t n_groups = (int64_t)NW * (32 / TPR);
+      for (int64_t row0 = row_lo; row0 < row_hi; row0 += n_groups) {
+        const int64_t row = row0 + gid;
+        double sacc = 0.0;
+        if (row < row_hi) {
+          const int64_t rs = P.row_ptr[row], re = P.row_ptr[row + 1];
+#pragma unroll 4
+          for (int64_t j = rs + sub; j < re; j += TPR)
+            sacc += ld_l2(val + j, stream) * (double)p[ld_l2(P.col + j, stream)];
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) sacc += __shfl_down_sync(0xffffffffu, sacc, o, TPR);
+        if (sub == 0 && row < row_hi) {
+          q[row] = (VT)sacc;
+          pq += (double)p[row] * sacc;
+        }
+      }
+    } else {
+      constexpr int DD = G * G;
+      const float* sval = (const float*)P.val;
+      const int NG = NW / kPKS, grp = warp / kPKS, kofs = warp % kPKS;
+      for (int64_t base = s_lo; base < s_hi; base += NG) {
+        const int64_t s = base + grp;
+        float y[G];
+#pragma unroll
+        for (int i = 0; i < G; ++i) y[i] = 0.f;
+        if (s < s_hi) {
+          const int64_t b0 = P.row_ptr[s];
+          const int len = (int)((P.row_ptr[s + 1] - b0) >> 5);
+          const int32_t* cp = P.col + b0 + lane;
+          const float* vp = sval + b0 * DD + lane;
+#pragma unroll 2
+          for (int k = kofs; k < len; k += kPKS) {
+            const int64_t cc = ld_l2(cp + (int64_t)k * 32, stream);
+            const float* vk = vp + (int64_t)k * DD * 32;
+            float m[DD];
+#pragma unroll
+            for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, stream);
+            float xv[G];
+#pragma unroll
+            for (int j = 0; j < G; ++j) xv[j] = (float)p[cc * G + j];
+#pragma unroll
+            for (int i = 0; i < G; ++i)
+#pragma unroll
+              for (int j = 0; j < G; ++j) y[i] = fmaf(m[i * G + j], xv[j], y[i]);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < G; ++i) ys[warp][i][lane] = y[i];
+        __syncthreads();
+        if (kofs == 0 && s < s_hi) {
+          const int64_t a = s * 32 + lane;
+          if (a < P.n_rows) {
+#pragma unroll
+            for (int i = 0; i < G; ++i) {
+              float t = ys[warp][i][lane];
+#pragma unroll
+              for (int v = 1; v < kPKS; ++v) t += ys[warp + v][i][lane];
+              q[a * G + i] = (VT)t;
+              pq += (double)p[a * G + i] * (double)t;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    pq = block_sum(pq, red);
+    if (threadIdx.x == 0) P.partial[3 * cta] = pq;
+    if (!grid_barrier(c, P.spin_limit)) break;
+    const double pq_tot = all_partials(P.partial, 0, red);
+    if (!(pq_tot > 0.0) || !isfinite(pq_tot)) {
+      if (cta == 0 && threadIdx.x == 0) {
+        c->done = isfinite(pq_tot) ? kDoneBreakdown : kDoneNonFinite;
+        c->iters = iters;
+      }
+      break;
+    }
+    const VT alpha = (VT)(rz / pq_tot);
+    // ---- phase B: x += alpha p, r -= alpha q, z = M r on own rows
+    double rzl = 0.0, rrl = 0.0;
+    for (int64_t a = row_lo + threadIdx.x; a < row_hi; a += blockDim.x) {
+      VT rv[G], zv[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int64_t k = a * G + g;
+        x[k] += alpha * p[k];
+        rv[g] = r[k] - alpha * q[k];
+        r[k] = rv[g];
+      }
+      apply_prec<G, VT>(P.prec, a, rv, zv);
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        z[a * G + g] = zv[g];
+        rzl += (double)rv[g] * (double)zv[g];
+        rrl += (double)rv[g] * (double)rv[g];
+      }
+    }
+    block_sum2(rzl, rrl, red2);
+    if (threadIdx.x == 0) {
+      P.partial[3 * cta + 1] = rzl;
+      P.partial[3 * cta + 2] = rrl;
+    }
+    if (!grid_barrier(c, P.spin_limit)) break;
+    const double rz_new = all_partials(P.partial, 1, red);
+    const double rr = all_partials(P.partial, 2, red);
+    iters += 1;
+    int stop = 0;  // 1 done, 2 replace
+    int done = kDoneNo;
+    if (!isfinite(rr) || !isfinite(rz_new)) {
+      stop = 1;
+      done = kDoneNonFinite;
+    } else if (mixed) {
+      if (rr <= tol2bb || rr <= delta2 * rr_ref) stop = 2;
+    } else if (rr <= tol2bb) {
+      stop = 1;
+      done = kDoneConverged;
+    }
+    if (!stop && iters >= max_iter) {
+      stop = 1;
+      done = kDoneMaxIter;
+    }
+    if (stop) {
+      if (cta == 0 && threadIdx.x == 0) {
+        c->iters = iters;
+        c->rr = rr;
+        c->alpha = (double)alpha;
+        c->rz_new = rz_new;
+        if (stop == 2) c->replace = 1;
+        else c->done = done;
+      }
+      break;
+    }
+    const VT beta = (VT)(rz_new / rz);
+    rz = rz_new;
+    // ---- phase C: p = z + beta p on own rows
+    for (int64_t k = row_lo * G + threadIdx.x; k < row_hi * G; k += blockDim.x) p[k] = z[k] + beta * p[k];
+    if (cta == 0 && threadIdx.x == 0) {
+      c->rz = rz;
+      c->rr = rr;
+      c->iters = iters;
+      c->beta = (double)beta;
+    }
+    if (!grid_barrier(c, P.spin_limit)) break;
+  }
+  if (cta == 0 && threadIdx.x == 0 && *(volatile int*)&c->bar_error) c->done = kDoneBarrierTimeout;
+}
+
 // ------------------------------------------------------------- host driver --
 constexpr int kThreads = 256;
-constexpr int kCsrTpr = 8;
 
 // SM count of the current device (cached per host thread).
 static int sm_count() {
@@ -658,8 +932,39 @@ static int64_t spmv_grid(const fem_matrix* A) {
   return sell_grid(A->n_rows);
 }
 
+// Persistent CG: CTAs per SM from the occupancy calculator (cached).
+template <int G, typename VT>
+static int persistent_blocks() {
+  static thread_local int blocks = 0;
+  if (blocks == 0) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_persistent<G, VT>, kPThreads, 0) !=
+            cudaSuccess ||
+        occ < 1)
+      occ = 1;
+    blocks = occ * sm_count();
+  }
+  return blocks;
+}
+
+// Upper bound on the persistent grid (at most 2048 / kPThreads CTAs per SM).
+static int64_t persistent_grid_bound() { return (int64_t)sm_count() * (2048 / kPThreads); }
+
+static int g_cg_path = -1;  // 1 persistent, 0 per-iteration kernels
+static thread_local bool g_persistent_refused = false;
+constexpr int FEM_COOP_TOO_LARGE = 100;  // internal: cooperative grid refused
+
+static bool use_persistent() {
+  if (g_cg_path < 0) {
+    const char* e = getenv("TORCHFEM_GB300_CG");
+    g_cg_path = (e && strcmp(e, "kernels") == 0) ? 0 : 1;
+  }
+  return g_cg_path == 1;
+}
+
 static int64_t max_grid(const fem_matrix* A) {
-  return std::max<int64_t>(spmv_grid(A), grid_for(A->n, kThreads));
+  return std::max<int64_t>(std::max<int64_t>(spmv_grid(A), grid_for(A->n, kThreads)),
+                           persistent_grid_bound());
 }
 
 static int status_of(int done) {
@@ -668,6 +973,7 @@ static int status_of(int done) {
     case kDoneMaxIter: return FEM_NOT_CONVERGED;
     case kDoneNonFinite: return FEM_NONFINITE;
     case kDoneBreakdown: return FEM_BREAKDOWN;
+    case kDoneBarrierTimeout: return FEM_CUDA_ERROR;
     default: return FEM_NOT_CONVERGED;
   }
 }
@@ -750,6 +1056,81 @@ static void launch_iteration(const fem_matrix* A, VT* x, VT* r, VT* z, VT* p, VT
   ::tfg::note_launch();
 }
 
+// One cooperative launch of the persistent CG kernel on the given vectors.
+template <int G, typename VT>
+static int launch_persistent(const fem_matrix* A, VT* x, VT* r, VT* z, VT* p, VT* q, double* partial,
+                             Ctrl* ctrl, cudaStream_t st) {
+  PersistParams P;
+  P.n = A->n;
+  P.n_rows = A->n_rows;
+  P.row_ptr = A->row_ptr;
+  P.col = A->col;
+  P.val = A->val;
+  P.prec = A->precond;
+  P.x = x;
+  P.r = r;
+  P.z = z;
+  P.p = p;
+  P.q = q;
+  P.partial = partial;
+  P.ctrl = ctrl;
+  P.spin_limit = 2000000000LL;  // about one second of clock cycles
+  void* args[] = {&P};
+  const int blocks = persistent_blocks<G, VT>();
+  const cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_pcg_persistent<G, VT>, dim3(blocks),
+                                                    dim3(kPThreads), args, 0, st);
+  ::tfg::note_launch();
+  if (e != cudaSuccess) {
+    set_last_error("persistent CG launch: %s", cudaGetErrorString(e));
+    cudaGetLastError();
+    return e == cudaErrorCooperativeLaunchTooLarge ? FEM_COOP_TOO_LARGE : FEM_CUDA_ERROR;
+  }
+  return FEM_OK;
+}
+
+// Runs CG iterations until the control block reports done or a pending
+// replacement: persistent kernel by default, per-iteration kernels when
+// TORCHFEM_GB300_CG=kernels.  Updates *h from the device.
+template <int G, typename VT>
+static int iterate(const fem_matrix* A, VT* x, VT* r, VT* z, VT* p, VT* q, double* partial, Ctrl* ctrl,
+                   Ctrl* h, bool timing, int* chunk, cudaStream_t st) {
+  const long long before = h->iters;
+  if (use_persistent() && !g_persistent_refused) {
+    if (timing) cudaEventRecord(g_timer.ev[0], st);
+    int rc = launch_persistent<G, VT>(A, x, r, z, p, q, partial, ctrl, st);
+    if (rc == FEM_COOP_TOO_LARGE) {
+      // the device cannot hold the whole grid at once (shared with other
+      // work): run this solve with per-iteration kernels instead
+      g_persistent_refused = true;
+      return iterate<G, VT>(A, x, r, z, p, q, partial, ctrl, h, timing, chunk, st);
+    }
+    if (rc) return rc;
+    if (timing) cudaEventRecord(g_timer.ev[1], st);
+    rc = read_ctrl(ctrl, h, st);
+    if (rc) return rc;
+    if (timing) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, g_timer.ev[0], g_timer.ev[1]) == cudaSuccess) {
+        g_timer.ms += t;
+        g_timer.timed += h->iters - before;
+      }
+    }
+    if (h->done == kDoneNo && !h->replace) {
+      set_last_error("persistent CG returned without progress");
+      return FEM_CUDA_ERROR;
+    }
+    return FEM_OK;
+  }
+  for (int c = 0; c < *chunk; ++c)
+    launch_iteration<G, VT>(A, x, r, z, p, q, partial, ctrl, st, timing ? c : -1);
+  TFG_CHECK_LAUNCH("CG iterate");
+  int rc = read_ctrl(ctrl, h, st);
+  if (rc) return rc;
+  if (timing) g_timer.collect((int)(h->iters - before));
+  *chunk = std::min(*chunk * 2, kMaxChunk);
+  return FEM_OK;
+}
+
 struct Vecs {
   Ctrl* ctrl;
   void *x, *r, *z, *p, *q;
@@ -795,6 +1176,7 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
     return check_cuda("fem_pcg ctrl");
   VT* xv = (G == 1) ? reinterpret_cast<VT*>(x) : reinterpret_cast<VT*>(v.x);
   const int64_t ng = A->n / G;
+  g_persistent_refused = false;
   k_init<G, VT><<<grid_for(ng, kThreads), kThreads, 0, st>>>(
       ng, b, xv, (VT*)v.r, (VT*)v.z, (VT*)v.p, A->precond, v.partial, v.ctrl, rtol * rtol);
       ::tfg::note_launch();
@@ -806,15 +1188,9 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
   g_timer.timed = 0;
   int chunk = 8;
   while (h.done == kDoneNo) {
-    const long long before = h.iters;
-    for (int c = 0; c < chunk; ++c)
-      launch_iteration<G, VT>(A, xv, (VT*)v.r, (VT*)v.z, (VT*)v.p, (VT*)v.q, v.partial, v.ctrl, st,
-                              timing ? c : -1);
-    TFG_CHECK_LAUNCH("fem_pcg iterate");
-    rc = read_ctrl(v.ctrl, &h, st);
+    rc = iterate<G, VT>(A, xv, (VT*)v.r, (VT*)v.z, (VT*)v.p, (VT*)v.q, v.partial, v.ctrl, &h, timing,
+                        &chunk, st);
     if (rc) return rc;
-    if (timing) g_timer.collect((int)(h.iters - before));
-    chunk = std::min(chunk * 2, kMaxChunk);
   }
   if (G != 1) k_copy_cast<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, (const float*)v.x, x);
   ::tfg::note_launch();
@@ -840,6 +1216,9 @@ using namespace tfg;
 extern "C" {
 
 void fem_set_timing(int enable) { g_timing = enable; }
+
+void fem_set_cg_path(int persistent) { g_cg_path = persistent ? 1 : 0; }
+int fem_get_cg_path(void) { return use_persistent() ? 1 : 0; }
 
 int fem_assemble_csr(const fem_blocks* B, int ke_dtype, const void* ke, const int64_t* row_ptr,
                      const uint8_t* con_mask, double* val, void* stream) {
@@ -1012,6 +1391,7 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
     return check_cuda("fem_pcg_mixed ctrl");
   const int G = A->block;
   const int64_t ng = A->n / G;
+  g_persistent_refused = false;
   float *xl = (float*)v.x, *r = (float*)v.r, *z = (float*)v.z, *p = (float*)v.p, *q = (float*)v.q;
   cudaMemsetAsync(x, 0, sizeof(double) * A->n, st);
   if (G == 2)
@@ -1053,16 +1433,9 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
       if (rc) return rc;
       continue;
     }
-    const long long before = h.iters;
-    for (int c = 0; c < chunk; ++c) {
-      if (G == 2) launch_iteration<2, float>(A, xl, r, z, p, q, v.partial, v.ctrl, st, timing ? c : -1);
-      else launch_iteration<3, float>(A, xl, r, z, p, q, v.partial, v.ctrl, st, timing ? c : -1);
-    }
-    TFG_CHECK_LAUNCH("fem_pcg_mixed iterate");
-    rc = read_ctrl(v.ctrl, &h, st);
+    if (G == 2) rc = iterate<2, float>(A, xl, r, z, p, q, v.partial, v.ctrl, &h, timing, &chunk, st);
+    else rc = iterate<3, float>(A, xl, r, z, p, q, v.partial, v.ctrl, &h, timing, &chunk, st);
     if (rc) return rc;
-    if (timing) g_timer.collect((int)(h.iters - before));
-    chunk = std::min(chunk * 2, kMaxChunk);
   }
   // fold whatever correction is left (max-iter exit) into x
   k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl);

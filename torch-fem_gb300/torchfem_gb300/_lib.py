@@ -144,6 +144,8 @@ _SIGNATURES = {
     "fem_jacobi": (C.c_int, [vp, vp, i64, vp, vp, vp]),
     "fem_block_jacobi": (C.c_int, [_P(FemBlocks), vp, vp, vp, vp, vp]),
     "fem_set_timing": (None, [C.c_int]),
+    "fem_set_cg_path": (None, [C.c_int]),
+    "fem_get_cg_path": (C.c_int, []),
     "fem_pcg_workspace_bytes": (C.c_size_t, [_P(FemMatrix)]),
     "fem_pcg": (
         C.c_int,
