@@ -212,6 +212,56 @@ int fem_element_vjp(const fem_mesh* mesh, const fem_material* mat, const double*
                     double* gthick, double* gde0, double* gve, int32_t* status, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Nonlinear material points fused with element integration.                */
+/* ------------------------------------------------------------------------ */
+
+/* Neo-Hookean solid at finite strain (Hyperelastic3D with
+ * psi = mu/2 (tr C - 3) - mu ln J + lambda/2 (ln J)^2, hyperelasticity.py:66-127,
+ * integrated with nlgeom as in base.py:1050-1083).  params [n_elem][2] =
+ * (mu, lambda).  Per point F = F_prev + grad(v) (F_prev, F_out
+ * [nip][n_elem][3][3]), P = dpsi/dF (P_out), tangent A = d2psi/dF2
+ * [nip][n_elem][81], flux = F P / J (base.py:1072-1074); all outputs but fe
+ * nullable.  v / con_* as in fem_element_force. */
+int fem_hyper_force(const fem_mesh* mesh, const double* params, const double* v,
+                    const uint8_t* con_mask, const double* con_values, int con_mode,
+                    const double* F_prev, double* fe, double* P_out, double* tangent,
+                    double* flux, double* F_out, int32_t* status, void* stream);
+
+/* Vector-Jacobian product of fem_hyper_force: cotangents g (assembled
+ * forces), gflux and gF (point outputs) pulled back to F_prev (gFprev),
+ * params (gparams [n_elem][2]) and the element field (gve). */
+int fem_hyper_vjp(const fem_mesh* mesh, const double* params, const double* v,
+                  const uint8_t* con_mask, const double* con_values, int con_mode,
+                  const double* F_prev, const double* g, const double* gflux, const double* gF,
+                  double* gFprev, double* gparams, double* gve, void* stream);
+
+/* J2 plasticity in plane strain with linear hardening sigma_f = sigma_y + H q
+ * (IsotropicPlasticityPlaneStrain, plasticity.py:430-590): trial stress,
+ * sigma_zz = nu (s_xx + s_yy) - E eps_z^p, radial return by the local Newton
+ * of plasticity.py:548-560 (tolerance tol, at most max_iter steps), stress,
+ * state (q, eps_z^p) and the consistent tangent of plasticity.py:577-588.
+ * params [n_elem][4] = (E, nu, sigma_y, H); sigma [nip][n_elem][2][2],
+ * state [nip][n_elem][2], tangent [nip][n_elem][16], hgrad = H_inc. */
+int fem_plastic_force(const fem_mesh* mesh, const double* params, double tol, int max_iter,
+                      const double* v, const uint8_t* con_mask, const double* con_values,
+                      int con_mode, const double* sigma_prev, const double* state_prev,
+                      const double* de0, double* fe, double* sigma_out, double* state_out,
+                      double* tangent, double* hgrad, int32_t* status, void* stream);
+
+/* Vector-Jacobian product of fem_plastic_force at the saved increment inputs
+ * (the checkpoint): cotangents of the assembled forces (g), of the stress
+ * and state outputs and of hgrad pulled back to sigma_prev, state_prev,
+ * thickness and the element field.  Differentiates the return mapping in
+ * closed form, which for linear hardening equals differentiating its local
+ * Newton iterations. */
+int fem_plastic_vjp(const fem_mesh* mesh, const double* params, double tol, int max_iter,
+                    const double* v, const uint8_t* con_mask, const double* con_values,
+                    int con_mode, const double* sigma_prev, const double* state_prev,
+                    const double* de0, const double* g, const double* gsig_out,
+                    const double* gstate_out, const double* ghgrad, double* gsig_prev,
+                    double* gstate_prev, double* gthick, double* gve, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Assembly: FEM.assemble_matrix (base.py:398-426).                         */
 /* ------------------------------------------------------------------------ */
 

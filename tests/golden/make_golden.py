@@ -204,15 +204,111 @@ def make_patterns(tf):
     )
 
 
+def _repo_mesh():
+    """This repository's mesh module (the reference has no 6-tet split or O-grid)."""
+    sys.path.insert(0, str(OUT.parents[1] / "torch-fem_gb300"))
+    from torchfem_gb300 import mesh
+
+    return mesh
+
+
+def hyper_problem(nx, ny, nz, seed=0):
+    """Config 4 geometry: box [0,3]x[0,1]^2 split into Tetra2, x=0 clamped,
+    x=3 pulled by +0.5; per-element E = 1000 (1 + 0.1 N(0,1)), nu = 0.45."""
+    from torchfem import Solid
+    from torchfem.materials import Hyperelastic3D
+
+    mesh = _repo_mesh()
+    nodes, elements = mesh.linear_to_quadratic(*mesh.box_tetra6(nx + 1, ny + 1, nz + 1, 3.0, 1.0, 1.0))
+    gen = torch.Generator().manual_seed(seed)
+    E = 1000.0 * (1.0 + 0.1 * torch.randn(len(elements), generator=gen, dtype=torch.float64))
+    E.requires_grad_(True)
+    nu = 0.45
+    mu = E / (2.0 * (1.0 + nu))
+    lbd = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+
+    def psi(F, params):
+        MU, LBD = params[0], params[1]
+        C = F.transpose(-1, -2) @ F
+        logJ = 0.5 * torch.logdet(C)
+        return MU / 2 * (torch.trace(C) - 3.0) - MU * logJ + LBD / 2 * logJ**2
+
+    model = Solid(nodes, elements, Hyperelastic3D(psi, torch.stack([mu, lbd], dim=-1)))
+    right = nodes[:, 0] == 3.0
+    model.constraints[nodes[:, 0] == 0.0, :] = True
+    model.constraints[right, 0] = True
+    model.displacements[right, 0] = 0.5
+    return model, E, right, nodes, elements
+
+
+def make_hyper(tf, nx=6, ny=2, nz=2):
+    model, E, right, nodes, elements = hyper_problem(nx, ny, nz)
+    inc = torch.linspace(0.0, 1.0, 11)
+    u, f, s, F, _ = model.solve(increments=inc, nlgeom=True, method="spsolve", rtol=1e-12, atol=1e-12,
+                                max_iter=20, differentiable_parameters=E)
+    R = f[right, 0].sum()
+    (gE,) = torch.autograd.grad(R, E)
+    np.savez_compressed(
+        OUT / "hyper_tet2_6x2x2.npz", nodes=nodes.numpy(), elements=elements.numpy(), E=E.detach().numpy(),
+        u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(), F=F.detach().numpy(),
+        reaction=R.detach().numpy(), grad_E=gE.numpy(),
+    )
+
+
+def plastic_problem(n_theta, n_rad):
+    """Config 5 geometry: 2 x 1 plate, centred hole r = 0.25, O-grid; left
+    edge fixed in x plus one y pin, right edge pulled to u_x = 0.02."""
+    from torchfem import Planar
+    from torchfem.materials import IsotropicPlasticityPlaneStrain
+
+    mesh = _repo_mesh()
+    nodes, elements = mesh.plate_hole_ogrid(n_theta, n_rad)
+    mat = IsotropicPlasticityPlaneStrain(
+        1000.0, 0.3, lambda q: 1.0 + 100.0 * q, lambda q: 100.0 * torch.ones_like(q)
+    )
+    t = torch.ones(len(elements), dtype=torch.float64, requires_grad=True)
+    model = Planar(nodes, elements, mat, thickness=t)
+    left = torch.isclose(nodes[:, 0], torch.tensor(0.0, dtype=torch.float64))
+    right = torch.isclose(nodes[:, 0], torch.tensor(2.0, dtype=torch.float64))
+    model.constraints[left, 0] = True
+    pin = torch.argmin(((nodes - torch.tensor([0.0, 0.5])) ** 2).sum(1))
+    model.constraints[pin, 1] = True
+    model.constraints[right, 0] = True
+    model.displacements[right, 0] = 0.02
+    return model, t, right, nodes, elements
+
+
+def make_plastic(tf, n_theta=32, n_rad=8):
+    model, t, right, nodes, elements = plastic_problem(n_theta, n_rad)
+    inc = torch.linspace(0.0, 1.0, 21)
+    # the reference's plane-strain tangent is not the exact derivative of its
+    # stress update, so Newton converges linearly and needs more iterations
+    u, f, s, F, st = model.solve(increments=inc, method="spsolve", rtol=1e-12, atol=1e-12, max_iter=80,
+                                 differentiable_parameters=t)
+    R = f[right, 0].sum()
+    (gt,) = torch.autograd.grad(R, t)
+    np.savez_compressed(
+        OUT / "plastic_ogrid_32x8.npz", nodes=nodes.numpy(), elements=elements.numpy(),
+        u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(), state=st.detach().numpy(),
+        reaction=R.detach().numpy(), grad_t=gt.numpy(),
+    )
+
+
+MAKERS = {
+    "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
+    "simp_small": lambda tf: make_simp(tf, 20, 10, "simp_20x10.npz"),
+    "simp_full": lambda tf: make_simp(tf, 400, 200, "simp_400x200.npz", sample=20),
+    "hyper": make_hyper, "plastic": make_plastic,
+}
+
+
 def main():
     torch.set_default_dtype(torch.float64)
     tf = import_reference()
-    make_c1(tf)
-    make_hexa_jitter3(tf)
-    make_patterns(tf)
-    make_simp(tf, 20, 10, "simp_20x10.npz")
-    make_simp(tf, 400, 200, "simp_400x200.npz", sample=20)
-    print("fixtures written to", OUT)
+    names = sys.argv[1:] or list(MAKERS)
+    for name in names:
+        MAKERS[name](tf)
+    print("fixtures written to", OUT, names)
 
 
 if __name__ == "__main__":

@@ -277,3 +277,86 @@ def test_persistent_and_kernel_cg_paths_agree(cuda, precision):
     assert rel(out[1], out[0]) <= 1e-10
     for a, b in zip(iters[1], iters[0]):
         assert abs(a - b) <= max(2, 0.02 * b)
+
+
+# ----------------------------------------------------------------- nonlinear --
+def _hyper_model(g):
+    from torchfem_gb300.materials import Hyperelastic3D, neo_hookean_psi
+
+    nodes = torch.tensor(g["nodes"])
+    el = torch.tensor(g["elements"])
+    E = torch.tensor(g["E"], requires_grad=True)
+    nu = 0.45
+    mu = E / (2.0 * (1.0 + nu))
+    lbd = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+
+    def psi(F, params):  # the user's energy, as in the reference benchmark
+        MU, LBD = params[0], params[1]
+        C = F.transpose(-1, -2) @ F
+        logJ = 0.5 * torch.logdet(C)
+        return MU / 2 * (torch.trace(C) - 3.0) - MU * logJ + LBD / 2 * logJ**2
+
+    m = Solid(nodes, el, Hyperelastic3D(psi, torch.stack([mu, lbd], dim=-1)))
+    right = nodes[:, 0] == 3.0
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    m.constraints[right, 0] = True
+    m.displacements[right, 0] = 0.5
+    return m, E, right
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_neo_hookean_tetra2_vs_reference(cuda, golden, precision):
+    """Config 4 at small size: Tetra2, Neo-Hookean, nlgeom, 10 increments;
+    tip reaction and its gradient w.r.t. per-element E against the reference."""
+    g = golden("hyper_tet2_6x2x2.npz")
+    m, E, right = _hyper_model(g)
+    # Newton to 1e-10 relative: 1e-12 is at this problem's FP64 residual floor
+    u, f, s, F, _ = m.solve(increments=torch.linspace(0.0, 1.0, 11), nlgeom=True, rtol=1e-10, atol=1e-10,
+                            max_iter=20, stol=1e-13, precision=precision, differentiable_parameters=E)
+    assert rel(u, g["u"]) <= 1e-8
+    assert rel(f, g["f"]) <= 1e-8
+    assert rel(s, g["sigma"]) <= 1e-8
+    assert rel(F, g["F"]) <= 1e-8
+    R = f[right, 0].sum()
+    assert abs(float(R.detach()) - float(g["reaction"])) <= 1e-8 * abs(float(g["reaction"]))
+    (gE,) = torch.autograd.grad(R, E)
+    assert rel(gE, g["grad_E"]) <= 1e-7
+
+
+def _plastic_model(g):
+    from torchfem_gb300.materials import IsotropicPlasticityPlaneStrain
+
+    nodes = torch.tensor(g["nodes"])
+    el = torch.tensor(g["elements"])
+    mat = IsotropicPlasticityPlaneStrain(1000.0, 0.3, lambda q: 1.0 + 100.0 * q,
+                                         lambda q: 100.0 * torch.ones_like(q))
+    t = torch.ones(len(el), dtype=torch.float64, requires_grad=True)
+    m = Planar(nodes, el, mat, thickness=t)
+    left = torch.isclose(nodes[:, 0], torch.tensor(0.0, dtype=torch.float64))
+    right = torch.isclose(nodes[:, 0], torch.tensor(2.0, dtype=torch.float64))
+    m.constraints[left, 0] = True
+    pin = torch.argmin(((nodes - torch.tensor([0.0, 0.5])) ** 2).sum(1))
+    m.constraints[pin, 1] = True
+    m.constraints[right, 0] = True
+    m.displacements[right, 0] = 0.02
+    return m, t, right
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_plane_strain_plasticity_vs_reference(cuda, golden, precision):
+    """Config 5 at small size: O-grid plate with hole, J2 plane strain,
+    20 increments; reaction and its gradient w.r.t. element thickness through
+    the per-increment checkpointed adjoint, against the reference."""
+    g = golden("plastic_ogrid_32x8.npz")
+    m, t, right = _plastic_model(g)
+    u, f, s, _, st = m.solve(increments=torch.linspace(0.0, 1.0, 21), rtol=1e-12, atol=1e-12, max_iter=80,
+                             stol=1e-13, precision=precision, differentiable_parameters=t)
+    assert float(st[:, 0].max()) > 0.0  # the plate yields
+    assert rel(u, g["u"]) <= 1e-8
+    assert rel(f, g["f"]) <= 1e-8
+    assert rel(s, g["sigma"]) <= 1e-8
+    assert rel(st, g["state"]) <= 1e-8
+    R = f[right, 0].sum()
+    assert abs(float(R.detach()) - float(g["reaction"])) <= 1e-8 * abs(float(g["reaction"]))
+    (gt,) = torch.autograd.grad(R, t)
+    assert rel(gt, g["grad_t"]) <= 1e-7

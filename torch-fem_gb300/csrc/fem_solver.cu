@@ -271,7 +271,7 @@ k_spmv_csr(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __rest
     const double tot = sum_partials(partial, gridDim.x, 1, 0, red);
     if (threadIdx.x == 0) {
       ctrl->counter = 0;
-      if (!(tot > 0.0) || !isfinite(tot)) {
+      if (tot == 0.0 || !isfinite(tot)) {
         ctrl->done = isfinite(tot) ? kDoneBreakdown : kDoneNonFinite;
       } else {
         ctrl->alpha = ctrl->rz / tot;
@@ -346,7 +346,7 @@ k_spmv_sell(int64_t n_rows, const int64_t* __restrict__ sell_base, const int32_t
     const double tot = sum_partials(partial, gridDim.x, 1, 0, red);
     if (threadIdx.x == 0) {
       ctrl->counter = 0;
-      if (!(tot > 0.0) || !isfinite(tot)) {
+      if (tot == 0.0 || !isfinite(tot)) {
         ctrl->done = isfinite(tot) ? kDoneBreakdown : kDoneNonFinite;
       } else {
         ctrl->alpha = ctrl->rz / tot;
@@ -802,7 +802,7 @@ __global__ void __launch_bounds__(kPThreads, 2) k_pcg_persistent(PersistParams P
     if (threadIdx.x == 0) P.partial[3 * cta] = pq;
     if (!grid_barrier(c, P.spin_limit)) break;
     const double pq_tot = all_partials(P.partial, 0, red);
-    if (!(pq_tot > 0.0) || !isfinite(pq_tot)) {
+    if (pq_tot == 0.0 || !isfinite(pq_tot)) {
       if (cta == 0 && threadIdx.x == 0) {
         c->done = isfinite(pq_tot) ? kDoneBreakdown : kDoneNonFinite;
         c->iters = iters;

@@ -369,14 +369,16 @@ class DeviceMesh:
         return sysm
 
     def solve(self, sysm: LinearSystem, b: Tensor, rtol: float, max_iter: int | None = None,
-              delta: float = 0.1) -> Tensor:
-        """x with A x = b (A the condensed system), from x = 0."""
+              delta: float = 0.1, refine: bool = True) -> Tensor:
+        """x with A x = b (A the condensed system), from x = 0.  For the mixed
+        system, refine=False runs the FP32 CG alone (an inner Newton solve
+        whose FP64 refinement is the Newton iteration itself)."""
         x = self._empty(self.n_dofs, torch.float64)
         info = _lib.FemSolveInfo()
         if max_iter is None:
             max_iter = 10 * self.n_dofs
         b = b.contiguous()
-        if sysm.precision == "fp64":
+        if sysm.precision == "fp64" or not refine:
             rc = self.lib.fem_pcg(
                 C.byref(sysm.matrix), ptr(b), ptr(x), rtol, max_iter, ptr(sysm.ws), sysm.ws.numel(),
                 C.byref(info), self.stream,
@@ -392,3 +394,74 @@ class DeviceMesh:
             raise RuntimeError(f"CG failed with exit code {info.iterations}")
         check(rc, "linear solve")
         return x
+
+    # ------------------------------------------------------ nonlinear points --
+    def hyper_force(self, mesh, params, v, con_mask=None, con_values=None, con_mode=0, F_prev=None,
+                    want_tangent=False, want_flux=False, want_F=False, want_P=False):
+        n_ip_e = self.nip * self.n_elem
+        fe = self._empty(self.n_elem * self.n_e * 3, torch.float64)
+        tangent = self._empty(n_ip_e * 81, torch.float64) if want_tangent else None
+        flux = self._empty(n_ip_e * 9, torch.float64) if want_flux else None
+        F_out = self._empty(n_ip_e * 9, torch.float64) if want_F else None
+        P_out = self._empty(n_ip_e * 9, torch.float64) if want_P else None
+        check(
+            self.lib.fem_hyper_force(
+                C.byref(mesh), ptr(params), ptr(v), ptr(con_mask), ptr(con_values), con_mode, ptr(F_prev),
+                ptr(fe), ptr(P_out), ptr(tangent), ptr(flux), ptr(F_out), ptr(self.status), self.stream,
+            ),
+            "fem_hyper_force",
+        )
+        return fe, tangent, flux, F_out, P_out
+
+    def hyper_vjp(self, mesh, params, v, g, con_mask=None, con_values=None, con_mode=0, F_prev=None,
+                  gflux=None, gF=None, want_Fprev=False, want_params=False, want_v=False):
+        n_ip_e = self.nip * self.n_elem
+        gFprev = self._empty(n_ip_e * 9, torch.float64) if want_Fprev else None
+        gparams = self._empty(self.n_elem * 2, torch.float64) if want_params else None
+        gve = self._empty(self.n_elem * self.n_e * 3, torch.float64) if want_v else None
+        check(
+            self.lib.fem_hyper_vjp(
+                C.byref(mesh), ptr(params), ptr(v), ptr(con_mask), ptr(con_values), con_mode, ptr(F_prev),
+                ptr(g), ptr(gflux), ptr(gF), ptr(gFprev), ptr(gparams), ptr(gve), self.stream,
+            ),
+            "fem_hyper_vjp",
+        )
+        gv = self.gather(gve)[0] if want_v else None
+        return gFprev, gparams, gv
+
+    def plastic_force(self, mesh, params, tol, max_iter, v, con_mask=None, con_values=None, con_mode=0,
+                      sigma_prev=None, state_prev=None, de0=None, want_tangent=False, want_outputs=False):
+        n_ip_e = self.nip * self.n_elem
+        fe = self._empty(self.n_elem * self.n_e * 2, torch.float64)
+        tangent = self._empty(n_ip_e * 16, torch.float64) if want_tangent else None
+        sig = self._empty(n_ip_e * 4, torch.float64) if want_outputs else None
+        state = self._empty(n_ip_e * 2, torch.float64) if want_outputs else None
+        hg = self._empty(n_ip_e * 4, torch.float64) if want_outputs else None
+        check(
+            self.lib.fem_plastic_force(
+                C.byref(mesh), ptr(params), tol, max_iter, ptr(v), ptr(con_mask), ptr(con_values), con_mode,
+                ptr(sigma_prev), ptr(state_prev), ptr(de0), ptr(fe), ptr(sig), ptr(state), ptr(tangent),
+                ptr(hg), ptr(self.status), self.stream,
+            ),
+            "fem_plastic_force",
+        )
+        return fe, tangent, sig, state, hg
+
+    def plastic_vjp(self, mesh, params, tol, max_iter, v, g, con_mask=None, con_values=None, con_mode=0,
+                    sigma_prev=None, state_prev=None, de0=None, gsig=None, gstate=None, gh=None,
+                    want_sig=False, want_state=False, want_thick=False, want_v=False):
+        n_ip_e = self.nip * self.n_elem
+        gsp = self._empty(n_ip_e * 4, torch.float64) if want_sig else None
+        gst = self._empty(n_ip_e * 2, torch.float64) if want_state else None
+        gth = self._empty(self.n_elem, torch.float64) if want_thick else None
+        gve = self._empty(self.n_elem * self.n_e * 2, torch.float64) if want_v else None
+        check(
+            self.lib.fem_plastic_vjp(
+                C.byref(mesh), ptr(params), tol, max_iter, ptr(v), ptr(con_mask), ptr(con_values), con_mode,
+                ptr(sigma_prev), ptr(state_prev), ptr(de0), ptr(g), ptr(gsig), ptr(gstate), ptr(gh),
+                ptr(gsp), ptr(gst), ptr(gth), ptr(gve), self.stream,
+            ),
+            "fem_plastic_vjp",
+        )
+        gv = self.gather(gve)[0] if want_v else None
+        return gsp, gst, gth, gv

@@ -136,6 +136,22 @@ _SIGNATURES = {
         [_P(FemMesh), _P(FemMaterial), vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
          vp, vp],
     ),
+    "fem_hyper_force": (
+        C.c_int, [_P(FemMesh), vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
+    ),
+    "fem_hyper_vjp": (
+        C.c_int, [_P(FemMesh), vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
+    ),
+    "fem_plastic_force": (
+        C.c_int,
+        [_P(FemMesh), vp, C.c_double, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp,
+         vp, vp],
+    ),
+    "fem_plastic_vjp": (
+        C.c_int,
+        [_P(FemMesh), vp, C.c_double, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp,
+         vp, vp, vp, vp],
+    ),
     "fem_assemble_csr": (C.c_int, [_P(FemBlocks), C.c_int, vp, vp, vp, vp, vp]),
     "fem_sell_workspace_bytes": (C.c_size_t, [i64]),
     "fem_sell_layout": (C.c_int, [_P(FemBlocks), vp, _P(i64), vp, C.c_size_t, vp]),

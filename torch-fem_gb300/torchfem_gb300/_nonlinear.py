@@ -1,0 +1,187 @@
+"""Newton solve and adjoint for materials with a changing tangent.
+
+Mirrors `NewtonRaphsonAdjoint` (src/torchfem/sparse.py:517-724) for the
+Neo-Hookean solid at finite strain and for plane-strain J2 plasticity.  The
+forward assembles the consistent tangent at every Newton iteration
+(base.py:1031-1033: stateful or nlgeom materials rebuild K).  Each increment's
+autograd node saves only its inputs (du, previous F / stress / state, loads,
+material data): that is the per-increment checkpoint.  The backward recomputes
+the tangent at the converged point from it, solves K lambda = grad_du on the
+GPU CG and pulls -lambda back through the material update with one vjp kernel
+(fem_hyper_vjp / fem_plastic_vjp).  Gradients reach the previous increment's
+state, so the reverse sweep chains across increments like the reference's
+autograd replay does.
+"""
+
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .sparse import SolveContext
+
+
+class NLContext(SolveContext):
+    """SolveContext plus the material kind and its local-Newton settings."""
+
+    def __init__(self, *args, kind: str, local_tol: float = 1e-5, local_max_iter: int = 10,
+                 nlgeom: bool = False, **kw):
+        super().__init__(*args, **kw)
+        self.kind = kind
+        self.local_tol = local_tol
+        self.local_max_iter = local_max_iter
+        self.nlgeom = nlgeom
+
+    def point_forces(self, v, con_mode, DU, F_prev, sigma_prev, state_prev, de0, mat_data, thickness,
+                     want_tangent=False, want_outputs=False):
+        """Element forces (and optionally tangent / point outputs) of a field."""
+        dm = self.dm
+        mesh = dm.make_mesh(thickness)
+        con = self.con_mask if con_mode else None
+        if self.kind == "neo_hookean":
+            fe, tangent, flux, F_out, P_out = dm.hyper_force(
+                mesh, mat_data, v, con, DU, con_mode, F_prev, want_tangent=want_tangent,
+                want_flux=want_outputs and self.nlgeom, want_F=want_outputs, want_P=want_outputs and not self.nlgeom,
+            )
+            outs = (flux if self.nlgeom else P_out, F_out, None)
+        else:
+            fe, tangent, sig, state, hg = dm.plastic_force(
+                mesh, mat_data, self.local_tol, self.local_max_iter, v, con, DU, con_mode, sigma_prev,
+                state_prev, de0, want_tangent=want_tangent, want_outputs=want_outputs,
+            )
+            outs = (sig, hg, state)
+        return fe, tangent, outs
+
+    def tangent_system(self, tangent, thickness):
+        mesh = self.dm.make_mesh(thickness)
+        mat = _lib.FemMaterial(_lib.FEM_MAT_TANGENT_IP, tangent.data_ptr())
+        self.system = self.dm.build_system(mesh, mat, self.con_mask, self.precision,
+                                           keep_refs=(tangent, thickness, mesh, mat))
+        self.system_key = None
+        return self.system
+
+
+class NewtonNonlinear(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, sc: NLContext, du, F_ext, DU, F_prev, sigma_prev, state_prev, de0, mat_data, thickness):
+        du = du.detach().clone()
+        res0 = None
+        converged = False
+        for i in range(sc.max_iter):
+            fe, tangent, _ = sc.point_forces(du, 1, DU, F_prev, sigma_prev, state_prev, de0, mat_data,
+                                             thickness, want_tangent=True)
+            res, sumsq = sc.dm.gather(fe, sub=F_ext, con_mask=sc.con_mask, con_mode=1, want_norm=True)
+            sc.dm.check_status("material update")
+            res_norm = float(sumsq.sqrt().item())
+            if i == 0:
+                res0 = res_norm
+            if sc.verbose:
+                last = sc.system.stats if sc.system is not None else None
+                cg = f" | CG {last.iterations} it, rel {last.rel_residual:.2e}" if (last and i) else ""
+                print(f"  newton {i:2d}  |res| = {res_norm:.6e}{cg}")
+            if res_norm < sc.rtol * res0 or res_norm < sc.atol:
+                converged = True
+                sc.newton_iterations.append(i)
+                break
+            if res_norm != res_norm or res_norm in (float("inf"), float("-inf")):
+                break
+            sc.tangent_system(tangent, thickness)
+            du = du - sc.solve(res, inner=True)
+        if not converged:
+            raise RuntimeError("Newton-Raphson iteration did not converge.")
+        ctx.sc = sc
+        ctx.save_for_backward(du, DU, F_prev, sigma_prev, state_prev, de0, mat_data, thickness)
+        return du
+
+    @staticmethod
+    def backward(ctx, grad_du):
+        sc: NLContext = ctx.sc
+        du, DU, F_prev, sigma_prev, state_prev, de0, mat_data, thickness = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        g = torch.where(sc.con_bool, torch.zeros_like(grad_du), grad_du).contiguous()
+        # recompute the converged tangent from the increment's checkpoint
+        _, tangent, _ = sc.point_forces(du, 1, DU, F_prev, sigma_prev, state_prev, de0, mat_data, thickness,
+                                        want_tangent=True)
+        sc.tangent_system(tangent, thickness)
+        lam = sc.solve(g)
+        neg = (-lam).contiguous()
+        dm = sc.dm
+        mesh = dm.make_mesh(thickness)
+        gF = gsig = gstate = gmat = gthick = gv = None
+        if sc.kind == "neo_hookean":
+            gF, gmat, gv = dm.hyper_vjp(mesh, mat_data, du, neg, sc.con_mask, DU, 1, F_prev,
+                                        want_Fprev=need[4], want_params=need[8], want_v=need[3])
+        else:
+            gsig, gstate, gthick, gv = dm.plastic_vjp(
+                mesh, mat_data, sc.local_tol, sc.local_max_iter, du, neg, sc.con_mask, DU, 1, sigma_prev,
+                state_prev, de0, want_sig=need[5], want_state=need[6],
+                want_thick=need[9] and thickness is not None, want_v=need[3],
+            )
+        g_DU = torch.where(sc.con_bool, gv, torch.zeros_like(gv)) if need[3] else None
+        return (
+            None, None, lam if need[2] else None, g_DU,
+            None if gF is None else gF.view_as(F_prev),
+            None if gsig is None else gsig.view_as(sigma_prev),
+            None if gstate is None else gstate.view_as(state_prev),
+            None,
+            None if gmat is None else gmat.view_as(mat_data),
+            gthick,
+        )
+
+
+class IntegrateNonlinear(torch.autograd.Function):
+    """Converged-state evaluation: (F_int, flux, F, state) of an increment."""
+
+    @staticmethod
+    def forward(ctx, sc: NLContext, du_eval, F_prev, sigma_prev, state_prev, de0, mat_data, thickness):
+        dm = sc.dm
+        fe, _, (flux, second, state) = sc.point_forces(du_eval, 0, None, F_prev, sigma_prev, state_prev, de0,
+                                                       mat_data, thickness, want_outputs=True)
+        f_int, _ = dm.gather(fe)
+        d = dm.d
+        shape = (dm.nip, dm.n_elem, d, d)
+        if sc.kind == "neo_hookean":
+            F_new = second.view(shape)
+            state_new = state_prev.clone()
+        else:
+            F_new = F_prev + second.view(shape)
+            state_new = state.view(state_prev.shape)
+        ctx.sc = sc
+        ctx.save_for_backward(du_eval, F_prev, sigma_prev, state_prev, de0, mat_data, thickness)
+        return f_int, flux.view(shape), F_new, state_new
+
+    @staticmethod
+    def backward(ctx, g_f, g_flux, g_F, g_state):
+        sc: NLContext = ctx.sc
+        du_eval, F_prev, sigma_prev, state_prev, de0, mat_data, thickness = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        dm = sc.dm
+        mesh = dm.make_mesh(thickness)
+        cont = lambda t: None if t is None else t.contiguous()  # noqa: E731
+        gF = gsig = gstate = gmat = gthick = gv = None
+        if sc.kind == "neo_hookean":
+            if not sc.nlgeom:
+                raise NotImplementedError("Hyperelastic3D gradients need nlgeom=True")
+            gF, gmat, gv = dm.hyper_vjp(mesh, mat_data, du_eval, cont(g_f), None, None, 0, F_prev,
+                                        gflux=cont(g_flux), gF=cont(g_F), want_Fprev=need[2],
+                                        want_params=need[6], want_v=need[1])
+            g_state_prev = g_state if need[4] else None
+        else:
+            gsig, gstate, gthick, gv = dm.plastic_vjp(
+                mesh, mat_data, sc.local_tol, sc.local_max_iter, du_eval, cont(g_f), None, None, 0,
+                sigma_prev, state_prev, de0, gsig=cont(g_flux), gstate=cont(g_state), gh=cont(g_F),
+                want_sig=need[3], want_state=need[4], want_thick=need[7] and thickness is not None,
+                want_v=need[1],
+            )
+            gF = g_F if need[2] else None  # F_new = F_prev + H
+            g_state_prev = None if gstate is None else gstate.view_as(state_prev)
+        return (
+            None,
+            gv,
+            None if gF is None else gF.reshape(F_prev.shape),
+            None if gsig is None else gsig.view_as(sigma_prev),
+            g_state_prev,
+            None,
+            None if gmat is None else gmat.view_as(mat_data),
+            gthick,
+        )

@@ -16,6 +16,7 @@ from . import _lib
 from ._device import DeviceMesh
 from .elements import Element
 from .materials import Material
+from ._nonlinear import IntegrateNonlinear, NewtonNonlinear, NLContext
 from .sparse import IntegrateMaterial, NewtonLinear, SolveContext
 
 _REFERENCE_METHODS = ("spsolve", "minres", "cg", "pardiso", "amgx")
@@ -163,19 +164,15 @@ class FEM:
         Same arguments and results as the reference.  `method` selects the
         GPU solver ("cg"/None: FP64 Jacobi-CG; "gb300-mixed": FP32 CG with
         FP64 residual replacement) and `precision` may override it.  `stol` is
-        the relative residual of each linear solve.  `use_cached_solve` and
-        `verbose` are accepted; the CG always starts from zero and nothing is
-        printed.
+        the relative residual of each linear solve.  `verbose` prints the
+        Newton residuals and CG iteration counts.  `use_cached_solve` is
+        accepted; the CG always starts from zero.
         """
         prec = resolve_precision(method, precision)
         if device is not None and torch.device(device).type != "cuda":
             raise RuntimeError("torchfem_gb300 solves on a CUDA device only")
         if alpha > 0.0:
             raise NotImplementedError("viscous stabilization (alpha > 0) is not implemented")
-        if nlgeom or self.n_state != 0:
-            raise NotImplementedError(
-                "nonlinear materials / nlgeom are not implemented on the GPU path yet"
-            )
         increments = torch.tensor([0.0, 1.0]) if increments is None else increments
         N = len(increments)
 
@@ -195,6 +192,13 @@ class FEM:
         con_mask = con_bool.to(torch.uint8).contiguous()
         assert self.material is not None
         mat_kind, mat_data = self.material.kernel_data(self.n_elem)
+        nonlinear = isinstance(mat_kind, str)
+        if not nonlinear and nlgeom:
+            raise NotImplementedError("nlgeom=True is implemented for Hyperelastic3D only")
+        if mat_kind == "neo_hookean" and not nlgeom:
+            raise NotImplementedError("Hyperelastic3D runs with nlgeom=True on the GPU path")
+        if mat_kind == "j2_plane_strain" and nlgeom:
+            raise NotImplementedError("plane-strain plasticity runs with nlgeom=False")
 
         with torch.set_grad_enabled(track):
             mat_data = mat_data.to(dev, torch.float64)
@@ -207,7 +211,14 @@ class FEM:
                 self._external_gradient.to(dev, torch.float64) if self._external_gradient_set else None
             )
 
-        sc = SolveContext(dm, con_mask, mat_kind, prec, max_iter, rtol, atol, stol, cg_max_iter)
+        if nonlinear:
+            mat = self.material
+            sc = NLContext(dm, con_mask, -1, prec, max_iter, rtol, atol, stol, cg_max_iter, kind=mat_kind,
+                           local_tol=float(getattr(mat, "tolerance", 1e-5)),
+                           local_max_iter=int(getattr(mat, "max_iter", 10)), nlgeom=nlgeom)
+        else:
+            sc = SolveContext(dm, con_mask, mat_kind, prec, max_iter, rtol, atol, stol, cg_max_iter)
+        sc.verbose = verbose
         self.last_solve = sc
 
         shape_ip = (dm.nip, self.n_elem, *self.n_flux)
@@ -231,16 +242,28 @@ class FEM:
                 min_step = abs(span) * cutback_factor**max_cutbacks
                 while abs(target - lam) > 1e-12 * max(1.0, abs(target)):
                     step = direction * min(step_size, abs(target - lam))
+                    if verbose:
+                        print(f"increment {n}: load {lam + step:.6g}")
                     F_ext = (lam + step) * F_neu
                     DU = step * DU_dir
                     de0 = None if de0_full is None else (step * de0_full).contiguous()
                     sigma_prev = flux_cur if track else flux_cur.detach()
+                    F_prev = grad_cur if track else grad_cur.detach()
+                    st_prev = state_cur if track else state_cur.detach()
                     try:
-                        du = NewtonLinear.apply(
-                            sc, du.detach(), F_ext.contiguous(), DU.contiguous(),
-                            sigma_prev.contiguous(), de0, mat_data, thickness,
-                        )
+                        if nonlinear:
+                            du = NewtonNonlinear.apply(
+                                sc, du.detach(), F_ext.contiguous(), DU.contiguous(), F_prev.contiguous(),
+                                sigma_prev.contiguous(), st_prev.contiguous(), de0, mat_data, thickness,
+                            )
+                        else:
+                            du = NewtonLinear.apply(
+                                sc, du.detach(), F_ext.contiguous(), DU.contiguous(),
+                                sigma_prev.contiguous(), de0, mat_data, thickness,
+                            )
                     except RuntimeError as err:
+                        if verbose:
+                            print(f"  cutback: {err}")
                         if isinstance(err, _lib.FemError) and err.code not in (
                             _lib.FEM_NOT_CONVERGED, _lib.FEM_NONFINITE, _lib.FEM_BREAKDOWN
                         ):
@@ -253,13 +276,21 @@ class FEM:
                             ) from err
                         continue
                     du_eval = torch.where(con_bool, DU, du)
-                    f_int, flux_new, h_inc = IntegrateMaterial.apply(
-                        sc, du_eval.contiguous(), sigma_prev.contiguous(), de0, mat_data, thickness
-                    )
+                    if nonlinear:
+                        f_int, flux_new, grad_new, state_new = IntegrateNonlinear.apply(
+                            sc, du_eval.contiguous(), F_prev.contiguous(), sigma_prev.contiguous(),
+                            st_prev.contiguous(), de0, mat_data, thickness,
+                        )
+                        grad_cur = grad_new
+                        state_cur = state_new
+                    else:
+                        f_int, flux_new, h_inc = IntegrateMaterial.apply(
+                            sc, du_eval.contiguous(), sigma_prev.contiguous(), de0, mat_data, thickness
+                        )
+                        grad_cur = grad_cur + h_inc
                     f_cur = f_int
                     u_cur = u_cur + du_eval
                     flux_cur = flux_new
-                    grad_cur = grad_cur + h_inc
                     du = du_eval
                     lam += step
                     step_size = min(growth_factor * step_size, abs(span))

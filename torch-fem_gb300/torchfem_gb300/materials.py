@@ -139,3 +139,169 @@ def _planar_c(c_diag: Tensor, c_off: Tensor, c_shear: Tensor, E: Tensor) -> Tens
         c_off, z, z, c_diag,
     ]
     return torch.stack(rows, dim=-1).reshape(*E.shape, 2, 2, 2, 2)
+
+
+# ------------------------------------------------------------ finite strain ---
+def neo_hookean_psi(F: Tensor, params: Tensor) -> Tensor:
+    """Neo-Hookean energy with params = (mu, lambda):
+    psi = mu/2 (tr C - 3) - mu ln J + lambda/2 (ln J)^2, C = F^T F."""
+    mu, lbd = params[0], params[1]
+    C = F.transpose(-1, -2) @ F
+    log_j = 0.5 * torch.logdet(C)
+    return mu / 2 * (torch.trace(C) - 3.0) - mu * log_j + lbd / 2 * log_j**2
+
+
+def _neo_hookean_stress(F: Tensor, mu: Tensor, lbd: Tensor) -> Tensor:
+    Fit = torch.linalg.inv(F).transpose(-1, -2)
+    log_j = torch.log(torch.det(F))
+    return mu[..., None, None] * F + (lbd * log_j - mu)[..., None, None] * Fit
+
+
+class Hyperelastic3D(Material):
+    """Hyperelastic material defined by an energy psi(F, params)
+    (materials/hyperelasticity.py:12-127).
+
+    `step` differentiates psi with torch.func like the reference.  The GPU
+    kernels implement the Neo-Hookean energy in closed form; a psi is accepted
+    for them if it is `neo_hookean_psi` or agrees with it (stress to 1e-10 on
+    sample deformations), with params = (mu, lambda) per element.
+    """
+
+    def __init__(self, psi, params, rho=1.0):
+        self.psi = psi
+        self.params = torch.as_tensor(params)
+        self.n_state = 0
+        self.rho = torch.as_tensor(rho)
+        self.is_vectorized = self.params.dim() > 1
+
+    def step(self, H_inc, F, stress, state, de0, cl, iter):
+        from torch.func import jacrev, vmap
+
+        params = self.params if self.params.dim() > 1 else self.params.expand(H_inc.shape[0], -1)
+        with torch.enable_grad():
+            F_new = (F + H_inc).requires_grad_(True)
+            P_new = vmap(jacrev(self.psi))(F_new, params)
+            ddsdde = vmap(jacrev(jacrev(self.psi)))(F_new, params)
+        return P_new, state, ddsdde
+
+    def _is_neo_hookean(self) -> bool:
+        if self.psi is neo_hookean_psi or getattr(self.psi, "gpu_model", None) == "neo_hookean":
+            return True
+        from torch.func import jacrev
+
+        p = self.params.detach().reshape(-1, self.params.shape[-1])[0].to(torch.float64)
+        if p.numel() != 2:
+            return False
+        gen = torch.Generator().manual_seed(0)
+        for _ in range(3):
+            F = torch.eye(3, dtype=torch.float64) + 0.2 * torch.rand(3, 3, generator=gen, dtype=torch.float64)
+            try:
+                P = jacrev(self.psi)(F, p)
+            except Exception:  # noqa: BLE001 - any failure means "not the known energy"
+                return False
+            ref = _neo_hookean_stress(F, p[0], p[1])
+            if not torch.allclose(P.to(torch.float64), ref, rtol=1e-10, atol=1e-10 * float(ref.abs().max())):
+                return False
+        return True
+
+    def kernel_data(self, n_elem: int):
+        if not self._is_neo_hookean():
+            raise NotImplementedError(
+                "Hyperelastic3D runs on the GPU for the Neo-Hookean energy only (params = (mu, lambda))"
+            )
+        data = self.params.to(torch.float64)
+        if data.dim() == 1:
+            data = data.expand(n_elem, 2)
+        return "neo_hookean", data.contiguous()
+
+
+# --------------------------------------------------------------- plasticity ---
+class IsotropicPlasticityPlaneStrain(IsotropicElasticityPlaneStrain):
+    """J2 plasticity in plane strain (materials/plasticity.py:430-590), with
+    state (q, eps_z^p).  The GPU kernels implement linear hardening
+    sigma_f(q) = sigma_y + H q; other hardening laws raise on solve."""
+
+    def __init__(self, E, nu, sigma_f, sigma_f_prime, tolerance=1e-5, max_iter=10, rho=1.0):
+        super().__init__(E, nu, rho)
+        self.sigma_f = sigma_f
+        self.sigma_f_prime = sigma_f_prime
+        self.n_state = 2
+        self.tolerance = tolerance
+        self.max_iter = max_iter
+
+    def _linear_hardening(self):
+        q = torch.tensor([0.0, 0.1, 1.0, 10.0], dtype=torch.float64)
+        sf = torch.as_tensor(self.sigma_f(q), dtype=torch.float64)
+        sfp = torch.as_tensor(self.sigma_f_prime(q), dtype=torch.float64)
+        if sf.shape != q.shape:
+            sf = sf.expand(q.shape)
+        if sfp.shape != q.shape:
+            sfp = sfp.expand(q.shape)
+        sy, H = float(sf[0]), float(sfp[0])
+        ok = torch.allclose(sf, sy + H * q, rtol=1e-12, atol=1e-12) and torch.allclose(
+            sfp, torch.full_like(q, H), rtol=1e-12, atol=1e-12
+        )
+        if not ok:
+            raise NotImplementedError(
+                "IsotropicPlasticityPlaneStrain runs on the GPU for linear hardening "
+                "sigma_f(q) = sigma_y + H q only"
+            )
+        return sy, H
+
+    def kernel_data(self, n_elem: int):
+        sy, H = self._linear_hardening()
+        E = torch.as_tensor(self.E, dtype=torch.float64).expand(n_elem)
+        nu = torch.as_tensor(self.nu, dtype=torch.float64).expand(n_elem)
+        data = torch.stack([E, nu, torch.full_like(E, sy), torch.full_like(E, H)], dim=-1)
+        return "j2_plane_strain", data.contiguous()
+
+    def step(self, H_inc, F, stress, state, de0, cl, iter):
+        """Return mapping of plasticity.py:504-590 written with torch ops."""
+        from math import sqrt
+
+        de = 0.5 * (H_inc.transpose(-1, -2) + H_inc)
+        C = self.C if self.C.dim() > 4 else self.C.expand(H_inc.shape[0], 2, 2, 2, 2)
+        E = torch.as_tensor(self.E).expand(H_inc.shape[0])
+        nu = torch.as_tensor(self.nu).expand(H_inc.shape[0])
+        G = torch.as_tensor(self.G).expand(H_inc.shape[0])
+        q, ez = state[..., 0].clone(), state[..., 1].clone()
+        s2 = stress + torch.einsum("...ijkl,...kl->...ij", C, de - de0)
+        s3 = torch.zeros(stress.shape[0], 3, 3, dtype=stress.dtype)
+        s3[..., :2, :2] = s2
+        s3[..., 2, 2] = nu * (s2[..., 0, 0] + s2[..., 1, 1]) - E * ez
+        dev = s3 - torch.einsum("...ii->...", s3)[..., None, None] / 3 * torch.eye(3, dtype=s3.dtype)
+        nrm = torch.linalg.norm(dev, dim=(-1, -2))
+        f = nrm - sqrt(2.0 / 3.0) * self.sigma_f(q)
+        fm = f > 0
+        stress_new = s2.clone()
+        ddsdde = C.clone()
+        if fm.any():
+            n = dev[fm] / nrm[fm][:, None, None]
+            dG = torch.zeros_like(f[fm])
+            qf = q[fm]
+            for _ in range(self.max_iter):
+                res = nrm[fm] - 2.0 * G[fm] * dG - sqrt(2.0 / 3.0) * self.sigma_f(qf)
+                dd = res / (2.0 * G[fm] + 2.0 / 3.0 * self.sigma_f_prime(qf))
+                dG = dG + dd
+                qf = qf + sqrt(2.0 / 3.0) * dd
+                if (res.abs() < self.tolerance).all():
+                    break
+            stress_new[fm] = (s3[fm] - (2.0 * G[fm] * dG)[:, None, None] * n)[..., :2, :2]
+            q[fm] = qf
+            ez[fm] = ez[fm] + dG * n[:, 2, 2]
+            Gf = G[fm]
+            A = 2.0 * Gf / (1.0 + self.sigma_f_prime(qf) / (3.0 * Gf))
+            B = 4.0 * Gf**2 * dG / nrm[fm]
+            n00, n11, n01, n10 = n[:, 0, 0], n[:, 1, 1], n[:, 0, 1], n[:, 1, 0]
+            d = ddsdde[fm]
+            d[:, 0, 0, 0, 0] += -A * n00**2 - B * (2 / 3 - n00**2)
+            d[:, 1, 1, 1, 1] += -A * n11**2 - B * (2 / 3 - n11**2)
+            d[:, 0, 0, 1, 1] += -A * n00 * n11 - B * (-1 / 3 - n00 * n11)
+            d[:, 1, 1, 0, 0] += -A * n00 * n11 - B * (-1 / 3 - n00 * n11)
+            d[:, 0, 1, 0, 1] += -A * n01**2 - B * (1 / 2 - n01**2)
+            d[:, 0, 1, 1, 0] += -A * n01**2 - B * (1 / 2 - n10**2)
+            d[:, 1, 0, 0, 1] += -A * n10**2 - B * (1 / 2 - n01**2)
+            d[:, 1, 0, 1, 0] += -A * n10**2 - B * (1 / 2 - n10**2)
+            ddsdde[fm] = d
+        state_new = torch.stack([q, ez], dim=-1)
+        return stress_new, state_new, ddsdde

@@ -47,6 +47,8 @@ class SolveContext:
         self.system_key = None
         self.iterations: list[int] = []
         self.newton_iterations: list[int] = []
+        self.verbose = False
+        self.inner_rtol = 1e-6
 
     def structs(self, mat_data: Tensor, thickness: Tensor | None):
         from . import _lib
@@ -67,9 +69,16 @@ class SolveContext:
             self.system_key = key
         return self.system
 
-    def solve(self, b: Tensor) -> Tensor:
+    def solve(self, b: Tensor, inner: bool = False) -> Tensor:
+        """Linear solve on the current system.  inner=True marks a Newton
+        correction of a nonlinear material: in mixed precision it runs the FP32
+        CG alone to max(stol, inner_rtol), the FP64 Newton residual being the
+        refinement."""
         assert self.system is not None
-        x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, self.delta)
+        if inner and self.precision == "mixed":
+            x = self.dm.solve(self.system, b, max(self.stol, self.inner_rtol), self.cg_max_iter, refine=False)
+        else:
+            x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, self.delta)
         self.iterations.append(self.system.stats.iterations)
         return x
 
@@ -97,6 +106,10 @@ class NewtonLinear(torch.autograd.Function):
             res_norm = float(sumsq.sqrt().item())
             if i == 0:
                 res0 = res_norm
+            if sc.verbose:
+                last = sc.system.stats if sc.system is not None else None
+                cg = f" | CG {last.iterations} it, rel {last.rel_residual:.2e}" if (last and i) else ""
+                print(f"  newton {i:2d}  |res| = {res_norm:.6e}{cg}")
             if res_norm < sc.rtol * res0 or res_norm < sc.atol:
                 converged = True
                 sc.newton_iterations.append(i)
