@@ -19,6 +19,9 @@ Restated reference code (paths relative to the torch-fem repository):
   assemble_rhs         src/torchfem/base.py:428-445
   solve (linear)       src/torchfem/base.py:597-923 with sparse.py:271-514
   adjoint              src/torchfem/sparse.py:641-724
+  Neo-Hookean point    materials/hyperelasticity.py:117-123 with the energy of
+                       benchmarks/hyperelasticity.py:24-30
+  J2 plane strain      materials/plasticity.py:504-590
 """
 
 from __future__ import annotations
@@ -303,3 +306,72 @@ def rect_quad(Nx, Ny, Lx=1.0, Ly=1.0):
     ids = np.arange(Nx * Ny).reshape(Nx, Ny)
     c = lambda i, j: ids[i : Nx - 1 + i, j : Ny - 1 + j].ravel()  # noqa: E731
     return nodes, np.stack([c(0, 0), c(1, 0), c(1, 1), c(0, 1)], 1)
+
+
+# ------------------------------------------------------- nonlinear points ---
+def neo_hookean_point(F, mu, lam):
+    """First Piola stress and tangent of the Neo-Hookean energy
+    psi = mu/2 (tr C - 3) - mu ln J + lam/2 (ln J)^2 (the energy of
+    benchmarks/hyperelasticity.py:24-30, differentiated by jacrev in
+    materials/hyperelasticity.py:117-123).  F [n, 3, 3]; mu, lam [n]."""
+    Fi = np.linalg.inv(F)
+    lnJ = np.log(np.linalg.det(F))
+    P = mu[:, None, None] * F + (lam * lnJ - mu)[:, None, None] * Fi.transpose(0, 2, 1)
+    I = np.eye(3)
+    A = (mu[:, None, None, None, None] * np.einsum("ik,JL->iJkL", I, I)
+         + lam[:, None, None, None, None] * np.einsum("nJi,nLk->niJkL", Fi, Fi)
+         + (mu - lam * lnJ)[:, None, None, None, None] * np.einsum("nJk,nLi->niJkL", Fi, Fi))
+    return P, A
+
+
+def j2_plane_strain_point(H_inc, stress, state, E, nu, sigma_y, hard, de0=None, tol=1e-5, max_iter=10):
+    """Return mapping of IsotropicPlasticityPlaneStrain.step
+    (materials/plasticity.py:504-590) with linear hardening
+    sigma_f(q) = sigma_y + hard q.  H_inc, stress [n, 2, 2]; state [n, 2]
+    = (q, eps_z^p).  Returns stress_new, state_new, ddsdde [n, 2, 2, 2, 2]."""
+    n = H_inc.shape[0]
+    lbd = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    G = E / (2.0 * (1.0 + nu))
+    C = elastic_c("plane_strain", E, nu, n)
+    de = 0.5 * (H_inc.transpose(0, 2, 1) + H_inc) - (0.0 if de0 is None else de0)
+    q = state[:, 0].copy()
+    ez = state[:, 1].copy()
+    s2 = stress + np.einsum("nijkl,nkl->nij", C, de)
+    s3 = np.zeros((n, 3, 3))
+    s3[:, :2, :2] = s2
+    s3[:, 2, 2] = nu * (s2[:, 0, 0] + s2[:, 1, 1]) - E * ez
+    dev = s3 - np.trace(s3, axis1=1, axis2=2)[:, None, None] / 3.0 * np.eye(3)
+    nrm = np.linalg.norm(dev, axis=(1, 2))
+    c = np.sqrt(2.0 / 3.0)
+    fm = nrm - c * (sigma_y + hard * q) > 0
+    stress_new = s2.copy()
+    ddsdde = C.copy()
+    if fm.any():
+        nn = dev[fm] / nrm[fm][:, None, None]
+        Gf = np.broadcast_to(G, (n,))[fm]
+        dG = np.zeros(fm.sum())
+        qf = q[fm]
+        for _ in range(max_iter):
+            res = nrm[fm] - 2.0 * Gf * dG - c * (sigma_y + hard * qf)
+            dd = res / (2.0 * Gf + 2.0 / 3.0 * hard)
+            dG = dG + dd
+            qf = qf + c * dd
+            if (np.abs(res) < tol).all():
+                break
+        stress_new[fm] = (s3[fm] - (2.0 * Gf * dG)[:, None, None] * nn)[:, :2, :2]
+        q[fm] = qf
+        ez[fm] = ez[fm] + dG * nn[:, 2, 2]
+        A = 2.0 * Gf / (1.0 + hard / (3.0 * Gf))
+        B = 4.0 * Gf**2 * dG / nrm[fm]
+        n00, n11, n01, n10 = nn[:, 0, 0], nn[:, 1, 1], nn[:, 0, 1], nn[:, 1, 0]
+        d = ddsdde[fm]
+        d[:, 0, 0, 0, 0] += -A * n00**2 - B * (2 / 3 - n00**2)
+        d[:, 1, 1, 1, 1] += -A * n11**2 - B * (2 / 3 - n11**2)
+        d[:, 0, 0, 1, 1] += -A * n00 * n11 - B * (-1 / 3 - n00 * n11)
+        d[:, 1, 1, 0, 0] += -A * n00 * n11 - B * (-1 / 3 - n00 * n11)
+        d[:, 0, 1, 0, 1] += -A * n01**2 - B * (1 / 2 - n01**2)
+        d[:, 0, 1, 1, 0] += -A * n01**2 - B * (1 / 2 - n10**2)
+        d[:, 1, 0, 0, 1] += -A * n10**2 - B * (1 / 2 - n01**2)
+        d[:, 1, 0, 1, 0] += -A * n10**2 - B * (1 / 2 - n10**2)
+        ddsdde[fm] = d
+    return stress_new, np.stack([q, ez], axis=-1), ddsdde

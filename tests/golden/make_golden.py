@@ -294,7 +294,44 @@ def make_plastic(tf, n_theta=32, n_rad=8):
     )
 
 
+def make_material_points(tf):
+    """Per-point outputs of the reference's Material.step for the
+    Neo-Hookean energy (via jacrev) and plane-strain J2 plasticity."""
+    from torchfem.materials import Hyperelastic3D, IsotropicPlasticityPlaneStrain
+
+    gen = torch.Generator().manual_seed(5)
+    n = 16
+    F = torch.eye(3) + 0.15 * (torch.rand(n, 3, 3, generator=gen, dtype=torch.float64) - 0.5)
+    mu = 300.0 + 100.0 * torch.rand(n, generator=gen, dtype=torch.float64)
+    lam = 800.0 + 400.0 * torch.rand(n, generator=gen, dtype=torch.float64)
+
+    def psi(Fm, params):
+        MU, LBD = params[0], params[1]
+        Cm = Fm.transpose(-1, -2) @ Fm
+        logJ = 0.5 * torch.logdet(Cm)
+        return MU / 2 * (torch.trace(Cm) - 3.0) - MU * logJ + LBD / 2 * logJ**2
+
+    hy = Hyperelastic3D(psi, torch.stack([mu, lam], dim=-1))
+    zero = torch.zeros(n, 3, 3)
+    P, _, A = hy.step(zero, F, zero, torch.zeros(n, 0), zero, None, 0)
+    pl = IsotropicPlasticityPlaneStrain(
+        1000.0, 0.3, lambda q: 1.0 + 100.0 * q, lambda q: 100.0 * torch.ones_like(q)
+    ).vectorize(n)
+    H = 4e-3 * (torch.rand(n, 2, 2, generator=gen, dtype=torch.float64) - 0.5)
+    stress = 2.0 * (torch.rand(n, 2, 2, generator=gen, dtype=torch.float64) - 0.5)
+    stress = 0.5 * (stress + stress.transpose(-1, -2))
+    state = torch.stack([0.01 * torch.rand(n, generator=gen, dtype=torch.float64),
+                         1e-3 * (torch.rand(n, generator=gen, dtype=torch.float64) - 0.5)], dim=-1)
+    s_new, st_new, D = pl.step(H, None, stress, state, torch.zeros(n, 2, 2), None, 0)
+    np.savez_compressed(
+        OUT / "material_points.npz", F=F.numpy(), mu=mu.numpy(), lam=lam.numpy(), P=P.detach().numpy(),
+        A=A.detach().numpy(), H=H.numpy(), stress=stress.numpy(), state=state.numpy(),
+        stress_new=s_new.numpy(), state_new=st_new.numpy(), ddsdde=D.numpy(),
+    )
+
+
 MAKERS = {
+    "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
     "simp_small": lambda tf: make_simp(tf, 20, 10, "simp_20x10.npz"),
     "simp_full": lambda tf: make_simp(tf, 400, 200, "simp_400x200.npz", sample=20),

@@ -78,3 +78,17 @@ def test_simp_small(golden):
     gC = m.compliance_grad_c(u.ravel())
     grho = (gC * C).sum(axis=(1, 2, 3, 4)) * 3.0 / rho  # E = rho^3
     assert np.abs(grho - g["grad_rho"]).max() <= 1e-9 * np.abs(g["grad_rho"]).max()
+
+
+def test_material_points(golden):
+    """Neo-Hookean stress/tangent and plane-strain J2 return mapping of the
+    oracle against the reference's Material.step outputs."""
+    g = golden("material_points.npz")
+    P, A = O.neo_hookean_point(g["F"], g["mu"], g["lam"])
+    assert np.abs(P - g["P"]).max() <= 1e-11 * np.abs(g["P"]).max()
+    assert np.abs(A - g["A"]).max() <= 1e-11 * np.abs(g["A"]).max()
+    s, st, D = O.j2_plane_strain_point(g["H"], g["stress"], g["state"], 1000.0, 0.3, 1.0, 100.0)
+    assert np.abs(s - g["stress_new"]).max() <= 1e-12 * np.abs(g["stress_new"]).max()
+    assert np.abs(st - g["state_new"]).max() <= 1e-12 * max(np.abs(g["state_new"]).max(), 1e-12)
+    assert np.abs(D - g["ddsdde"]).max() <= 1e-12 * np.abs(g["ddsdde"]).max()
+    assert (st[:, 0] > g["state"][:, 0]).any()  # some points yield

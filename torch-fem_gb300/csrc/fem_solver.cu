@@ -1408,6 +1408,11 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
   g_timer.ms = 0.0;
   g_timer.timed = 0;
   int chunk = 8;
+  // stagnation guard: the FP64 residual must halve within kStallReplacements
+  // replacements, else FP32 storage cannot refine this system
+  constexpr int kStallReplacements = 8;
+  double best_rr = -1.0;
+  int stalled = 0;
   while (h.done == kDoneNo) {
     if (h.replace) {
       // FP64 reliable update: x += x_lo; r = b - A x (matrix-free FP64).
@@ -1431,6 +1436,25 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
       TFG_CHECK_LAUNCH("fem_pcg_mixed replace");
       rc = read_ctrl(v.ctrl, &h, st);
       if (rc) return rc;
+      if (h.done == kDoneNo) {
+        if (best_rr < 0.0 || h.rr_true < 0.25 * best_rr) {
+          best_rr = h.rr_true;
+          stalled = 0;
+        } else if (++stalled >= kStallReplacements) {
+          set_last_error("mixed CG stagnated at relative residual %.3e after %lld iterations: FP32 "
+                         "storage cannot refine this system; use precision fp64",
+                         h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0, h.iters);
+          k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl);
+          ::tfg::note_launch();
+          if (info) {
+            info->iterations = h.iters;
+            info->replacements = h.replacements;
+            info->rel_residual = h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0;
+            info->status = FEM_NOT_CONVERGED;
+          }
+          return FEM_NOT_CONVERGED;
+        }
+      }
       continue;
     }
     if (G == 2) rc = iterate<2, float>(A, xl, r, z, p, q, v.partial, v.ctrl, &h, timing, &chunk, st);
