@@ -233,7 +233,7 @@ def run_profile(args):
     from torchfem_gb300 import _lib
 
     dev = torch.device("cuda", 0)
-    _lib.load().fem_set_cg_path(1 if args.cg_path == "persistent" else 0)
+    _lib.load().fem_set_cg_path({"persistent": 1, "persistent-regs": 2, "kernels": 0}[args.cg_path])
     m, forces = cube_workload(args.n, dev)
     dm = m.device_mesh
     kind, data = m.material.kernel_data(m.n_elem)
@@ -265,7 +265,7 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="profiling mode: assemble one system and run --profile-iters CG iterations")
     ap.add_argument("--profile-iters", type=int, default=20)
-    ap.add_argument("--cg-path", choices=["persistent", "kernels"], default="persistent")
+    ap.add_argument("--cg-path", choices=["persistent", "persistent-regs", "kernels"], default="persistent")
     args = ap.parse_args()
     torch.set_default_dtype(torch.float64)
     if args.impl == "reference":
@@ -281,7 +281,7 @@ def main():
     from torchfem_gb300 import _lib
 
     lib = _lib.load()
-    lib.fem_set_cg_path(1 if args.cg_path == "persistent" else 0)
+    lib.fem_set_cg_path({"persistent": 1, "persistent-regs": 2, "kernels": 0}[args.cg_path])
     m, forces = cube_workload(args.n, dev)
     dm = m.device_mesh
     n_dofs = m.n_dofs
@@ -350,13 +350,13 @@ def main():
                   "rel_err_mixed_vs_fp64": {"u": err_u, "sigma": err_s, "grad": err_g}}
 
     peak, peak_kind = measured_peak_hbm()
-    persistent = lib.fem_get_cg_path() == 1
+    persistent = lib.fem_get_cg_path() in (1, 2)
     if persistent:
         # CUDA events around each persistent CG launch; spmv_n counts the
         # iterations those launches ran
         unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
         sb = cg_iteration_bytes(dm)
-        kernel_name = "k_pcg_persistent<3,float> (one CG iteration)"
+        kernel_name = "k_pcg_persistent<3,float,%d> (one CG iteration)" % (1 if lib.fem_get_cg_path() == 1 else 0)
     else:
         unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
         sb = spmv_bytes(dm)

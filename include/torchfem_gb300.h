@@ -345,9 +345,11 @@ typedef struct fem_solve_info {
 void fem_set_timing(int enable);
 
 /* CG iteration path: 1 (default) one persistent cooperative kernel per run
- * of iterations; 0 three kernels per iteration.  Also selectable with the
- * environment variable TORCHFEM_GB300_CG=kernels. */
-void fem_set_cg_path(int persistent);
+ * of iterations, streaming the FP32 3x3 sliced matrix through shared memory
+ * with TMA bulk copies; 2 the same kernel with register loads; 0 three
+ * kernels per iteration.  Also selectable with the environment variables
+ * TORCHFEM_GB300_CG=kernels and TORCHFEM_GB300_TMA=0. */
+void fem_set_cg_path(int path);
 int fem_get_cg_path(void);
 
 size_t fem_pcg_workspace_bytes(const fem_matrix* A);

@@ -254,8 +254,9 @@ def test_cg_iteration_cap_cuts_back_then_raises(cuda):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_persistent_and_kernel_cg_paths_agree(cuda, precision):
-    """The persistent cooperative CG and the three-kernels-per-iteration CG
-    run the same iteration: same solution to 1e-10, same iteration counts."""
+    """The persistent cooperative CG (with and without the TMA-staged SpMV)
+    and the three-kernels-per-iteration CG run the same iteration: same
+    solution to 1e-10, same iteration counts."""
     from torchfem_gb300 import _lib
 
     lib = _lib.load()
@@ -265,7 +266,7 @@ def test_persistent_and_kernel_cg_paths_agree(cuda, precision):
     nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen) * 2 - 1) * 0.01
     out, iters = {}, {}
     try:
-        for path in (1, 0):
+        for path in (1, 2, 0):
             lib.fem_set_cg_path(path)
             m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
             m.constraints[nodes[:, 0] == 0.0, :] = True
@@ -274,9 +275,10 @@ def test_persistent_and_kernel_cg_paths_agree(cuda, precision):
             iters[path] = m.last_solve.iterations
     finally:
         lib.fem_set_cg_path(1)
-    assert rel(out[1], out[0]) <= 1e-10
-    for a, b in zip(iters[1], iters[0]):
-        assert abs(a - b) <= max(2, 0.02 * b)
+    for path in (1, 2):
+        assert rel(out[path], out[0]) <= 1e-10
+        for a, b in zip(iters[path], iters[0]):
+            assert abs(a - b) <= max(2, 0.02 * b)
 
 
 # ----------------------------------------------------------------- nonlinear --

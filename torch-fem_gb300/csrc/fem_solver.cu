@@ -691,8 +691,75 @@ __device__ __forceinline__ double all_partials(const double* partial, int k, dou
   return r;
 }
 
-template <int G, typename VT>
-__global__ void __launch_bounds__(kPThreads, 2) k_pcg_persistent(PersistParams P) {
+// ---- TMA bulk-copy pipeline for the sliced FP32 matrix (one ring per warp)
+constexpr int kTmaStages = 4;   // ring depth per warp
+constexpr int kTmaRows = 2;     // slot-rows (32 rows x 1 block slot) per stage
+constexpr int kSlotVal = 32 * 9 * 4;  // value bytes of a 3x3 slot-row
+constexpr int kSlotCol = 32 * 4;      // column bytes of a slot-row
+constexpr int kStageBytes = kTmaRows * (kSlotVal + kSlotCol);
+constexpr int kWarpRing = 128 + kTmaStages * kStageBytes;  // barriers + buffers
+constexpr int kTmaSmem = (kPThreads / 32) * kWarpRing;
+constexpr long long kMbarSpin = 2000000000LL;  // clock cycles a stage wait may last
+
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kMbarSpin) return false;
+  }
+}
+
+// One stage: nrows slot-rows of values then columns, both 16-byte aligned
+// (slice starts are multiples of 32 slots), completing on the stage barrier.
+__device__ __forceinline__ void tma_stage(uint32_t bar, uint32_t dst, const float* sval, const int32_t* col,
+                                          int64_t slot0, int nrows, uint64_t policy) {
+  const uint32_t bv = (uint32_t)(nrows * kSlotVal), bc = (uint32_t)(nrows * kSlotCol);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bv + bc) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(dst),
+      "l"(sval + slot0 * 9), "r"(bv), "r"(bar), "l"(policy)
+      : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(dst + bv),
+      "l"(col + slot0), "r"(bc), "r"(bar), "l"(policy)
+      : "memory");
+}
+
+// Chunk iterator over a warp's slices s = first, first + stride, ... < end.
+struct ChunkIt {
+  int64_t s;
+  int64_t end;
+  int64_t stride;
+  int k0;
+  __device__ bool valid() const { return s < end; }
+  __device__ void advance(const int64_t* sell_base) {
+    const int len = (int)((sell_base[s + 1] - sell_base[s]) >> 5);
+    k0 += kTmaRows;
+    if (k0 >= len) {
+      k0 = 0;
+      s += stride;
+      // skip empty slices
+      while (s < end && sell_base[s + 1] == sell_base[s]) s += stride;
+    }
+  }
+};
+
+template <int G, typename VT, int MODE>
+__global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent(PersistParams P) {
   __shared__ double red[32];
   __shared__ double2 red2[32];
   __shared__ float ys[kPThreads / 32][G][32];
@@ -717,6 +784,20 @@ __global__ void __launch_bounds__(kPThreads, 2) k_pcg_persistent(PersistParams P
     s_hi = ns * (cta + 1) / NC;
     row_lo = min(s_lo * 32, P.n_rows);
     row_hi = min(s_hi * 32, P.n_rows);
+  }
+  // per-warp TMA ring (MODE 1): barriers then kTmaStages stage buffers
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  unsigned char* ring_base = dyn_smem + (size_t)warp * kWarpRing + 128;
+  const uint32_t bars = smem_u32(dyn_smem + (size_t)warp * kWarpRing);
+  const uint32_t bufs = smem_u32(ring_base);
+  int64_t issued = 0, consumed = 0;
+  bool ring_ok = true;
+  if constexpr (MODE == 1) {
+    if (lane == 0) {
+      for (int st = 0; st < kTmaStages; ++st) mbar_init(bars + 8u * st);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
   }
   double rz = c->rz;
   long long iters = c->iters;
@@ -747,6 +828,97 @@ __global__ void __launch_bounds__(kPThreads, 2) k_pcg_persistent(PersistParams P
         if (sub == 0 && row < row_hi) {
           q[row] = (VT)sacc;
           pq += (double)p[row] * sacc;
+        }
+      }
+    } else if constexpr (MODE == 1 && G == 3) {
+      // TMA ring per warp: whole slices per warp, no cross-warp reduction
+      const float* sval = (const float*)P.val;
+      if (ring_ok) {
+        ChunkIt prod{s_lo + warp, s_hi, NW, 0}, cons{s_lo + warp, s_hi, NW, 0};
+        while (prod.valid() && P.row_ptr[prod.s + 1] == P.row_ptr[prod.s]) prod.s += NW;
+        cons.s = prod.s;
+        if (lane == 0) {
+          for (int st = 0; st < kTmaStages && prod.valid(); ++st) {
+            const int64_t g = issued + st;
+            const int slot = (int)(g % kTmaStages);
+            const int len = (int)((P.row_ptr[prod.s + 1] - P.row_ptr[prod.s]) >> 5);
+            tma_stage(bars + 8u * slot, bufs + (uint32_t)slot * kStageBytes, sval, P.col,
+                      P.row_ptr[prod.s] + (int64_t)prod.k0 * 32, min(kTmaRows, len - prod.k0), stream);
+            prod.advance(P.row_ptr);
+          }
+        }
+        int64_t pi = issued;
+        {
+          // producer position is re-derived by every lane so lane 0 can keep issuing
+          ChunkIt tmp{cons.s, s_hi, NW, 0};
+          int n = 0;
+          while (tmp.valid() && n < kTmaStages) {
+            tmp.advance(P.row_ptr);
+            ++n;
+          }
+          prod = tmp;
+          pi = issued + n;
+        }
+        float y[G];
+#pragma unroll
+        for (int i = 0; i < G; ++i) y[i] = 0.f;
+        while (cons.valid()) {
+          const int slot = (int)(consumed % kTmaStages);
+          const uint32_t parity = (uint32_t)((consumed / kTmaStages) & 1);
+          if (!mbar_wait(bars + 8u * slot, parity)) {
+            ring_ok = false;
+            atomicExch(&c->bar_error, 1);
+            break;
+          }
+          const int len = (int)((P.row_ptr[cons.s + 1] - P.row_ptr[cons.s]) >> 5);
+          const int nr = min(kTmaRows, len - cons.k0);
+          const float* vb = (const float*)(ring_base + (size_t)slot * kStageBytes);
+          const int32_t* cb = (const int32_t*)(ring_base + (size_t)slot * kStageBytes + (size_t)nr * kSlotVal);
+          for (int r = 0; r < nr; ++r) {
+            const int64_t cc = cb[r * 32 + lane];
+            float xv[G];
+#pragma unroll
+            for (int j = 0; j < G; ++j) xv[j] = (float)p[cc * G + j];
+#pragma unroll
+            for (int i = 0; i < G; ++i)
+#pragma unroll
+              for (int j = 0; j < G; ++j) y[i] = fmaf(vb[(r * 9 + i * G + j) * 32 + lane], xv[j], y[i]);
+          }
+          ++consumed;
+          if (cons.k0 + nr >= len) {  // slice done: rows of this warp
+            const int64_t a = cons.s * 32 + lane;
+            if (a < P.n_rows) {
+#pragma unroll
+              for (int i = 0; i < G; ++i) {
+                q[a * G + i] = (VT)y[i];
+                pq += (double)p[a * G + i] * (double)y[i];
+              }
+            }
+#pragma unroll
+            for (int i = 0; i < G; ++i) y[i] = 0.f;
+          }
+          cons.advance(P.row_ptr);
+          __syncwarp();
+          if (lane == 0 && prod.valid()) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const int ps = (int)(pi % kTmaStages);
+            const int plen = (int)((P.row_ptr[prod.s + 1] - P.row_ptr[prod.s]) >> 5);
+            tma_stage(bars + 8u * ps, bufs + (uint32_t)ps * kStageBytes, sval, P.col,
+                      P.row_ptr[prod.s] + (int64_t)prod.k0 * 32, min(kTmaRows, plen - prod.k0), stream);
+          }
+          if (prod.valid()) {
+            prod.advance(P.row_ptr);
+            ++pi;
+          }
+        }
+        issued = pi;
+        if (!ring_ok) {
+          // drain this warp's copies still in flight before leaving
+          while (consumed < issued) {
+            const int slot = (int)(consumed % kTmaStages);
+            mbar_wait(bars + 8u * slot, (uint32_t)((consumed / kTmaStages) & 1));
+            ++consumed;
+          }
         }
       }
     } else {
@@ -933,18 +1105,31 @@ static int64_t spmv_grid(const fem_matrix* A) {
 }
 
 // Persistent CG: CTAs per SM from the occupancy calculator (cached).
-template <int G, typename VT>
+template <int G, typename VT, int MODE>
 static int persistent_blocks() {
   static thread_local int blocks = 0;
   if (blocks == 0) {
+    const int smem = MODE == 1 ? kTmaSmem : 0;
+    if (MODE == 1)
+      cudaFuncSetAttribute(k_pcg_persistent<G, VT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_persistent<G, VT>, kPThreads, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_persistent<G, VT, MODE>, kPThreads, smem) !=
             cudaSuccess ||
         occ < 1)
       occ = 1;
     blocks = occ * sm_count();
   }
   return blocks;
+}
+
+// The TMA-pipelined SpMV serves the FP32 3x3 sliced layout (the mixed path).
+static int g_tma_spmv = -1;
+static bool use_tma_spmv() {
+  if (g_tma_spmv < 0) {
+    const char* e = getenv("TORCHFEM_GB300_TMA");
+    g_tma_spmv = (e && strcmp(e, "0") == 0) ? 0 : 1;
+  }
+  return g_tma_spmv == 1;
 }
 
 // Upper bound on the persistent grid (at most 2048 / kPThreads CTAs per SM).
@@ -1076,9 +1261,16 @@ static int launch_persistent(const fem_matrix* A, VT* x, VT* r, VT* z, VT* p, VT
   P.ctrl = ctrl;
   P.spin_limit = 2000000000LL;  // about one second of clock cycles
   void* args[] = {&P};
-  const int blocks = persistent_blocks<G, VT>();
-  const cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_pcg_persistent<G, VT>, dim3(blocks),
-                                                    dim3(kPThreads), args, 0, st);
+  cudaError_t e;
+  if (G == 3 && use_tma_spmv()) {
+    const int blocks = persistent_blocks<G, VT, 1>();
+    e = cudaLaunchCooperativeKernel((const void*)k_pcg_persistent<G, VT, 1>, dim3(blocks), dim3(kPThreads), args,
+                                    kTmaSmem, st);
+  } else {
+    const int blocks = persistent_blocks<G, VT, 0>();
+    e = cudaLaunchCooperativeKernel((const void*)k_pcg_persistent<G, VT, 0>, dim3(blocks), dim3(kPThreads), args,
+                                    0, st);
+  }
   ::tfg::note_launch();
   if (e != cudaSuccess) {
     set_last_error("persistent CG launch: %s", cudaGetErrorString(e));
@@ -1217,8 +1409,12 @@ extern "C" {
 
 void fem_set_timing(int enable) { g_timing = enable; }
 
-void fem_set_cg_path(int persistent) { g_cg_path = persistent ? 1 : 0; }
-int fem_get_cg_path(void) { return use_persistent() ? 1 : 0; }
+void fem_set_cg_path(int path) {
+  g_cg_path = path == 0 ? 0 : 1;
+  if (path == 1) g_tma_spmv = 1;
+  if (path == 2) g_tma_spmv = 0;
+}
+int fem_get_cg_path(void) { return use_persistent() ? (use_tma_spmv() ? 1 : 2) : 0; }
 
 int fem_assemble_csr(const fem_blocks* B, int ke_dtype, const void* ke, const int64_t* row_ptr,
                      const uint8_t* con_mask, double* val, void* stream) {
