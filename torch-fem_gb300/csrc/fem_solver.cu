@@ -625,7 +625,10 @@ __global__ void k_copy_cast(int64_t n, const float* __restrict__ in, double* __r
 // order, so all CTAs take identical decisions and results are deterministic.
 // The matrix is streamed with L2 evict_first; the CG vectors stay in L2.
 constexpr int kCsrTpr = 8;  // lanes per scalar CSR row
-constexpr int kPThreads = 512;
+#ifndef TFG_PTHREADS
+#define TFG_PTHREADS 512
+#endif
+constexpr int kPThreads = TFG_PTHREADS;
 constexpr int kPKS = 4;  // warps sharing one slice (sliced layout)
 
 struct PersistParams {
@@ -692,8 +695,16 @@ __device__ __forceinline__ double all_partials(const double* partial, int k, dou
 }
 
 // ---- TMA bulk-copy pipeline for the sliced FP32 matrix (one ring per warp)
-constexpr int kTmaStages = 4;   // ring depth per warp
-constexpr int kTmaRows = 2;     // slot-rows (32 rows x 1 block slot) per stage
+// Ring shape: 4 slot-rows x 2 stages timed best of {2x4, 4x2, 3x3} on the
+// 1M-unknown cube (the compile-time knobs keep the other shapes buildable).
+#ifndef TFG_TMA_STAGES
+#define TFG_TMA_STAGES 2
+#endif
+#ifndef TFG_TMA_ROWS
+#define TFG_TMA_ROWS 4
+#endif
+constexpr int kTmaStages = TFG_TMA_STAGES;  // ring depth per warp
+constexpr int kTmaRows = TFG_TMA_ROWS;      // slot-rows (32 rows x 1 block slot) per stage
 constexpr int kSlotVal = 32 * 9 * 4;  // value bytes of a 3x3 slot-row
 constexpr int kSlotCol = 32 * 4;      // column bytes of a slot-row
 constexpr int kStageBytes = kTmaRows * (kSlotVal + kSlotCol);

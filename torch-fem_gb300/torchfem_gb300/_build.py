@@ -51,7 +51,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     def compile_one(src: str) -> Path:
         obj = obj_dir / (Path(src).stem + ".o")
-        cmd = [nvcc, *FLAGS, *ARCH, "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
+        extra = os.environ.get("TORCHFEM_GB300_NVCC_FLAGS", "").split()
+        cmd = [nvcc, *FLAGS, *ARCH, *extra, "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{res.stderr}")
