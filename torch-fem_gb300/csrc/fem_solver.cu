@@ -157,6 +157,8 @@ struct Ctrl {
   double rr_true;  // ||b - A x||^2 from the last FP64 replacement (mixed)
   double bb;       // ||b||^2
   double tol2bb;   // rtol^2 ||b||^2
+  double rscale;   // power of two applied to the residual held by the CG vectors (mixed; 1 for FP64)
+  double tol2_lo;  // tol2bb in the units of the CG vectors (tol2bb * rscale^2)
   double delta2;   // replacement threshold (mixed)
   long long iters;
   long long max_iter;
@@ -165,9 +167,8 @@ struct Ctrl {
   int replace;
   int mixed;
   unsigned int counter;
-  unsigned int bar_count;  // persistent kernel: grid-barrier arrivals
-  unsigned int bar_gen;    // persistent kernel: grid-barrier generation
-  int bar_error;           // persistent kernel: a barrier wait ran out
+  int bar_error;             // persistent kernel: a barrier wait ran out
+  unsigned long long bar_seq;  // persistent kernel: grid-barrier arrivals, never reset within a solve
 };
 
 __device__ __forceinline__ bool arrive_last(unsigned int* counter) {
@@ -411,12 +412,12 @@ __device__ void finish_update(Ctrl* c, double rz_new, double rr, bool count_iter
   }
   bool stop = false;
   if (c->mixed) {
-    if (rr <= c->tol2bb || rr <= c->delta2 * c->rr_ref) {
+    if (rr <= c->tol2_lo || rr <= c->delta2 * c->rr_ref) {
       c->replace = 1;
       c->rz_new = rz_new;
       stop = true;
     }
-  } else if (rr <= c->tol2bb) {
+  } else if (rr <= c->tol2_lo) {
     c->done = kDoneConverged;
     stop = true;
   }
@@ -484,7 +485,7 @@ __global__ void __launch_bounds__(256) k_pupdate(int64_t n, const VT* __restrict
     p[i] = z[i] + beta * p[i];
 }
 
-// Start (x = 0): r = b, z = M r, p = z; rz, rr, bb; tolerances.
+// Start (x = 0): r = b * rscale, z = M r, p = z; rz, rr, bb; tolerances.
 template <int G, typename VT>
 __global__ void __launch_bounds__(256)
 k_init(int64_t n_groups, const double* __restrict__ b, VT* __restrict__ x, VT* __restrict__ r,
@@ -492,6 +493,7 @@ k_init(int64_t n_groups, const double* __restrict__ b, VT* __restrict__ x, VT* _
        double* __restrict__ partial, Ctrl* ctrl, double rtol2) {
   __shared__ double red[32];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double sc = ctrl->rscale;
   double rz = 0.0, rr = 0.0, bb = 0.0;
   if (i < n_groups) {
     VT rv[G], zv[G];
@@ -499,7 +501,7 @@ k_init(int64_t n_groups, const double* __restrict__ b, VT* __restrict__ x, VT* _
     for (int g = 0; g < G; ++g) {
       const double bv = b[i * G + g];
       bb += bv * bv;
-      rv[g] = (VT)bv;
+      rv[g] = (VT)(bv * sc);
       r[i * G + g] = rv[g];
       x[i * G + g] = VT(0);
     }
@@ -532,26 +534,60 @@ k_init(int64_t n_groups, const double* __restrict__ b, VT* __restrict__ x, VT* _
       ctrl->rr_true = t3;
       ctrl->bb = t3;
       ctrl->tol2bb = rtol2 * t3;
+      ctrl->tol2_lo = ctrl->tol2bb * sc * sc;
       ctrl->iters = 0;
       ctrl->replacements = 0;
       ctrl->replace = 0;
       if (!isfinite(t1) || !isfinite(t3)) ctrl->done = kDoneNonFinite;
-      else if (t3 == 0.0 || t2 <= ctrl->tol2bb) ctrl->done = kDoneConverged;
+      else if (t3 == 0.0 || t2 <= ctrl->tol2_lo) ctrl->done = kDoneConverged;
       else ctrl->done = kDoneNo;
     }
   }
 }
 
-// Mixed precision: fold the FP32 correction into the FP64 solution.
-__global__ void k_fold(int64_t n, double* __restrict__ x64, float* __restrict__ xlo) {
+// Mixed precision keeps the residual it iterates on near unit norm: the FP32
+// vectors hold r * rscale with rscale a power of two (exact to apply and to
+// undo), so their dot products stay far from FP32 underflow and overflow at
+// any problem scale and any depth of refinement.
+__device__ __forceinline__ double unit_scale(double norm2) {
+  if (!(norm2 > 0.0) || !isfinite(norm2)) return 1.0;
+  int e;
+  frexp(norm2, &e);
+  return ldexp(1.0, -(e / 2));
+}
+
+// Mixed precision start: ||b||^2 and the first residual scale.
+__global__ void __launch_bounds__(256) k_bnorm(int64_t n, const double* __restrict__ b,
+                                               double* __restrict__ partial, Ctrl* ctrl) {
+  __shared__ double red[32];
+  double t = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    t += b[i] * b[i];
+  t = block_sum(t, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (arrive_last(&ctrl->counter)) {
+    const double bb = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      ctrl->rscale = unit_scale(bb);
+    }
+  }
+}
+
+// Mixed precision: fold the FP32 correction (in residual-scale units) into
+// the FP64 solution.
+__global__ void k_fold(int64_t n, double* __restrict__ x64, float* __restrict__ xlo, const Ctrl* ctrl) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  x64[i] += (double)xlo[i];
+  const double inv = 1.0 / ctrl->rscale;  // a power of two: exact
+  x64[i] += (double)xlo[i] * inv;
   xlo[i] = 0.f;
 }
 
-// Mixed precision replacement: r = b - y (FP64), r_lo = (float) r, z = M r_lo,
-// new r.z / r.r; convergence is decided on the FP64 residual.
+// Mixed precision replacement: r = b - y (FP64), r_lo = (float)(r * s) with s
+// the unit scale of the previous true residual, z = M r_lo, new r.z / r.r;
+// the kept direction p is rescaled through beta.  Convergence is decided on
+// the FP64 residual.
 template <int G>
 __global__ void __launch_bounds__(256)
 k_replace(int64_t n_groups, const double* __restrict__ b, const double* __restrict__ y,
@@ -559,6 +595,8 @@ k_replace(int64_t n_groups, const double* __restrict__ b, const double* __restri
           double* __restrict__ partial, Ctrl* ctrl) {
   __shared__ double red[32];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double sc_old = ctrl->rscale;
+  const double sc = unit_scale(ctrl->rr_true);
   double rz = 0.0, rr = 0.0, r64 = 0.0;
   if (i < n_groups) {
     float rv[G], zv[G];
@@ -567,7 +605,7 @@ k_replace(int64_t n_groups, const double* __restrict__ b, const double* __restri
       const int64_t k = i * G + g;
       const double rd = b[k] - y[k];
       r64 += rd * rd;
-      rv[g] = (float)rd;
+      rv[g] = (float)(rd * sc);
       rlo[k] = rv[g];
     }
     apply_prec<G, float>(prec, i, rv, zv);
@@ -600,18 +638,23 @@ k_replace(int64_t n_groups, const double* __restrict__ b, const double* __restri
       } else if (t3 <= ctrl->tol2bb) {
         ctrl->done = kDoneConverged;
       } else if (ctrl->done == kDoneNo) {
+        // p_old holds the old scale: p = z + beta * p with beta = (t1 / rz) / f
+        // (f = sc / sc_old) continues the same direction in the new scale
         ctrl->rr = t2;
         ctrl->rr_ref = t2;
-        ctrl->beta = t1 / ctrl->rz;
+        ctrl->beta = t1 / ctrl->rz * (sc_old / sc);
         ctrl->rz = t1;
+        ctrl->rscale = sc;
+        ctrl->tol2_lo = ctrl->tol2bb * sc * sc;
       }
     }
   }
 }
 
-__global__ void k_copy_cast(int64_t n, const float* __restrict__ in, double* __restrict__ out) {
+// FP32 solution (in residual-scale units) to FP64.
+__global__ void k_copy_cast(int64_t n, const float* __restrict__ in, double* __restrict__ out, const Ctrl* ctrl) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (double)in[i];
+  if (i < n) out[i] = (double)in[i] * (1.0 / ctrl->rscale);
 }
 
 
@@ -648,50 +691,259 @@ struct PersistParams {
   long long spin_limit;  // clock cycles a barrier wait may last
 };
 
-// Grid barrier with a bounded wait.  Returns false (on every thread) once
-// any CTA's wait has run out; the kernel then stops.
-__device__ __forceinline__ bool grid_barrier(Ctrl* c, long long spin_limit) {
+// Grid barrier with a bounded wait, fused with the fixed-order sum of NK
+// per-CTA partials.  One monotonic 64-bit arrival counter: every CTA adds 1
+// (release) and polls (relaxed, with a short sleep, so that polling neither
+// floods the counter's L2 slice nor invalidates L1 lines a co-resident CTA is
+// using) until the count reaches the next multiple of the grid size; one
+// acquire fence follows.  No reset step sits on the critical path: the counter
+// starts at 0 for each solve and every launch passes whole barriers only.
+// Then warp 0 alone sums partial[3*i + k0 + j] over the CTAs i in one fixed
+// order and shares the sums through shared memory, so every thread of every
+// CTA holds identical values.  Returns false (on every thread) once any CTA's
+// wait has run out; the kernel then stops.
+template <int NK, typename F>
+__device__ __forceinline__ bool grid_barrier(Ctrl* c, long long spin_limit, const double* partial, int k0, F&& on_sums) {
   __shared__ int ok;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned int* gen = &c->bar_gen;
-    const unsigned int g0 = *gen;
-    __threadfence();
-    const unsigned int arrived = atomicAdd(&c->bar_count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&c->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
-    } else {
+  if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) {
+      unsigned long long old;
+      asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(old) : "l"(&c->bar_seq) : "memory");
+      const unsigned long long target = (old / gridDim.x + 1) * gridDim.x;
       const long long t0 = clock64();
-      while (*gen == g0) {
+      while (true) {
+        unsigned long long now;
+        asm volatile("ld.relaxed.gpu.u64 %0, [%1];" : "=l"(now) : "l"(&c->bar_seq) : "memory");
+        if (now >= target) break;
         if (*(volatile int*)&c->bar_error) break;
         if (clock64() - t0 > spin_limit) {
           atomicExch(&c->bar_error, 1);
           break;
         }
-        __nanosleep(64);
+        __nanosleep(32);
       }
+      asm volatile("fence.acq_rel.gpu;" ::: "memory");
+      ok = (*(volatile int*)&c->bar_error) == 0;
     }
-    __threadfence();
-    ok = (*(volatile int*)&c->bar_error) == 0;
+    __syncwarp();
+    if constexpr (NK > 0) {
+      const int lane = threadIdx.x;
+      double sums[NK];
+#pragma unroll
+      for (int j = 0; j < NK; ++j) {
+        double v = 0.0;
+        for (int i = lane; i < (int)gridDim.x; i += 32) v += __ldcg(partial + 3 * i + k0 + j);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        sums[j] = v;
+      }
+      if (lane == 0) on_sums(sums);
+    }
   }
   __syncthreads();
   return ok != 0;
 }
 
-// Sum over CTAs of partial[3*i + k], same fixed order in every CTA; the
-// result is returned to every thread.
-__device__ __forceinline__ double all_partials(const double* partial, int k, double* red) {
-  __shared__ double out;
+// Fixed-order CTA sum of N per-thread accumulators: shuffle tree within each
+// warp, then thread 0 adds the warp sums in FP64 and stores them to out[j].
+template <int N, typename ACC>
+__device__ __forceinline__ void cta_partials(ACC (&v)[N], double* out, double (*wsum)[2]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[j].shfl_down(o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) wsum[warp][j] = v[j].value();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w][j];
+      out[j] = t;
+    }
+  }
+}
+
+// Dot-product accumulators of the persistent CG.  On the FP32 (mixed) path a
+// float-float pair: each product is split exactly (a*b and its FMA residual)
+// and summed with Knuth's TwoSum, which keeps the sums as accurate as FP64
+// accumulation of the FP32 products while running on the FP32 pipe (the FP64
+// pipe of this GPU is a small fraction of the FP32 rate).  On the FP64 path a
+// plain double.
+template <typename VT> struct DotAcc;
+template <> struct DotAcc<double> {
   double v = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v += __ldcg(partial + 3 * i + k);
-  v = block_sum(v, red);
-  if (threadIdx.x == 0) out = v;
-  __syncthreads();
-  const double r = out;
-  __syncthreads();
-  return r;
+  __device__ __forceinline__ void fma(double a, double b) { v = ::fma(a, b, v); }
+  __device__ __forceinline__ void shfl_down(int o) { v += __shfl_down_sync(0xffffffffu, v, o); }
+  __device__ __forceinline__ double value() const { return v; }
+};
+// (round-to-nearest intrinsics: never contracted into an FMA)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+template <> struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x, float x_lo) {
+    float s, e;
+    two_sum(hi, x, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, x_lo));
+  }
+  __device__ __forceinline__ void fma(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    add(p, fmaf(a, b, -p));
+  }
+  __device__ __forceinline__ void shfl_down(int o) {
+    const float h = __shfl_down_sync(0xffffffffu, hi, o);
+    const float l = __shfl_down_sync(0xffffffffu, lo, o);
+    add(h, l);
+    const float t = __fadd_rn(hi, lo);  // renormalise
+    lo = __fsub_rn(lo, __fsub_rn(t, hi));
+    hi = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// First i in [0, n] with base[i] >= target (base non-decreasing).
+__device__ __forceinline__ int64_t lower_bound_i64(const int64_t* base, int64_t n, int64_t target) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (base[mid] < target) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <typename VT> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int W = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int W = 2; };
+
+template <typename V, typename T>
+__device__ __forceinline__ T& lane_of(V& v, int i) { return reinterpret_cast<T*>(&v)[i]; }
+
+// p[k] = z[k] + beta p[k] for k in [lo, hi): 16-byte vectors over the aligned
+// middle, U per thread in flight, scalar head and tail.
+template <typename VT, int U>
+__device__ __forceinline__ void direction_update(VT* __restrict__ p, const VT* __restrict__ z, VT beta,
+                                                 int64_t lo, int64_t hi) {
+  using V = typename Vec16<VT>::type;
+  constexpr int W = Vec16<VT>::W;
+  const int64_t a = min(hi, (lo + W - 1) / W * W);
+  const int64_t b = max(a, hi / W * W);
+  for (int64_t k = lo + threadIdx.x; k < a; k += blockDim.x) p[k] = z[k] + beta * p[k];
+  for (int64_t k = b + threadIdx.x; k < hi; k += blockDim.x) p[k] = z[k] + beta * p[k];
+  V* pv = reinterpret_cast<V*>(p + a);
+  const V* zv = reinterpret_cast<const V*>(z + a);
+  const int64_t nv = (b - a) / W;
+  for (int64_t i0 = threadIdx.x; i0 < nv; i0 += U * (int64_t)blockDim.x) {
+    V pp[U], zz[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + (int64_t)u * blockDim.x;
+      if (i < nv) {
+        pp[u] = pv[i];
+        zz[u] = zv[i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + (int64_t)u * blockDim.x;
+      if (i < nv) {
+#pragma unroll
+        for (int w = 0; w < W; ++w) lane_of<V, VT>(pp[u], w) = lane_of<V, VT>(zz[u], w) + beta * lane_of<V, VT>(pp[u], w);
+        pv[i] = pp[u];
+      }
+    }
+  }
+}
+
+// One node of the solution/residual update: x += alpha p, r -= alpha q,
+// z = M r; accumulates r.z and r.r.
+template <int G, typename VT>
+__device__ __forceinline__ void node_update(const void* prec, int64_t a, VT alpha, VT* __restrict__ x,
+                                            VT* __restrict__ r, VT* __restrict__ z, const VT* __restrict__ p,
+                                            const VT* __restrict__ q, DotAcc<VT>& rz, DotAcc<VT>& rr) {
+  VT rv[G], zv[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    const int64_t k = a * G + g;
+    x[k] += alpha * p[k];
+    rv[g] = r[k] - alpha * q[k];
+    r[k] = rv[g];
+  }
+  apply_prec<G, VT>(prec, a, rv, zv);
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    z[a * G + g] = zv[g];
+    rz.fma(rv[g], zv[g]);
+    rr.fma(rv[g], rv[g]);
+  }
+}
+
+// The same update for the 3x3-block FP32 layout, four nodes (twelve values,
+// three 16-byte vectors per array; 36 inverse-block values, nine vectors) per
+// thread step, all loads issued before any store.  Nodes [lo, hi), lo a
+// multiple of 4.
+__device__ __forceinline__ void node_update_b3(const float* __restrict__ minv, int64_t lo, int64_t hi, float alpha,
+                                               float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
+                                               const float* __restrict__ p, const float* __restrict__ q,
+                                               DotAcc<float>& rz, DotAcc<float>& rr) {
+  const int64_t g_lo = lo >> 2, g_full = hi >> 2;  // groups [g_lo, g_full) are complete
+  for (int64_t gi = g_lo + threadIdx.x; gi < g_full; gi += blockDim.x) {
+    float4 xv[3], pv[3], rv[3], qv[3], mv[9];
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      xv[u] = reinterpret_cast<const float4*>(x)[gi * 3 + u];
+      pv[u] = reinterpret_cast<const float4*>(p)[gi * 3 + u];
+      rv[u] = reinterpret_cast<const float4*>(r)[gi * 3 + u];
+      qv[u] = reinterpret_cast<const float4*>(q)[gi * 3 + u];
+    }
+#pragma unroll
+    for (int u = 0; u < 9; ++u) mv[u] = reinterpret_cast<const float4*>(minv)[gi * 9 + u];
+    const float* pf = reinterpret_cast<const float*>(pv);
+    const float* qf = reinterpret_cast<const float*>(qv);
+    const float* mf = reinterpret_cast<const float*>(mv);
+    float* xf = reinterpret_cast<float*>(xv);
+    float* rf = reinterpret_cast<float*>(rv);
+    float zf[12];
+#pragma unroll
+    for (int e = 0; e < 12; ++e) {
+      xf[e] += alpha * pf[e];
+      rf[e] = rf[e] - alpha * qf[e];
+    }
+#pragma unroll
+    for (int nd = 0; nd < 4; ++nd) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        float t = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t = fmaf(mf[nd * 9 + i * 3 + j], rf[nd * 3 + j], t);
+        zf[nd * 3 + i] = t;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 12; ++e) {
+      rz.fma(rf[e], zf[e]);
+      rr.fma(rf[e], rf[e]);
+    }
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      reinterpret_cast<float4*>(x)[gi * 3 + u] = xv[u];
+      reinterpret_cast<float4*>(r)[gi * 3 + u] = rv[u];
+      reinterpret_cast<float4*>(z)[gi * 3 + u] = make_float4(zf[4 * u], zf[4 * u + 1], zf[4 * u + 2], zf[4 * u + 3]);
+    }
+  }
+  for (int64_t a = max(lo, g_full * 4) + threadIdx.x; a < hi; a += blockDim.x)
+    node_update<3, float>(minv, a, alpha, x, r, z, p, q, rz, rr);
 }
 
 // ---- TMA bulk-copy pipeline for the sliced FP32 matrix (one ring per warp)
@@ -771,9 +1023,11 @@ struct ChunkIt {
 
 template <int G, typename VT, int MODE>
 __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent(PersistParams P) {
-  __shared__ double red[32];
-  __shared__ double2 red2[32];
+  using ACC = DotAcc<VT>;
+  __shared__ double wsum[kPThreads / 32][2];
   __shared__ float ys[kPThreads / 32][G][32];
+  __shared__ VT sh_alpha, sh_beta;
+  __shared__ int sh_stop;
   Ctrl* c = P.ctrl;
   if (ctrl_idle(c)) return;
   const int cta = blockIdx.x, NC = gridDim.x;
@@ -784,15 +1038,18 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
   VT* __restrict__ p = (VT*)P.p;
   VT* __restrict__ q = (VT*)P.q;
   const uint64_t stream = l2_policy(false);
-  // rows owned by this CTA
+  // rows owned by this CTA: equal shares of the stored entries (CSR) or of
+  // the stored slot-rows (sliced layout), the SpMV being the dominant phase
   int64_t row_lo, row_hi, s_lo = 0, s_hi = 0;
   if constexpr (G == 1) {
-    row_lo = P.n_rows * cta / NC;
-    row_hi = P.n_rows * (cta + 1) / NC;
+    const int64_t total = P.row_ptr[P.n_rows];
+    row_lo = lower_bound_i64(P.row_ptr, P.n_rows, total * cta / NC);
+    row_hi = cta == NC - 1 ? P.n_rows : lower_bound_i64(P.row_ptr, P.n_rows, total * (cta + 1) / NC);
   } else {
     const int64_t ns = (P.n_rows + 31) >> 5;
-    s_lo = ns * cta / NC;
-    s_hi = ns * (cta + 1) / NC;
+    const int64_t total = P.row_ptr[ns];
+    s_lo = lower_bound_i64(P.row_ptr, ns, total * cta / NC);
+    s_hi = cta == NC - 1 ? ns : lower_bound_i64(P.row_ptr, ns, total * (cta + 1) / NC);
     row_lo = min(s_lo * 32, P.n_rows);
     row_hi = min(s_hi * 32, P.n_rows);
   }
@@ -803,21 +1060,42 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
   const uint32_t bufs = smem_u32(ring_base);
   int64_t issued = 0, consumed = 0;
   bool ring_ok = true;
+  // this warp's chunks (whole slices s_lo + warp, + NW, ...), cycled across
+  // iterations: the producer stays kTmaStages chunks ahead of the consumer,
+  // so the first chunks of the next iteration stream in during the vector
+  // phases and barriers
+  ChunkIt first{s_lo + warp, s_hi, NW, 0};
+  ChunkIt prod = first;
   if constexpr (MODE == 1) {
     if (lane == 0) {
       for (int st = 0; st < kTmaStages; ++st) mbar_init(bars + 8u * st);
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
+    while (first.valid() && P.row_ptr[first.s + 1] == P.row_ptr[first.s]) first.s += NW;
+    prod = first;
+    if (G == 3 && first.valid()) {
+      for (int st = 0; st < kTmaStages; ++st) {
+        if (lane == 0) {
+          const int len = (int)((P.row_ptr[prod.s + 1] - P.row_ptr[prod.s]) >> 5);
+          tma_stage(bars + 8u * st, bufs + (uint32_t)st * kStageBytes, (const float*)P.val, P.col,
+                    P.row_ptr[prod.s] + (int64_t)prod.k0 * 32, min(kTmaRows, len - prod.k0), stream);
+        }
+        prod.advance(P.row_ptr);
+        if (!prod.valid()) prod = first;
+        ++issued;
+      }
+    }
   }
-  double rz = c->rz;
+  double rz = c->rz;        // thread 0 keeps the CG scalars
+  double alpha_d = 0.0;
   long long iters = c->iters;
   const long long max_iter = c->max_iter;
-  const double tol2bb = c->tol2bb, delta2 = c->delta2, rr_ref = c->rr_ref;
+  const double tol2bb = c->tol2_lo, delta2 = c->delta2, rr_ref = c->rr_ref;
   const int mixed = c->mixed;
   while (true) {
     // ---- phase A: q = A p on own rows, partial p.q
-    double pq = 0.0;
+    ACC pq[1];
     if constexpr (G == 1) {
       // groups of kCsrTpr lanes per scalar row, 32 / kCsrTpr rows per warp
       constexpr int TPR = kCsrTpr;
@@ -838,38 +1116,14 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
         for (int o = TPR / 2; o > 0; o >>= 1) sacc += __shfl_down_sync(0xffffffffu, sacc, o, TPR);
         if (sub == 0 && row < row_hi) {
           q[row] = (VT)sacc;
-          pq += (double)p[row] * sacc;
+          pq[0].fma(p[row], (VT)sacc);
         }
       }
     } else if constexpr (MODE == 1 && G == 3) {
       // TMA ring per warp: whole slices per warp, no cross-warp reduction
       const float* sval = (const float*)P.val;
-      if (ring_ok) {
-        ChunkIt prod{s_lo + warp, s_hi, NW, 0}, cons{s_lo + warp, s_hi, NW, 0};
-        while (prod.valid() && P.row_ptr[prod.s + 1] == P.row_ptr[prod.s]) prod.s += NW;
-        cons.s = prod.s;
-        if (lane == 0) {
-          for (int st = 0; st < kTmaStages && prod.valid(); ++st) {
-            const int64_t g = issued + st;
-            const int slot = (int)(g % kTmaStages);
-            const int len = (int)((P.row_ptr[prod.s + 1] - P.row_ptr[prod.s]) >> 5);
-            tma_stage(bars + 8u * slot, bufs + (uint32_t)slot * kStageBytes, sval, P.col,
-                      P.row_ptr[prod.s] + (int64_t)prod.k0 * 32, min(kTmaRows, len - prod.k0), stream);
-            prod.advance(P.row_ptr);
-          }
-        }
-        int64_t pi = issued;
-        {
-          // producer position is re-derived by every lane so lane 0 can keep issuing
-          ChunkIt tmp{cons.s, s_hi, NW, 0};
-          int n = 0;
-          while (tmp.valid() && n < kTmaStages) {
-            tmp.advance(P.row_ptr);
-            ++n;
-          }
-          prod = tmp;
-          pi = issued + n;
-        }
+      if (ring_ok && first.valid()) {
+        ChunkIt cons = first;
         float y[G];
 #pragma unroll
         for (int i = 0; i < G; ++i) y[i] = 0.f;
@@ -885,15 +1139,15 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
           const int nr = min(kTmaRows, len - cons.k0);
           const float* vb = (const float*)(ring_base + (size_t)slot * kStageBytes);
           const int32_t* cb = (const int32_t*)(ring_base + (size_t)slot * kStageBytes + (size_t)nr * kSlotVal);
-          for (int r = 0; r < nr; ++r) {
-            const int64_t cc = cb[r * 32 + lane];
+          for (int rr = 0; rr < nr; ++rr) {
+            const int64_t cc = cb[rr * 32 + lane];
             float xv[G];
 #pragma unroll
             for (int j = 0; j < G; ++j) xv[j] = (float)p[cc * G + j];
 #pragma unroll
             for (int i = 0; i < G; ++i)
 #pragma unroll
-              for (int j = 0; j < G; ++j) y[i] = fmaf(vb[(r * 9 + i * G + j) * 32 + lane], xv[j], y[i]);
+              for (int j = 0; j < G; ++j) y[i] = fmaf(vb[(rr * 9 + i * G + j) * 32 + lane], xv[j], y[i]);
           }
           ++consumed;
           if (cons.k0 + nr >= len) {  // slice done: rows of this warp
@@ -902,34 +1156,25 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
 #pragma unroll
               for (int i = 0; i < G; ++i) {
                 q[a * G + i] = (VT)y[i];
-                pq += (double)p[a * G + i] * (double)y[i];
+                pq[0].fma(p[a * G + i], (VT)y[i]);
               }
             }
 #pragma unroll
             for (int i = 0; i < G; ++i) y[i] = 0.f;
           }
           cons.advance(P.row_ptr);
+          // refill the slot just read with the chunk kTmaStages ahead
           __syncwarp();
-          if (lane == 0 && prod.valid()) {
+          if (lane == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const int ps = (int)(pi % kTmaStages);
+            const int ps = (int)(issued % kTmaStages);
             const int plen = (int)((P.row_ptr[prod.s + 1] - P.row_ptr[prod.s]) >> 5);
             tma_stage(bars + 8u * ps, bufs + (uint32_t)ps * kStageBytes, sval, P.col,
                       P.row_ptr[prod.s] + (int64_t)prod.k0 * 32, min(kTmaRows, plen - prod.k0), stream);
           }
-          if (prod.valid()) {
-            prod.advance(P.row_ptr);
-            ++pi;
-          }
-        }
-        issued = pi;
-        if (!ring_ok) {
-          // drain this warp's copies still in flight before leaving
-          while (consumed < issued) {
-            const int slot = (int)(consumed % kTmaStages);
-            mbar_wait(bars + 8u * slot, (uint32_t)((consumed / kTmaStages) & 1));
-            ++consumed;
-          }
+          prod.advance(P.row_ptr);
+          if (!prod.valid()) prod = first;
+          ++issued;
         }
       }
     } else {
@@ -974,90 +1219,92 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
 #pragma unroll
               for (int v = 1; v < kPKS; ++v) t += ys[warp + v][i][lane];
               q[a * G + i] = (VT)t;
-              pq += (double)p[a * G + i] * (double)t;
+              pq[0].fma(p[a * G + i], (VT)t);
             }
           }
         }
         __syncthreads();
       }
     }
-    pq = block_sum(pq, red);
-    if (threadIdx.x == 0) P.partial[3 * cta] = pq;
-    if (!grid_barrier(c, P.spin_limit)) break;
-    const double pq_tot = all_partials(P.partial, 0, red);
-    if (pq_tot == 0.0 || !isfinite(pq_tot)) {
-      if (cta == 0 && threadIdx.x == 0) {
-        c->done = isfinite(pq_tot) ? kDoneBreakdown : kDoneNonFinite;
-        c->iters = iters;
+    cta_partials<1, ACC>(pq, P.partial + 3 * cta, wsum);
+    const bool ok1 = grid_barrier<1>(c, P.spin_limit, P.partial, 0, [&](const double* sm) {
+      const double pq_tot = sm[0];
+      if (pq_tot == 0.0 || !isfinite(pq_tot)) {
+        sh_stop = 1;
+        if (cta == 0) {
+          c->done = isfinite(pq_tot) ? kDoneBreakdown : kDoneNonFinite;
+          c->iters = iters;
+        }
+      } else {
+        sh_stop = 0;
+        alpha_d = (double)(VT)(rz / pq_tot);
+        sh_alpha = (VT)alpha_d;
       }
-      break;
-    }
-    const VT alpha = (VT)(rz / pq_tot);
+    });
+    if (!ok1 || sh_stop) break;
+    const VT alpha = sh_alpha;
     // ---- phase B: x += alpha p, r -= alpha q, z = M r on own rows
-    double rzl = 0.0, rrl = 0.0;
-    for (int64_t a = row_lo + threadIdx.x; a < row_hi; a += blockDim.x) {
-      VT rv[G], zv[G];
-#pragma unroll
-      for (int g = 0; g < G; ++g) {
-        const int64_t k = a * G + g;
-        x[k] += alpha * p[k];
-        rv[g] = r[k] - alpha * q[k];
-        r[k] = rv[g];
+    ACC rzrr[2];
+    if constexpr (G == 3 && sizeof(VT) == 4 && MODE == 1) {
+      node_update_b3((const float*)P.prec, row_lo, row_hi, (float)alpha, (float*)x, (float*)r, (float*)z,
+                     (const float*)p, (const float*)q, rzrr[0], rzrr[1]);
+    } else {
+      for (int64_t a = row_lo + threadIdx.x; a < row_hi; a += blockDim.x)
+        node_update<G, VT>(P.prec, a, alpha, x, r, z, p, q, rzrr[0], rzrr[1]);
+    }
+    cta_partials<2, ACC>(rzrr, P.partial + 3 * cta + 1, wsum);
+    const bool ok2 = grid_barrier<2>(c, P.spin_limit, P.partial, 1, [&](const double* sm) {
+      const double rz_new = sm[0], rr = sm[1];
+      iters += 1;
+      int stop = 0;  // 1 done, 2 replace
+      int done = kDoneNo;
+      if (!isfinite(rr) || !isfinite(rz_new)) {
+        stop = 1;
+        done = kDoneNonFinite;
+      } else if (mixed) {
+        if (rr <= tol2bb || rr <= delta2 * rr_ref) stop = 2;
+      } else if (rr <= tol2bb) {
+        stop = 1;
+        done = kDoneConverged;
       }
-      apply_prec<G, VT>(P.prec, a, rv, zv);
-#pragma unroll
-      for (int g = 0; g < G; ++g) {
-        z[a * G + g] = zv[g];
-        rzl += (double)rv[g] * (double)zv[g];
-        rrl += (double)rv[g] * (double)rv[g];
+      if (!stop && iters >= max_iter) {
+        stop = 1;
+        done = kDoneMaxIter;
       }
-    }
-    block_sum2(rzl, rrl, red2);
-    if (threadIdx.x == 0) {
-      P.partial[3 * cta + 1] = rzl;
-      P.partial[3 * cta + 2] = rrl;
-    }
-    if (!grid_barrier(c, P.spin_limit)) break;
-    const double rz_new = all_partials(P.partial, 1, red);
-    const double rr = all_partials(P.partial, 2, red);
-    iters += 1;
-    int stop = 0;  // 1 done, 2 replace
-    int done = kDoneNo;
-    if (!isfinite(rr) || !isfinite(rz_new)) {
-      stop = 1;
-      done = kDoneNonFinite;
-    } else if (mixed) {
-      if (rr <= tol2bb || rr <= delta2 * rr_ref) stop = 2;
-    } else if (rr <= tol2bb) {
-      stop = 1;
-      done = kDoneConverged;
-    }
-    if (!stop && iters >= max_iter) {
-      stop = 1;
-      done = kDoneMaxIter;
-    }
-    if (stop) {
-      if (cta == 0 && threadIdx.x == 0) {
-        c->iters = iters;
+      if (stop) {
+        sh_stop = 1;
+        if (cta == 0) {
+          c->iters = iters;
+          c->rr = rr;
+          c->alpha = alpha_d;
+          c->rz_new = rz_new;
+          if (stop == 2) c->replace = 1;
+          else c->done = done;
+        }
+        return;
+      }
+      sh_stop = 0;
+      const VT beta = (VT)(rz_new / rz);
+      sh_beta = beta;
+      rz = rz_new;
+      if (cta == 0) {
+        c->rz = rz;
         c->rr = rr;
-        c->alpha = (double)alpha;
-        c->rz_new = rz_new;
-        if (stop == 2) c->replace = 1;
-        else c->done = done;
+        c->iters = iters;
+        c->beta = (double)beta;
       }
-      break;
-    }
-    const VT beta = (VT)(rz_new / rz);
-    rz = rz_new;
+    });
+    if (!ok2 || sh_stop) break;
     // ---- phase C: p = z + beta p on own rows
-    for (int64_t k = row_lo * G + threadIdx.x; k < row_hi * G; k += blockDim.x) p[k] = z[k] + beta * p[k];
-    if (cta == 0 && threadIdx.x == 0) {
-      c->rz = rz;
-      c->rr = rr;
-      c->iters = iters;
-      c->beta = (double)beta;
+    direction_update<VT, MODE == 1 ? 4 : 2>(p, z, sh_beta, row_lo * G, row_hi * G);
+    if (!grid_barrier<0>(c, P.spin_limit, nullptr, 0, [](const double*) {})) break;
+  }
+  if constexpr (MODE == 1) {
+    // wait for this warp's prefetched chunks before the CTA exits
+    while (consumed < issued) {
+      mbar_wait(bars + 8u * (uint32_t)(consumed % kTmaStages), (uint32_t)((consumed / kTmaStages) & 1));
+      ++consumed;
     }
-    if (!grid_barrier(c, P.spin_limit)) break;
   }
   if (cta == 0 && threadIdx.x == 0 && *(volatile int*)&c->bar_error) c->done = kDoneBarrierTimeout;
 }
@@ -1375,11 +1622,16 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
   memset(&h, 0, sizeof(h));
   h.max_iter = max_iter;
   h.mixed = 0;
+  h.rscale = 1.0;
   if (cudaMemcpyAsync(v.ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return check_cuda("fem_pcg ctrl");
   VT* xv = (G == 1) ? reinterpret_cast<VT*>(x) : reinterpret_cast<VT*>(v.x);
   const int64_t ng = A->n / G;
   g_persistent_refused = false;
+  if (sizeof(VT) == 4) {  // FP32 vectors iterate on b scaled to near unit norm
+    k_bnorm<<<vec_grid(A->n), kThreads, 0, st>>>(A->n, b, v.partial, v.ctrl);
+    ::tfg::note_launch();
+  }
   k_init<G, VT><<<grid_for(ng, kThreads), kThreads, 0, st>>>(
       ng, b, xv, (VT*)v.r, (VT*)v.z, (VT*)v.p, A->precond, v.partial, v.ctrl, rtol * rtol);
       ::tfg::note_launch();
@@ -1395,20 +1647,20 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
                         &chunk, st);
     if (rc) return rc;
   }
-  if (G != 1) k_copy_cast<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, (const float*)v.x, x);
+  if (G != 1) k_copy_cast<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, (const float*)v.x, x, v.ctrl);
   ::tfg::note_launch();
   TFG_CHECK_LAUNCH("fem_pcg finish");
   if (info) {
     info->iterations = h.iters;
     info->replacements = 0;
-    info->rel_residual = h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0;
+    info->rel_residual = h.bb > 0 ? sqrt(h.rr / h.bb) / h.rscale : 0.0;
     info->status = status_of(h.done);
     info->spmv_ms = g_timer.ms;
     info->spmv_timed = g_timer.timed;
   }
   if (h.done != kDoneConverged)
     set_last_error("CG did not converge: %lld iterations, relative residual %.3e, code %d", h.iters,
-                   h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0, h.done);
+                   h.bb > 0 ? sqrt(h.rr / h.bb) / h.rscale : 0.0, h.done);
   return status_of(h.done);
 }
 
@@ -1594,6 +1846,7 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
   h.max_iter = max_iter;
   h.mixed = 1;
   h.delta2 = delta * delta;
+  h.rscale = 1.0;
   if (cudaMemcpyAsync(v.ctrl, &h, sizeof(Ctrl), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return check_cuda("fem_pcg_mixed ctrl");
   const int G = A->block;
@@ -1601,6 +1854,8 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
   g_persistent_refused = false;
   float *xl = (float*)v.x, *r = (float*)v.r, *z = (float*)v.z, *p = (float*)v.p, *q = (float*)v.q;
   cudaMemsetAsync(x, 0, sizeof(double) * A->n, st);
+  k_bnorm<<<vec_grid(A->n), kThreads, 0, st>>>(A->n, b, v.partial, v.ctrl);
+  ::tfg::note_launch();
   if (G == 2)
     k_init<2, float><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, b, xl, r, z, p, A->precond,
                                                                   v.partial, v.ctrl, rtol * rtol);
@@ -1623,7 +1878,7 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
   while (h.done == kDoneNo) {
     if (h.replace) {
       // FP64 reliable update: x += x_lo; r = b - A x (matrix-free FP64).
-      k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl);
+      k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl, v.ctrl);
       ::tfg::note_launch();
       rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, v.fe,
                              nullptr, nullptr, nullptr, stream);
@@ -1651,7 +1906,7 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
           set_last_error("mixed CG stagnated at relative residual %.3e after %lld iterations: FP32 "
                          "storage cannot refine this system; use precision fp64",
                          h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0, h.iters);
-          k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl);
+          k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl, v.ctrl);
           ::tfg::note_launch();
           if (info) {
             info->iterations = h.iters;
@@ -1669,7 +1924,7 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
     if (rc) return rc;
   }
   // fold whatever correction is left (max-iter exit) into x
-  k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl);
+  k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl, v.ctrl);
   ::tfg::note_launch();
   TFG_CHECK_LAUNCH("fem_pcg_mixed finish");
   rc = read_ctrl(v.ctrl, &h, st);
