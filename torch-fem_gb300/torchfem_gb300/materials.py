@@ -14,6 +14,7 @@ user built the constants from (E, rho, ...).
 from __future__ import annotations
 
 import copy
+from collections import OrderedDict
 
 import torch
 from torch import Tensor
@@ -50,20 +51,50 @@ class Material:
         raise NotImplementedError(f"{type(self).__name__} has no GPU kernel in torchfem_gb300")
 
 
-def _iso_or_general(C: Tensor, n_elem: int, d: int) -> tuple[int, Tensor]:
-    """ISO (lambda, G) per element when C has the isotropic form, else C.
+# isotropy decisions per stiffness tensor, valid while the tensor is unchanged
+# (same object, same in-place version counter); the tensor is held so that
+# its id cannot be reused by another tensor while the entry lives
+_ISO_CACHE: "OrderedDict[int, tuple[Tensor, int, bool]]" = OrderedDict()
+_ISO_CACHE_SIZE = 8
 
-    Both are computed from C by indexing, so autograd links them to C.
-    """
-    Cb = C if C.dim() > 4 else C.unsqueeze(0)
-    lam = Cb[..., 0, 0, 1, 1]
-    G = Cb[..., 0, 1, 0, 1]
+
+def _is_isotropic(Cb: Tensor, lam: Tensor, G: Tensor, d: int) -> bool:
+    hit = _ISO_CACHE.get(id(Cb))
+    if hit is not None and hit[0] is Cb and hit[1] == Cb._version:
+        _ISO_CACHE.move_to_end(id(Cb))
+        return hit[2]
     with torch.no_grad():
-        eye = torch.eye(d, dtype=C.dtype, device=C.device)
+        eye = torch.eye(d, dtype=Cb.dtype, device=Cb.device)
         i4 = torch.einsum("ij,kl->ijkl", eye, eye)
         i4s = torch.einsum("ik,jl->ijkl", eye, eye) + torch.einsum("il,jk->ijkl", eye, eye)
         rec = lam[..., None, None, None, None] * i4 + G[..., None, None, None, None] * i4s
         iso = bool(torch.allclose(rec, Cb, rtol=1e-14, atol=0.0))
+    _ISO_CACHE[id(Cb)] = (Cb, Cb._version, iso)
+    if len(_ISO_CACHE) > _ISO_CACHE_SIZE:
+        _ISO_CACHE.popitem(last=False)
+    return iso
+
+
+def _is_isotropic_small(Cb: Tensor, lam: Tensor, G: Tensor, d: int) -> bool:
+    with torch.no_grad():
+        eye = torch.eye(d, dtype=Cb.dtype, device=Cb.device)
+        i4 = torch.einsum("ij,kl->ijkl", eye, eye)
+        i4s = torch.einsum("ik,jl->ijkl", eye, eye) + torch.einsum("il,jk->ijkl", eye, eye)
+        rec = lam[..., None, None, None, None] * i4 + G[..., None, None, None, None] * i4s
+        return bool(torch.allclose(rec, Cb, rtol=1e-14, atol=0.0))
+
+
+def _iso_or_general(C: Tensor, n_elem: int, d: int) -> tuple[int, Tensor]:
+    """ISO (lambda, G) per element when C has the isotropic form, else C.
+
+    Both are computed from C by indexing, so autograd links them to C.  The
+    isotropy test (a full comparison of C) runs once per stiffness tensor and
+    is reused while the tensor is not modified.
+    """
+    Cb = C if C.dim() > 4 else C.unsqueeze(0)
+    lam = Cb[..., 0, 0, 1, 1]
+    G = Cb[..., 0, 1, 0, 1]
+    iso = _is_isotropic(C, lam, G, d) if C.dim() > 4 else _is_isotropic_small(Cb, lam, G, d)
     if iso:
         data = torch.stack([lam, G], dim=-1).to(torch.float64)
         if data.shape[0] != n_elem:
