@@ -363,12 +363,15 @@ def main():
         kernel_name = "k_spmv_sell<3>"
     avg_spmv_s = unit_s
     achieved = sb / unit_s / 1e9 if unit_s else None
-    traffic_file = ROOT / "profiles" / "spmv_sell_traffic.json"
+    # DRAM bytes per CG iteration from one ncu capture of the persistent kernel
+    # (dram__bytes_read.sum + dram__bytes_write.sum over a 20-iteration launch),
+    # per stored block so that it scales to this workload's matrix
+    traffic_file = ROOT / "profiles" / "pcg_persistent_traffic.json"
     traffic = None
-    if traffic_file.exists():
+    if persistent and traffic_file.exists():
         try:
             tj = json.loads(traffic_file.read_text())
-            traffic = tj["bytes_per_block"] * dm.n_blocks
+            traffic = tj["dram_bytes_per_block_per_iteration"] * dm.n_blocks
         except (KeyError, ValueError):
             traffic = None
 

@@ -1658,7 +1658,10 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
     info->spmv_ms = g_timer.ms;
     info->spmv_timed = g_timer.timed;
   }
-  if (h.done != kDoneConverged)
+  if (h.done == kDoneBarrierTimeout)
+    set_last_error("persistent CG: a grid-barrier or TMA-stage wait ran out (barrier timeout) after %lld iterations",
+                   h.iters);
+  else if (h.done != kDoneConverged)
     set_last_error("CG did not converge: %lld iterations, relative residual %.3e, code %d", h.iters,
                    h.bb > 0 ? sqrt(h.rr / h.bb) / h.rscale : 0.0, h.done);
   return status_of(h.done);
@@ -1937,7 +1940,10 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
     info->spmv_ms = g_timer.ms;
     info->spmv_timed = g_timer.timed;
   }
-  if (h.done != kDoneConverged)
+  if (h.done == kDoneBarrierTimeout)
+    set_last_error("persistent CG: a grid-barrier or TMA-stage wait ran out (barrier timeout) after %lld iterations",
+                   h.iters);
+  else if (h.done != kDoneConverged)
     set_last_error("mixed CG did not converge: %lld iterations, relative residual %.3e, code %d",
                    h.iters, h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0, h.done);
   return status_of(h.done);
