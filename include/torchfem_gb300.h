@@ -61,7 +61,9 @@ enum {
   FEM_TETRA1 = 4, /* 4 nodes, 3D, 1 point    (elements.py:727-790)  */
   FEM_TRIA1 = 5,  /* 3 nodes, 2D, 1 point    (elements.py:309-382)  */
   FEM_QUAD2 = 6,  /* 8 nodes, 2D, 4 points   (elements.py:570-724)  */
-  FEM_TRIA2 = 7   /* 6 nodes, 2D, 3 points   (elements.py:385-488)  */
+  FEM_TRIA2 = 7,  /* 6 nodes, 2D, 3 points   (elements.py:385-488)  */
+  FEM_SHELL3 = 8  /* Tria1 flat-facet shell: 3 nodes, 6 DOF per node (shell.py);
+                     used by fem_gather_nodal, the shell kernels take fem_shell */
 };
 
 /* Material data layouts consumed by the element kernels. */
@@ -401,6 +403,49 @@ size_t fem_pcg_mixed_workspace_bytes(const fem_matrix* A32, const fem_operator64
 int fem_pcg_mixed(const fem_matrix* A32, const fem_operator64* op, const double* b, double* x,
                   double rtol, double delta, int64_t max_iter, void* ws, size_t ws_bytes,
                   fem_solve_info* info, void* stream);
+
+/* ---------------------------------------------------------------- shell --
+ * Tria1 flat-facet shell, homogeneous linear-elastic section (the reference's
+ * Shell with a plane-stress material, src/torchfem/shell.py:48-603).  Nodes
+ * carry (u, v, w, rx, ry, rz); element DOFs are node-major, 18 per element. */
+typedef struct fem_shell {
+  int64_t n_nod;
+  int64_t n_elem;
+  const double* nodes;        /* [n_nod][3] */
+  const int32_t* elements;    /* [n_elem][3] */
+  const double* orientation;  /* [n_elem][3] material reference direction, NULL = global x */
+  const double* thickness;    /* [n_elem] */
+  int n_z;                    /* through-thickness stations (odd, Simpson) */
+  const double* z;            /* [n_z] station positions / thickness, in [-1/2, 1/2] */
+  const double* w;            /* [n_z] station weights / thickness, summing to one */
+  double kappa;               /* transverse shear correction factor */
+  double nu_t;                /* Poisson's ratio of the transverse shear scaling */
+  double drill;               /* drilling-rotation penalty */
+} fem_shell;
+
+/* Element matrices ke [n_elem][18][18] (global axes) of the shell with per-
+ * element material data mat [n_elem][11] = (plane-stress tangent in Voigt
+ * form, row-major 3x3; transverse shear moduli G_xz, G_yz).
+ * Replaces Shell.integrate_material's stiffness (shell.py:456-586) with the
+ * frames of Shell.eval_shape_functions (shell.py:358-387) and the strain
+ * operators _Dm/_Db/_Ds (shell.py:263-356). */
+int fem_shell_stiffness(const fem_shell* shell, const double* mat, double* ke, int32_t* status, void* stream);
+
+/* Element forces fe [n_elem][18] = ke u_e of the total nodal DOFs u
+ * [n_nod][6], and optionally the station stresses [n_z][n_elem][2][2]
+ * (local axes) of u from zero prestress (shell.py:474-504, 588-603). */
+int fem_shell_force(const fem_shell* shell, const double* mat, const double* ke, const double* u, double* fe,
+                    double* stress, void* stream);
+
+/* Vector-Jacobian product of (assembled forces, station stresses) with the
+ * nodal force cotangent a [n_nod][6] (may be NULL) and the stress cotangent
+ * gstress [n_z][n_elem][2][2] (may be NULL): gradients for mat
+ * [n_elem][11], thickness [n_elem] and the stress part of the element-DOF
+ * gradient gue [n_elem][18] (each output may be NULL).  Replaces the autograd
+ * replay of Shell.integrate_material inside NewtonRaphsonAdjoint
+ * (sparse.py:690-705). */
+int fem_shell_vjp(const fem_shell* shell, const double* mat, const double* u, const double* a,
+                  const double* gstress, double* gmat, double* gthick, double* gue, void* stream);
 
 #ifdef __cplusplus
 }

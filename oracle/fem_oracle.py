@@ -22,6 +22,9 @@ Restated reference code (paths relative to the torch-fem repository):
   Neo-Hookean point    materials/hyperelasticity.py:117-123 with the energy of
                        benchmarks/hyperelasticity.py:24-30
   J2 plane strain      materials/plasticity.py:504-590
+  Tria1 flat shell     src/torchfem/shell.py:48-177 (section), :263-356
+                       (strain operators), :358-387 (frames), :416-603
+                       (stiffness, forces, station stresses)
 """
 
 from __future__ import annotations
@@ -284,6 +287,160 @@ class LinearModel:
             eps = 0.5 * (H + H.transpose(0, 2, 1))
             g -= (self.w[i] * self.detJ[i] * t)[:, None, None, None, None] * np.einsum("eij,ekl->eijkl", eps, eps)
         return g
+
+
+# ------------------------------------------------------------------ shell ---
+def simpson_stations(n: int):
+    """Normalised through-thickness stations in [-1/2, 1/2] and Simpson
+    weights summing to one (shell.py:136-144)."""
+    z = np.linspace(-0.5, 0.5, n)
+    w = np.ones(n)
+    w[1:-1:2] = 4.0
+    w[2:-2:2] = 2.0
+    return z, w / (3.0 * (n - 1))
+
+
+def shell_frames(nodes, elements, orientation=None):
+    """Element frames (rows: material axis 1, axis 2, normal) and the nodes'
+    in-plane coordinates relative to node 0 (shell.py:358-380)."""
+    X = np.asarray(nodes, dtype=np.float64)[np.asarray(elements)]
+    n = np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 1])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    o = np.broadcast_to(np.asarray([1.0, 0.0, 0.0] if orientation is None else orientation, dtype=np.float64),
+                        n.shape)
+    proj = o - (o * n).sum(1, keepdims=True) * n
+    degenerate = np.linalg.norm(proj, axis=1, keepdims=True) < 1e-8
+    a1 = np.where(degenerate, X[:, 1] - X[:, 0], proj)
+    a1 /= np.linalg.norm(a1, axis=1, keepdims=True)
+    a2 = np.cross(n, a1)
+    a2 /= np.linalg.norm(a2, axis=1, keepdims=True)
+    t = np.stack([a1, a2, n], axis=1)
+    loc = np.einsum("eij,eaj->eai", t[:, :2], X - X[:, :1])
+    return t, loc
+
+
+def shell_operators(loc):
+    """Per element: area A, in-plane shape gradients B [2, 3] and the
+    generalised strain operators on the 18 local DOFs (u, v, w, rx, ry, rz
+    per node): membrane Dm [3, 18], curvature Db [3, 18] and the averaged
+    transverse shear Ds [2, 18] (shell.py:263-356)."""
+    dn = np.array([[-1.0, 1.0, 0.0], [-1.0, 0.0, 1.0]])
+    J = np.einsum("iN,eNj->eij", dn, loc)
+    detJ = np.linalg.det(J)
+    if np.any(detJ <= 0.0):
+        raise ValueError("Negative Jacobian")
+    B = np.linalg.inv(J) @ dn
+    E = loc.shape[0]
+    A = detJ / 2.0
+    Dm = np.zeros((E, 3, 18))
+    Db = np.zeros((E, 3, 18))
+    for a in range(3):
+        bx, by = B[:, 0, a], B[:, 1, a]
+        Dm[:, 0, 6 * a] = bx
+        Dm[:, 1, 6 * a + 1] = by
+        Dm[:, 2, 6 * a] = by
+        Dm[:, 2, 6 * a + 1] = bx
+        Db[:, 0, 6 * a + 4] = bx
+        Db[:, 1, 6 * a + 3] = -by
+        Db[:, 2, 6 * a + 3] = -bx
+        Db[:, 2, 6 * a + 4] = by
+    Ds = np.zeros((E, 2, 18))
+    for p0, p1, p2 in ((0, 1, 2), (1, 2, 0), (2, 0, 1)):
+        a = loc[:, p1, 0] - loc[:, p0, 0]
+        b = loc[:, p1, 1] - loc[:, p0, 1]
+        c = loc[:, p2, 0] - loc[:, p0, 0]
+        d = loc[:, p2, 1] - loc[:, p0, 1]
+        Ds[:, 0, 6 * p0 + 2] += b - d
+        Ds[:, 0, 6 * p0 + 4] += A
+        Ds[:, 1, 6 * p0 + 2] += c - a
+        Ds[:, 1, 6 * p0 + 3] += -A
+        Ds[:, 0, 6 * p1 + 2] += d
+        Ds[:, 0, 6 * p1 + 3] += -b * d / 2.0
+        Ds[:, 0, 6 * p1 + 4] += a * d / 2.0
+        Ds[:, 1, 6 * p1 + 2] += -c
+        Ds[:, 1, 6 * p1 + 3] += b * c / 2.0
+        Ds[:, 1, 6 * p1 + 4] += -a * c / 2.0
+        Ds[:, 0, 6 * p2 + 2] += -b
+        Ds[:, 0, 6 * p2 + 3] += b * d / 2.0
+        Ds[:, 0, 6 * p2 + 4] += -b * c / 2.0
+        Ds[:, 1, 6 * p2 + 2] += a
+        Ds[:, 1, 6 * p2 + 3] += -a * d / 2.0
+        Ds[:, 1, 6 * p2 + 4] += a * c / 2.0
+    Ds /= (3.0 * 2.0 * A)[:, None, None]
+    return A, B, detJ, Dm, Db, Ds
+
+
+def shell_rotation(t):
+    """Block-diagonal [18, 18] map from global to local DOFs (six copies of t)."""
+    T = np.zeros((t.shape[0], 18, 18))
+    for k in range(6):
+        T[:, 3 * k:3 * k + 3, 3 * k:3 * k + 3] = t
+    return T
+
+
+def plane_stress_voigt(E, nu):
+    """Voigt [3, 3] of the isotropic plane-stress tensor (elasticity.py:130-182)."""
+    E = np.asarray(E, dtype=np.float64)
+    f = E / (1.0 - nu**2)
+    C = np.zeros(E.shape + (3, 3))
+    C[..., 0, 0] = C[..., 1, 1] = f
+    C[..., 0, 1] = C[..., 1, 0] = f * nu
+    C[..., 2, 2] = f * (1.0 - nu) / 2.0
+    return C
+
+
+def shell_stiffness(nodes, elements, Cv, Gs, h, kappa=5.0 / 6.0, nu_t=0.5, drill=1.0, n_simpson=3,
+                    orientation=None):
+    """Global element matrices [E, 18, 18] of the homogeneous Tria1 shell:
+    T^T (km + kb + kc + ks + kd) T with ABD from Simpson stations, transverse
+    shear scaled by psi = kappa h^2 / (h^2 + alpha he^2) (shell.py:416-586)."""
+    t, loc = shell_frames(nodes, elements, orientation)
+    A, _, detJ, Dm, Db, Ds = shell_operators(loc)
+    h = np.asarray(h, dtype=np.float64)
+    zh, wh = simpson_stations(n_simpson)
+    Am = np.zeros_like(Cv)
+    Bm = np.zeros_like(Cv)
+    Dmat = np.zeros_like(Cv)
+    for z, w in zip(zh, wh):
+        zz, ww = (z * h)[:, None, None], (w * h)[:, None, None]
+        Am += Cv * ww
+        Bm += Cv * ww * zz
+        Dmat += Cv * ww * zz**2
+    wd = (0.5 * detJ)[:, None, None]  # Tria1 weight 1/2 times detJ
+    km = wd * np.einsum("eji,ejk,ekl->eil", Dm, Am, Dm)
+    kb = wd * np.einsum("eji,ejk,ekl->eil", Db, Dmat, Db)
+    kc = wd * (np.einsum("eji,ejk,ekl->eil", Dm, Bm, Db) + np.einsum("eji,ejk,ekl->eil", Db, Bm, Dm))
+    he = np.sqrt(2.0) * np.sqrt(A)
+    alpha = kappa / (2.0 * (1.0 + nu_t))
+    psi = kappa * h**2 / (h**2 + alpha * he**2)
+    As = np.zeros((len(h), 2, 2))
+    As[:, 0, 0] = h * Gs[:, 0]
+    As[:, 1, 1] = h * Gs[:, 1]
+    ks = wd * np.einsum("eji,ejk,ekl->eil", Ds, psi[:, None, None] * As, Ds)
+    kl = km + kb + kc + ks
+    for a in range(3):
+        kl[:, 6 * a + 5, 6 * a + 5] += drill
+    T = shell_rotation(t)
+    return np.einsum("eji,ejk,ekl->eil", T, kl, T)
+
+
+def shell_station_stress(nodes, elements, Cv, h, u, n_simpson=3, orientation=None):
+    """Cauchy stresses [n_stations, E, 2, 2] of the total displacements u
+    [n_nod, 6] from zero prestress: C (eps_m + z kappa) at each station
+    (shell.py:474-504)."""
+    t, loc = shell_frames(nodes, elements, orientation)
+    _, _, _, Dm, Db, _ = shell_operators(loc)
+    ue = np.asarray(u, dtype=np.float64)[np.asarray(elements)].reshape(len(elements), 18)
+    ul = np.einsum("eij,ej->ei", shell_rotation(t), ue)
+    em = np.einsum("eij,ej->ei", Dm, ul)
+    kb = np.einsum("eij,ej->ei", Db, ul)
+    zh, _ = simpson_stations(n_simpson)
+    out = []
+    for z in zh:
+        ev = em + (z * h)[:, None] * kb
+        sv = np.einsum("eij,ej->ei", Cv, ev)
+        out.append(np.stack([np.stack([sv[:, 0], sv[:, 2]], -1), np.stack([sv[:, 2], sv[:, 1]], -1)], -2))
+    return np.stack(out)
 
 
 # ------------------------------------------------------------- workloads ---

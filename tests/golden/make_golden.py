@@ -330,12 +330,69 @@ def make_material_points(tf):
     )
 
 
+def shell_problem(n_arc=9, n_len=7, seed=0):
+    """Tria1 shell on a cylindrical roof (axis y, 80 degrees, R = 1, L = 2):
+    the y = 0 edge clamped, the y = 2 edge held in x and z and pushed by a
+    prescribed u_y; self-weight-like z loads, moments about x on the free
+    straight edges; per-element thickness and E (seeded) for the gradients."""
+    from torchfem import Shell
+    from torchfem.materials import IsotropicElasticityPlaneStress
+
+    mesh = _repo_mesh()
+    nodes, elements = mesh.cylinder_patch_tria(n_arc, n_len, 1.0, 2.0, 80.0)
+    gen = torch.Generator().manual_seed(seed)
+    n_elem = len(elements)
+    E = 1000.0 * (1.0 + 0.1 * torch.randn(n_elem, generator=gen, dtype=torch.float64))
+    t = 0.05 * (1.0 + 0.2 * torch.rand(n_elem, generator=gen, dtype=torch.float64))
+    E.requires_grad_(True)
+    t.requires_grad_(True)
+    model = Shell(nodes, elements, IsotropicElasticityPlaneStress(E, 0.3), thickness=t)
+    y0 = nodes[:, 1] == 0.0
+    y1 = nodes[:, 1] == 2.0
+    side = (nodes[:, 0] - nodes[:, 0].min()).abs() < 1e-12
+    model.constraints[y0, :] = True
+    model.constraints[y1, 0] = True
+    model.constraints[y1, 2] = True
+    model.displacements[y1, 0] = 0.0
+    model.constraints[y1, 1] = True
+    model.displacements[y1, 1] = 1e-3
+    model.forces[:, 2] = -1.0 / len(nodes)
+    model.forces[side, 3] = 2e-3
+    return model, E, t, nodes, elements
+
+
+def make_shell(tf):
+    model, E, t, nodes, elements = shell_problem()
+    u, f, s, F, st = model.solve(method="spsolve", rtol=1e-12, atol=1e-14, differentiable_parameters=(E, t))
+    _, _, s_ip, _, _ = model.solve(method="spsolve", rtol=1e-12, atol=1e-14, aggregate_integration_points=False)
+    free = ~model.constraints
+    L = (u * free).pow(2).sum() + (f[:, 2] * u[:, 2]).sum()
+    gE, gt = torch.autograd.grad(L, (E, t))
+    with torch.no_grad():
+        ke = model.k0()
+        con = model.constraints.reshape(-1)
+        K = torch.zeros(model.n_dofs * model.n_dofs, dtype=torch.float64).index_add_(
+            0, model.glob_idx[0] * model.n_dofs + model.glob_idx[1],
+            torch.zeros(len(model.glob_idx[0]), dtype=torch.float64).index_add_(0, model.k_map, ke.ravel()),
+        ).reshape(model.n_dofs, model.n_dofs)
+        K[con, :] = 0.0
+        K[:, con] = 0.0
+        K[con, con] = 1.0
+    np.savez_compressed(
+        OUT / "shell_roof_9x7.npz", nodes=nodes.numpy(), elements=elements.numpy(), E=E.detach().numpy(),
+        ke=ke.numpy(), glob_idx=model.glob_idx.numpy(), k_map=model.k_map.numpy(),
+        t=t.detach().numpy(), u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(),
+        sigma_ip=s_ip.detach().numpy(), F=F.detach().numpy(), loss=L.detach().numpy(),
+        grad_E=gE.numpy(), grad_t=gt.numpy(), K=K.numpy(),
+    )
+
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
     "simp_small": lambda tf: make_simp(tf, 20, 10, "simp_20x10.npz"),
     "simp_full": lambda tf: make_simp(tf, 400, 200, "simp_400x200.npz", sample=20),
-    "hyper": make_hyper, "plastic": make_plastic,
+    "hyper": make_hyper, "plastic": make_plastic, "shell": make_shell,
 }
 
 

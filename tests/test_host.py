@@ -111,3 +111,23 @@ def test_solve_without_cuda_fails_loudly():
     m.constraints[n[:, 0] == 0, :] = True
     with pytest.raises(RuntimeError, match="CUDA"):
         m.solve()
+
+
+def test_shell_constructor_validates_like_reference():
+    """Shell keeps the reference's section checks (shell.py:134-170)."""
+    from torchfem_gb300 import Shell
+    from torchfem_gb300.materials import IsotropicElasticityPlaneStress
+
+    nodes = torch.tensor([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]])
+    el = torch.tensor([[0, 1, 2]])
+    mat = IsotropicElasticityPlaneStress(1000.0, 0.3)
+    with pytest.raises(ValueError, match="odd integer"):
+        Shell(nodes, el, mat, n_simpson=4)
+    s = Shell(nodes, el, mat, thickness=torch.tensor([0.2]))
+    assert s.n_dof_per_node == 6 and s.n_int == 3 and "Tria1" in repr(s)
+    assert torch.allclose(s.As[0], 0.2 * mat.G * torch.eye(2))
+    data = s.kernel_data()
+    assert data.shape == (1, 11)
+    f = 1000.0 / (1 - 0.09)
+    assert torch.allclose(data[0, :9], torch.tensor([f, 0.3 * f, 0, 0.3 * f, f, 0, 0, 0, f * 0.35]))
+    assert torch.allclose(data[0, 9:], mat.G * torch.ones(2))

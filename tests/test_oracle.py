@@ -92,3 +92,52 @@ def test_material_points(golden):
     assert np.abs(st - g["state_new"]).max() <= 1e-12 * max(np.abs(g["state_new"]).max(), 1e-12)
     assert np.abs(D - g["ddsdde"]).max() <= 1e-12 * np.abs(g["ddsdde"]).max()
     assert (st[:, 0] > g["state"][:, 0]).any()  # some points yield
+
+
+def test_shell_roof(golden):
+    """Tria1 flat-facet shell: element matrices against the reference's k0(),
+    assembly bit-exact given them, and the linear solution, forces and
+    station stresses of the cylindrical-roof fixture."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    g = golden("shell_roof_9x7.npz")
+    nodes, el, E, h = g["nodes"], g["elements"], g["E"], g["t"]
+    nu = 0.3
+    Cv = O.plane_stress_voigt(E, nu)
+    Gs = np.stack([E / (2 * (1 + nu))] * 2, axis=1)
+    ke = O.shell_stiffness(nodes, el, Cv, Gs, h)
+    assert np.abs(ke - g["ke"]).max() <= 1e-13 * np.abs(g["ke"]).max()
+    glob_idx, k_map, diag_map, _ = O.pattern(el, len(nodes), 6)
+    assert np.array_equal(glob_idx, g["glob_idx"]) and np.array_equal(k_map, g["k_map"])
+    n_dofs = 6 * len(nodes)
+    y0, y1 = nodes[:, 1] == 0.0, nodes[:, 1] == 2.0
+    con = np.zeros((len(nodes), 6), dtype=bool)
+    con[y0, :] = True
+    con[y1, :3] = True
+    DU = np.zeros((len(nodes), 6))
+    DU[y1, 1] = 1e-3
+    F = np.zeros((len(nodes), 6))
+    F[:, 2] = -1.0 / len(nodes)
+    F[np.abs(nodes[:, 0] - nodes[:, 0].min()) < 1e-12, 3] = 2e-3
+    cidx = np.nonzero(con.ravel())[0]
+    val = O.assemble_matrix(g["ke"], k_map, glob_idx.shape[1], glob_idx, diag_map, cidx)
+    K = sp.csr_matrix((val, (glob_idx[0], glob_idx[1])), shape=(n_dofs, n_dofs))
+    assert np.array_equal(K.toarray(), g["K"])
+    valf = np.zeros(glob_idx.shape[1])
+    np.add.at(valf, k_map, ke.ravel())
+    Kf = sp.csr_matrix((valf, (glob_idx[0], glob_idx[1])), shape=(n_dofs, n_dofs))
+    Kc = sp.csr_matrix((O.assemble_matrix(ke, k_map, glob_idx.shape[1], glob_idx, diag_map, cidx),
+                        (glob_idx[0], glob_idx[1])), shape=(n_dofs, n_dofs))
+    u = np.zeros(n_dofs)
+    u[cidx] = DU.ravel()[cidx]
+    res = Kf @ u - F.ravel()
+    res[cidx] = 0.0
+    u = u - spla.spsolve(Kc.tocsc(), res)
+    u[cidx] = DU.ravel()[cidx]
+    rel = lambda a, b: np.abs(a - b).max() / np.abs(b).max()  # noqa: E731
+    assert rel(u.reshape(-1, 6), g["u"]) <= 1e-10
+    assert rel((Kf @ u).reshape(-1, 6), g["f"]) <= 1e-10
+    s = O.shell_station_stress(nodes, el, Cv, h, u.reshape(-1, 6))
+    assert rel(s, g["sigma_ip"]) <= 1e-10
+    assert rel(s.mean(0), g["sigma"]) <= 1e-10

@@ -46,6 +46,7 @@ int etype_info(int etype, int* ne, int* d, int* nip) {
     case FEM_TRIA1: *ne = 3; *d = 2; *nip = 1; return FEM_OK;
     case FEM_QUAD2: *ne = 8; *d = 2; *nip = 4; return FEM_OK;
     case FEM_TRIA2: *ne = 6; *d = 2; *nip = 3; return FEM_OK;
+    case FEM_SHELL3: *ne = 3; *d = 6; *nip = 1; return FEM_OK;  // d: DOFs per node
     default: return FEM_INVALID;
   }
 }

@@ -33,7 +33,7 @@ __device__ __forceinline__ int64_t sell_index(const int64_t* __restrict__ sell_b
   return sell_base[s] * DD + (k * DD + c) * 32 + lane;
 }
 
-template <typename KT, typename AT, bool kSELL>
+template <typename KT, typename AT, bool kSELL, int MAXD = 3>
 __global__ void k_assemble(int n_e, int D, int64_t n_blocks, const int64_t* __restrict__ nbr_ptr,
                            const int32_t* __restrict__ nbr, const int64_t* __restrict__ blk_ptr,
                            const int32_t* __restrict__ contrib, const int32_t* __restrict__ blk_row,
@@ -48,11 +48,11 @@ __global__ void k_assemble(int n_e, int D, int64_t n_blocks, const int64_t* __re
   const int64_t k = blk - nbr_ptr[a];
   const int ND = n_e * D;
   const int nn = n_e * n_e;
-  AT acc[3][3];
+  AT acc[MAXD][MAXD];
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+  for (int i = 0; i < MAXD; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) acc[i][j] = AT(0);
+    for (int j = 0; j < MAXD; ++j) acc[i][j] = AT(0);
   for (int64_t q = blk_ptr[blk]; q < blk_ptr[blk + 1]; ++q) {
     const int32_t c = contrib[q];
     const int64_t e = c / nn;
@@ -1685,12 +1685,24 @@ int fem_get_cg_path(void) { return use_persistent() ? (use_tma_spmv() ? 1 : 2) :
 int fem_assemble_csr(const fem_blocks* B, int ke_dtype, const void* ke, const int64_t* row_ptr,
                      const uint8_t* con_mask, double* val, void* stream) {
   cudaStream_t st = as_stream(stream);
-  if (B->dim < 1 || B->dim > 3) {
-    set_last_error("fem_assemble_csr: dim must be 1..3");
+  if (B->dim < 1 || B->dim > 6) {
+    set_last_error("fem_assemble_csr: DOFs per node must be 1..6");
     return FEM_INVALID;
   }
   if (B->n_blocks == 0) return FEM_OK;
   const unsigned g = grid_for(B->n_blocks, 128);
+  if (B->dim > 3) {  // shells: six DOFs per node
+    if (ke_dtype == FEM_F64)
+      k_assemble<double, double, false, 6><<<g, 128, 0, st>>>(
+          B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
+          B->inc_ptr, (const double*)ke, row_ptr, con_mask, val, nullptr, nullptr);
+    else
+      k_assemble<float, double, false, 6><<<g, 128, 0, st>>>(
+          B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,
+          B->inc_ptr, (const float*)ke, row_ptr, con_mask, val, nullptr, nullptr);
+    ::tfg::note_launch();
+    return check_cuda("fem_assemble_csr");
+  }
   if (ke_dtype == FEM_F64)
     k_assemble<double, double, false><<<g, 128, 0, st>>>(
         B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row,

@@ -1,6 +1,6 @@
 """Builds the CUDA shared library ``libtorchfem_gb300.so`` for sm_103a.
 
-Plain ``nvcc`` on the three translation units in ``csrc/`` (compiled in
+Plain ``nvcc`` on the translation units in ``csrc/`` (compiled in
 parallel), then one link step.  No torch headers are involved: the library is
 a C ABI (``include/torchfem_gb300.h``) that Python reaches through ctypes.
 """
@@ -17,7 +17,7 @@ PKG_DIR = Path(__file__).resolve().parent
 CSRC = PKG_DIR.parent / "csrc"
 INCLUDE = PKG_DIR.parent.parent / "include"
 LIB_PATH = PKG_DIR / "libtorchfem_gb300.so"
-SOURCES = ("fem_pattern.cu", "fem_element.cu", "fem_solver.cu", "fem_nonlinear.cu")
+SOURCES = ("fem_pattern.cu", "fem_element.cu", "fem_solver.cu", "fem_nonlinear.cu", "fem_shell.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

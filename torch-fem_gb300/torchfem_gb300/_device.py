@@ -60,14 +60,14 @@ class LinearSystem:
 class DeviceMesh:
     """Pattern, geometry and kernels for one mesh on one CUDA device."""
 
-    def __init__(self, nodes: Tensor, elements: Tensor, etype, dof_per_node: int):
+    def __init__(self, nodes: Tensor, elements: Tensor, etype, dof_per_node: int, geometry: bool = True):
         self.device = _lib.require_cuda()
         self.lib = _lib.load()
         self.etype = etype
         self.n_e = etype.nodes
         self.dim = nodes.shape[1]
         self.d = dof_per_node
-        if self.d != self.dim:
+        if geometry and self.d != self.dim:
             raise NotImplementedError("only mechanics with one DOF per spatial dimension")
         self.n_nod = nodes.shape[0]
         self.n_elem = elements.shape[0]
@@ -81,7 +81,10 @@ class DeviceMesh:
         self.weights = etype.iweights().to(dev, torch.float64).contiguous()
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self._build_pattern()
-        self._build_geometry()
+        if geometry:
+            self._build_geometry()
+        else:  # structural elements (shells) bring their own element kernels
+            self.mesh = self.make_mesh(None)
 
     # ------------------------------------------------------------ plumbing --
     @property

@@ -22,7 +22,7 @@ FEM_INVALID = 5
 FEM_CUDA_ERROR = 6
 FEM_BREAKDOWN = 7
 
-FEM_QUAD1, FEM_HEXA1, FEM_TETRA2, FEM_TETRA1, FEM_TRIA1, FEM_QUAD2, FEM_TRIA2 = range(1, 8)
+FEM_QUAD1, FEM_HEXA1, FEM_TETRA2, FEM_TETRA1, FEM_TRIA1, FEM_QUAD2, FEM_TRIA2, FEM_SHELL3 = range(1, 9)
 FEM_MAT_ISO, FEM_MAT_GENERAL, FEM_MAT_TANGENT_IP = 1, 2, 3
 FEM_F64, FEM_F32 = 0, 1
 FEM_FMT_CSR_F64, FEM_FMT_SELL_F32 = 1, 2
@@ -91,6 +91,23 @@ class FemSolveInfo(C.Structure):
     ]
 
 
+class FemShell(C.Structure):
+    _fields_ = [
+        ("n_nod", i64),
+        ("n_elem", i64),
+        ("nodes", vp),
+        ("elements", vp),
+        ("orientation", vp),
+        ("thickness", vp),
+        ("n_z", C.c_int),
+        ("z", vp),
+        ("w", vp),
+        ("kappa", C.c_double),
+        ("nu_t", C.c_double),
+        ("drill", C.c_double),
+    ]
+
+
 class FemOperator64(C.Structure):
     _fields_ = [
         ("mesh", C.POINTER(FemMesh)),
@@ -101,6 +118,9 @@ class FemOperator64(C.Structure):
 
 _P = C.POINTER
 _SIGNATURES = {
+    "fem_shell_stiffness": (C.c_int, [_P(FemShell), vp, vp, vp, vp]),
+    "fem_shell_force": (C.c_int, [_P(FemShell), vp, vp, vp, vp, vp, vp]),
+    "fem_shell_vjp": (C.c_int, [_P(FemShell), vp, vp, vp, vp, vp, vp, vp, vp]),
     "fem_last_error": (C.c_char_p, []),
     "fem_abi_version": (C.c_int, []),
     "fem_launch_count": (i64, []),

@@ -146,3 +146,39 @@ def plate_hole_ogrid(n_theta: int, n_rad: int, Lx: float = 2.0, Ly: float = 1.0,
         [ids[:, :-1], ids[:, 1:], nxt[:, 1:], nxt[:, :-1]], dim=-1
     ).reshape(-1, 4)
     return nodes, elements
+
+
+def strip_tria(Nx: int, Ny: int, Lx: float = 1.0, Ly: float = 1.0):
+    """Flat Tria1 strip in the z = 0 plane: an Nx x Ny node grid, each cell
+    split along alternating diagonals.  Shell meshes (3D nodes)."""
+    X = torch.linspace(0, Lx, Nx, dtype=torch.float64)
+    Y = torch.linspace(0, Ly, Ny, dtype=torch.float64)
+    x, y = torch.meshgrid(X, Y, indexing="ij")
+    nodes = torch.stack([x.ravel(), y.ravel(), torch.zeros(Nx * Ny, dtype=torch.float64)], dim=1)
+    return nodes, _grid_triangles(Nx, Ny)
+
+
+def cylinder_patch_tria(n_arc: int, n_len: int, radius: float = 1.0, length: float = 2.0,
+                        angle: float = 80.0):
+    """Tria1 mesh of a cylindrical roof: the cylinder's axis is y, the arc
+    spans +-angle/2 degrees about the z axis (apex at z = radius), n_arc x
+    n_len nodes, each cell split along alternating diagonals."""
+    half = math.radians(angle) / 2.0
+    th = torch.linspace(-half, half, n_arc, dtype=torch.float64)
+    Y = torch.linspace(0.0, length, n_len, dtype=torch.float64)
+    t, y = torch.meshgrid(th, Y, indexing="ij")
+    nodes = torch.stack([radius * torch.sin(t).ravel(), y.ravel(), radius * torch.cos(t).ravel()], dim=1)
+    return nodes, _grid_triangles(n_arc, n_len)
+
+
+def _grid_triangles(Nx: int, Ny: int) -> Tensor:
+    """Counter-clockwise triangles of an Nx x Ny node grid (node i * Ny + j)."""
+    tris = []
+    for i in range(Nx - 1):
+        for j in range(Ny - 1):
+            a, b, c, d = i * Ny + j, (i + 1) * Ny + j, (i + 1) * Ny + j + 1, i * Ny + j + 1
+            if (i + j) % 2 == 0:
+                tris += [(a, b, c), (a, c, d)]
+            else:
+                tris += [(a, b, d), (b, c, d)]
+    return torch.tensor(tris, dtype=torch.int64)
