@@ -1093,6 +1093,11 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
   const long long max_iter = c->max_iter;
   const double tol2bb = c->tol2_lo, delta2 = c->delta2, rr_ref = c->rr_ref;
   const int mixed = c->mixed;
+  // two barriers per iteration on the TMA path (direction update inside the SpMV)
+  constexpr bool kCarry = MODE == 1 && G == 3 && sizeof(VT) == 4;
+  bool carry = false;
+  if (threadIdx.x == 0) sh_beta = (VT)0;
+  __syncthreads();
   while (true) {
     // ---- phase A: q = A p on own rows, partial p.q
     ACC pq[1];
@@ -1120,8 +1125,14 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
         }
       }
     } else if constexpr (MODE == 1 && G == 3) {
-      // TMA ring per warp: whole slices per warp, no cross-warp reduction
+      // TMA ring per warp: whole slices per warp, no cross-warp reduction.
+      // First iteration of a launch: q = A p.  Later ones fold the direction
+      // update into the SpMV: gather z, then q = A z + beta q and
+      // p = z + beta p on the rows just produced (q carries A p by
+      // recurrence within a launch, so one barrier less per iteration).
       const float* sval = (const float*)P.val;
+      const VT* gsrc = carry ? z : p;
+      const VT beta = sh_beta;
       if (ring_ok && first.valid()) {
         ChunkIt cons = first;
         float y[G];
@@ -1143,7 +1154,7 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
             const int64_t cc = cb[rr * 32 + lane];
             float xv[G];
 #pragma unroll
-            for (int j = 0; j < G; ++j) xv[j] = (float)p[cc * G + j];
+            for (int j = 0; j < G; ++j) xv[j] = (float)gsrc[cc * G + j];
 #pragma unroll
             for (int i = 0; i < G; ++i)
 #pragma unroll
@@ -1155,8 +1166,15 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
             if (a < P.n_rows) {
 #pragma unroll
               for (int i = 0; i < G; ++i) {
-                q[a * G + i] = (VT)y[i];
-                pq[0].fma(p[a * G + i], (VT)y[i]);
+                const int64_t k = a * G + i;
+                VT qv = (VT)y[i], pv = p[k];
+                if (carry) {
+                  qv = fmaf(beta, q[k], qv);
+                  pv = fmaf(beta, pv, z[k]);
+                  p[k] = pv;
+                }
+                q[k] = qv;
+                pq[0].fma(pv, qv);
               }
             }
 #pragma unroll
@@ -1295,9 +1313,13 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
       }
     });
     if (!ok2 || sh_stop) break;
-    // ---- phase C: p = z + beta p on own rows
-    direction_update<VT, MODE == 1 ? 4 : 2>(p, z, sh_beta, row_lo * G, row_hi * G);
-    if (!grid_barrier<0>(c, P.spin_limit, nullptr, 0, [](const double*) {})) break;
+    if constexpr (kCarry) {
+      carry = true;  // the next SpMV applies p = z + beta p itself
+    } else {
+      // ---- phase C: p = z + beta p on own rows
+      direction_update<VT, MODE == 1 ? 4 : 2>(p, z, sh_beta, row_lo * G, row_hi * G);
+      if (!grid_barrier<0>(c, P.spin_limit, nullptr, 0, [](const double*) {})) break;
+    }
   }
   if constexpr (MODE == 1) {
     // wait for this warp's prefetched chunks before the CTA exits
