@@ -62,8 +62,9 @@ enum {
   FEM_TRIA1 = 5,  /* 3 nodes, 2D, 1 point    (elements.py:309-382)  */
   FEM_QUAD2 = 6,  /* 8 nodes, 2D, 4 points   (elements.py:570-724)  */
   FEM_TRIA2 = 7,  /* 6 nodes, 2D, 3 points   (elements.py:385-488)  */
-  FEM_SHELL3 = 8  /* Tria1 flat-facet shell: 3 nodes, 6 DOF per node (shell.py);
+  FEM_SHELL3 = 8, /* Tria1 flat-facet shell: 3 nodes, 6 DOF per node (shell.py);
                      used by fem_gather_nodal, the shell kernels take fem_shell */
+  FEM_HEXA2 = 9   /* 20 nodes, 3D, 8 points  (elements.py:1078-1406) */
 };
 
 /* Material data layouts consumed by the element kernels. */

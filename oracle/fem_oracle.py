@@ -80,6 +80,32 @@ def _tria1_dn(xi):
     return np.broadcast_to(b, (xi.shape[0], 2, 3)).copy()
 
 
+_HEX2_COORDS = np.concatenate([_HEX_SIGNS, np.array(
+    [(0, -1, -1), (1, 0, -1), (0, 1, -1), (-1, 0, -1), (0, -1, 1), (1, 0, 1), (0, 1, 1), (-1, 0, 1),
+     (-1, -1, 0), (1, -1, 0), (1, 1, 0), (-1, 1, 0)], dtype=np.float64)])
+
+
+def _hexa2_dn(xi):
+    """Serendipity 20-node gradients: corners (1+s.x) products times
+    (s.x_sum - 2), mid-edge nodes (1 - t^2) times the two edge-normal factors."""
+    out = np.zeros((xi.shape[0], 3, 20))
+    for a, s in enumerate(_HEX2_COORDS):
+        for k in range(3):  # derivative direction
+            val = np.ones(xi.shape[0])
+            if np.all(s != 0):
+                f = 1.0 + s * xi  # [nip, 3]
+                g = (s * xi).sum(1) - 2.0
+                others = np.prod(np.delete(f, k, axis=1), axis=1)
+                val = 0.125 * s[k] * others * (g + f[:, k])
+            else:
+                m = int(np.nonzero(s == 0)[0][0])  # coordinate along the edge
+                fac = [(1.0 - xi[:, j] ** 2) if j == m else (1.0 + s[j] * xi[:, j]) for j in range(3)]
+                dfac = [(-2.0 * xi[:, j]) if j == m else np.full(xi.shape[0], s[j]) for j in range(3)]
+                val = 0.25 * np.prod([dfac[j] if j == k else fac[j] for j in range(3)], axis=0)
+            out[:, k, a] = val
+    return out
+
+
 _S3 = 1.0 / sqrt(3.0)
 ELEMENTS = {
     # name: (nodes, dim, ipoints, weights, dN/dxi)
@@ -91,11 +117,14 @@ ELEMENTS = {
                np.full(4, 0.041666667), _tetra2_dn),
     "Tetra1": (4, 3, np.array([[0.25, 0.25, 0.25]]), np.array([1.0 / 6.0]), _tetra1_dn),
     "Tria1": (3, 2, np.array([[1.0 / 3.0, 1.0 / 3.0]]), np.array([0.5]), _tria1_dn),
+    "Hexa2": (20, 3, np.array([[a * _S3, b * _S3, c * _S3] for c in (-1.0, 1.0) for b in (-1.0, 1.0) for a in (-1.0, 1.0)]),
+              np.ones(8), _hexa2_dn),
 }
 
 
 def element_name(n_e: int, dim: int) -> str:
-    table = {(8, 3): "Hexa1", (10, 3): "Tetra2", (4, 3): "Tetra1", (4, 2): "Quad1", (3, 2): "Tria1"}
+    table = {(8, 3): "Hexa1", (10, 3): "Tetra2", (4, 3): "Tetra1", (4, 2): "Quad1", (3, 2): "Tria1",
+             (20, 3): "Hexa2"}
     return table[(n_e, dim)]
 
 

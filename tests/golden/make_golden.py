@@ -387,12 +387,37 @@ def make_shell(tf):
     )
 
 
+def make_hexa2(tf):
+    """Hexa2 (20-node serendipity): the reference's linear_to_quadratic of a
+    jittered 2^3 Hexa1 cube, its pattern, element matrices and the solution."""
+    from torchfem import Solid
+    from torchfem.elements import linear_to_quadratic
+    from torchfem.materials import IsotropicElasticity3D
+    from torchfem.mesh import cube_hexa
+
+    nodes, elements = cube_hexa(3, 3, 3)
+    nodes = jitter(nodes, 1.0 / 2.0)
+    nodes, elements = linear_to_quadratic(nodes, elements)
+    model = Solid(nodes, elements, IsotropicElasticity3D(1000.0, 0.3))
+    model.constraints[nodes[:, 0] == 0.0, :] = True
+    model.forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    u, f, s, F, _ = model.solve(method="spsolve", rtol=1e-12)
+    with torch.no_grad():
+        ke = model.k0()
+    np.savez_compressed(
+        OUT / "hexa2_jitter2.npz", nodes=nodes.numpy(), elements=elements.numpy(), ke=ke.numpy(),
+        glob_idx=model.glob_idx.numpy(), k_map=model.k_map.numpy(), u=u.numpy(), f=f.numpy(),
+        sigma=s.numpy(), F=F.numpy(),
+    )
+
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
     "simp_small": lambda tf: make_simp(tf, 20, 10, "simp_20x10.npz"),
     "simp_full": lambda tf: make_simp(tf, 400, 200, "simp_400x200.npz", sample=20),
     "hyper": make_hyper, "plastic": make_plastic, "shell": make_shell,
+    "hexa2": make_hexa2,
 }
 
 

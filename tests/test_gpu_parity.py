@@ -80,6 +80,30 @@ def test_element_stiffness_vs_reference(cuda, golden):
     assert rel(ke, torch.tensor(g["ke"])) <= 1e-13
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_hexa2_vs_reference(cuda, golden, precision):
+    """Hexa2 (20-node serendipity): pattern, element matrices and the solution
+    of the reference's jittered quadratic cube."""
+    g = golden("hexa2_jitter2.npz")
+    nodes, el = torch.tensor(g["nodes"]), torch.tensor(g["elements"])
+    m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+    assert m.etype.__name__ == "Hexa2"
+    assert np.array_equal(m.glob_idx.cpu().numpy(), g["glob_idx"])
+    assert np.array_equal(m.k_map.cpu().numpy(), g["k_map"])
+    from torchfem_gb300 import _lib
+
+    kind, data = m.material.kernel_data(m.n_elem)
+    dm = m.device_mesh
+    ke = dm.element_stiffness(dm.make_mesh(None), _lib.FemMaterial(kind, data.to(cuda).contiguous().data_ptr()))
+    assert rel(ke, torch.tensor(g["ke"])) <= 1e-13
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    m.forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    u, f, s, _, _ = m.solve(stol=1e-12, precision=precision)
+    assert rel(u, g["u"]) <= RTOL
+    assert rel(f, g["f"]) <= RTOL
+    assert rel(s, g["sigma"]) <= RTOL
+
+
 def test_c1_forward_and_adjoint(cuda, golden):
     g = golden("c1_cube10.npz")
     nodes, el = mesh.cube_hexa(11, 11, 11)
@@ -167,7 +191,7 @@ PATCH_2D = torch.tensor([[1.0e-3, 2.0e-4], [3.0e-4, -1.0e-3]])
 PATCH_3D = torch.tensor([[1.0e-3, 2.0e-4, -1.0e-4], [3.0e-4, -1.0e-3, 5.0e-5], [1.0e-4, 2.0e-4, 7.0e-4]])
 
 
-@pytest.mark.parametrize("etype", ["Quad1", "Hexa1", "Tetra1", "Tetra2", "Tria1", "Tria2", "Quad2"])
+@pytest.mark.parametrize("etype", ["Quad1", "Hexa1", "Tetra1", "Tetra2", "Tria1", "Tria2", "Quad2", "Hexa2"])
 def test_patch(cuda, etype):
     """A linear displacement field prescribed on the boundary is reproduced
     inside, with uniform stress (reference tests/test_models.py:54-71)."""
@@ -176,11 +200,11 @@ def test_patch(cuda, etype):
     elif etype in ("Tria1", "Tria2"):
         nodes, q = mesh.rect_quad(4, 4)
         el = torch.cat([q[:, [0, 1, 2]], q[:, [0, 2, 3]]])
-    elif etype == "Hexa1":
+    elif etype in ("Hexa1", "Hexa2"):
         nodes, el = mesh.cube_hexa(3, 3, 3)
     else:
         nodes, el = mesh.cube_tetra(3, 3, 3)
-    if etype in ("Quad2", "Tria2", "Tetra2"):
+    if etype in ("Quad2", "Tria2", "Tetra2", "Hexa2"):
         nodes, el = mesh.linear_to_quadratic(nodes, el)
     dim = nodes.shape[1]
     if dim == 2:

@@ -19,14 +19,14 @@ from torchfem_gb300.materials import (
 
 def test_element_tables_match_oracle():
     for cls, name in ((E.Hexa1, "Hexa1"), (E.Quad1, "Quad1"), (E.Tetra2, "Tetra2"), (E.Tetra1, "Tetra1"),
-                      (E.Tria1, "Tria1")):
+                      (E.Tria1, "Tria1"), (E.Hexa2, "Hexa2")):
         n_e, dim, ip, w, dn = O.ELEMENTS[name]
-        assert np.array_equal(cls.gradient_table().numpy(), dn(ip))
+        np.testing.assert_allclose(cls.gradient_table().numpy(), dn(ip), rtol=0, atol=1e-15)
         assert np.array_equal(cls.iweights().numpy().astype(np.float64), w)
 
 
 def test_shape_functions_partition_of_unity():
-    for cls in (E.Hexa1, E.Quad1, E.Quad2, E.Tria1, E.Tria2, E.Tetra1, E.Tetra2):
+    for cls in (E.Hexa1, E.Quad1, E.Quad2, E.Tria1, E.Tria2, E.Tetra1, E.Tetra2, E.Hexa2):
         xi = cls.ipoints()
         assert torch.allclose(cls.N(xi).sum(-1), torch.ones(len(xi), dtype=torch.float64))
         assert torch.allclose(cls.B(xi).sum(-1), torch.zeros(len(xi), cls.iso_dim, dtype=torch.float64), atol=1e-14)

@@ -141,3 +141,21 @@ def test_shell_roof(golden):
     s = O.shell_station_stress(nodes, el, Cv, h, u.reshape(-1, 6))
     assert rel(s, g["sigma_ip"]) <= 1e-10
     assert rel(s.mean(0), g["sigma"]) <= 1e-10
+
+
+def test_hexa2(golden):
+    """Hexa2 (20-node serendipity): pattern, element matrices against the
+    reference's k0() and the linear solution of a jittered cube."""
+    g = golden("hexa2_jitter2.npz")
+    nodes, el = g["nodes"], g["elements"]
+    m = O.LinearModel(nodes, el, O.elastic_c("3d", 1000.0, 0.3, len(el)))
+    assert np.array_equal(m.glob_idx, g["glob_idx"]) and np.array_equal(m.k_map, g["k_map"])
+    k = m.stiffness()
+    assert np.abs(k - g["ke"]).max() <= 1e-13 * np.abs(g["ke"]).max()
+    con = np.zeros(nodes.shape, dtype=bool)
+    con[nodes[:, 0] == 0.0, :] = True
+    F = np.zeros(nodes.shape)
+    F[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    u, f, s = m.solve(F, con)
+    rel = lambda a, b: np.abs(a - b).max() / np.abs(b).max()  # noqa: E731
+    assert rel(u, g["u"]) <= 1e-10 and rel(f, g["f"]) <= 1e-10 and rel(s, g["sigma"]) <= 1e-10

@@ -32,6 +32,7 @@ namespace tfg {
     TFG_ETYPE_CASE(FEM_TRIA1, 3, 2, 1)                   \
     TFG_ETYPE_CASE(FEM_QUAD2, 8, 2, 4)                   \
     TFG_ETYPE_CASE(FEM_TRIA2, 6, 2, 3)                   \
+    TFG_ETYPE_CASE(FEM_HEXA2, 20, 3, 8)                  \
     default:                                             \
       set_last_error("unsupported element type %d", etype); \
       return FEM_INVALID;                                \
@@ -47,6 +48,7 @@ int etype_info(int etype, int* ne, int* d, int* nip) {
     case FEM_QUAD2: *ne = 8; *d = 2; *nip = 4; return FEM_OK;
     case FEM_TRIA2: *ne = 6; *d = 2; *nip = 3; return FEM_OK;
     case FEM_SHELL3: *ne = 3; *d = 6; *nip = 1; return FEM_OK;  // d: DOFs per node
+    case FEM_HEXA2: *ne = 20; *d = 3; *nip = 8; return FEM_OK;
     default: return FEM_INVALID;
   }
 }

@@ -22,7 +22,7 @@ FEM_INVALID = 5
 FEM_CUDA_ERROR = 6
 FEM_BREAKDOWN = 7
 
-FEM_QUAD1, FEM_HEXA1, FEM_TETRA2, FEM_TETRA1, FEM_TRIA1, FEM_QUAD2, FEM_TRIA2, FEM_SHELL3 = range(1, 9)
+FEM_QUAD1, FEM_HEXA1, FEM_TETRA2, FEM_TETRA1, FEM_TRIA1, FEM_QUAD2, FEM_TRIA2, FEM_SHELL3, FEM_HEXA2 = range(1, 10)
 FEM_MAT_ISO, FEM_MAT_GENERAL, FEM_MAT_TANGENT_IP = 1, 2, 3
 FEM_F64, FEM_F32 = 0, 1
 FEM_FMT_CSR_F64, FEM_FMT_SELL_F32 = 1, 2

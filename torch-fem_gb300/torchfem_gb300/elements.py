@@ -299,5 +299,69 @@ class Hexa1(Element):
         return _f64([1.0] * 8)
 
 
-SOLID_TYPES = {4: Tetra1, 8: Hexa1, 10: Tetra2}
+class Hexa2(Element):
+    """Twenty-node serendipity hexahedron with the 2 x 2 x 2 rule of Hexa1
+    (elements.py:1078-1406): corner functions
+    (1 + s1 x)(1 + s2 y)(1 + s3 z)(s1 x + s2 y + s3 z - 2) / 8, mid-edge
+    functions (1 - t^2)(1 + s y)(1 + s' z) / 4 with t the coordinate along
+    the edge."""
+
+    nodes, iso_dim, etype_id = 20, 3, _lib.FEM_HEXA2
+
+    # iso coordinates of the 8 corners and the 12 mid-edge nodes, reference order
+    _COORDS = Hexa1._SIGNS + ((0, -1, -1), (1, 0, -1), (0, 1, -1), (-1, 0, -1),
+                              (0, -1, 1), (1, 0, 1), (0, 1, 1), (-1, 0, 1),
+                              (-1, -1, 0), (1, -1, 0), (1, 1, 0), (-1, 1, 0))
+
+    @classmethod
+    def _terms(cls, xi):
+        x, y, z = xi[..., 0], xi[..., 1], xi[..., 2]
+        N, dx, dy, dz = [], [], [], []
+        for sx, sy, sz in cls._COORDS:
+            if sx and sy and sz:
+                a, b, c = 1.0 + sx * x, 1.0 + sy * y, 1.0 + sz * z
+                g = sx * x + sy * y + sz * z - 2.0
+                N.append(0.125 * a * b * c * g)
+                dx.append(0.125 * sx * b * c * (g + a))
+                dy.append(0.125 * sy * a * c * (g + b))
+                dz.append(0.125 * sz * a * b * (g + c))
+            elif sx == 0:
+                b, c = 1.0 + sy * y, 1.0 + sz * z
+                N.append(0.25 * (1.0 - x * x) * b * c)
+                dx.append(-0.5 * x * b * c)
+                dy.append(0.25 * (1.0 - x * x) * sy * c)
+                dz.append(0.25 * (1.0 - x * x) * b * sz)
+            elif sy == 0:
+                a, c = 1.0 + sx * x, 1.0 + sz * z
+                N.append(0.25 * a * (1.0 - y * y) * c)
+                dx.append(0.25 * sx * (1.0 - y * y) * c)
+                dy.append(-0.5 * y * a * c)
+                dz.append(0.25 * a * (1.0 - y * y) * sz)
+            else:
+                a, b = 1.0 + sx * x, 1.0 + sy * y
+                N.append(0.25 * a * b * (1.0 - z * z))
+                dx.append(0.25 * sx * b * (1.0 - z * z))
+                dy.append(0.25 * a * sy * (1.0 - z * z))
+                dz.append(-0.5 * z * a * b)
+        return N, dx, dy, dz
+
+    @classmethod
+    def N(cls, xi):
+        return torch.stack(cls._terms(xi)[0], dim=-1)
+
+    @classmethod
+    def B(cls, xi):
+        _, dx, dy, dz = cls._terms(xi)
+        return torch.stack([torch.stack(dx, dim=-1), torch.stack(dy, dim=-1), torch.stack(dz, dim=-1)], dim=-2)
+
+    @classmethod
+    def ipoints(cls):
+        return Hexa1.ipoints()
+
+    @classmethod
+    def iweights(cls):
+        return _f64([1.0] * 8)
+
+
+SOLID_TYPES = {4: Tetra1, 8: Hexa1, 10: Tetra2, 20: Hexa2}
 PLANAR_TYPES = {3: Tria1, 4: Quad1, 6: Tria2, 8: Quad2}

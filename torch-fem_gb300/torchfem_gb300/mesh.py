@@ -64,6 +64,8 @@ _EDGES = {
     (3, 2): [[0, 1], [1, 2], [2, 0]],  # Tria1
     (4, 2): [[0, 1], [1, 2], [2, 3], [3, 0]],  # Quad1
     (4, 3): [[0, 1], [1, 2], [0, 2], [3, 0], [1, 3], [2, 3]],  # Tetra1
+    (8, 3): [[0, 1], [1, 2], [2, 3], [3, 0], [4, 5], [5, 6], [6, 7], [7, 4],
+             [0, 4], [1, 5], [2, 6], [3, 7]],  # Hexa1
 }
 
 

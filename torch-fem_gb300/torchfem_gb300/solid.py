@@ -7,7 +7,7 @@ from .elements import SOLID_TYPES
 
 
 class Solid(Mechanics):
-    """Solid mechanics model: Hexa1, Tetra1 or Tetra2 connectivity, picked by
+    """Solid mechanics model: Hexa1, Hexa2, Tetra1 or Tetra2 connectivity, picked by
     the number of nodes per element (solid.py:32-44).  Plotting is not part of
     this library."""
 
