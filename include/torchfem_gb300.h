@@ -405,6 +405,17 @@ int fem_pcg_mixed(const fem_matrix* A32, const fem_operator64* op, const double*
                   double rtol, double delta, int64_t max_iter, void* ws, size_t ws_bytes,
                   fem_solve_info* info, void* stream);
 
+/* Workspace bytes of fem_minres for the FP64 scalar CSR matrix A. */
+size_t fem_minres_workspace_bytes(const fem_matrix* A);
+
+/* Jacobi-preconditioned MINRES (Paige-Saunders) from x = 0 on the FP64 CSR
+ * matrix (precond = inverse diagonal, fem_jacobi): the reference's GPU
+ * method="minres", CuPy's minres with a Jacobi M (sparse.py:405-412).  Stops
+ * when the preconditioned residual estimate falls below rtol times its
+ * initial value.  Symmetric A (definite or not), positive M. */
+int fem_minres(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter, void* ws,
+               size_t ws_bytes, fem_solve_info* info, void* stream);
+
 /* ---------------------------------------------------------------- shell --
  * Tria1 flat-facet shell, homogeneous linear-elastic section (the reference's
  * Shell with a plane-stress material, src/torchfem/shell.py:48-603).  Nodes

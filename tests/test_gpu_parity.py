@@ -141,6 +141,26 @@ def test_jittered_cube_gradients(cuda, golden, precision):
     assert rel(gE, g["grad_E"]) <= RTOL
 
 
+def test_minres_jittered_cube_vs_reference(cuda, golden):
+    """method="minres" (Jacobi MINRES, the reference GPU branch's other
+    Krylov method): forward and adjoint against the reference."""
+    g = golden("hexa_jitter3.npz")
+    E = torch.tensor(g["E"], requires_grad=True)
+    m = cube_model(g, E)
+    forces = m.forces.clone().requires_grad_(True)
+    m.forces = forces
+    u, f, s, _, _ = m.solve(stol=1e-12, method="minres", differentiable_parameters=(forces, E))
+    assert m.last_solve.linear == "minres"
+    assert rel(u, g["u"]) <= RTOL
+    assert rel(f, g["f"]) <= RTOL
+    assert rel(s, g["sigma"]) <= RTOL
+    (gf,) = torch.autograd.grad(u.sum(), forces, retain_graph=True)
+    assert rel(gf, g["grad_forces"]) <= RTOL
+    L = torch.inner(f.ravel(), u.ravel())
+    (gE,) = torch.autograd.grad(L, E)
+    assert rel(gE, g["grad_E"]) <= RTOL
+
+
 def simp(Nx, Ny, rho):
     nodes, el = mesh.rect_quad(Nx + 1, Ny + 1, 2.0, 1.0)
     m = Planar(nodes, el, IsotropicElasticityPlaneStress(rho**3 * 1.0, 0.3))
@@ -350,6 +370,19 @@ def test_neo_hookean_tetra2_vs_reference(cuda, golden, precision):
     assert rel(F, g["F"]) <= 1e-8
     R = f[right, 0].sum()
     assert abs(float(R.detach()) - float(g["reaction"])) <= 1e-8 * abs(float(g["reaction"]))
+    (gE,) = torch.autograd.grad(R, E)
+    assert rel(gE, g["grad_E"]) <= 1e-7
+
+
+def test_neo_hookean_with_minres(cuda, golden):
+    """MINRES also carries the Newton solves of the indefinite Neo-Hookean
+    tangents (config 4 at small size)."""
+    g = golden("hyper_tet2_6x2x2.npz")
+    m, E, right = _hyper_model(g)
+    u, f, s, F, _ = m.solve(increments=torch.linspace(0.0, 1.0, 11), nlgeom=True, rtol=1e-10, atol=1e-10,
+                            max_iter=20, stol=1e-13, method="minres", differentiable_parameters=E)
+    assert rel(u, g["u"]) <= 1e-8
+    R = f[right, 0].sum()
     (gE,) = torch.autograd.grad(R, E)
     assert rel(gE, g["grad_E"]) <= 1e-7
 

@@ -86,6 +86,9 @@ def test_method_resolution():
         resolve_precision("foo", None)
     with pytest.raises(RuntimeError):
         resolve_precision("spsolve", None)
+    assert resolve_precision("minres", None) == "fp64"
+    with pytest.raises(ValueError):
+        resolve_precision("minres", "mixed")
 
 
 def test_material_kernel_data_and_step():

@@ -1331,6 +1331,176 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
   if (cta == 0 && threadIdx.x == 0 && *(volatile int*)&c->bar_error) c->done = kDoneBarrierTimeout;
 }
 
+// ------------------------------------------------------------------ MINRES --
+// Jacobi-preconditioned MINRES (Paige & Saunders, SIAM J. Numer. Anal. 12,
+// 1975) on the FP64 CSR matrix: the reference's GPU `method="minres"`
+// (sparse.py:405-412, CuPy's minres with a Jacobi M).  Three kernels per
+// iteration; every scalar of the Lanczos / Givens recurrences lives in the
+// control block and is updated by the last-arriving CTA, so the host only
+// reads the control block between chunks of iterations.  Buffers rotate
+// (r1, r2, y and w1, w2, w) by host-side indexing instead of copies.
+// Stops when the preconditioned residual estimate phibar <= rtol * beta1.
+struct MrCtrl {
+  double beta1, beta, oldb, alfa, dbar, epsln, oldeps, phibar, phi, cs, sn, gamma, delta, tnorm2;
+  double rtol;
+  long long itn, max_iter;
+  int done;
+  int pending;  // a w / x update of the last iteration has not been applied yet
+  unsigned int counter;
+};
+
+__device__ __forceinline__ bool mr_idle(const MrCtrl* c) { return (*(volatile const int*)&c->done) != 0; }
+
+// x = 0, r1 = r2 = b, pz = M b; beta1 = sqrt(b . M b).
+__global__ void __launch_bounds__(256) k_mr_init(int64_t n, const double* __restrict__ b, const double* __restrict__ dinv,
+                                                 double* __restrict__ x, double* __restrict__ r1,
+                                                 double* __restrict__ r2, double* __restrict__ pz,
+                                                 double* __restrict__ partial, MrCtrl* c) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double bi = b[i], zi = dinv[i] * bi;
+    x[i] = 0.0;
+    r1[i] = bi;
+    r2[i] = bi;
+    pz[i] = zi;
+    s += bi * zi;
+  }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (arrive_last(&c->counter)) {
+    const double t = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      c->counter = 0;
+      if (!(t >= 0.0) || !isfinite(t)) {
+        c->done = kDoneNonFinite;
+      } else {
+        const double b1 = sqrt(t);
+        c->beta1 = c->beta = c->phibar = b1;
+        c->oldb = c->dbar = c->epsln = c->oldeps = c->phi = c->gamma = c->delta = c->tnorm2 = c->alfa = 0.0;
+        c->cs = -1.0;
+        c->sn = 0.0;
+        c->itn = 0;
+        c->pending = 0;
+        c->done = b1 == 0.0 ? kDoneConverged : kDoneNo;
+      }
+    }
+  }
+}
+
+// Pending update of the previous iteration (w = (v - oldeps w1 - delta w2) /
+// gamma, x += phi w) with that iteration's v, then v = pz / beta for this one.
+__global__ void __launch_bounds__(256) k_mr_step(int64_t n, double* __restrict__ v, const double* __restrict__ pz,
+                                                 const double* __restrict__ w1, const double* __restrict__ w2,
+                                                 double* __restrict__ w, double* __restrict__ x, MrCtrl* c) {
+  const int pending = c->pending;
+  const bool run = !mr_idle(c);
+  if (!pending && !run) return;
+  const double oldeps = c->oldeps, delta = c->delta, gamma = c->gamma, phi = c->phi, s = 1.0 / c->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (pending) {
+      const double wi = (v[i] - oldeps * w1[i] - delta * w2[i]) / gamma;
+      w[i] = wi;
+      x[i] += phi * wi;
+    }
+    if (run) v[i] = s * pz[i];
+  }
+  if (arrive_last(&c->counter) && threadIdx.x == 0) {
+    c->counter = 0;
+    c->pending = 0;
+  }
+}
+
+// y = A v - (beta / oldb) r1 (scalar CSR, TPR lanes per row); alfa = v . y.
+template <int TPR>
+__global__ void __launch_bounds__(256) k_mr_spmv(int64_t n, const int64_t* __restrict__ row_ptr,
+                                                 const int32_t* __restrict__ col, const double* __restrict__ val,
+                                                 const double* __restrict__ v, const double* __restrict__ r1,
+                                                 double* __restrict__ y, double* __restrict__ partial, MrCtrl* c) {
+  __shared__ double red[32];
+  if (mr_idle(c)) return;
+  const double f = c->itn >= 1 ? c->beta / c->oldb : 0.0;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = t / TPR;
+  const int sub = (int)(t % TPR);
+  double s = 0.0, vy = 0.0;
+  if (row < n) {
+    const int64_t rs = row_ptr[row], re = row_ptr[row + 1];
+    for (int64_t j = rs + sub; j < re; j += TPR) s += val[j] * v[col[j]];
+  }
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
+  if (row < n && sub == 0) {
+    const double yi = s - f * r1[row];
+    y[row] = yi;
+    vy = v[row] * yi;
+  }
+  vy = block_sum(vy, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = vy;
+  if (arrive_last(&c->counter)) {
+    const double a = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      c->counter = 0;
+      c->alfa = a;
+      if (!isfinite(a)) c->done = kDoneNonFinite;
+    }
+  }
+}
+
+// y -= (alfa / beta) r2; pz = M y; beta' = sqrt(y . pz); then the Lanczos
+// and Givens recurrences and the stopping test (last CTA).
+__global__ void __launch_bounds__(256) k_mr_update(int64_t n, double* __restrict__ y, const double* __restrict__ r2,
+                                                   const double* __restrict__ dinv, double* __restrict__ pz,
+                                                   double* __restrict__ partial, MrCtrl* c) {
+  __shared__ double red[32];
+  if (mr_idle(c)) return;
+  const double f = c->alfa / c->beta;
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double yi = y[i] - f * r2[i];
+    const double zi = dinv[i] * yi;
+    y[i] = yi;
+    pz[i] = zi;
+    s += yi * zi;
+  }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (arrive_last(&c->counter)) {
+    const double t = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      c->counter = 0;
+      if (!(t >= 0.0) || !isfinite(t)) {  // M must be positive definite
+        c->done = isfinite(t) ? kDoneBreakdown : kDoneNonFinite;
+      } else {
+        const double alfa = c->alfa;
+        c->oldb = c->beta;
+        const double beta = sqrt(t);
+        c->beta = beta;
+        c->tnorm2 += alfa * alfa + c->oldb * c->oldb + beta * beta;
+        // previous rotation on the new column
+        c->oldeps = c->epsln;
+        const double delta = c->cs * c->dbar + c->sn * alfa;
+        const double gbar = c->sn * c->dbar - c->cs * alfa;
+        c->epsln = c->sn * beta;
+        c->dbar = -c->cs * beta;
+        // new rotation
+        double gamma = sqrt(gbar * gbar + beta * beta);
+        if (gamma < 1e-300) gamma = 1e-300;
+        c->cs = gbar / gamma;
+        c->sn = beta / gamma;
+        c->phi = c->cs * c->phibar;
+        c->phibar = c->sn * c->phibar;
+        c->delta = delta;
+        c->gamma = gamma;
+        c->pending = 1;
+        c->itn += 1;
+        if (c->phibar <= c->rtol * c->beta1 || beta == 0.0) c->done = kDoneConverged;
+        else if (c->itn >= c->max_iter) c->done = kDoneMaxIter;
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------- host driver --
 constexpr int kThreads = 256;
 
@@ -1980,6 +2150,119 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
   else if (h.done != kDoneConverged)
     set_last_error("mixed CG did not converge: %lld iterations, relative residual %.3e, code %d",
                    h.iters, h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0, h.done);
+  return status_of(h.done);
+}
+
+}  // extern "C"
+
+// --------------------------------------------------------------- MINRES --
+namespace tfg {
+
+struct MrVecs {
+  MrCtrl* ctrl;
+  double *v, *pz, *R[3], *W[3];
+  double* partial;
+};
+
+static size_t mr_layout(int64_t n, unsigned grid, MrVecs* v, void* ws) {
+  char* base = reinterpret_cast<char*>(ws);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* ptr = base ? base + off : nullptr;
+    off += align256(bytes);
+    return ptr;
+  };
+  MrVecs t;
+  t.ctrl = reinterpret_cast<MrCtrl*>(take(sizeof(MrCtrl)));
+  t.v = reinterpret_cast<double*>(take(n * sizeof(double)));
+  t.pz = reinterpret_cast<double*>(take(n * sizeof(double)));
+  for (int i = 0; i < 3; ++i) t.R[i] = reinterpret_cast<double*>(take(n * sizeof(double)));
+  for (int i = 0; i < 3; ++i) t.W[i] = reinterpret_cast<double*>(take(n * sizeof(double)));
+  t.partial = reinterpret_cast<double*>(take(sizeof(double) * (grid + 1)));
+  if (v) *v = t;
+  return off;
+}
+
+static unsigned mr_grid(const fem_matrix* A) {
+  return std::max<unsigned>(vec_grid(A->n), grid_for(A->n_rows * kCsrTpr, kThreads));
+}
+
+}  // namespace tfg
+
+extern "C" {
+
+size_t fem_minres_workspace_bytes(const fem_matrix* A) {
+  if (validate_matrix(A) != FEM_OK || A->format != FEM_FMT_CSR_F64 || A->block != 1) return 0;
+  return mr_layout(A->n, mr_grid(A), nullptr, nullptr);
+}
+
+int fem_minres(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter, void* ws,
+               size_t ws_bytes, fem_solve_info* info, void* stream) {
+  int rc = validate_matrix(A);
+  if (rc) return rc;
+  if (A->format != FEM_FMT_CSR_F64 || A->block != 1) {
+    set_last_error("fem_minres: needs the FP64 scalar CSR matrix with its inverse diagonal");
+    return FEM_INVALID;
+  }
+  const size_t need = fem_minres_workspace_bytes(A);
+  if (need == 0 || ws_bytes < need) {
+    set_last_error("fem_minres: workspace too small");
+    return FEM_INVALID;
+  }
+  cudaStream_t st = as_stream(stream);
+  const int64_t n = A->n;
+  MrVecs v;
+  mr_layout(n, mr_grid(A), &v, ws);
+  MrCtrl h;
+  memset(&h, 0, sizeof(h));
+  h.rtol = rtol;
+  h.max_iter = max_iter;
+  if (cudaMemcpyAsync(v.ctrl, &h, sizeof(MrCtrl), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return check_cuda("fem_minres ctrl");
+  for (int i = 0; i < 3; ++i) cudaMemsetAsync(v.W[i], 0, sizeof(double) * n, st);
+  const double* dinv = (const double*)A->precond;
+  const unsigned vg = vec_grid(n);
+  k_mr_init<<<vg, kThreads, 0, st>>>(n, b, dinv, x, v.R[0], v.R[1], v.pz, v.partial, v.ctrl);
+  note_launch();
+  TFG_CHECK_LAUNCH("fem_minres init");
+  if (cudaMemcpyAsync(&h, v.ctrl, sizeof(MrCtrl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda("fem_minres read");
+  const unsigned sg = grid_for(A->n_rows * kCsrTpr, kThreads);
+  int64_t k = 0;
+  int chunk = 8;
+  while (h.done == kDoneNo) {
+    for (int c = 0; c < chunk; ++c, ++k) {
+      k_mr_step<<<vg, kThreads, 0, st>>>(n, v.v, v.pz, v.W[k % 3], v.W[(k + 1) % 3], v.W[(k + 2) % 3], x, v.ctrl);
+      k_mr_spmv<kCsrTpr><<<sg, kThreads, 0, st>>>(A->n_rows, A->row_ptr, A->col, (const double*)A->val, v.v,
+                                                  v.R[k % 3], v.R[(k + 2) % 3], v.partial, v.ctrl);
+      k_mr_update<<<vg, kThreads, 0, st>>>(n, v.R[(k + 2) % 3], v.R[(k + 1) % 3], dinv, v.pz, v.partial, v.ctrl);
+      note_launch();
+      note_launch();
+      note_launch();
+    }
+    TFG_CHECK_LAUNCH("fem_minres iterate");
+    if (cudaMemcpyAsync(&h, v.ctrl, sizeof(MrCtrl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return check_cuda("fem_minres read");
+    chunk = std::min(chunk * 2, 256);
+  }
+  // the last iteration's w / x update
+  k_mr_step<<<vg, kThreads, 0, st>>>(n, v.v, v.pz, v.W[k % 3], v.W[(k + 1) % 3], v.W[(k + 2) % 3], x, v.ctrl);
+  note_launch();
+  TFG_CHECK_LAUNCH("fem_minres finish");
+  if (cudaStreamSynchronize(st) != cudaSuccess) return check_cuda("fem_minres sync");
+  if (info) {
+    info->iterations = h.itn;
+    info->replacements = 0;
+    info->rel_residual = h.beta1 > 0 ? h.phibar / h.beta1 : 0.0;
+    info->status = status_of(h.done);
+    info->spmv_ms = 0.0;
+    info->spmv_timed = 0;
+  }
+  if (h.done != kDoneConverged)
+    set_last_error("MINRES did not converge: %lld iterations, preconditioned residual %.3e, code %d", h.itn,
+                   h.beta1 > 0 ? h.phibar / h.beta1 : 0.0, h.done);
   return status_of(h.done);
 }
 

@@ -372,15 +372,30 @@ class DeviceMesh:
         return sysm
 
     def solve(self, sysm: LinearSystem, b: Tensor, rtol: float, max_iter: int | None = None,
-              delta: float = 0.1, refine: bool = True) -> Tensor:
+              delta: float = 0.1, refine: bool = True, linear: str = "cg") -> Tensor:
         """x with A x = b (A the condensed system), from x = 0.  For the mixed
         system, refine=False runs the FP32 CG alone (an inner Newton solve
-        whose FP64 refinement is the Newton iteration itself)."""
+        whose FP64 refinement is the Newton iteration itself).  linear="minres"
+        runs MINRES on the FP64 system."""
         x = self._empty(self.n_dofs, torch.float64)
         info = _lib.FemSolveInfo()
         if max_iter is None:
             max_iter = 10 * self.n_dofs
         b = b.contiguous()
+        if linear == "minres":
+            if sysm.precision != "fp64":
+                raise ValueError("MINRES runs on the FP64 system")
+            if getattr(sysm, "mr_ws", None) is None:
+                sysm.mr_ws = self._ws(self.lib.fem_minres_workspace_bytes(C.byref(sysm.matrix)))
+            rc = self.lib.fem_minres(
+                C.byref(sysm.matrix), ptr(b), ptr(x), rtol, max_iter, ptr(sysm.mr_ws), sysm.mr_ws.numel(),
+                C.byref(info), self.stream,
+            )
+            sysm.stats = SolveStats(info.iterations, 0, info.rel_residual, 0.0, 0)
+            if rc == _lib.FEM_NOT_CONVERGED:
+                raise RuntimeError(f"minres failed with exit code {info.iterations}")
+            check(rc, "linear solve")
+            return x
         if sysm.precision == "fp64" or not refine:
             rc = self.lib.fem_pcg(
                 C.byref(sysm.matrix), ptr(b), ptr(x), rtol, max_iter, ptr(sysm.ws), sysm.ws.numel(),

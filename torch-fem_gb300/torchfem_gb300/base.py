@@ -27,19 +27,24 @@ def resolve_precision(method: str | None, precision: str | None) -> str:
     """Maps `method` / `precision` to the solver variant.
 
     "cg" (and None) is the Jacobi-preconditioned CG of the reference's CUDA
-    branch in FP64; "gb300-mixed" or precision="mixed" selects FP32 storage
-    and CG inside FP64 residual replacement.  The reference's direct and
-    third-party backends are not part of this library.
+    branch in FP64, "minres" its Jacobi-preconditioned MINRES (FP64);
+    "gb300-mixed" or precision="mixed" selects FP32 storage and CG inside
+    FP64 residual replacement.  The reference's direct and third-party
+    backends are not part of this library.
     """
     if method is not None and method not in _REFERENCE_METHODS and method not in _GPU_METHODS:
         raise ValueError(
             f"Method {method} is not supported. Choose from 'cg', 'gb300' or 'gb300-mixed'."
         )
-    if method in ("spsolve", "minres", "pardiso", "amgx"):
+    if method in ("spsolve", "pardiso", "amgx"):
         raise RuntimeError(
             f"Method '{method}' is a CPU/third-party backend of torch-fem; torchfem_gb300 "
-            "solves with its own GPU CG ('cg', 'gb300', 'gb300-mixed')."
+            "solves with its own GPU Krylov methods ('cg', 'minres', 'gb300', 'gb300-mixed')."
         )
+    if method == "minres":
+        if precision not in (None, "fp64"):
+            raise ValueError("method 'minres' runs in FP64")
+        return "fp64"
     p = _GPU_METHODS[method]
     if precision is not None:
         if precision not in ("fp64", "mixed"):
@@ -219,6 +224,7 @@ class FEM:
         else:
             sc = SolveContext(dm, con_mask, mat_kind, prec, max_iter, rtol, atol, stol, cg_max_iter)
         sc.verbose = verbose
+        sc.linear = "minres" if method == "minres" else "cg"
         self.last_solve = sc
 
         shape_ip = (dm.nip, self.n_elem, *self.n_flux)

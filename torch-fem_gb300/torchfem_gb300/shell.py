@@ -169,6 +169,7 @@ class Shell(Mechanics):
         con_bool = self._constraints.reshape(-1).to(dev)
         sc = ShellContext(self, dm, con_bool, max_iter, rtol, atol, stol, cg_max_iter)
         sc.verbose = verbose
+        sc.linear = "minres" if method == "minres" else "cg"
         self.last_solve = sc
         with torch.set_grad_enabled(track):
             mat = self.kernel_data().to(dev, torch.float64).contiguous()
@@ -251,6 +252,7 @@ class ShellContext:
         self.max_iter, self.rtol, self.atol, self.stol = max_iter, rtol, atol, stol
         self.cg_max_iter = cg_max_iter
         self.verbose = False
+        self.linear = "cg"
         self.n_z = model.n_z
         self.z = model.z_simpson.to(dev, torch.float64).contiguous()
         self.w = model.w_simpson.to(dev, torch.float64).contiguous()
@@ -325,7 +327,7 @@ class ShellContext:
         return (None if gmat is None else gmat.view(dm.n_elem, 11)), gthick, gu
 
     def solve(self, b: Tensor) -> Tensor:
-        x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter)
+        x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, linear=self.linear)
         self.iterations.append(self.system.stats.iterations)
         return x
 

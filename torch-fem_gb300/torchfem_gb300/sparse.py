@@ -49,6 +49,7 @@ class SolveContext:
         self.newton_iterations: list[int] = []
         self.verbose = False
         self.inner_rtol = 1e-6
+        self.linear = "cg"  # or "minres" (FP64 path)
 
     def structs(self, mat_data: Tensor, thickness: Tensor | None):
         from . import _lib
@@ -78,7 +79,7 @@ class SolveContext:
         if inner and self.precision == "mixed":
             x = self.dm.solve(self.system, b, max(self.stol, self.inner_rtol), self.cg_max_iter, refine=False)
         else:
-            x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, self.delta)
+            x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, self.delta, linear=self.linear)
         self.iterations.append(self.system.stats.iterations)
         return x
 
