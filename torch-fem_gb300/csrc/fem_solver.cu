@@ -1150,15 +1150,24 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
           const int nr = min(kTmaRows, len - cons.k0);
           const float* vb = (const float*)(ring_base + (size_t)slot * kStageBytes);
           const int32_t* cb = (const int32_t*)(ring_base + (size_t)slot * kStageBytes + (size_t)nr * kSlotVal);
-          for (int rr = 0; rr < nr; ++rr) {
-            const int64_t cc = cb[rr * 32 + lane];
-            float xv[G];
+          // all gathers of the stage in flight before the products
+          float xs[kTmaRows][G];
 #pragma unroll
-            for (int j = 0; j < G; ++j) xv[j] = (float)gsrc[cc * G + j];
+          for (int rr = 0; rr < kTmaRows; ++rr) {
+            if (rr < nr) {
+              const int64_t cc = cb[rr * 32 + lane];
 #pragma unroll
-            for (int i = 0; i < G; ++i)
+              for (int j = 0; j < G; ++j) xs[rr][j] = (float)gsrc[cc * G + j];
+            }
+          }
 #pragma unroll
-              for (int j = 0; j < G; ++j) y[i] = fmaf(vb[(rr * 9 + i * G + j) * 32 + lane], xv[j], y[i]);
+          for (int rr = 0; rr < kTmaRows; ++rr) {
+            if (rr < nr) {
+#pragma unroll
+              for (int i = 0; i < G; ++i)
+#pragma unroll
+                for (int j = 0; j < G; ++j) y[i] = fmaf(vb[(rr * 9 + i * G + j) * 32 + lane], xs[rr][j], y[i]);
+            }
           }
           ++consumed;
           if (cons.k0 + nr >= len) {  // slice done: rows of this warp
