@@ -416,6 +416,14 @@ size_t fem_minres_workspace_bytes(const fem_matrix* A);
 int fem_minres(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter, void* ws,
                size_t ws_bytes, fem_solve_info* info, void* stream);
 
+/* Diagnostic of the bounded waits (no counterpart in the reference): one CTA
+ * waits at a two-CTA grid barrier that the other CTA never reaches.  The
+ * wait gives up after spin_limit clock cycles and the call returns
+ * FEM_CUDA_ERROR with the barrier-timeout message; the context stays usable.
+ * ws: fem_diag_workspace_bytes() bytes of device memory. */
+size_t fem_diag_workspace_bytes(void);
+int fem_diag_barrier_timeout(void* ws, size_t ws_bytes, long long spin_limit, void* stream);
+
 /* ---------------------------------------------------------------- shell --
  * Tria1 flat-facet shell, homogeneous linear-elastic section (the reference's
  * Shell with a plane-stress material, src/torchfem/shell.py:48-603).  Nodes

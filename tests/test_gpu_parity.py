@@ -290,6 +290,25 @@ def test_negative_jacobian_raises(cuda):
         m.solve()
 
 
+def test_barrier_wait_runs_out_cleanly(cuda):
+    """A grid-barrier wait that can never complete gives up after its cycle
+    limit and reports the timeout; the context stays usable afterwards."""
+    from torchfem_gb300 import _lib
+
+    lib = _lib.load()
+    ws = torch.zeros(lib.fem_diag_workspace_bytes(), dtype=torch.uint8, device=cuda)
+    rc = lib.fem_diag_barrier_timeout(ws.data_ptr(), ws.numel(), 2_000_000, _lib.stream_handle(cuda))
+    assert rc == _lib.FEM_CUDA_ERROR
+    assert b"barrier timeout" in lib.fem_last_error()
+    torch.cuda.synchronize()
+    nodes, el = mesh.cube_hexa(3, 3, 3)
+    m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    m.forces[nodes[:, 0] == 1.0, 2] = -1.0
+    u = m.solve(stol=1e-12)[0]
+    assert torch.isfinite(u).all() and float(u.abs().max()) > 0.0
+
+
 def test_cg_iteration_cap_cuts_back_then_raises(cuda):
     nodes, el = mesh.cube_hexa(5, 5, 5)
     m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))

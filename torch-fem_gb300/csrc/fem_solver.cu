@@ -1510,6 +1510,14 @@ __global__ void __launch_bounds__(256) k_mr_update(int64_t n, double* __restrict
   }
 }
 
+// Diagnostic for the bounded waits: CTA 1 leaves at once, CTA 0 waits at a
+// grid barrier of two CTAs that therefore never completes; the wait must run
+// out after spin_limit cycles, set bar_error and return.
+__global__ void k_diag_barrier(Ctrl* c, long long spin_limit) {
+  if (blockIdx.x != 0) return;
+  grid_barrier<0>(c, spin_limit, nullptr, 0, [](const double*) {});
+}
+
 // ------------------------------------------------------------- host driver --
 constexpr int kThreads = 256;
 
@@ -2161,6 +2169,35 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
                    h.iters, h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0, h.done);
   return status_of(h.done);
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------- diagnostics --
+extern "C" {
+
+int fem_diag_barrier_timeout(void* ws, size_t ws_bytes, long long spin_limit, void* stream) {
+  if (!ws || ws_bytes < sizeof(Ctrl) || spin_limit <= 0) {
+    set_last_error("fem_diag_barrier_timeout: needs a workspace of %zu bytes and a positive limit", sizeof(Ctrl));
+    return FEM_INVALID;
+  }
+  cudaStream_t st = as_stream(stream);
+  Ctrl* c = reinterpret_cast<Ctrl*>(ws);
+  if (cudaMemsetAsync(c, 0, sizeof(Ctrl), st) != cudaSuccess) return check_cuda("fem_diag_barrier_timeout memset");
+  k_diag_barrier<<<2, 32, 0, st>>>(c, spin_limit);
+  note_launch();
+  TFG_CHECK_LAUNCH("fem_diag_barrier_timeout");
+  int err = 0;
+  if (cudaMemcpyAsync(&err, &c->bar_error, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda("fem_diag_barrier_timeout read");
+  if (err) {
+    set_last_error("persistent CG: a grid-barrier or TMA-stage wait ran out (barrier timeout)");
+    return FEM_CUDA_ERROR;
+  }
+  return FEM_OK;
+}
+
+size_t fem_diag_workspace_bytes(void) { return sizeof(Ctrl); }
 
 }  // extern "C"
 

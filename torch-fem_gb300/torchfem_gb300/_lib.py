@@ -118,6 +118,8 @@ class FemOperator64(C.Structure):
 
 _P = C.POINTER
 _SIGNATURES = {
+    "fem_diag_workspace_bytes": (C.c_size_t, []),
+    "fem_diag_barrier_timeout": (C.c_int, [vp, C.c_size_t, C.c_longlong, vp]),
     "fem_minres_workspace_bytes": (C.c_size_t, [_P(FemMatrix)]),
     "fem_minres": (C.c_int, [_P(FemMatrix), vp, vp, C.c_double, i64, vp, C.c_size_t, _P(FemSolveInfo), vp]),
     "fem_shell_stiffness": (C.c_int, [_P(FemShell), vp, vp, vp, vp]),
