@@ -278,7 +278,7 @@ def plastic_problem(n_theta, n_rad):
     return model, t, right, nodes, elements
 
 
-def make_plastic(tf, n_theta=32, n_rad=8):
+def make_plastic(tf, n_theta=32, n_rad=8, name="plastic_ogrid_32x8.npz"):
     model, t, right, nodes, elements = plastic_problem(n_theta, n_rad)
     inc = torch.linspace(0.0, 1.0, 21)
     # the reference's plane-strain tangent is not the exact derivative of its
@@ -288,7 +288,7 @@ def make_plastic(tf, n_theta=32, n_rad=8):
     R = f[right, 0].sum()
     (gt,) = torch.autograd.grad(R, t)
     np.savez_compressed(
-        OUT / "plastic_ogrid_32x8.npz", nodes=nodes.numpy(), elements=elements.numpy(),
+        OUT / name, nodes=nodes.numpy(), elements=elements.numpy(),
         u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(), state=st.detach().numpy(),
         reaction=R.detach().numpy(), grad_t=gt.numpy(),
     )
@@ -417,6 +417,7 @@ MAKERS = {
     "simp_small": lambda tf: make_simp(tf, 20, 10, "simp_20x10.npz"),
     "simp_full": lambda tf: make_simp(tf, 400, 200, "simp_400x200.npz", sample=20),
     "hyper": make_hyper, "plastic": make_plastic, "shell": make_shell,
+    "plastic_full": lambda tf: make_plastic(tf, 256, 64, "plastic_ogrid_256x64.npz"),
     "hexa2": make_hexa2,
 }
 

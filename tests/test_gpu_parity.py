@@ -486,3 +486,83 @@ def test_simp_full_size_central_differences(cuda, golden):
             Lm = float(compliance(simp(400, 200, rm), rm, stol=1e-14))
         errs.append(abs((Lp - Lm) / (2 * h) - float(gr[i])) / abs(float(gr[i])))
     assert max(errs) <= 1e-3, errs
+
+
+# ------------------------------------------------------------ full sizes ---
+def test_config2_full_size_mixed_matches_fp64(cuda):
+    """Config 2 at full size (70^3 jittered Hexa1, 1,073,733 DOF): the mixed
+    path (FP32 storage and CG inside FP64 residual replacement) against the
+    FP64 path: u, sigma and d(sum u)/d(forces) to 1e-8 relative."""
+    import bench
+
+    m, forces = bench.cube_workload(70, cuda)
+    um, fm, sm, _, _, gm = bench.step(m, forces, "mixed", 1e-10)
+    up, fp, sp, _, _, gp = bench.step(m, forces, "fp64", 1e-10)
+    assert m.n_dofs == 1_073_733
+    assert rel(um, up) <= RTOL
+    assert rel(sm, sp) <= RTOL
+    assert rel(gm, gp) <= RTOL
+
+
+def test_config4_full_size_gradient_central_differences(cuda):
+    """Config 4 at full size (30 x 10 x 10 box, 6 Tetra2 per hex, 80,703 DOF,
+    Neo-Hookean, nlgeom, x = 3 face pulled to +0.5): d(tip reaction)/dE_e
+    through the adjoint against central differences on the 2 most sensitive
+    elements (h = 1e-3 E_e).  40 load increments: the substepping keeps the
+    reference's warm start (the previous substep's du, unscaled), which on
+    this mesh overshoots into inverted elements after a cutback with 10 or 20
+    increments, the same in the reference's algorithm as here."""
+    from torchfem_gb300.materials import Hyperelastic3D, neo_hookean_psi
+
+    nodes, el = mesh.linear_to_quadratic(*mesh.box_tetra6(31, 11, 11, 3.0, 1.0, 1.0))
+    gen = torch.Generator().manual_seed(0)
+    E0 = 1000.0 * (1.0 + 0.1 * torch.randn(len(el), generator=gen, dtype=torch.float64))
+    nu = 0.45
+    right = nodes[:, 0] == 3.0
+
+    def reaction(E):
+        mu = E / (2.0 * (1.0 + nu))
+        lbd = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+        m = Solid(nodes, el, Hyperelastic3D(neo_hookean_psi, torch.stack([mu, lbd], dim=-1)))
+        m.constraints[nodes[:, 0] == 0.0, :] = True
+        m.constraints[right, 0] = True
+        m.displacements[right, 0] = 0.5
+        assert m.n_dofs == 80_703
+        _, f, _, _, _ = m.solve(increments=torch.linspace(0.0, 1.0, 41), nlgeom=True, rtol=1e-10, atol=1e-10,
+                                max_iter=20, stol=1e-12, differentiable_parameters=E)
+        return f[right, 0].sum()
+
+    E = E0.clone().requires_grad_(True)
+    (gE,) = torch.autograd.grad(reaction(E), E)
+    # the two most sensitive elements: their difference quotients stand well
+    # above the solves' stopping noise
+    idx = torch.argsort(gE.abs(), descending=True)[:2]
+    for i in idx.tolist():
+        h = 1e-3 * float(E0[i])
+        Ep, Em = E0.clone(), E0.clone()
+        Ep[i] += h
+        Em[i] -= h
+        with torch.no_grad():
+            fd = (float(reaction(Ep)) - float(reaction(Em))) / (2 * h)
+        assert abs(fd - float(gE[i])) <= 1e-4 * abs(float(gE[i])) + 1e-12
+
+
+def test_config5_full_size_vs_reference(cuda, golden):
+    """Config 5 at full size (O-grid 256 x 64 plate with a hole, J2 plane
+    strain, 20 increments, 33,280 DOF): u, f, state and the reaction's
+    thickness gradient through the checkpointed adjoint against the
+    reference (its own solve and autograd at the same size)."""
+    g = golden("plastic_ogrid_256x64.npz")
+    m, t, right = _plastic_model(g)
+    assert m.n_dofs == 33_280
+    u, f, s, _, st = m.solve(increments=torch.linspace(0.0, 1.0, 21), rtol=1e-12, atol=1e-12, max_iter=80,
+                             stol=1e-13, differentiable_parameters=t)
+    assert float(st[:, 0].max()) > 0.0
+    assert rel(u, g["u"]) <= 1e-8
+    assert rel(f, g["f"]) <= 1e-8
+    assert rel(s, g["sigma"]) <= 1e-8
+    assert rel(st, g["state"]) <= 1e-8
+    R = f[right, 0].sum()
+    assert abs(float(R.detach()) - float(g["reaction"])) <= 1e-8 * abs(float(g["reaction"]))
+    (gt,) = torch.autograd.grad(R, t)
+    assert rel(gt, g["grad_t"]) <= 1e-7
