@@ -1093,7 +1093,12 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
   const long long max_iter = c->max_iter;
   const double tol2bb = c->tol2_lo, delta2 = c->delta2, rr_ref = c->rr_ref;
   const int mixed = c->mixed;
-  // two barriers per iteration on the TMA path (direction update inside the SpMV)
+  // two barriers per iteration on the TMA path (direction update inside the
+  // SpMV).  Only there: q then carries A p by recurrence, and its drift from
+  // the explicit product grows with the length of a launch.  Mixed solves
+  // relaunch at every FP64 replacement (q = A p afresh) and inner Newton
+  // solves stop at 1e-6; a plain FP64 solve is one long launch, where the
+  // drift measurably degrades tight tolerances, so it keeps three barriers.
   constexpr bool kCarry = MODE == 1 && G == 3 && sizeof(VT) == 4;
   bool carry = false;
   if (threadIdx.x == 0) sh_beta = (VT)0;

@@ -72,12 +72,17 @@ class SolveContext:
 
     def solve(self, b: Tensor, inner: bool = False) -> Tensor:
         """Linear solve on the current system.  inner=True marks a Newton
-        correction of a nonlinear material: in mixed precision it runs the FP32
-        CG alone to max(stol, inner_rtol), the FP64 Newton residual being the
-        refinement."""
+        correction of a nonlinear material, solved to max(stol, inner_rtol)
+        (inexact Newton: the FP64 Newton residual, checked against rtol and
+        atol, decides convergence, so the converged state is unchanged); in
+        mixed precision the FP32 CG runs alone, the Newton iteration being its
+        refinement.  Adjoint and linear-material solves use stol."""
         assert self.system is not None
         if inner and self.precision == "mixed":
             x = self.dm.solve(self.system, b, max(self.stol, self.inner_rtol), self.cg_max_iter, refine=False)
+        elif inner:
+            x = self.dm.solve(self.system, b, max(self.stol, self.inner_rtol), self.cg_max_iter, self.delta,
+                              linear=self.linear)
         else:
             x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, self.delta, linear=self.linear)
         self.iterations.append(self.system.stats.iterations)
