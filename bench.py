@@ -65,10 +65,11 @@ def cube_workload(n: int, device):
     return m, forces
 
 
-def step(m, forces, precision, stol):
+def step(m, forces, precision, stol, precond=None):
     f = forces.detach().requires_grad_(True)
     m.forces = f
-    u, fi, s, gr, st = m.solve(stol=stol, precision=precision, differentiable_parameters=f)
+    u, fi, s, gr, st = m.solve(stol=stol, precision=precision, differentiable_parameters=f,
+                               preconditioner=precond)
     (g,) = torch.autograd.grad(u.sum(), f)
     return u, fi, s, gr, st, g
 

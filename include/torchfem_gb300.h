@@ -405,6 +405,73 @@ int fem_pcg_mixed(const fem_matrix* A32, const fem_operator64* op, const double*
                   double rtol, double delta, int64_t max_iter, void* ws, size_t ws_bytes,
                   fem_solve_info* info, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Smoothed-aggregation multigrid (SA-AMG) preconditioner for the FP32       */
+/* sliced-block systems: the GPU counterpart of the AMG the reference builds */
+/* for its iterative solves, pyamg.smoothed_aggregation_solver(A, B,         */
+/* smooth="jacobi") with B = FEM.compute_B() (sparse.py:495-507,             */
+/* base.py:316-344), and AmgXSolver on CUDA (amgx.py: create, setup, solve,  */
+/* destroy).  Like the AmgX handle, the hierarchy owns its device memory,    */
+/* whose size depends on the aggregation: the one exception to the           */
+/* no-allocation convention.  fem_amg_destroy frees it.                      */
+/* ------------------------------------------------------------------------ */
+typedef struct fem_amg fem_amg;
+
+/* Symbolic hierarchy of one mesh and constraint set: aggregation of the
+ * node graph (distance-2 independent-set roots), the tentative prolongator
+ * from the rigid-body modes of the node coordinates [n_nod][dim] with the
+ * constrained components of con_mask [n_nod*dim] (nullable) removed, and
+ * the sparsity of every prolongator and coarse operator, down to a coarsest
+ * level of at most 96 unknowns.  dim (= blocks->dim) is 2 or 3.  Keeps
+ * pointers to blocks->nbr_ptr / nbr, which must outlive the handle. */
+int fem_amg_create(const fem_blocks* blocks, const double* coords, const uint8_t* con_mask, fem_amg** out,
+                   void* stream);
+
+/* Numeric hierarchy for one FP32 sliced-block matrix of that mesh (A32 with
+ * its block-Jacobi inverse in precond, from fem_block_jacobi): spectral
+ * estimates of D^-1 A, smoothed prolongators, Galerkin coarse operators,
+ * coarse block inverses and the dense coarsest inverse.  A32 must stay
+ * unchanged until the next setup. */
+int fem_amg_setup(fem_amg* amg, const fem_matrix* A32, void* stream);
+
+/* CG preconditioned by one V-cycle (Chebyshev smoothing) on the matrix of
+ * the last fem_amg_setup, from x = 0.  With op != NULL: FP64 residual
+ * replacement as in fem_pcg_mixed (threshold delta), stopping at
+ * ||b - A x|| <= rtol ||b|| in FP64.  With op == NULL: FP32 CG alone,
+ * stopping on its recursive residual. */
+size_t fem_amg_pcg_workspace_bytes(const fem_amg* amg, const fem_operator64* op);
+int fem_amg_pcg(fem_amg* amg, const fem_matrix* A32, const fem_operator64* op, const double* b, double* x,
+                double rtol, double delta, int64_t max_iter, void* ws, size_t ws_bytes, fem_solve_info* info,
+                void* stream);
+
+void fem_amg_destroy(fem_amg* amg);
+
+/* Read-only view of one level (device pointers owned by the handle). */
+typedef struct fem_amg_level {
+  int64_t n;                /* block rows */
+  int block;                /* block size (dim on level 0, then 6 in 3D / 3 in 2D) */
+  int64_t a_nnz;            /* coarse operator blocks (levels >= 1) */
+  const int64_t* a_ptr;
+  const int32_t* a_col;
+  const float* a_val;       /* [a_nnz][block][block] */
+  int64_t n_agg;            /* aggregates (0 on the coarsest level) */
+  const int32_t* agg;       /* [n] aggregate of each block row, -1 when not aggregated */
+  const float* tval;        /* [n][block][K] tentative prolongator rows */
+  int64_t p_nnz;
+  const int64_t* p_ptr;     /* smoothed prolongator, block CSR [n+1] */
+  const int32_t* p_col;
+  const float* p_val;       /* [p_nnz][block][K] */
+  double rho;               /* spectral estimate of D^-1 A used by the level */
+  const float* coarse_inv;  /* coarsest level: dense inverse [n*block]^2 */
+  int64_t dropped;          /* near-null modes dropped as dependent (all levels) */
+} fem_amg_level;
+
+int fem_amg_levels(const fem_amg* amg);
+int fem_amg_level_info(const fem_amg* amg, int level, fem_amg_level* out);
+
+/* Device-to-device copy on the stream (reads handle-owned arrays). */
+int fem_copy_device(void* dst, const void* src, size_t bytes, void* stream);
+
 /* Workspace bytes of fem_minres for the FP64 scalar CSR matrix A. */
 size_t fem_minres_workspace_bytes(const fem_matrix* A);
 

@@ -159,3 +159,76 @@ def test_hexa2(golden):
     u, f, s = m.solve(F, con)
     rel = lambda a, b: np.abs(a - b).max() / np.abs(b).max()  # noqa: E731
     assert rel(u, g["u"]) <= 1e-10 and rel(f, g["f"]) <= 1e-10 and rel(s, g["sigma"]) <= 1e-10
+
+
+# ------------------------------------------------------ multigrid oracle ---
+def _amg_cube(n=8, seed=0):
+    nodes, el = O.cube_hexa(n + 1, n + 1, n + 1)
+    rng = np.random.default_rng(seed)
+    inner = np.all((nodes > 0) & (nodes < 1), axis=1)
+    nodes = nodes.copy()
+    nodes[inner] += rng.uniform(-0.1 / n, 0.1 / n, size=(inner.sum(), 3))
+    model = O.LinearModel(nodes, el, O.elastic_c("3d", 1000.0, 0.3, len(el)))
+    con = np.zeros((len(nodes), 3), bool)
+    con[nodes[:, 0] == 0.0] = True
+    con[nodes[:, 0] == 1.0, 0] = True
+    K = model.matrix(np.nonzero(con.ravel())[0]).tocsr()
+    return nodes, K, con
+
+
+def test_amg_oracle_aggregation_invariants():
+    from oracle import amg_oracle as AO
+
+    nodes, K, con = _amg_cube()
+    ptr, idx, _ = AO.block_pattern(K, 3)
+    n = len(nodes)
+    active = ~np.all(con, axis=1)
+    agg, na = AO.aggregate(ptr, idx, active)
+    assert np.all(agg[active] >= 0) and np.all(agg[~active] == -1)
+    assert set(np.unique(agg[active])) == set(range(na))
+    adj = [set(idx[ptr[i]:ptr[i + 1]]) for i in range(n)]
+    for a in range(na):  # every aggregate is connected in the node graph
+        mem = set(np.nonzero(agg == a)[0])
+        seen, todo = set(), [min(mem)]
+        while todo:
+            v = todo.pop()
+            if v in seen:
+                continue
+            seen.add(v)
+            todo.extend((adj[v] & mem) - seen)
+        assert seen == mem
+
+
+def test_amg_oracle_tentative_reproduces_rigid_modes():
+    from oracle import amg_oracle as AO
+
+    nodes, K, con = _amg_cube()
+    ptr, idx, _ = AO.block_pattern(K, 3)
+    active = ~np.all(con, axis=1)
+    agg, na = AO.aggregate(ptr, idx, active)
+    T, Bc = AO.tentative(agg, na, 3, 6, coords=nodes, con=con.ravel())
+    Ts = AO.to_sparse_T(T, agg, 6)
+    assert np.abs((Ts.T @ Ts).toarray() - np.eye(6 * na)).max() <= 1e-12
+    # on each aggregate, T Bc reproduces the rigid-body rows about the global centroid
+    B = AO.null_rows(nodes, con.ravel(), 3, 6, nodes.mean(axis=0)).reshape(-1, 6)
+    rows = np.repeat(agg, 3)
+    got = np.zeros_like(B)
+    for a in range(na):
+        sel = rows == a
+        got[sel] = Ts[sel][:, 6 * a:6 * a + 6] @ Bc[a]
+    assert np.abs(got - B).max() <= 1e-10 * np.abs(B).max()
+
+
+def test_amg_oracle_vcycle_symmetric_and_converges():
+    from oracle import amg_oracle as AO
+
+    nodes, K, con = _amg_cube()
+    levels = AO.hierarchy(K, nodes, con.ravel(), 3)
+    rng = np.random.default_rng(1)
+    u, v = rng.standard_normal(K.shape[0]), rng.standard_normal(K.shape[0])
+    a, b = u @ AO.vcycle(levels, v), v @ AO.vcycle(levels, u)
+    assert abs(a - b) <= 1e-10 * abs(a)
+    rhs = rng.standard_normal(K.shape[0])
+    x, it = AO.pcg(K, rhs, levels, rtol=1e-10)
+    assert np.linalg.norm(rhs - K @ x) <= 1e-10 * np.linalg.norm(rhs)
+    assert it <= 25

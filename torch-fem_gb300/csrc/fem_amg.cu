@@ -1,0 +1,2257 @@
+// Smoothed-aggregation algebraic multigrid (SA-AMG) for the FP32 block systems
+// of the mixed-precision solver, and the multigrid-preconditioned CG built on
+// it.  This is the GPU counterpart of the preconditioner the reference builds
+// for its iterative solves: on the CPU pyamg.smoothed_aggregation_solver(A, B,
+// smooth="jacobi") with B the rigid-body modes of FEM.compute_B
+// (src/torchfem/sparse.py:495-507, src/torchfem/base.py:316-344), on the GPU
+// AmgX aggregation AMG (src/torchfem/amgx.py:62-91).
+//
+// Published methods, restated for this library:
+//  - aggregation: roots form a distance-2 maximal independent set chosen with
+//    fixed pseudo-random priorities, then two passes attach every remaining
+//    node to the aggregate of a neighbour (Bell, Dalton & Olson, "Exposing
+//    fine-grained parallelism in algebraic multigrid methods", SIAM J. Sci.
+//    Comput. 34 (2012) C123-C152);
+//  - tentative prolongator T: per aggregate, an orthonormal basis of the
+//    near-null space (rigid-body modes with constrained components removed)
+//    from a Cholesky-QR with rank drop; its triangular factor is the coarse
+//    near-null space of the next level (Vanek, Mandel & Brezina, Computing 56
+//    (1996) 179-196);
+//  - prolongator smoothing P = (I - w D^-1 A) T, w = 4 / (3 rho(D^-1 A)), D
+//    the block diagonal (pyamg's smooth="jacobi" default);
+//  - Galerkin coarse operators A_c = P^T A P;
+//  - smoothing: Chebyshev polynomial of degree 2 in D^-1 A on
+//    [0.1, 1.1] rho (Adams, Brezina, Hu & Tuminaro, J. Comput. Phys. 188 (2003)
+//    593-610), rho estimated by 12 CG-Lanczos steps; a symmetric smoother, so
+//    the V-cycle is a symmetric positive definite preconditioner and plain CG
+//    applies (the reference's CPU path also runs CG);
+//  - coarsest level (at most 96 unknowns): dense inverse.
+//
+// Determinism: no floating-point atomics; every sum runs in a fixed order and
+// the aggregation priorities are fixed, so hierarchy and iterates are identical
+// run to run.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fem_common.cuh"
+
+namespace tfg {
+
+int etype_info(int etype, int* ne, int* d, int* nip);
+size_t scan_workspace_bytes(int64_t n);
+int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
+
+namespace {
+
+constexpr int kMaxLevels = 10;
+constexpr int kMaxPRow = 64;       // aggregates adjacent to one node
+constexpr int kMaxAPRow = 128;     // block columns of one row of A P
+constexpr int kMaxCRow = 128;      // block columns of one coarse row
+constexpr int kCoarseMaxDof = 96;  // the coarsest level is inverted densely
+constexpr int kLanczos = 12;       // CG-Lanczos steps of the spectral estimate
+constexpr double kChebLo = 0.1, kChebHi = 1.1;
+constexpr double kOmega = 4.0 / 3.0;
+constexpr double kDropTol = 1e-10;  // relative pivot below which a mode is dropped
+constexpr int kT = 256;             // threads of the row-parallel kernels
+constexpr int kSellW = 4;           // warps sharing one 32-row slice (level 0)
+
+int g_sm = 0;
+int sm_count() {
+  if (g_sm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&g_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || g_sm <= 0) g_sm = 132;
+  }
+  return g_sm;
+}
+unsigned capped(int64_t blocks_needed, int per_sm) {
+  const int64_t cap = (int64_t)sm_count() * per_sm;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks_needed, cap));
+}
+
+// ------------------------------------------------------------ priorities --
+// lowbias32 integer hash (C. Wellons, 2018): fixed pseudo-random priorities.
+__host__ __device__ __forceinline__ uint32_t amg_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
+// MIS key: (state, priority, index), compared as one 64-bit word.  State 0
+// (decided out, or inactive) maps to 0; 1 undecided; 2 root.
+__device__ __forceinline__ uint64_t mis_key(int64_t i, int st) {
+  return st == 0 ? 0ull
+                 : ((uint64_t)st << 62) | ((uint64_t)(amg_hash((uint32_t)i) >> 2) << 32) | (uint64_t)(uint32_t)i;
+}
+
+__device__ __forceinline__ uint64_t join_key(int64_t j) {
+  return (1ull << 63) | ((uint64_t)(amg_hash((uint32_t)j) >> 2) << 32) | (uint64_t)(uint32_t)j;
+}
+
+// ------------------------------------------------------------ control ----
+enum { kRun = 0, kConverged = 1, kMaxIter = 2, kNonFinite = 3, kBreakdown = 4 };
+
+struct AmgCtrl {
+  double rz;       // r.z of the current direction
+  double pscale;   // factor on beta: 0 before the first direction, sc_old / sc after a replacement
+  double alpha;
+  double beta;
+  double rr;       // ||r||^2 of the FP32 residual (scaled units)
+  double rr_ref;   // rr at the last FP64 replacement
+  double rr_true;  // ||b - A x||^2 of the last FP64 replacement
+  double bb;
+  double tol2bb;
+  double rscale;   // power of two applied to the FP32 residual
+  double tol2_lo;  // tol2bb * rscale^2
+  double delta2;
+  long long iters;
+  long long max_iter;
+  long long replacements;
+  int done;
+  int replace;
+  int mixed;
+  unsigned int counter;
+  int lz_step;
+};
+
+__device__ __forceinline__ bool amg_idle(const AmgCtrl* c) {
+  return (*(volatile const int*)&c->done) != 0 || (*(volatile const int*)&c->replace) != 0;
+}
+
+template <int B>
+__device__ __forceinline__ void block_mv(const float* __restrict__ m, const float (&v)[B], float (&out)[B]) {
+#pragma unroll
+  for (int a = 0; a < B; ++a) {
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < B; ++c) s = fmaf(m[a * B + c], v[c], s);
+    out[a] = s;
+  }
+}
+
+// ================================================================ symbolic ==
+struct Graph {
+  int64_t n;
+  const int64_t* ptr;
+  const int32_t* idx;
+};
+
+__global__ void k_centroid(int64_t n, int dim, const double* __restrict__ x, double* __restrict__ out) {
+  __shared__ double red[32];
+  for (int c = 0; c < dim; ++c) {
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += x[i * dim + c];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) out[c] = n > 0 ? s / (double)n : 0.0;
+    __syncthreads();
+  }
+}
+
+__global__ void k_agg_active(int64_t n, int b, const uint8_t* __restrict__ con, uint8_t* __restrict__ active,
+                             uint8_t* __restrict__ state) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  bool act = true;
+  if (con) {
+    act = false;
+    for (int r = 0; r < b; ++r) act = act || !con[i * b + r];
+  }
+  active[i] = act;
+  state[i] = act ? 1 : 0;
+}
+
+// k1[i] = largest key over the active closed neighbourhood of an active node.
+__global__ void k_mis_max1(Graph g, const uint8_t* __restrict__ active, const uint8_t* __restrict__ state,
+                           uint64_t* __restrict__ k1) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  uint64_t m = 0;
+  if (active[i])
+    for (int64_t e = g.ptr[i]; e < g.ptr[i + 1]; ++e) {
+      const int32_t j = g.idx[e];
+      if (active[j]) m = max(m, mis_key(j, state[j]));
+    }
+  k1[i] = m;
+}
+
+// Distance-2 maximum; an undecided node that holds it becomes a root, one
+// that sees a root within distance 2 drops out.
+__global__ void k_mis_max2(Graph g, const uint8_t* __restrict__ active, uint8_t* __restrict__ state,
+                           const uint64_t* __restrict__ k1, unsigned long long* __restrict__ undecided) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool und = false;
+  if (i < g.n && active[i] && state[i] == 1) {
+    uint64_t m = 0;
+    for (int64_t e = g.ptr[i]; e < g.ptr[i + 1]; ++e) {
+      const int32_t j = g.idx[e];
+      if (active[j]) m = max(m, k1[j]);
+    }
+    if (m == mis_key(i, 1)) state[i] = 2;
+    else if ((m >> 62) == 2) state[i] = 0;
+    else und = true;
+  }
+  const unsigned bal = __ballot_sync(0xffffffffu, und);
+  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(undecided, (unsigned long long)__popc(bal));
+}
+
+__global__ void k_root_flags(int64_t n, const uint8_t* __restrict__ state, int64_t* __restrict__ flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flags[i] = state[i] == 2 ? 1 : 0;
+}
+
+__global__ void k_root_ids(int64_t n, const uint8_t* __restrict__ state, const int64_t* __restrict__ ids,
+                           int32_t* __restrict__ agg) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) agg[i] = state[i] == 2 ? (int32_t)ids[i] : -1;
+}
+
+// An unassigned active node joins the aggregate of its assigned neighbour of
+// largest (priority, index).
+__global__ void k_agg_join(Graph g, const uint8_t* __restrict__ active, const int32_t* __restrict__ agg_in,
+                           int32_t* __restrict__ agg_out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  int32_t a = agg_in[i];
+  if (a < 0 && active[i]) {
+    uint64_t best = 0;
+    for (int64_t e = g.ptr[i]; e < g.ptr[i + 1]; ++e) {
+      const int32_t j = g.idx[e];
+      const int32_t aj = agg_in[j];
+      if (aj >= 0) {
+        const uint64_t k = join_key(j);
+        if (k > best) {
+          best = k;
+          a = aj;
+        }
+      }
+    }
+  }
+  agg_out[i] = a;
+}
+
+__global__ void k_count_unassigned(int64_t n, const uint8_t* __restrict__ active, const int32_t* __restrict__ agg,
+                                   unsigned long long* __restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool bad = i < n && active[i] && agg[i] < 0;
+  const unsigned bal = __ballot_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(cnt, (unsigned long long)__popc(bal));
+}
+
+// Counting sort by key, in two kernels: counts, then an unordered fill that
+// k_sort_rows puts in ascending order.
+__global__ void k_count_keys(int64_t n, const int32_t* __restrict__ key, int64_t* __restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && key[i] >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(cnt + key[i]), 1ull);
+}
+
+__global__ void k_fill_keys(int64_t n, const int32_t* __restrict__ key, int64_t* __restrict__ cursor,
+                            int32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && key[i] >= 0) {
+    const int64_t pos = (int64_t)atomicAdd(reinterpret_cast<unsigned long long*>(cursor + key[i]), 1ull);
+    out[pos] = (int32_t)i;
+  }
+}
+
+// Transpose of a row pattern: counts per column, then (column -> row) fill.
+__global__ void k_count_cols(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                             int64_t* __restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) atomicAdd(reinterpret_cast<unsigned long long*>(cnt + col[e]), 1ull);
+}
+
+__global__ void k_fill_cols(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                            int64_t* __restrict__ cursor, int32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+    const int64_t pos = (int64_t)atomicAdd(reinterpret_cast<unsigned long long*>(cursor + col[e]), 1ull);
+    out[pos] = (int32_t)i;
+  }
+}
+
+// Warp per row: out = the row of `in` in ascending order (distinct values).
+__global__ void k_sort_rows(int64_t n_rows, const int64_t* __restrict__ ptr, const int32_t* __restrict__ in,
+                            int32_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= n_rows) return;
+  const int64_t e0 = ptr[r], e1 = ptr[r + 1];
+  for (int64_t e = e0 + lane; e < e1; e += 32) {
+    const int32_t v = in[e];
+    int64_t rank = 0;
+    for (int64_t f = e0; f < e1; ++f) rank += in[f] < v;
+    out[e0 + rank] = v;
+  }
+}
+
+// Position in P of every transposed entry: the slot of coarse column I in the
+// P row of fine node pt_row[e].
+__global__ void k_pt_pos(int64_t n_c, const int64_t* __restrict__ pt_ptr, const int32_t* __restrict__ pt_row,
+                         const int64_t* __restrict__ p_ptr, const int32_t* __restrict__ p_col,
+                         int64_t* __restrict__ pt_pos) {
+  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n_c) return;
+  for (int64_t e = pt_ptr[I]; e < pt_ptr[I + 1]; ++e) {
+    const int32_t i = pt_row[e];
+    int64_t pos = -1;
+    for (int64_t f = p_ptr[i]; f < p_ptr[i + 1]; ++f)
+      if (p_col[f] == (int32_t)I) pos = f;
+    pt_pos[e] = pos;
+  }
+}
+
+// Sorted insertion of v into s[0..m) (distinct values); false when full.
+template <int CAP>
+__device__ __forceinline__ bool insert_unique(int32_t (&s)[CAP], int& m, int32_t v) {
+  int k = m;
+  while (k > 0 && s[k - 1] > v) --k;
+  if (k > 0 && s[k - 1] == v) return true;
+  if (m == CAP) return false;
+  for (int t = m; t > k; --t) s[t] = s[t - 1];
+  s[k] = v;
+  ++m;
+  return true;
+}
+
+// P pattern: row i holds the aggregates of its active neighbours.  Count
+// pass (cnt) or fill pass (col at ptr).
+template <bool kFill>
+__global__ void k_p_rows(Graph g, const uint8_t* __restrict__ active, const int32_t* __restrict__ agg,
+                         int64_t* __restrict__ cnt, const int64_t* __restrict__ ptr, int32_t* __restrict__ col,
+                         int32_t* __restrict__ status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  int32_t s[kMaxPRow];
+  int m = 0;
+  if (!active || active[i])
+    for (int64_t e = g.ptr[i]; e < g.ptr[i + 1]; ++e) {
+      const int32_t a = agg[g.idx[e]];
+      if (a >= 0 && !insert_unique(s, m, a)) {
+        flag_status(status, kStatBounds);
+        break;
+      }
+    }
+  if (!kFill) {
+    cnt[i] = m;
+  } else {
+    for (int k = 0; k < m; ++k) col[ptr[i] + k] = s[k];
+  }
+}
+
+// Union pattern: row i holds the union over u in outer(i) of inner(u);
+// rows of inactive nodes (active[i] == 0) stay empty.
+template <int CAP, bool kFill>
+__global__ void k_union_rows(int64_t n, const uint8_t* __restrict__ active, const int64_t* __restrict__ optr,
+                             const int32_t* __restrict__ oidx, const int64_t* __restrict__ iptr,
+                             const int32_t* __restrict__ icol, int64_t* __restrict__ cnt,
+                             const int64_t* __restrict__ ptr, int32_t* __restrict__ col, int32_t* __restrict__ status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int32_t s[CAP];
+  int m = 0;
+  bool ok = !active || active[i];
+  for (int64_t e = optr[i]; e < optr[i + 1] && ok; ++e) {
+    const int32_t u = oidx[e];
+    for (int64_t f = iptr[u]; f < iptr[u + 1]; ++f)
+      if (!insert_unique(s, m, icol[f])) {
+        flag_status(status, kStatBounds);
+        ok = false;
+        break;
+      }
+  }
+  if (!kFill) {
+    cnt[i] = m;
+  } else {
+    for (int k = 0; k < m; ++k) col[ptr[i] + k] = s[k];
+  }
+}
+
+// Row r (component) of the near-null space of node i: rigid-body modes about
+// the origin c (level 0: coordinates, constrained components zero) or the
+// stored rows bn [n][B][K] (coarser levels).
+template <int B, int K>
+__device__ __forceinline__ void null_row(int64_t i, int r, const double* __restrict__ x, const uint8_t* __restrict__ con,
+                                         const double* __restrict__ bn, const double (&c)[3], double (&row)[K]) {
+  if (bn) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) row[k] = bn[(i * B + r) * K + k];
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) row[k] = 0.0;
+  if (con && con[i * B + r]) return;
+  row[r] = 1.0;
+  if constexpr (B == 3 && K == 6) {
+    // columns of FEM.compute_B (base.py:322-332): (0,-z,y), (z,0,-x), (-y,x,0)
+    const double px = x[i * 3] - c[0], py = x[i * 3 + 1] - c[1], pz = x[i * 3 + 2] - c[2];
+    if (r == 0) {
+      row[4] = pz;
+      row[5] = -py;
+    } else if (r == 1) {
+      row[3] = -pz;
+      row[5] = px;
+    } else {
+      row[3] = py;
+      row[4] = -px;
+    }
+  } else if constexpr (B == 2 && K == 3) {
+    // compute_B in 2D (base.py:333-338): (y, -x)
+    const double px = x[i * 2] - c[0], py = x[i * 2 + 1] - c[1];
+    row[2] = r == 0 ? py : -px;
+  }
+}
+
+// Warp per aggregate: Gram matrix of the members' near-null rows, Cholesky
+// with rank drop (the R of a modified Gram-Schmidt QR that skips dependent
+// columns), T = rows of Q, and the coarse near-null rows R (expressed about
+// the global origin when the fine rows were taken about the centroid).
+template <int B, int K>
+__global__ void __launch_bounds__(128) k_tentative(int64_t n_agg, const int64_t* __restrict__ agg_ptr,
+                                                   const int32_t* __restrict__ agg_nodes,
+                                                   const double* __restrict__ x, const uint8_t* __restrict__ con,
+                                                   const double* __restrict__ origin, const double* __restrict__ bn,
+                                                   float* __restrict__ tval, double* __restrict__ bc,
+                                                   unsigned long long* __restrict__ dropped) {
+  constexpr int NG = K * (K + 1) / 2;
+  __shared__ double Rs[4][K][K];
+  __shared__ int keep[4][K];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t a = (int64_t)blockIdx.x * 4 + w;
+  if (a >= n_agg) return;
+  const int64_t m0 = agg_ptr[a], m1 = agg_ptr[a + 1];
+  constexpr int DC = B < 3 ? B : 3;  // coordinate components (finest level)
+  double c[3] = {0.0, 0.0, 0.0};
+  if (!bn) {
+    // rows about the aggregate centroid: the same column space, better conditioned
+#pragma unroll
+    for (int d = 0; d < DC; ++d) {
+      double s = 0.0;
+      for (int64_t e = m0 + lane; e < m1; e += 32) s += x[(int64_t)agg_nodes[e] * B + d];
+      s = warp_sum(s);
+      c[d] = s / (double)(m1 - m0);
+    }
+  }
+  double G[NG];
+#pragma unroll
+  for (int t = 0; t < NG; ++t) G[t] = 0.0;
+  for (int64_t e = m0 + lane; e < m1; e += 32) {
+    const int64_t i = agg_nodes[e];
+    for (int r = 0; r < B; ++r) {
+      double row[K];
+      null_row<B, K>(i, r, x, con, bn, c, row);
+      int t = 0;
+#pragma unroll
+      for (int p = 0; p < K; ++p)
+#pragma unroll
+        for (int q = p; q < K; ++q) G[t++] += row[p] * row[q];
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < NG; ++t) G[t] = warp_sum(G[t]);
+  if (lane == 0) {
+    double R[K][K];
+    int nd = 0;
+    for (int p = 0; p < K; ++p)
+      for (int q = 0; q < K; ++q) R[p][q] = 0.0;
+    auto gidx = [](int p, int q) { return p * K - p * (p - 1) / 2 + (q - p); };
+    for (int j = 0; j < K; ++j) {
+      double d = G[gidx(j, j)];
+      for (int l = 0; l < j; ++l) d -= R[l][j] * R[l][j];
+      const bool kp = G[gidx(j, j)] > 0.0 && d > kDropTol * G[gidx(j, j)];
+      keep[w][j] = kp;
+      if (!kp) {
+        ++nd;
+        continue;
+      }
+      R[j][j] = sqrt(d);
+      for (int q = j + 1; q < K; ++q) {
+        double v = G[gidx(j, q)];
+        for (int l = 0; l < j; ++l) v -= R[l][j] * R[l][q];
+        R[j][q] = v / R[j][j];
+      }
+    }
+    for (int p = 0; p < K; ++p)
+      for (int q = 0; q < K; ++q) Rs[w][p][q] = R[p][q];
+    if (nd) atomicAdd(dropped, (unsigned long long)nd);
+  }
+  __syncwarp();
+  for (int64_t e = m0 + lane; e < m1; e += 32) {
+    const int64_t i = agg_nodes[e];
+    for (int r = 0; r < B; ++r) {
+      double row[K], q[K];
+      null_row<B, K>(i, r, x, con, bn, c, row);
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        double v = row[k];
+        for (int l = 0; l < k; ++l) v -= q[l] * Rs[w][l][k];
+        q[k] = keep[w][k] ? v / Rs[w][k][k] : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k) tval[(i * B + r) * K + k] = (float)q[k];
+    }
+  }
+  // coarse rows: R S, with S the unit upper-triangular change from modes
+  // about c to modes about the global origin (translations added to rotations)
+  double S[K][K];
+#pragma unroll
+  for (int p = 0; p < K; ++p)
+#pragma unroll
+    for (int q = 0; q < K; ++q) S[p][q] = p == q ? 1.0 : 0.0;
+  if (!bn) {
+    const double cx = c[0] - origin[0], cy = c[1] - origin[1];
+    if constexpr (B == 3 && K == 6) {
+      const double cz = c[2] - origin[2];
+      S[1][3] = -cz;
+      S[2][3] = cy;
+      S[0][4] = cz;
+      S[2][4] = -cx;
+      S[0][5] = -cy;
+      S[1][5] = cx;
+    } else if constexpr (B == 2 && K == 3) {
+      S[0][2] = cy;
+      S[1][2] = -cx;
+    }
+  }
+  for (int t = lane; t < K * K; t += 32) {
+    const int p = t / K, q = t % K;
+    double v = 0.0;
+    for (int l = 0; l < K; ++l) v += Rs[w][p][l] * S[l][q];
+    bc[a * K * K + t] = v;
+  }
+}
+
+// ================================================================ numeric ==
+// Block (i, slot kk) of the level operator: level 0 reads the sliced FP32
+// matrix, coarser levels a block CSR.
+template <int B, bool kSell>
+struct OpView {
+  const int64_t* base;  // sell_base (kSell) or row pointers
+  const float* val;
+  __device__ __forceinline__ float at(int64_t i, int64_t kk, int c) const {
+    if constexpr (kSell) return val[base[i >> 5] * (B * B) + (kk * (B * B) + c) * 32 + (i & 31)];
+    else return val[(base[i] + kk) * (B * B) + c];
+  }
+};
+
+// Slot of v in the warp's sorted list s[0..m) (v is present).
+__device__ __forceinline__ int find_slot(const int32_t* s, int m, int32_t v) {
+  const int lane = threadIdx.x & 31;
+  for (int b0 = 0; b0 < m; b0 += 32) {
+    const bool hit = b0 + lane < m && s[b0 + lane] == v;
+    const unsigned bal = __ballot_sync(0xffffffffu, hit);
+    if (bal) return b0 + __ffs(bal) - 1;
+  }
+  return -1;
+}
+
+// P = T - w D^-1 A T, warp per fine row, accumulators in shared memory.
+template <int B, int K, bool kSell>
+__global__ void __launch_bounds__(128) k_p_numeric(Graph g, OpView<B, kSell> A, const float* __restrict__ dinv,
+                                                   const int32_t* __restrict__ agg, const float* __restrict__ tval,
+                                                   const int64_t* __restrict__ p_ptr, const int32_t* __restrict__ p_col,
+                                                   float* __restrict__ p_val, float omega) {
+  constexpr int BK = B * K;
+  __shared__ int32_t cols[4][kMaxPRow];
+  __shared__ float acc[4][kMaxPRow][BK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 4 + w;
+  if (i >= g.n) return;
+  const int64_t e0 = p_ptr[i];
+  const int m = (int)(p_ptr[i + 1] - e0);
+  if (m == 0) return;
+  for (int s = lane; s < m; s += 32) cols[w][s] = p_col[e0 + s];
+  for (int t = lane; t < m * BK; t += 32) acc[w][t / BK][t % BK] = 0.f;
+  __syncwarp();
+  const int64_t nb = g.ptr[i];
+  const int deg = (int)(g.ptr[i + 1] - nb);
+  for (int kk = 0; kk < deg; ++kk) {
+    const int32_t j = g.idx[nb + kk];
+    const int32_t aj = agg[j];
+    if (aj < 0) continue;
+    const int s = find_slot(cols[w], m, aj);
+    if (s < 0) continue;  // cannot happen: the row lists every neighbour's aggregate
+    for (int c = lane; c < BK; c += 32) {
+      const int r = c / K, k = c % K;
+      float v = acc[w][s][c];
+#pragma unroll
+      for (int q = 0; q < B; ++q) v = fmaf(A.at(i, kk, r * B + q), tval[((int64_t)j * B + q) * K + k], v);
+      acc[w][s][c] = v;
+    }
+    __syncwarp();
+  }
+  const int32_t ai = agg[i];
+  for (int s = 0; s < m; ++s) {
+    for (int c = lane; c < BK; c += 32) {
+      const int r = c / K, k = c % K;
+      float v = 0.f;
+#pragma unroll
+      for (int q = 0; q < B; ++q) v = fmaf(dinv[(i * B + r) * B + q], acc[w][s][q * K + k], v);
+      const float t = cols[w][s] == ai ? tval[(i * B + r) * K + k] : 0.f;
+      p_val[(e0 + s) * BK + c] = t - omega * v;
+    }
+  }
+}
+
+// A P, warp per fine row.
+template <int B, int K, bool kSell>
+__global__ void __launch_bounds__(64) k_ap_numeric(Graph g, OpView<B, kSell> A, const int64_t* __restrict__ p_ptr,
+                                                   const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
+                                                   const int64_t* __restrict__ ap_ptr,
+                                                   const int32_t* __restrict__ ap_col, float* __restrict__ ap_val) {
+  constexpr int BK = B * K;
+  __shared__ int32_t cols[2][kMaxAPRow];
+  __shared__ float acc[2][kMaxAPRow][BK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 2 + w;
+  if (i >= g.n) return;
+  const int64_t e0 = ap_ptr[i];
+  const int m = (int)(ap_ptr[i + 1] - e0);
+  if (m == 0) return;
+  for (int s = lane; s < m; s += 32) cols[w][s] = ap_col[e0 + s];
+  for (int t = lane; t < m * BK; t += 32) acc[w][t / BK][t % BK] = 0.f;
+  __syncwarp();
+  const int64_t nb = g.ptr[i];
+  const int deg = (int)(g.ptr[i + 1] - nb);
+  for (int kk = 0; kk < deg; ++kk) {
+    const int32_t j = g.idx[nb + kk];
+    float a[B * B];
+#pragma unroll
+    for (int c = 0; c < B * B; ++c) a[c] = A.at(i, kk, c);
+    for (int64_t pe = p_ptr[j]; pe < p_ptr[j + 1]; ++pe) {
+      const int s = find_slot(cols[w], m, p_col[pe]);
+      if (s < 0) continue;  // cannot happen: the row is the union of these columns
+      const float* pv = p_val + pe * BK;
+      for (int c = lane; c < BK; c += 32) {
+        const int r = c / K, k = c % K;
+        float v = acc[w][s][c];
+#pragma unroll
+        for (int q = 0; q < B; ++q) v = fmaf(a[r * B + q], pv[q * K + k], v);
+        acc[w][s][c] = v;
+      }
+      __syncwarp();
+    }
+  }
+  for (int t = lane; t < m * BK; t += 32) ap_val[e0 * BK + t] = acc[w][t / BK][t % BK];
+}
+
+// A_c = P^T (A P), warp per coarse row; decoupled coarse DOFs (a dropped
+// mode: zero row and column) get a unit diagonal.
+template <int B, int K>
+__global__ void __launch_bounds__(64) k_ac_numeric(int64_t n_c, const int64_t* __restrict__ pt_ptr,
+                                                   const int32_t* __restrict__ pt_row,
+                                                   const int64_t* __restrict__ pt_pos, const float* __restrict__ p_val,
+                                                   const int64_t* __restrict__ ap_ptr,
+                                                   const int32_t* __restrict__ ap_col, const float* __restrict__ ap_val,
+                                                   const int64_t* __restrict__ ac_ptr,
+                                                   const int32_t* __restrict__ ac_col, float* __restrict__ ac_val) {
+  constexpr int BK = B * K, KK = K * K;
+  __shared__ int32_t cols[2][kMaxCRow];
+  __shared__ float acc[2][kMaxCRow][KK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t I = (int64_t)blockIdx.x * 2 + w;
+  if (I >= n_c) return;
+  const int64_t e0 = ac_ptr[I];
+  const int m = (int)(ac_ptr[I + 1] - e0);
+  for (int s = lane; s < m; s += 32) cols[w][s] = ac_col[e0 + s];
+  for (int t = lane; t < m * KK; t += 32) acc[w][t / KK][t % KK] = 0.f;
+  __syncwarp();
+  for (int64_t pe = pt_ptr[I]; pe < pt_ptr[I + 1]; ++pe) {
+    const int32_t i = pt_row[pe];
+    if (pt_pos[pe] < 0) continue;  // cannot happen: P^T lists entries of P
+    const float* pv = p_val + pt_pos[pe] * BK;
+    for (int64_t ae = ap_ptr[i]; ae < ap_ptr[i + 1]; ++ae) {
+      const int s = find_slot(cols[w], m, ap_col[ae]);
+      if (s < 0) continue;
+      const float* wv = ap_val + ae * BK;
+      for (int c = lane; c < KK; c += 32) {
+        const int k1 = c / K, k2 = c % K;
+        float v = acc[w][s][c];
+#pragma unroll
+        for (int q = 0; q < B; ++q) v = fmaf(pv[q * K + k1], wv[q * K + k2], v);
+        acc[w][s][c] = v;
+      }
+      __syncwarp();
+    }
+  }
+  for (int t = lane; t < m * KK; t += 32) {
+    const int s = t / KK, c = t % KK;
+    float v = acc[w][s][c];
+    if (cols[w][s] == (int32_t)I && c / K == c % K && v == 0.f) v = 1.f;
+    ac_val[e0 * KK + t] = v;
+  }
+}
+
+// Inverse of the diagonal block of every coarse row (Gauss-Jordan, partial
+// pivoting, FP64).
+template <int K>
+__global__ void k_block_inv(int64_t n, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                            const float* __restrict__ val, float* __restrict__ dinv, int32_t* __restrict__ status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t d = -1;
+  for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e)
+    if (col[e] == (int32_t)i) d = e;
+  double M[K][2 * K];
+  for (int p = 0; p < K; ++p)
+    for (int q = 0; q < K; ++q) {
+      M[p][q] = d >= 0 ? (double)val[d * K * K + p * K + q] : 0.0;
+      M[p][K + q] = p == q ? 1.0 : 0.0;
+    }
+  bool ok = d >= 0;
+  for (int c = 0; c < K && ok; ++c) {
+    int piv = c;
+    for (int p = c + 1; p < K; ++p)
+      if (fabs(M[p][c]) > fabs(M[piv][c])) piv = p;
+    if (!(fabs(M[piv][c]) > 0.0)) {
+      ok = false;
+      break;
+    }
+    if (piv != c)
+      for (int q = 0; q < 2 * K; ++q) {
+        const double t = M[c][q];
+        M[c][q] = M[piv][q];
+        M[piv][q] = t;
+      }
+    const double inv = 1.0 / M[c][c];
+    for (int q = 0; q < 2 * K; ++q) M[c][q] *= inv;
+    for (int p = 0; p < K; ++p)
+      if (p != c) {
+        const double f = M[p][c];
+        for (int q = 0; q < 2 * K; ++q) M[p][q] -= f * M[c][q];
+      }
+  }
+  if (!ok) flag_status(status, kStatNonFinite);
+  for (int p = 0; p < K; ++p)
+    for (int q = 0; q < K; ++q) dinv[(i * K + p) * K + q] = ok ? (float)M[p][K + q] : 0.f;
+}
+
+// Dense inverse of the coarsest operator (m <= kCoarseMaxDof), one CTA,
+// Gauss-Jordan with partial pivoting in FP64 on [A | I] held in `work`
+// (m x 2m), symmetrised on output.
+__global__ void __launch_bounds__(1024) k_coarse_inverse(int64_t n, int K, const int64_t* __restrict__ ptr,
+                                                         const int32_t* __restrict__ col,
+                                                         const float* __restrict__ val, double* __restrict__ work,
+                                                         float* __restrict__ inv, int32_t* __restrict__ status) {
+  __shared__ int piv_s;
+  __shared__ bool ok_s;
+  __shared__ double fcol[kCoarseMaxDof];
+  const int m = (int)(n * K);
+  const int w2 = 2 * m;
+  for (int t = threadIdx.x; t < m * w2; t += blockDim.x) work[t] = (t % w2) - m == t / w2 ? 1.0 : 0.0;
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e)
+      for (int p = 0; p < K; ++p)
+        for (int q = 0; q < K; ++q) work[(i * K + p) * w2 + (int64_t)col[e] * K + q] = val[e * K * K + p * K + q];
+  if (threadIdx.x == 0) ok_s = true;
+  __syncthreads();
+  for (int c = 0; c < m; ++c) {
+    if (threadIdx.x == 0) {
+      int piv = c;
+      for (int p = c + 1; p < m; ++p)
+        if (fabs(work[p * w2 + c]) > fabs(work[piv * w2 + c])) piv = p;
+      if (!(fabs(work[piv * w2 + c]) > 0.0)) ok_s = false;
+      piv_s = piv;
+    }
+    __syncthreads();
+    if (!ok_s) break;
+    const int piv = piv_s;
+    if (piv != c)
+      for (int q = threadIdx.x; q < w2; q += blockDim.x) {
+        const double t = work[c * w2 + q];
+        work[c * w2 + q] = work[piv * w2 + q];
+        work[piv * w2 + q] = t;
+      }
+    __syncthreads();
+    const double inv_p = 1.0 / work[c * w2 + c];
+    __syncthreads();
+    for (int q = threadIdx.x; q < w2; q += blockDim.x) work[c * w2 + q] *= inv_p;
+    __syncthreads();
+    // multipliers first: the elimination below overwrites column c
+    for (int p = threadIdx.x; p < m; p += blockDim.x) fcol[p] = p == c ? 0.0 : work[p * w2 + c];
+    __syncthreads();
+    for (int t = threadIdx.x; t < m * w2; t += blockDim.x) {
+      const int p = t / w2, q = t % w2;
+      if (p != c) work[t] -= fcol[p] * work[c * w2 + q];
+    }
+    __syncthreads();
+  }
+  if (!ok_s) {
+    if (threadIdx.x == 0) flag_status(status, kStatNonFinite);
+    return;
+  }
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    const int p = t / m, q = t % m;
+    inv[t] = (float)(0.5 * (work[p * w2 + m + q] + work[q * w2 + m + p]));
+  }
+}
+
+// ================================================================== solve ==
+enum { kOpS1 = 1, kOpS2, kOpS3, kOpS4, kOpS4Dot, kOpQ, kOpLzQ };
+
+// Level vectors of the V-cycle and the CG scalars the fused kernels touch.
+struct OpArgs {
+  float* f;        // right-hand side of the level
+  float* x;        // pre-smoothed iterate
+  float* xb;       // post-smoothed iterate (the level's output)
+  float* r;        // residual
+  float* d;        // Chebyshev directions (two buffers: the SpMV operand is never written)
+  float* db;
+  const float* dinv;
+  float theta_inv, c1, c2;
+  const float* p;  // kOpQ / kOpLzQ operand
+  float* q;
+  double* partial;
+  AmgCtrl* ctrl;
+  double* lz;      // Lanczos coefficients (kOpLzQ)
+};
+
+template <int MODE>
+__device__ __forceinline__ const float* op_operand(const OpArgs& a) {
+  if constexpr (MODE == kOpS1 || MODE == kOpS4 || MODE == kOpS4Dot) return a.d;
+  else if constexpr (MODE == kOpS2) return a.db;
+  else if constexpr (MODE == kOpS3) return a.x;
+  else return a.p;
+}
+
+// Row epilogue shared by the sliced and CSR kernels: y = (A v)_i; returns the
+// row's contribution to the kernel's dot product.
+template <int B, int MODE>
+__device__ __forceinline__ double op_epilogue(const OpArgs& a, int64_t i, const float (&y)[B]) {
+  const int64_t o = i * B;
+  float t[B], rn[B];
+  double dot = 0.0;
+  if constexpr (MODE == kOpS1) {
+#pragma unroll
+    for (int c = 0; c < B; ++c) rn[c] = a.f[o + c] - y[c];
+    block_mv<B>(a.dinv + i * B * B, rn, t);
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      const float dn = a.c1 * a.d[o + c] + a.c2 * t[c];
+      a.r[o + c] = rn[c];
+      a.db[o + c] = dn;
+      a.x[o + c] += dn;
+    }
+  } else if constexpr (MODE == kOpS2) {
+#pragma unroll
+    for (int c = 0; c < B; ++c) a.r[o + c] -= y[c];
+  } else if constexpr (MODE == kOpS3) {
+#pragma unroll
+    for (int c = 0; c < B; ++c) rn[c] = a.f[o + c] - y[c];
+    block_mv<B>(a.dinv + i * B * B, rn, t);
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      const float dn = a.theta_inv * t[c];
+      a.r[o + c] = rn[c];
+      a.d[o + c] = dn;
+      a.xb[o + c] = a.x[o + c] + dn;
+    }
+  } else if constexpr (MODE == kOpS4 || MODE == kOpS4Dot) {
+#pragma unroll
+    for (int c = 0; c < B; ++c) rn[c] = a.r[o + c] - y[c];
+    block_mv<B>(a.dinv + i * B * B, rn, t);
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      const float z = a.xb[o + c] + (a.c1 * a.d[o + c] + a.c2 * t[c]);
+      a.xb[o + c] = z;
+      if constexpr (MODE == kOpS4Dot) dot += (double)a.f[o + c] * (double)z;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      a.q[o + c] = y[c];
+      dot += (double)a.p[o + c] * (double)y[c];
+    }
+  }
+  return dot;
+}
+
+template <int MODE>
+__device__ __forceinline__ void op_finish(const OpArgs& a, double tot) {
+  AmgCtrl* c = a.ctrl;
+  if constexpr (MODE == kOpS4Dot) {
+    if (!isfinite(tot)) c->done = kNonFinite;
+    else if (!(tot > 0.0)) c->done = kBreakdown;
+    else {
+      c->beta = tot / c->rz * c->pscale;
+      c->rz = tot;
+      c->pscale = 1.0;
+    }
+  } else if constexpr (MODE == kOpQ || MODE == kOpLzQ) {
+    if (!isfinite(tot)) c->done = kNonFinite;
+    else if (!(tot > 0.0)) c->done = kBreakdown;
+    else {
+      c->alpha = c->rz / tot;
+      if constexpr (MODE == kOpLzQ) a.lz[2 * c->lz_step] = c->alpha;
+    }
+  }
+}
+
+template <int MODE>
+__host__ __device__ constexpr bool op_has_dot() {
+  return MODE == kOpS4Dot || MODE == kOpQ || MODE == kOpLzQ;
+}
+
+// Level 0: the sliced FP32 matrix, thread per row, kSellW warps sharing each
+// slice's slots (the layout of fem_assemble_sell).  The matrix streams with
+// L2 evict_first; the vectors stay in L2.
+template <int D, int MODE>
+__global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const int64_t* __restrict__ sell_base,
+                                                         const int32_t* __restrict__ col,
+                                                         const float* __restrict__ sval, OpArgs a) {
+  constexpr int DD = D * D;
+  __shared__ float ys[kSellW][D][32];
+  __shared__ double red[32];
+  if (amg_idle(a.ctrl)) return;
+  const float* __restrict__ v = op_operand<MODE>(a);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t n_slices = (n_rows + 31) >> 5;
+  const uint64_t pol = l2_policy(false);
+  double dot = 0.0;
+  for (int64_t s = blockIdx.x; s < n_slices; s += gridDim.x) {
+    const int64_t b0 = sell_base[s];
+    const int len = (int)((sell_base[s + 1] - b0) >> 5);
+    const int32_t* cp = col + b0 + lane;
+    const float* vp = sval + b0 * DD + lane;
+    float y[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) y[c] = 0.f;
+#pragma unroll 2
+    for (int k = w; k < len; k += kSellW) {
+      const int64_t cc = ld_l2(cp + (int64_t)k * 32, pol);
+      const float* vk = vp + (int64_t)k * DD * 32;
+      float m[DD];
+#pragma unroll
+      for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, pol);
+      float xv[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) xv[j] = v[cc * D + j];
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int j = 0; j < D; ++j) y[r] = fmaf(m[r * D + j], xv[j], y[r]);
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) ys[w][c][lane] = y[c];
+    __syncthreads();
+    if (w == 0) {
+      const int64_t i = s * 32 + lane;
+      if (i < n_rows) {
+        float yt[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          float t = ys[0][c][lane];
+#pragma unroll
+          for (int u = 1; u < kSellW; ++u) t += ys[u][c][lane];
+          yt[c] = t;
+        }
+        dot += op_epilogue<D, MODE>(a, i, yt);
+      }
+    }
+    __syncthreads();
+  }
+  if constexpr (op_has_dot<MODE>()) {
+    const double bsum = block_sum(dot, red);
+    if (threadIdx.x == 0) a.partial[blockIdx.x] = bsum;
+    if (arrive_last(&a.ctrl->counter)) {
+      const double tot = sum_partials(a.partial, gridDim.x, 1, 0, red);
+      if (threadIdx.x == 0) {
+        a.ctrl->counter = 0;
+        op_finish<MODE>(a, tot);
+      }
+    }
+  }
+}
+
+// Coarser levels: block CSR (B x B blocks), warp per row; lane (u, r) takes
+// row r of every (32 / B)-th block.  Coarse operators are read evict_last so
+// they stay in L2 across the cycle.
+template <int B, int MODE>
+__global__ void __launch_bounds__(256) k_csr_op(int64_t n, const int64_t* __restrict__ ptr,
+                                                const int32_t* __restrict__ col, const float* __restrict__ val,
+                                                OpArgs a) {
+  constexpr int PB = 32 / B;
+  __shared__ double red[32];
+  if (amg_idle(a.ctrl)) return;
+  const float* __restrict__ v = op_operand<MODE>(a);
+  const int lane = threadIdx.x & 31;
+  const int u = lane / B, r = lane % B;
+  const uint64_t pol = l2_policy(true);
+  double dot = 0.0;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw) {
+    float y = 0.f;
+    if (u < PB)
+      for (int64_t e = ptr[i] + u; e < ptr[i + 1]; e += PB) {
+        const int64_t c = ld_l2(col + e, pol);
+        const float* m = val + e * B * B + r * B;
+        const float* xv = v + c * B;
+#pragma unroll
+        for (int q = 0; q < B; ++q) y = fmaf(ld_l2(m + q, pol), xv[q], y);
+      }
+    float yt = 0.f;
+#pragma unroll
+    for (int t = 0; t < PB; ++t) yt += __shfl_sync(0xffffffffu, y, r + t * B);
+    float ys[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) ys[c] = __shfl_sync(0xffffffffu, yt, c);
+    if (lane == 0) dot += op_epilogue<B, MODE>(a, i, ys);
+  }
+  if constexpr (op_has_dot<MODE>()) {
+    const double bsum = block_sum(dot, red);
+    if (threadIdx.x == 0) a.partial[blockIdx.x] = bsum;
+    if (arrive_last(&a.ctrl->counter)) {
+      const double tot = sum_partials(a.partial, gridDim.x, 1, 0, red);
+      if (threadIdx.x == 0) {
+        a.ctrl->counter = 0;
+        op_finish<MODE>(a, tot);
+      }
+    }
+  }
+}
+
+// Restriction f_c = P^T r, warp per coarse row, followed by the first
+// Chebyshev step of the coarse level: d = D^-1 f / theta, x = d.
+template <int BF, int K>
+__global__ void __launch_bounds__(256) k_restrict(int64_t n_c, const int64_t* __restrict__ pt_ptr,
+                                                  const int32_t* __restrict__ pt_row,
+                                                  const int64_t* __restrict__ pt_pos, const float* __restrict__ p_val,
+                                                  const float* __restrict__ rf, OpArgs c, const AmgCtrl* ctrl) {
+  if (amg_idle(ctrl)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (I >= n_c) return;
+  float acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.f;
+  for (int64_t e = pt_ptr[I] + lane; e < pt_ptr[I + 1]; e += 32) {
+    const int64_t i = pt_row[e];
+    if (pt_pos[e] < 0) continue;
+    const float* pv = p_val + pt_pos[e] * BF * K;
+#pragma unroll
+    for (int q = 0; q < BF; ++q) {
+      const float rv = rf[i * BF + q];
+#pragma unroll
+      for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+  if (lane < K) {
+    const float* m = c.dinv + (I * K + lane) * K;
+    float t = 0.f;
+#pragma unroll
+    for (int q = 0; q < K; ++q) t = fmaf(m[q], acc[q], t);
+    const float dn = c.theta_inv * t;
+    float fv = 0.f;
+#pragma unroll
+    for (int q = 0; q < K; ++q) fv = q == lane ? acc[q] : fv;
+    c.f[I * K + lane] = fv;
+    c.d[I * K + lane] = dn;
+    c.x[I * K + lane] = dn;
+  }
+}
+
+// Restriction onto the coarsest level and its dense solve, one CTA.
+template <int BF, int K>
+__global__ void __launch_bounds__(1024) k_restrict_solve(int64_t n_c, const int64_t* __restrict__ pt_ptr,
+                                                         const int32_t* __restrict__ pt_row,
+                                                         const int64_t* __restrict__ pt_pos,
+                                                         const float* __restrict__ p_val, const float* __restrict__ rf,
+                                                         const float* __restrict__ inv, float* __restrict__ xc,
+                                                         const AmgCtrl* ctrl) {
+  __shared__ float fs[kCoarseMaxDof];
+  if (amg_idle(ctrl)) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t I = w; I < n_c; I += blockDim.x >> 5) {
+    float acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.f;
+    for (int64_t e = pt_ptr[I] + lane; e < pt_ptr[I + 1]; e += 32) {
+      const int64_t i = pt_row[e];
+      if (pt_pos[e] < 0) continue;
+      const float* pv = p_val + pt_pos[e] * BF * K;
+#pragma unroll
+      for (int q = 0; q < BF; ++q) {
+        const float rv = rf[i * BF + q];
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < K; ++k) fs[I * K + k] = acc[k];
+  }
+  __syncthreads();
+  const int m = (int)(n_c * K);
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    float s = 0.f;
+    for (int j = 0; j < m; ++j) s = fmaf(inv[(int64_t)t * m + j], fs[j], s);
+    xc[t] = s;
+  }
+}
+
+// Prolongation x += P x_c, thread per fine row.
+template <int BF, int K>
+__global__ void __launch_bounds__(256) k_prolong(int64_t n, const int64_t* __restrict__ p_ptr,
+                                                 const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
+                                                 const float* __restrict__ xc, float* __restrict__ x,
+                                                 const AmgCtrl* ctrl) {
+  if (amg_idle(ctrl)) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t e0 = p_ptr[i], e1 = p_ptr[i + 1];
+  if (e0 == e1) return;
+  float acc[BF];
+#pragma unroll
+  for (int q = 0; q < BF; ++q) acc[q] = 0.f;
+  for (int64_t e = e0; e < e1; ++e) {
+    const float* pv = p_val + e * BF * K;
+    const float* cv = xc + (int64_t)p_col[e] * K;
+    float cx[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) cx[k] = cv[k];
+#pragma unroll
+    for (int q = 0; q < BF; ++q)
+#pragma unroll
+      for (int k = 0; k < K; ++k) acc[q] = fmaf(pv[q * K + k], cx[k], acc[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < BF; ++q) x[i * BF + q] += acc[q];
+}
+
+// ---------------------------------------------------------------- CG ------
+// p = z + beta p.
+__global__ void __launch_bounds__(256) k_pup(int64_t n, const float* __restrict__ z, float* __restrict__ p,
+                                             const AmgCtrl* ctrl) {
+  if (amg_idle(ctrl)) return;
+  const float beta = (float)ctrl->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+// ||b||^2, the first residual scale and the tolerances.
+__global__ void __launch_bounds__(256) k_cg_bnorm(int64_t n, const double* __restrict__ b, double rtol2,
+                                                  double* __restrict__ partial, AmgCtrl* ctrl) {
+  __shared__ double red[32];
+  double t = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    t += b[i] * b[i];
+  t = block_sum(t, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (arrive_last(&ctrl->counter)) {
+    const double bb = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      const double sc = unit_scale(bb);
+      ctrl->bb = bb;
+      ctrl->rscale = sc;
+      ctrl->tol2bb = rtol2 * bb;
+      ctrl->tol2_lo = rtol2 * bb * sc * sc;
+    }
+  }
+}
+
+// Level-0 first Chebyshev step on a fresh residual: d = D^-1 r / theta, x = d.
+template <int D>
+__device__ __forceinline__ void pre_step(const float* __restrict__ dinv, float theta_inv, int64_t i,
+                                         const float (&rv)[D], float* __restrict__ d, float* __restrict__ x) {
+  float t[D];
+  block_mv<D>(dinv + i * D * D, rv, t);
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const float dn = theta_inv * t[c];
+    d[i * D + c] = dn;
+    x[i * D + c] = dn;
+  }
+}
+
+// x = 0: r = b * rscale, ||r||^2, first smoothing step.
+template <int D>
+__global__ void __launch_bounds__(256) k_cg_init(int64_t n_nod, const double* __restrict__ b, float* __restrict__ r,
+                                                 const float* __restrict__ dinv, float theta_inv, float* __restrict__ d,
+                                                 float* __restrict__ mx, double* __restrict__ partial, AmgCtrl* ctrl) {
+  __shared__ double red[32];
+  const double sc = ctrl->rscale;
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_nod; i += (int64_t)gridDim.x * blockDim.x) {
+    float rv[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      rv[c] = (float)(b[i * D + c] * sc);
+      r[i * D + c] = rv[c];
+      rr += (double)rv[c] * (double)rv[c];
+    }
+    pre_step<D>(dinv, theta_inv, i, rv, d, mx);
+  }
+  rr = block_sum(rr, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = rr;
+  if (arrive_last(&ctrl->counter)) {
+    const double t = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      ctrl->rr = t;
+      ctrl->rr_ref = t;
+      ctrl->rr_true = ctrl->bb;
+      ctrl->rz = 1.0;
+      ctrl->pscale = 0.0;
+      ctrl->iters = 0;
+      ctrl->replacements = 0;
+      ctrl->replace = 0;
+      if (!isfinite(t) || !isfinite(ctrl->bb)) ctrl->done = kNonFinite;
+      else if (ctrl->bb == 0.0 || t <= ctrl->tol2_lo) ctrl->done = kConverged;
+      else ctrl->done = kRun;
+    }
+  }
+}
+
+// x_lo += alpha p; r -= alpha q; ||r||^2; first smoothing step of the next
+// cycle; convergence or replacement decision.
+template <int D>
+__global__ void __launch_bounds__(256) k_cg_update(int64_t n_nod, float* __restrict__ xlo, float* __restrict__ r,
+                                                   const float* __restrict__ p, const float* __restrict__ q,
+                                                   const float* __restrict__ dinv, float theta_inv,
+                                                   float* __restrict__ d, float* __restrict__ mx,
+                                                   double* __restrict__ partial, AmgCtrl* ctrl) {
+  __shared__ double red[32];
+  if (amg_idle(ctrl)) return;
+  const float alpha = (float)ctrl->alpha;
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_nod; i += (int64_t)gridDim.x * blockDim.x) {
+    float rv[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const int64_t k = i * D + c;
+      xlo[k] += alpha * p[k];
+      rv[c] = r[k] - alpha * q[k];
+      r[k] = rv[c];
+      rr += (double)rv[c] * (double)rv[c];
+    }
+    pre_step<D>(dinv, theta_inv, i, rv, d, mx);
+  }
+  rr = block_sum(rr, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = rr;
+  if (arrive_last(&ctrl->counter)) {
+    const double t = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      AmgCtrl* c = ctrl;
+      c->counter = 0;
+      c->iters += 1;
+      c->rr = t;
+      if (!isfinite(t)) {
+        c->done = kNonFinite;
+      } else if (c->mixed) {
+        if (t <= c->tol2_lo || t <= c->delta2 * c->rr_ref) c->replace = 1;
+      } else if (t <= c->tol2_lo) {
+        c->done = kConverged;
+      }
+      if (c->done == kRun && !c->replace && c->iters >= c->max_iter) c->done = kMaxIter;
+    }
+  }
+}
+
+// x64 += x_lo / rscale; x_lo = 0.
+__global__ void k_cg_fold(int64_t n, double* __restrict__ x64, float* __restrict__ xlo, const AmgCtrl* ctrl) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x64[i] += (double)xlo[i] * (1.0 / ctrl->rscale);
+  xlo[i] = 0.f;
+}
+
+// FP64 replacement: r = (b - y) * s with s the unit scale of the current
+// residual estimate, first smoothing step, FP64 convergence decision; the
+// kept direction continues through pscale.
+template <int D>
+__global__ void __launch_bounds__(256) k_cg_replace(int64_t n_nod, const double* __restrict__ b,
+                                                    const double* __restrict__ y, float* __restrict__ r,
+                                                    const float* __restrict__ dinv, float theta_inv,
+                                                    float* __restrict__ d, float* __restrict__ mx,
+                                                    double* __restrict__ partial, AmgCtrl* ctrl) {
+  __shared__ double red[32];
+  const double sc_old = ctrl->rscale;
+  const double sc = unit_scale(ctrl->rr / (sc_old * sc_old));
+  double rr = 0.0, r64 = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_nod; i += (int64_t)gridDim.x * blockDim.x) {
+    float rv[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const int64_t k = i * D + c;
+      const double rd = b[k] - y[k];
+      r64 += rd * rd;
+      rv[c] = (float)(rd * sc);
+      r[k] = rv[c];
+      rr += (double)rv[c] * (double)rv[c];
+    }
+    pre_step<D>(dinv, theta_inv, i, rv, d, mx);
+  }
+  const double s1 = block_sum(rr, red);
+  const double s2 = block_sum(r64, red);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = s1;
+    partial[2 * blockIdx.x + 1] = s2;
+  }
+  if (arrive_last(&ctrl->counter)) {
+    const double t1 = sum_partials(partial, gridDim.x, 2, 0, red);
+    const double t2 = sum_partials(partial, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      AmgCtrl* c = ctrl;
+      c->counter = 0;
+      c->rr_true = t2;
+      c->replacements += 1;
+      c->replace = 0;
+      if (!isfinite(t1) || !isfinite(t2)) {
+        c->done = kNonFinite;
+      } else if (t2 <= c->tol2bb) {
+        c->done = kConverged;
+      } else if (c->done == kRun) {
+        c->rr = t1;
+        c->rr_ref = t1;
+        c->pscale = sc_old / sc;
+        c->rscale = sc;
+        c->tol2_lo = c->tol2bb * sc * sc;
+      }
+    }
+  }
+}
+
+// FP32-only solve: x64 = x_lo / rscale.
+__global__ void k_cg_out(int64_t n, const float* __restrict__ xlo, double* __restrict__ x64, const AmgCtrl* ctrl) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x64[i] = (double)xlo[i] * (1.0 / ctrl->rscale);
+}
+
+// ------------------------------------------------------- CG-Lanczos -----
+// Jacobi-preconditioned CG on a fixed pseudo-random right-hand side; its
+// coefficients give the Lanczos tridiagonal of D^-1 A.
+template <int B>
+__global__ void __launch_bounds__(256) k_lz_init(int64_t n, const float* __restrict__ dinv, float* __restrict__ r,
+                                                 float* __restrict__ z, float* __restrict__ p,
+                                                 double* __restrict__ partial, AmgCtrl* ctrl) {
+  __shared__ double red[32];
+  double rz = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float rv[B], zv[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      const uint32_t h = amg_hash((uint32_t)(i * B + c) ^ 0x9e3779b9U);
+      rv[c] = (float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f;
+      r[i * B + c] = rv[c];
+    }
+    block_mv<B>(dinv + i * B * B, rv, zv);
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      z[i * B + c] = zv[c];
+      p[i * B + c] = zv[c];
+      rz += (double)rv[c] * (double)zv[c];
+    }
+  }
+  rz = block_sum(rz, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = rz;
+  if (arrive_last(&ctrl->counter)) {
+    const double t = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      ctrl->rz = t;
+      ctrl->lz_step = 0;
+      ctrl->replace = 0;
+      ctrl->done = (isfinite(t) && t > 0.0) ? kRun : kBreakdown;
+    }
+  }
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_lz_update(int64_t n, const float* __restrict__ dinv, float* __restrict__ r,
+                                                   float* __restrict__ z, const float* __restrict__ q,
+                                                   double* __restrict__ partial, AmgCtrl* ctrl,
+                                                   double* __restrict__ lz) {
+  __shared__ double red[32];
+  if (amg_idle(ctrl)) return;
+  const float alpha = (float)ctrl->alpha;
+  double rz = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float rv[B], zv[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      rv[c] = r[i * B + c] - alpha * q[i * B + c];
+      r[i * B + c] = rv[c];
+    }
+    block_mv<B>(dinv + i * B * B, rv, zv);
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      z[i * B + c] = zv[c];
+      rz += (double)rv[c] * (double)zv[c];
+    }
+  }
+  rz = block_sum(rz, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = rz;
+  if (arrive_last(&ctrl->counter)) {
+    const double t = sum_partials(partial, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      ctrl->counter = 0;
+      if (!(isfinite(t) && t > 0.0)) {
+        ctrl->done = kBreakdown;
+      } else {
+        ctrl->beta = t / ctrl->rz;
+        lz[2 * ctrl->lz_step + 1] = ctrl->beta;
+        ctrl->rz = t;
+        ctrl->lz_step += 1;
+      }
+    }
+  }
+}
+
+// Largest eigenvalue of the symmetric tridiagonal (diag a, off-diagonal b) by
+// Sturm-sequence bisection.
+double tridiag_max_eig(const std::vector<double>& a, const std::vector<double>& b) {
+  const int k = (int)a.size();
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < k; ++i) {
+    const double rad = (i > 0 ? fabs(b[i - 1]) : 0.0) + (i + 1 < k ? fabs(b[i]) : 0.0);
+    lo = std::min(lo, a[i] - rad);
+    hi = std::max(hi, a[i] + rad);
+  }
+  auto count_below = [&](double x) {  // eigenvalues < x
+    int cnt = 0;
+    double q = 1.0;
+    for (int i = 0; i < k; ++i) {
+      const double off = i > 0 ? b[i - 1] * b[i - 1] : 0.0;
+      q = a[i] - x - (i > 0 ? off / q : 0.0);
+      if (q == 0.0) q = -1e-300;
+      if (q < 0.0) ++cnt;
+    }
+    return cnt;
+  };
+  for (int it = 0; it < 200 && hi - lo > 1e-12 * std::max(1.0, fabs(hi)); ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (count_below(mid) >= k) hi = mid;
+    else lo = mid;
+  }
+  return hi;
+}
+
+}  // namespace
+
+// ================================================================= handle ==
+struct AmgLevel {
+  int64_t n = 0;  // block rows
+  int b = 0;      // block size
+  Graph g{};      // aggregation graph (level 0: mesh node graph; coarser: operator pattern)
+  // operator of a coarser level (block CSR, owned)
+  int64_t* a_ptr = nullptr;
+  int32_t* a_col = nullptr;
+  float* a_val = nullptr;
+  int64_t a_nnz = 0;
+  float* dinv = nullptr;
+  // transfer to the next level
+  int32_t* agg = nullptr;
+  int64_t n_agg = 0;
+  float* tval = nullptr;
+  int64_t* p_ptr = nullptr;
+  int32_t* p_col = nullptr;
+  float* p_val = nullptr;
+  int64_t p_nnz = 0;
+  int64_t* pt_ptr = nullptr;
+  int32_t* pt_row = nullptr;
+  int64_t* pt_pos = nullptr;
+  int64_t* ap_ptr = nullptr;
+  int32_t* ap_col = nullptr;
+  float* ap_val = nullptr;
+  int64_t ap_nnz = 0;
+  // smoother
+  double rho = 0.0;
+  float theta_inv = 0.f, c1 = 0.f, c2 = 0.f;
+  // vectors (level 0: f and xb are the CG residual and preconditioned residual)
+  float *f = nullptr, *x = nullptr, *xb = nullptr, *r = nullptr, *d = nullptr, *db = nullptr;
+};
+
+}  // namespace tfg
+
+struct fem_amg {
+  int dim = 0, K = 0, n_levels = 0;
+  tfg::AmgLevel L[tfg::kMaxLevels];
+  float* coarse_inv = nullptr;
+  double* coarse_work = nullptr;
+  int64_t m_coarse = 0;
+  uint8_t* active = nullptr;  // level 0: nodes with a free DOF
+  // CG state
+  float *xlo = nullptr, *rcg = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+  tfg::AmgCtrl* ctrl = nullptr;
+  tfg::AmgCtrl* lzc = nullptr;
+  double* lz = nullptr;
+  double* partial = nullptr;
+  int32_t* status = nullptr;
+  unsigned long long* counter = nullptr;
+  std::vector<void*> mem;
+  int64_t dropped = 0;
+  bool ready = false;
+  // level-0 operator captured at setup
+  const int64_t* sell_base = nullptr;
+  const int32_t* sell_col = nullptr;
+  const float* sell_val = nullptr;
+  const float* dinv0 = nullptr;
+
+  template <typename T>
+  T* alloc(int64_t count, cudaStream_t st) {
+    void* p = nullptr;
+    const size_t bytes = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+    (void)st;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    mem.push_back(p);
+    return static_cast<T*>(p);
+  }
+};
+
+namespace tfg {
+namespace {
+
+constexpr int kPartialLen = 8192;
+
+int read_u64(const unsigned long long* d, unsigned long long* h, cudaStream_t st) {
+  if (cudaMemcpyAsync(h, d, sizeof(*h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda("AMG read");
+  return FEM_OK;
+}
+
+int read_i64(const int64_t* d, int64_t* h, cudaStream_t st) {
+  if (cudaMemcpyAsync(h, d, sizeof(*h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda("AMG read");
+  return FEM_OK;
+}
+
+int read_status(fem_amg* h, cudaStream_t st, const char* what) {
+  int32_t s = 0;
+  if (cudaMemcpyAsync(&s, h->status, sizeof(s), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda(what);
+  if (s & kStatBounds) {
+    set_last_error("%s: a row of the multigrid hierarchy exceeds its size limit", what);
+    return FEM_BOUNDS;
+  }
+  if (s & kStatNonFinite) {
+    set_last_error("%s: singular or non-finite block in the multigrid hierarchy", what);
+    return FEM_NONFINITE;
+  }
+  return FEM_OK;
+}
+
+// Exclusive scan of cnt [n] into ptr [n+1]; returns the total on the host.
+int scan_total(fem_amg* h, const int64_t* cnt, int64_t* ptr, int64_t n, int64_t* total, cudaStream_t st) {
+  int64_t* ws = h->alloc<int64_t>((int64_t)(scan_workspace_bytes(n) / sizeof(int64_t)) + 1, st);
+  if (!ws) return check_cuda("AMG scan workspace");
+  int rc = scan_exclusive(cnt, ptr, n, ws, st);
+  if (rc) return rc;
+  return read_i64(ptr + n, total, st);
+}
+
+// Aggregation of level l's graph into h->L[l].agg; returns the aggregate count.
+int aggregate(fem_amg* h, int l, const uint8_t* con, cudaStream_t st) {
+  AmgLevel& L = h->L[l];
+  const int64_t n = L.n;
+  uint8_t* active = l == 0 ? h->active : h->alloc<uint8_t>(n, st);
+  uint8_t* state = h->alloc<uint8_t>(n, st);
+  uint64_t* k1 = h->alloc<uint64_t>(n, st);
+  int64_t* flags = h->alloc<int64_t>(n, st);
+  int64_t* ids = h->alloc<int64_t>(n + 1, st);
+  int32_t* agg2 = h->alloc<int32_t>(n, st);
+  L.agg = h->alloc<int32_t>(n, st);
+  if (!active || !state || !k1 || !flags || !ids || !agg2 || !L.agg) return check_cuda("AMG aggregation buffers");
+  const unsigned gn = grid_for(n, kT);
+  k_agg_active<<<gn, kT, 0, st>>>(n, L.b, l == 0 ? con : nullptr, active, state);
+  note_launch();
+  for (int round = 0;; ++round) {
+    if (round > 10000) {
+      set_last_error("AMG aggregation: the independent-set rounds did not terminate");
+      return FEM_CUDA_ERROR;
+    }
+    cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st);
+    k_mis_max1<<<gn, kT, 0, st>>>(L.g, active, state, k1);
+    note_launch();
+    k_mis_max2<<<gn, kT, 0, st>>>(L.g, active, state, k1, h->counter);
+    note_launch();
+    unsigned long long und = 0;
+    int rc = read_u64(h->counter, &und, st);
+    if (rc) return rc;
+    if (und == 0) break;
+  }
+  k_root_flags<<<gn, kT, 0, st>>>(n, state, flags);
+  note_launch();
+  int rc = scan_total(h, flags, ids, n, &L.n_agg, st);
+  if (rc) return rc;
+  k_root_ids<<<gn, kT, 0, st>>>(n, state, ids, agg2);
+  note_launch();
+  k_agg_join<<<gn, kT, 0, st>>>(L.g, active, agg2, L.agg);
+  note_launch();
+  k_agg_join<<<gn, kT, 0, st>>>(L.g, active, L.agg, agg2);
+  note_launch();
+  cudaMemcpyAsync(L.agg, agg2, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st);
+  cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st);
+  k_count_unassigned<<<gn, kT, 0, st>>>(n, active, L.agg, h->counter);
+  note_launch();
+  unsigned long long un = 0;
+  rc = read_u64(h->counter, &un, st);
+  if (rc) return rc;
+  if (un != 0) {
+    set_last_error("AMG aggregation left %llu nodes unassigned", un);
+    return FEM_CUDA_ERROR;
+  }
+  return FEM_OK;
+}
+
+template <int B, int K>
+int tentative(fem_amg* h, int l, const double* coords, const uint8_t* con, const double* origin, const double* bn,
+              double* bc, cudaStream_t st) {
+  AmgLevel& L = h->L[l];
+  const int64_t n = L.n, na = L.n_agg;
+  int64_t* cnt = h->alloc<int64_t>(na, st);
+  int64_t* aptr = h->alloc<int64_t>(na + 1, st);
+  int64_t* cur = h->alloc<int64_t>(na + 1, st);
+  int32_t* unsorted = h->alloc<int32_t>(n, st);
+  int32_t* nodes = h->alloc<int32_t>(n, st);
+  L.tval = h->alloc<float>(n * B * K, st);
+  if (!cnt || !aptr || !cur || !unsorted || !nodes || !L.tval) return check_cuda("AMG tentative buffers");
+  cudaMemsetAsync(cnt, 0, sizeof(int64_t) * na, st);
+  cudaMemsetAsync(L.tval, 0, sizeof(float) * n * B * K, st);
+  k_count_keys<<<grid_for(n, kT), kT, 0, st>>>(n, L.agg, cnt);
+  note_launch();
+  int64_t members = 0;
+  int rc = scan_total(h, cnt, aptr, na, &members, st);
+  if (rc) return rc;
+  cudaMemcpyAsync(cur, aptr, sizeof(int64_t) * (na + 1), cudaMemcpyDeviceToDevice, st);
+  k_fill_keys<<<grid_for(n, kT), kT, 0, st>>>(n, L.agg, cur, unsorted);
+  note_launch();
+  k_sort_rows<<<grid_for(na * 32, kT), kT, 0, st>>>(na, aptr, unsorted, nodes);
+  note_launch();
+  cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st);
+  k_tentative<B, K><<<grid_for(na, 4), 128, 0, st>>>(na, aptr, nodes, coords, con, origin, bn, L.tval, bc,
+                                                     h->counter);
+  note_launch();
+  unsigned long long nd = 0;
+  rc = read_u64(h->counter, &nd, st);
+  if (rc) return rc;
+  h->dropped += (int64_t)nd;
+  return check_cuda("AMG tentative prolongator");
+}
+
+// Patterns of P, P^T, A P and the coarse operator of level l.
+int patterns(fem_amg* h, int l, cudaStream_t st) {
+  AmgLevel& L = h->L[l];
+  AmgLevel& C = h->L[l + 1];
+  const int64_t n = L.n, na = L.n_agg;
+  const uint8_t* active = l == 0 ? h->active : nullptr;
+  int64_t* cnt = h->alloc<int64_t>(std::max(n, na) + 1, st);
+  L.p_ptr = h->alloc<int64_t>(n + 1, st);
+  if (!cnt || !L.p_ptr) return check_cuda("AMG pattern buffers");
+  const unsigned gn = grid_for(n, kT);
+  k_p_rows<false><<<gn, kT, 0, st>>>(L.g, active, L.agg, cnt, nullptr, nullptr, h->status);
+  note_launch();
+  int rc = scan_total(h, cnt, L.p_ptr, n, &L.p_nnz, st);
+  if (rc) return rc;
+  L.p_col = h->alloc<int32_t>(L.p_nnz, st);
+  if (!L.p_col) return check_cuda("AMG P pattern");
+  k_p_rows<true><<<gn, kT, 0, st>>>(L.g, active, L.agg, nullptr, L.p_ptr, L.p_col, h->status);
+  note_launch();
+  // P^T
+  L.pt_ptr = h->alloc<int64_t>(na + 1, st);
+  int64_t* cur = h->alloc<int64_t>(na + 1, st);
+  int32_t* unsorted = h->alloc<int32_t>(L.p_nnz, st);
+  L.pt_row = h->alloc<int32_t>(L.p_nnz, st);
+  L.pt_pos = h->alloc<int64_t>(L.p_nnz, st);
+  if (!L.pt_ptr || !cur || !unsorted || !L.pt_row || !L.pt_pos) return check_cuda("AMG transpose buffers");
+  cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (na + 1), st);
+  k_count_cols<<<gn, kT, 0, st>>>(n, L.p_ptr, L.p_col, cnt);
+  note_launch();
+  int64_t tot = 0;
+  rc = scan_total(h, cnt, L.pt_ptr, na, &tot, st);
+  if (rc) return rc;
+  cudaMemcpyAsync(cur, L.pt_ptr, sizeof(int64_t) * (na + 1), cudaMemcpyDeviceToDevice, st);
+  k_fill_cols<<<gn, kT, 0, st>>>(n, L.p_ptr, L.p_col, cur, unsorted);
+  note_launch();
+  k_sort_rows<<<grid_for(na * 32, kT), kT, 0, st>>>(na, L.pt_ptr, unsorted, L.pt_row);
+  note_launch();
+  k_pt_pos<<<grid_for(na, kT), kT, 0, st>>>(na, L.pt_ptr, L.pt_row, L.p_ptr, L.p_col, L.pt_pos);
+  note_launch();
+  // A P: union of the P rows of the neighbours (rows of inactive nodes stay
+  // empty: their P rows are empty and no coarse row reads them)
+  L.ap_ptr = h->alloc<int64_t>(n + 1, st);
+  if (!L.ap_ptr) return check_cuda("AMG AP pattern");
+  k_union_rows<kMaxAPRow, false><<<gn, kT, 0, st>>>(n, active, L.g.ptr, L.g.idx, L.p_ptr, L.p_col, cnt, nullptr,
+                                                     nullptr, h->status);
+  note_launch();
+  rc = scan_total(h, cnt, L.ap_ptr, n, &L.ap_nnz, st);
+  if (rc) return rc;
+  L.ap_col = h->alloc<int32_t>(L.ap_nnz, st);
+  if (!L.ap_col) return check_cuda("AMG AP pattern");
+  k_union_rows<kMaxAPRow, true><<<gn, kT, 0, st>>>(n, active, L.g.ptr, L.g.idx, L.p_ptr, L.p_col, nullptr,
+                                                    L.ap_ptr, L.ap_col, h->status);
+  note_launch();
+  // coarse operator: union over the P^T row of the A P rows
+  C.n = na;
+  C.b = h->K;
+  C.a_ptr = h->alloc<int64_t>(na + 1, st);
+  if (!C.a_ptr) return check_cuda("AMG coarse pattern");
+  k_union_rows<kMaxCRow, false><<<grid_for(na, kT), kT, 0, st>>>(na, nullptr, L.pt_ptr, L.pt_row, L.ap_ptr,
+                                                                 L.ap_col, cnt, nullptr, nullptr, h->status);
+  note_launch();
+  rc = scan_total(h, cnt, C.a_ptr, na, &C.a_nnz, st);
+  if (rc) return rc;
+  C.a_col = h->alloc<int32_t>(C.a_nnz, st);
+  if (!C.a_col) return check_cuda("AMG coarse pattern");
+  k_union_rows<kMaxCRow, true><<<grid_for(na, kT), kT, 0, st>>>(na, nullptr, L.pt_ptr, L.pt_row, L.ap_ptr,
+                                                                L.ap_col, nullptr, C.a_ptr, C.a_col, h->status);
+  note_launch();
+  C.g = Graph{na, C.a_ptr, C.a_col};
+  return read_status(h, st, "AMG patterns");
+}
+
+template <int B0, int K>
+int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uint8_t* con, cudaStream_t st) {
+  const int64_t n0 = B->n_nod;
+  h->L[0].n = n0;
+  h->L[0].b = B0;
+  h->L[0].g = Graph{n0, B->nbr_ptr, B->nbr};
+  h->active = h->alloc<uint8_t>(n0, st);
+  h->status = h->alloc<int32_t>(1, st);
+  h->counter = h->alloc<unsigned long long>(1, st);
+  h->ctrl = h->alloc<AmgCtrl>(1, st);
+  h->lzc = h->alloc<AmgCtrl>(1, st);
+  h->lz = h->alloc<double>(2 * kLanczos + 2, st);
+  h->partial = h->alloc<double>(2 * kPartialLen, st);
+  double* origin = h->alloc<double>(3, st);
+  if (!h->active || !h->status || !h->counter || !h->ctrl || !h->lzc || !h->lz || !h->partial || !origin)
+    return check_cuda("AMG buffers");
+  cudaMemsetAsync(h->status, 0, sizeof(int32_t), st);
+  cudaMemsetAsync(h->ctrl, 0, sizeof(AmgCtrl), st);
+  cudaMemsetAsync(h->lzc, 0, sizeof(AmgCtrl), st);
+  k_centroid<<<1, 1024, 0, st>>>(n0, B0, coords, origin);
+  note_launch();
+  double* bn = nullptr;  // near-null rows of the current level (coarser levels)
+  int l = 0;
+  for (;; ++l) {
+    AmgLevel& L = h->L[l];
+    const int b = L.b;
+    if (l >= 1 && L.n * b <= kCoarseMaxDof) break;
+    if (l == kMaxLevels - 1) {
+      set_last_error("AMG: %d levels do not reach a coarsest level of at most %d unknowns", kMaxLevels,
+                     kCoarseMaxDof);
+      return FEM_INVALID;
+    }
+    int rc = aggregate(h, l, con, st);
+    if (rc) return rc;
+    if (L.n_agg == 0) {
+      set_last_error("AMG: no free degree of freedom to aggregate");
+      return FEM_INVALID;
+    }
+    if (l >= 1 && L.n_agg >= L.n) {
+      set_last_error("AMG: coarsening stalled at level %d (%lld block rows)", l, (long long)L.n);
+      return FEM_INVALID;
+    }
+    double* bc = h->alloc<double>(L.n_agg * K * K, st);
+    if (!bc) return check_cuda("AMG coarse near-null space");
+    if (l == 0) rc = tentative<B0, K>(h, l, coords, con, origin, nullptr, bc, st);
+    else rc = tentative<K, K>(h, l, nullptr, nullptr, origin, bn, bc, st);
+    if (rc) return rc;
+    rc = patterns(h, l, st);
+    if (rc) return rc;
+    bn = bc;
+  }
+  h->n_levels = l + 1;
+  // numeric storage and vectors
+  for (int k = 0; k < h->n_levels; ++k) {
+    AmgLevel& L = h->L[k];
+    const int64_t nv = L.n * L.b;
+    if (k + 1 < h->n_levels) {
+      L.p_val = h->alloc<float>(L.p_nnz * L.b * K, st);
+      L.ap_val = h->alloc<float>(L.ap_nnz * L.b * K, st);
+      if (!L.p_val || !L.ap_val) return check_cuda("AMG transfer storage");
+    }
+    if (k >= 1) {
+      L.a_val = h->alloc<float>(L.a_nnz * K * K, st);
+      L.dinv = h->alloc<float>(L.n * K * K, st);
+      L.f = h->alloc<float>(nv, st);
+      L.xb = h->alloc<float>(nv, st);
+      if (!L.a_val || !L.dinv || !L.f || !L.xb) return check_cuda("AMG level storage");
+    }
+    L.x = h->alloc<float>(nv, st);
+    L.r = h->alloc<float>(nv, st);
+    L.d = h->alloc<float>(nv, st);
+    L.db = h->alloc<float>(nv, st);
+    if (!L.x || !L.r || !L.d || !L.db) return check_cuda("AMG vectors");
+  }
+  const int64_t n = n0 * B0;
+  h->xlo = h->alloc<float>(n, st);
+  h->rcg = h->alloc<float>(n, st);
+  h->z = h->alloc<float>(n, st);
+  h->p = h->alloc<float>(n, st);
+  h->q = h->alloc<float>(n, st);
+  AmgLevel& C = h->L[h->n_levels - 1];
+  h->m_coarse = C.n * K;
+  h->coarse_inv = h->alloc<float>(h->m_coarse * h->m_coarse, st);
+  h->coarse_work = h->alloc<double>(2 * h->m_coarse * h->m_coarse, st);
+  if (!h->xlo || !h->rcg || !h->z || !h->p || !h->q || !h->coarse_inv || !h->coarse_work)
+    return check_cuda("AMG CG vectors");
+  h->L[0].f = h->rcg;
+  h->L[0].xb = h->z;
+  cudaMemsetAsync(h->p, 0, sizeof(float) * n, st);
+  return read_status(h, st, "AMG create");
+}
+
+// ---------------------------------------------------------------- numeric --
+template <int B>
+OpArgs level_args(fem_amg* h, int l, AmgCtrl* ctrl) {
+  AmgLevel& L = h->L[l];
+  OpArgs a{};
+  a.f = L.f;
+  a.x = L.x;
+  a.xb = L.xb;
+  a.r = L.r;
+  a.d = L.d;
+  a.db = L.db;
+  a.dinv = l == 0 ? h->dinv0 : L.dinv;
+  a.theta_inv = L.theta_inv;
+  a.c1 = L.c1;
+  a.c2 = L.c2;
+  a.partial = h->partial;
+  a.ctrl = ctrl;
+  a.lz = h->lz;
+  return a;
+}
+
+// One operator pass of level l in mode MODE (B: the level's block size).
+template <int B0, int K, int MODE>
+void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
+  AmgLevel& L = h->L[l];
+  if (l == 0) {
+    const int64_t ns = (L.n + 31) / 32;
+    k_sell_op<B0, MODE><<<capped(ns, 16), kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
+  } else {
+    k_csr_op<K, MODE><<<capped((L.n + 7) / 8, 8), 256, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
+  }
+  note_launch();
+}
+
+template <int B>
+int lanczos_level(fem_amg* h, int l, int b0, cudaStream_t st, double* rho) {
+  AmgLevel& L = h->L[l];
+  const int64_t n = L.n;
+  const float* dinv = l == 0 ? h->dinv0 : L.dinv;
+  // scratch: r -> L.r, z -> L.d, p -> L.db, q -> L.x
+  const unsigned g = capped(grid_for(n, kT), 8);
+  k_lz_init<B><<<g, kT, 0, st>>>(n, dinv, L.r, L.d, L.db, h->partial, h->lzc);
+  note_launch();
+  (void)b0;
+  OpArgs a{};
+  a.p = L.db;
+  a.q = L.x;
+  a.partial = h->partial;
+  a.ctrl = h->lzc;
+  a.lz = h->lz;
+  for (int j = 0; j < kLanczos; ++j) {
+    if (l == 0) {
+      const int64_t ns = (n + 31) / 32;
+      if (b0 == 3)
+        k_sell_op<3, kOpLzQ><<<capped(ns, 16), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val, a);
+      else
+        k_sell_op<2, kOpLzQ><<<capped(ns, 16), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val, a);
+    } else {
+      k_csr_op<B, kOpLzQ><<<capped((n + 7) / 8, 8), 256, 0, st>>>(n, L.a_ptr, L.a_col, L.a_val, a);
+    }
+    note_launch();
+    k_lz_update<B><<<g, kT, 0, st>>>(n, dinv, L.r, L.d, L.x, h->partial, h->lzc, h->lz);
+    note_launch();
+    k_pup<<<capped(grid_for(n * B, kT), 8), kT, 0, st>>>(n * B, L.d, L.db, h->lzc);
+    note_launch();
+  }
+  AmgCtrl hc;
+  double lzh[2 * kLanczos + 2];
+  if (cudaMemcpyAsync(&hc, h->lzc, sizeof(hc), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(lzh, h->lz, sizeof(lzh), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda("AMG Lanczos");
+  // steps whose alpha and beta are both known
+  const int k = std::min(hc.lz_step, kLanczos);
+  if (k < 1) {
+    set_last_error("AMG: the spectral estimate of level %d broke down", l);
+    return FEM_BREAKDOWN;
+  }
+  std::vector<double> da(k), ob(k > 1 ? k - 1 : 0);
+  for (int j = 0; j < k; ++j) {
+    const double al = lzh[2 * j], be_prev = j > 0 ? lzh[2 * (j - 1) + 1] : 0.0, al_prev = j > 0 ? lzh[2 * (j - 1)] : 1.0;
+    da[j] = 1.0 / al + (j > 0 ? be_prev / al_prev : 0.0);
+    if (j + 1 < k) ob[j] = sqrt(lzh[2 * j + 1]) / al;
+  }
+  *rho = tridiag_max_eig(da, ob);
+  if (!(*rho > 0.0) || !std::isfinite(*rho)) {
+    set_last_error("AMG: invalid spectral estimate %g at level %d", *rho, l);
+    return FEM_BREAKDOWN;
+  }
+  return FEM_OK;
+}
+
+template <int B0, int K>
+int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
+  h->sell_base = A->row_ptr;
+  h->sell_col = A->col;
+  h->sell_val = static_cast<const float*>(A->val);
+  h->dinv0 = static_cast<const float*>(A->precond);
+  cudaMemsetAsync(h->status, 0, sizeof(int32_t), st);
+  for (int l = 0; l + 1 < h->n_levels; ++l) {
+    AmgLevel& L = h->L[l];
+    AmgLevel& C = h->L[l + 1];
+    double rho = 0.0;
+    int rc = l == 0 ? lanczos_level<B0>(h, l, B0, st, &rho) : lanczos_level<K>(h, l, B0, st, &rho);
+    if (rc) return rc;
+    L.rho = rho;
+    const double lo = kChebLo * rho, hi = kChebHi * rho;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    const double rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
+    L.theta_inv = (float)(1.0 / theta);
+    L.c1 = (float)(rho1 * rho0);
+    L.c2 = (float)(2.0 * rho1 / delta);
+    const float omega = (float)(kOmega / rho);
+    if (l == 0) {
+      OpView<B0, true> Av{h->sell_base, h->sell_val};
+      k_p_numeric<B0, K, true><<<grid_for(L.n, 4), 128, 0, st>>>(L.g, Av, h->dinv0, L.agg, L.tval, L.p_ptr, L.p_col,
+                                                                 L.p_val, omega);
+      note_launch();
+      k_ap_numeric<B0, K, true><<<grid_for(L.n, 2), 64, 0, st>>>(L.g, Av, L.p_ptr, L.p_col, L.p_val, L.ap_ptr,
+                                                                 L.ap_col, L.ap_val);
+      note_launch();
+      k_ac_numeric<B0, K><<<grid_for(C.n, 2), 64, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.ap_ptr,
+                                                          L.ap_col, L.ap_val, C.a_ptr, C.a_col, C.a_val);
+      note_launch();
+    } else {
+      OpView<K, false> Av{L.a_ptr, L.a_val};
+      k_p_numeric<K, K, false><<<grid_for(L.n, 4), 128, 0, st>>>(L.g, Av, L.dinv, L.agg, L.tval, L.p_ptr, L.p_col,
+                                                                 L.p_val, omega);
+      note_launch();
+      k_ap_numeric<K, K, false><<<grid_for(L.n, 2), 64, 0, st>>>(L.g, Av, L.p_ptr, L.p_col, L.p_val, L.ap_ptr,
+                                                                 L.ap_col, L.ap_val);
+      note_launch();
+      k_ac_numeric<K, K><<<grid_for(C.n, 2), 64, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.ap_ptr,
+                                                         L.ap_col, L.ap_val, C.a_ptr, C.a_col, C.a_val);
+      note_launch();
+    }
+    k_block_inv<K><<<grid_for(C.n, kT), kT, 0, st>>>(C.n, C.a_ptr, C.a_col, C.a_val, C.dinv, h->status);
+    note_launch();
+    int rc2 = check_cuda("AMG setup");
+    if (rc2) return rc2;
+  }
+  AmgLevel& C = h->L[h->n_levels - 1];
+  k_coarse_inverse<<<1, 1024, 0, st>>>(C.n, K, C.a_ptr, C.a_col, C.a_val, h->coarse_work, h->coarse_inv, h->status);
+  note_launch();
+  int rc = read_status(h, st, "AMG setup");
+  if (rc) return rc;
+  h->ready = true;
+  return FEM_OK;
+}
+
+// ------------------------------------------------------------------ solve --
+template <int B0, int K>
+void launch_vcycle(fem_amg* h, cudaStream_t st) {
+  const int nl = h->n_levels;
+  for (int l = 0; l + 1 < nl; ++l) {
+    AmgLevel& L = h->L[l];
+    AmgLevel& C = h->L[l + 1];
+    const OpArgs a = level_args<B0>(h, l, h->ctrl);
+    launch_op<B0, K, kOpS1>(h, l, a, st);
+    launch_op<B0, K, kOpS2>(h, l, a, st);
+    if (l + 2 == nl) {
+      if (l == 0)
+        k_restrict_solve<B0, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r, h->coarse_inv,
+                                                    C.xb, h->ctrl);
+      else
+        k_restrict_solve<K, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r, h->coarse_inv,
+                                                   C.xb, h->ctrl);
+    } else {
+      const OpArgs c = level_args<K>(h, l + 1, h->ctrl);
+      if (l == 0)
+        k_restrict<B0, K><<<grid_for(C.n * 32, 256), 256, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r,
+                                                                   c, h->ctrl);
+      else
+        k_restrict<K, K><<<grid_for(C.n * 32, 256), 256, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r, c,
+                                                                  h->ctrl);
+    }
+    note_launch();
+  }
+  for (int l = nl - 2; l >= 0; --l) {
+    AmgLevel& L = h->L[l];
+    AmgLevel& C = h->L[l + 1];
+    if (l == 0)
+      k_prolong<B0, K><<<grid_for(L.n, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+    else
+      k_prolong<K, K><<<grid_for(L.n, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+    note_launch();
+    const OpArgs a = level_args<B0>(h, l, h->ctrl);
+    launch_op<B0, K, kOpS3>(h, l, a, st);
+    if (l == 0) launch_op<B0, K, kOpS4Dot>(h, l, a, st);
+    else launch_op<B0, K, kOpS4>(h, l, a, st);
+  }
+}
+
+template <int B0, int K>
+void launch_iteration(fem_amg* h, cudaStream_t st) {
+  const int64_t n = h->L[0].n * B0;
+  launch_vcycle<B0, K>(h, st);
+  k_pup<<<capped(grid_for(n, kT), 8), kT, 0, st>>>(n, h->z, h->p, h->ctrl);
+  note_launch();
+  OpArgs a{};
+  a.p = h->p;
+  a.q = h->q;
+  a.partial = h->partial;
+  a.ctrl = h->ctrl;
+  launch_op<B0, K, kOpQ>(h, 0, a, st);
+  k_cg_update<B0><<<capped(grid_for(h->L[0].n, kT), 8), kT, 0, st>>>(h->L[0].n, h->xlo, h->rcg, h->p, h->q, h->dinv0,
+                                                                      h->L[0].theta_inv, h->L[0].d, h->L[0].x,
+                                                                      h->partial, h->ctrl);
+  note_launch();
+}
+
+int read_ctrl(fem_amg* h, AmgCtrl* c, cudaStream_t st) {
+  if (cudaMemcpyAsync(c, h->ctrl, sizeof(AmgCtrl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return check_cuda("AMG CG");
+  return FEM_OK;
+}
+
+int status_code(int done) {
+  switch (done) {
+    case kConverged: return FEM_OK;
+    case kMaxIter: return FEM_NOT_CONVERGED;
+    case kNonFinite: return FEM_NONFINITE;
+    default: return FEM_BREAKDOWN;
+  }
+}
+
+int64_t op_fe_len(const fem_operator64* op) {
+  int ne, d, nip;
+  if (!op || etype_info(op->mesh->etype, &ne, &d, &nip) != FEM_OK) return -1;
+  return op->mesh->n_elem * ne * d;
+}
+
+template <int B0, int K>
+int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, double rtol, double delta,
+             int64_t max_iter, void* ws, fem_solve_info* info, cudaStream_t st) {
+  const int64_t nn = h->L[0].n, n = nn * B0;
+  AmgCtrl c;
+  memset(&c, 0, sizeof(c));
+  c.max_iter = max_iter;
+  c.mixed = op ? 1 : 0;
+  c.delta2 = delta * delta;
+  c.rscale = 1.0;
+  cudaMemcpyAsync(h->ctrl, &c, sizeof(c), cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(x, 0, sizeof(double) * n, st);
+  cudaMemsetAsync(h->xlo, 0, sizeof(float) * n, st);
+  cudaMemsetAsync(h->p, 0, sizeof(float) * n, st);
+  const unsigned gv = capped(grid_for(nn, kT), 8);
+  k_cg_bnorm<<<capped(grid_for(n, kT), 8), kT, 0, st>>>(n, b, rtol * rtol, h->partial, h->ctrl);
+  note_launch();
+  k_cg_init<B0><<<gv, kT, 0, st>>>(nn, b, h->rcg, h->dinv0, h->L[0].theta_inv, h->L[0].d, h->L[0].x, h->partial,
+                                   h->ctrl);
+  note_launch();
+  int rc = read_ctrl(h, &c, st);
+  if (rc) return rc;
+  double* y64 = nullptr;
+  double* fe = nullptr;
+  if (op) {
+    y64 = static_cast<double*>(ws);
+    fe = y64 + ((n + 31) & ~int64_t(31));
+  }
+  constexpr int kStall = 8;
+  double best = -1.0;
+  int stalled = 0;
+  int chunk = 2;
+  while (c.done == kRun) {
+    if (c.replace) {
+      k_cg_fold<<<grid_for(n, kT), kT, 0, st>>>(n, x, h->xlo, h->ctrl);
+      note_launch();
+      rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, fe, nullptr, nullptr,
+                             nullptr, st);
+      if (rc) return rc;
+      rc = fem_gather_nodal(op->mesh, fe, nullptr, op->con_mask, 2, x, y64, nullptr, nullptr, 0, st);
+      if (rc) return rc;
+      k_cg_replace<B0><<<gv, kT, 0, st>>>(nn, b, y64, h->rcg, h->dinv0, h->L[0].theta_inv, h->L[0].d, h->L[0].x,
+                                          h->partial, h->ctrl);
+      note_launch();
+      rc = read_ctrl(h, &c, st);
+      if (rc) return rc;
+      if (c.done == kRun) {
+        if (best < 0.0 || c.rr_true < 0.25 * best) {
+          best = c.rr_true;
+          stalled = 0;
+        } else if (++stalled >= kStall) {
+          set_last_error("multigrid CG stagnated at relative residual %.3e after %lld iterations: FP32 storage "
+                         "cannot refine this system; use precision fp64",
+                         c.bb > 0 ? sqrt(c.rr_true / c.bb) : 0.0, c.iters);
+          if (info) {
+            info->iterations = c.iters;
+            info->replacements = c.replacements;
+            info->rel_residual = c.bb > 0 ? sqrt(c.rr_true / c.bb) : 0.0;
+            info->status = FEM_NOT_CONVERGED;
+          }
+          return FEM_NOT_CONVERGED;
+        }
+      }
+      continue;
+    }
+    for (int k = 0; k < chunk; ++k) launch_iteration<B0, K>(h, st);
+    rc = check_cuda("AMG CG iteration");
+    if (rc) return rc;
+    rc = read_ctrl(h, &c, st);
+    if (rc) return rc;
+    chunk = std::min(chunk + 1, 4);
+  }
+  if (op) {
+    k_cg_fold<<<grid_for(n, kT), kT, 0, st>>>(n, x, h->xlo, h->ctrl);
+  } else {
+    k_cg_out<<<grid_for(n, kT), kT, 0, st>>>(n, h->xlo, x, h->ctrl);
+  }
+  note_launch();
+  rc = check_cuda("AMG CG finish");
+  if (rc) return rc;
+  const double rel = c.bb > 0 ? (op ? sqrt(c.rr_true / c.bb) : sqrt(c.rr / c.bb) / c.rscale) : 0.0;
+  if (info) {
+    info->iterations = c.iters;
+    info->replacements = c.replacements;
+    info->rel_residual = rel;
+    info->status = status_code(c.done);
+    info->spmv_ms = 0.0;
+    info->spmv_timed = 0;
+  }
+  if (c.done != kConverged)
+    set_last_error("multigrid CG did not converge: %lld iterations, relative residual %.3e, code %d", c.iters, rel,
+                   c.done);
+  return status_code(c.done);
+}
+
+}  // namespace
+}  // namespace tfg
+
+using namespace tfg;
+
+extern "C" {
+
+int fem_amg_create(const fem_blocks* B, const double* coords, const uint8_t* con_mask, fem_amg** out,
+                   void* stream) {
+  if (!B || !coords || !out || B->n_nod <= 0 || !(B->dim == 2 || B->dim == 3)) {
+    set_last_error("fem_amg_create: needs the node graph, coordinates and 2 or 3 DOFs per node");
+    return FEM_INVALID;
+  }
+  if (B->n_nod >= (int64_t)1 << 31) {
+    set_last_error("fem_amg_create: at most 2^31 - 1 nodes");
+    return FEM_BOUNDS;
+  }
+  cudaStream_t st = as_stream(stream);
+  fem_amg* h = new fem_amg();
+  h->dim = B->dim;
+  h->K = B->dim == 3 ? 6 : 3;
+  const int rc = B->dim == 3 ? create_impl<3, 6>(h, B, coords, con_mask, st) : create_impl<2, 3>(h, B, coords, con_mask, st);
+  if (rc) {
+    fem_amg_destroy(h);
+    *out = nullptr;
+    return rc;
+  }
+  *out = h;
+  return FEM_OK;
+}
+
+void fem_amg_destroy(fem_amg* h) {
+  if (!h) return;
+  for (void* p : h->mem) cudaFree(p);
+  delete h;
+}
+
+int fem_amg_setup(fem_amg* h, const fem_matrix* A, void* stream) {
+  if (!h || !A || A->format != FEM_FMT_SELL_F32 || A->block != h->dim || A->n_rows != h->L[0].n || !A->precond) {
+    set_last_error("fem_amg_setup: needs the FP32 sliced-block matrix (with its block-Jacobi inverse) of the "
+                   "mesh the hierarchy was built on");
+    return FEM_INVALID;
+  }
+  cudaStream_t st = as_stream(stream);
+  h->ready = false;
+  return h->dim == 3 ? setup_impl<3, 6>(h, A, st) : setup_impl<2, 3>(h, A, st);
+}
+
+size_t fem_amg_pcg_workspace_bytes(const fem_amg* h, const fem_operator64* op) {
+  if (!h) return 0;
+  if (!op) return 256;
+  const int64_t fl = op_fe_len(op);
+  if (fl < 0) return 0;
+  const int64_t n = h->L[0].n * h->dim;
+  return sizeof(double) * (size_t)(((n + 31) & ~int64_t(31)) + std::max<int64_t>(fl, 1)) + 256;
+}
+
+int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const double* b, double* x, double rtol,
+                double delta, int64_t max_iter, void* ws, size_t ws_bytes, fem_solve_info* info, void* stream) {
+  if (!h || !h->ready) {
+    set_last_error("fem_amg_pcg: the hierarchy has no numeric setup (call fem_amg_setup)");
+    return FEM_INVALID;
+  }
+  if (!A || A->row_ptr != h->sell_base || A->val != h->sell_val || A->precond != h->dinv0) {
+    set_last_error("fem_amg_pcg: the matrix differs from the one of the last fem_amg_setup");
+    return FEM_INVALID;
+  }
+  if (ws_bytes < fem_amg_pcg_workspace_bytes(h, op) || (op && !ws)) {
+    set_last_error("fem_amg_pcg: workspace too small");
+    return FEM_INVALID;
+  }
+  if (!(delta > 0.0 && delta < 1.0)) {
+    set_last_error("fem_amg_pcg: delta must lie in (0, 1)");
+    return FEM_INVALID;
+  }
+  cudaStream_t st = as_stream(stream);
+  return h->dim == 3 ? pcg_impl<3, 6>(h, op, b, x, rtol, delta, max_iter, ws, info, st)
+                     : pcg_impl<2, 3>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
+}
+
+int fem_amg_levels(const fem_amg* h) { return h ? h->n_levels : 0; }
+
+int fem_amg_level_info(const fem_amg* h, int level, fem_amg_level* out) {
+  if (!h || !out || level < 0 || level >= h->n_levels) {
+    set_last_error("fem_amg_level_info: no such level");
+    return FEM_INVALID;
+  }
+  const AmgLevel& L = h->L[level];
+  fem_amg_level o;
+  memset(&o, 0, sizeof(o));
+  o.n = L.n;
+  o.block = L.b;
+  o.a_nnz = L.a_nnz;
+  o.a_ptr = L.a_ptr;
+  o.a_col = L.a_col;
+  o.a_val = L.a_val;
+  o.n_agg = level + 1 < h->n_levels ? L.n_agg : 0;
+  o.agg = L.agg;
+  o.tval = L.tval;
+  o.p_nnz = L.p_nnz;
+  o.p_ptr = L.p_ptr;
+  o.p_col = L.p_col;
+  o.p_val = L.p_val;
+  o.rho = L.rho;
+  o.coarse_inv = level + 1 == h->n_levels ? h->coarse_inv : nullptr;
+  o.dropped = h->dropped;
+  *out = o;
+  return FEM_OK;
+}
+
+int fem_copy_device(void* dst, const void* src, size_t bytes, void* stream) {
+  if (bytes == 0) return FEM_OK;
+  if (!dst || !src) {
+    set_last_error("fem_copy_device: null pointer");
+    return FEM_INVALID;
+  }
+  if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, as_stream(stream)) != cudaSuccess)
+    return check_cuda("fem_copy_device");
+  return FEM_OK;
+}
+
+}  // extern "C"

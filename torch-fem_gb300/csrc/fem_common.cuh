@@ -62,6 +62,67 @@ __device__ __forceinline__ double block_sum(double v, double* smem32) {
   return t;
 }
 
+// True in every thread of the CTA that arrives last at `counter` (one
+// arrival per CTA); the caller resets the counter.
+__device__ __forceinline__ bool arrive_last(unsigned int* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  return last;
+}
+
+// Sum of partial[0..n)*stride+k in a fixed order (single CTA).
+__device__ __forceinline__ double sum_partials(const double* partial, int n, int stride, int k,
+                                               double* red) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(partial + (int64_t)i * stride + k);
+  return block_sum(s, red);
+}
+
+// L2 eviction-priority hints (PTX createpolicy / ld.L2::cache_hint): the part
+// of the matrix that should stay resident in L2 across CG iterations is read
+// evict_last, the streamed remainder evict_first.
+__device__ __forceinline__ uint64_t l2_policy(bool keep) {
+  uint64_t pol;
+  if (keep) asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  else asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ float ld_l2(const float* ptr, uint64_t pol) {
+  float v;
+  asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+__device__ __forceinline__ double ld_l2(const double* ptr, uint64_t pol) {
+  double v;
+  asm("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+__device__ __forceinline__ int32_t ld_l2(const int32_t* ptr, uint64_t pol) {
+  int32_t v;
+  asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+// Mixed precision keeps the residual it iterates on near unit norm: the FP32
+// vectors hold r * rscale with rscale a power of two (exact to apply and to
+// undo), so their dot products stay far from FP32 underflow and overflow at
+// any problem scale and any depth of refinement.
+__device__ __forceinline__ double unit_scale(double norm2) {
+  if (!(norm2 > 0.0) || !isfinite(norm2)) return 1.0;
+  int e;
+  frexp(norm2, &e);
+  return ldexp(1.0, -(e / 2));
+}
+
 }  // namespace tfg
 
 #define TFG_CHECK_LAUNCH(where)                      \

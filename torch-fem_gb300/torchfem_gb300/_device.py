@@ -41,9 +41,12 @@ class LinearSystem:
 
     precision "fp64": scalar CSR in the reference pattern, FP64 values,
     Jacobi preconditioner (the CuPy branch of sparse.py:406-421).
-    precision "mixed": FP32 block-CSR over the node graph, FP32 block-Jacobi,
-    with FP64 matrix-free residual replacement.
+    precision "mixed": FP32 block-CSR over the node graph, FP32 block-Jacobi
+    or smoothed-aggregation multigrid (`amg`), with FP64 matrix-free
+    residual replacement.
     """
+
+    _tokens = 0
 
     def __init__(self, dm: "DeviceMesh", precision: str):
         self.dm = dm
@@ -55,6 +58,54 @@ class LinearSystem:
         self.ws: Tensor | None = None
         self.stats = SolveStats()
         self._op_refs = None
+        self.amg: AmgHierarchy | None = None
+        self.amg_ws: Tensor | None = None
+        LinearSystem._tokens += 1
+        self.token = LinearSystem._tokens
+
+
+class AmgHierarchy:
+    """Smoothed-aggregation multigrid hierarchy of one mesh and constraint set
+    (the fem_amg handle): the GPU counterpart of the pyamg / AmgX
+    preconditioners of the reference (sparse.py:495-507, amgx.py).  The
+    symbolic part (aggregation, tentative prolongator from the rigid-body
+    modes of FEM.compute_B, every sparsity pattern) is built once; the
+    numeric part is redone for each matrix (`setup`)."""
+
+    def __init__(self, dm: "DeviceMesh", con_mask: Tensor):
+        self.lib = dm.lib
+        self.con_mask = con_mask.clone()
+        handle = C.c_void_p()
+        check(
+            dm.lib.fem_amg_create(C.byref(dm.blocks), ptr(dm.nodes), ptr(self.con_mask), C.byref(handle),
+                                  dm.stream),
+            "fem_amg_create",
+        )
+        self.handle = handle
+        self.current = 0  # token of the LinearSystem whose matrix is set up
+
+    def setup(self, sysm: LinearSystem, stream: int) -> None:
+        check(self.lib.fem_amg_setup(self.handle, C.byref(sysm.matrix), stream), "fem_amg_setup")
+        self.current = sysm.token
+
+    def levels(self) -> list[_lib.FemAmgLevel]:
+        out = []
+        for k in range(self.lib.fem_amg_levels(self.handle)):
+            info = _lib.FemAmgLevel()
+            check(self.lib.fem_amg_level_info(self.handle, k, C.byref(info)), "fem_amg_level_info")
+            out.append(info)
+        return out
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.fem_amg_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # interpreter shutdown: the library may be gone
+            pass
 
 
 class DeviceMesh:
@@ -325,8 +376,21 @@ class DeviceMesh:
         )
         return sval
 
-    def build_system(self, mesh, mat, con_mask: Tensor, precision: str, keep_refs=()) -> LinearSystem:
-        """Element stiffness, assembly and preconditioner for one tangent."""
+    def amg_hierarchy(self, con_mask: Tensor) -> AmgHierarchy:
+        """The multigrid hierarchy of this mesh for the constraint mask (built
+        once per mask: it depends on the mesh and the constraints only)."""
+        h = getattr(self, "_amg", None)
+        if h is None or h.con_mask.shape != con_mask.shape or not torch.equal(h.con_mask, con_mask):
+            if h is not None:
+                h.close()
+            h = AmgHierarchy(self, con_mask)
+            self._amg = h
+        return h
+
+    def build_system(self, mesh, mat, con_mask: Tensor, precision: str, keep_refs=(),
+                     precond: str = "jacobi") -> LinearSystem:
+        """Element stiffness, assembly and preconditioner for one tangent.
+        precond "amg" adds the multigrid hierarchy to a mixed system."""
         sysm = LinearSystem(self, precision)
         L, st = self.lib, self.stream
         if precision == "fp64":
@@ -363,6 +427,10 @@ class DeviceMesh:
             sysm.op_mat = mat
             sysm.op = _lib.FemOperator64(C.pointer(mesh), C.pointer(mat), ptr(con_mask))
             ws_bytes = L.fem_pcg_mixed_workspace_bytes(C.byref(sysm.matrix), C.byref(sysm.op))
+            if precond == "amg":
+                sysm.amg = self.amg_hierarchy(con_mask)
+                sysm.amg.setup(sysm, st)
+                sysm.amg_ws = self._ws(L.fem_amg_pcg_workspace_bytes(sysm.amg.handle, C.byref(sysm.op)))
         else:
             raise ValueError(f"unknown precision {precision!r}")
         sysm.con_mask = con_mask
@@ -396,7 +464,15 @@ class DeviceMesh:
                 raise RuntimeError(f"minres failed with exit code {info.iterations}")
             check(rc, "linear solve")
             return x
-        if sysm.precision == "fp64" or not refine:
+        if sysm.amg is not None:
+            if sysm.amg.current != sysm.token:
+                sysm.amg.setup(sysm, self.stream)
+            op = C.byref(sysm.op) if refine else None
+            rc = self.lib.fem_amg_pcg(
+                sysm.amg.handle, C.byref(sysm.matrix), op, ptr(b), ptr(x), rtol, delta, max_iter,
+                ptr(sysm.amg_ws), sysm.amg_ws.numel(), C.byref(info), self.stream,
+            )
+        elif sysm.precision == "fp64" or not refine:
             rc = self.lib.fem_pcg(
                 C.byref(sysm.matrix), ptr(b), ptr(x), rtol, max_iter, ptr(sysm.ws), sysm.ws.numel(),
                 C.byref(info), self.stream,

@@ -116,8 +116,41 @@ class FemOperator64(C.Structure):
     ]
 
 
+class FemAmgLevel(C.Structure):
+    _fields_ = [
+        ("n", i64),
+        ("block", C.c_int),
+        ("a_nnz", i64),
+        ("a_ptr", vp),
+        ("a_col", vp),
+        ("a_val", vp),
+        ("n_agg", i64),
+        ("agg", vp),
+        ("tval", vp),
+        ("p_nnz", i64),
+        ("p_ptr", vp),
+        ("p_col", vp),
+        ("p_val", vp),
+        ("rho", C.c_double),
+        ("coarse_inv", vp),
+        ("dropped", i64),
+    ]
+
+
 _P = C.POINTER
 _SIGNATURES = {
+    "fem_amg_create": (C.c_int, [_P(FemBlocks), vp, vp, _P(vp), vp]),
+    "fem_amg_setup": (C.c_int, [vp, _P(FemMatrix), vp]),
+    "fem_amg_pcg_workspace_bytes": (C.c_size_t, [vp, _P(FemOperator64)]),
+    "fem_amg_pcg": (
+        C.c_int,
+        [vp, _P(FemMatrix), _P(FemOperator64), vp, vp, C.c_double, C.c_double, i64, vp, C.c_size_t,
+         _P(FemSolveInfo), vp],
+    ),
+    "fem_amg_destroy": (None, [vp]),
+    "fem_amg_levels": (C.c_int, [vp]),
+    "fem_amg_level_info": (C.c_int, [vp, C.c_int, _P(FemAmgLevel)]),
+    "fem_copy_device": (C.c_int, [vp, vp, C.c_size_t, vp]),
     "fem_diag_workspace_bytes": (C.c_size_t, []),
     "fem_diag_barrier_timeout": (C.c_int, [vp, C.c_size_t, C.c_longlong, vp]),
     "fem_minres_workspace_bytes": (C.c_size_t, [_P(FemMatrix)]),

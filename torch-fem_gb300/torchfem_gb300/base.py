@@ -21,6 +21,24 @@ from .sparse import IntegrateMaterial, NewtonLinear, SolveContext
 
 _REFERENCE_METHODS = ("spsolve", "minres", "cg", "pardiso", "amgx")
 _GPU_METHODS = {None: "fp64", "cg": "fp64", "gb300": "fp64", "gb300-mixed": "mixed"}
+_PRECONDITIONERS = ("jacobi", "amg")
+
+
+def resolve_preconditioner(preconditioner: str | None, precision: str, n_dof_per_node: int) -> str:
+    """'jacobi' (block Jacobi in mixed precision, Jacobi in FP64) or 'amg'
+    (smoothed-aggregation multigrid, the counterpart of the reference's
+    pyamg / AmgX preconditioners; mixed precision, 2 or 3 DOFs per node).
+    None picks the default: TORCHFEM_GB300_PRECOND if set, else 'jacobi'."""
+    import os
+
+    p = preconditioner if preconditioner is not None else os.environ.get("TORCHFEM_GB300_PRECOND", "jacobi")
+    if p not in _PRECONDITIONERS:
+        raise ValueError(f"preconditioner must be one of {_PRECONDITIONERS}")
+    if p == "amg" and (precision != "mixed" or n_dof_per_node not in (2, 3)):
+        if preconditioner is not None:
+            raise ValueError("the multigrid preconditioner runs with precision 'mixed' on 2 or 3 DOFs per node")
+        p = "jacobi"
+    return p
 
 
 def resolve_precision(method: str | None, precision: str | None) -> str:
@@ -163,17 +181,21 @@ class FEM:
         differentiable_parameters: Tensor | Iterable[Tensor] | None = None,
         precision: str | None = None,
         cg_max_iter: int | None = None,
+        preconditioner: str | None = None,
     ) -> tuple[Tensor, Tensor, Tensor, Tensor, Tensor]:
         """Quasi-static solve by load increments (base.py:597-923).
 
         Same arguments and results as the reference.  `method` selects the
         GPU solver ("cg"/None: FP64 Jacobi-CG; "gb300-mixed": FP32 CG with
-        FP64 residual replacement) and `precision` may override it.  `stol` is
+        FP64 residual replacement) and `precision` may override it;
+        `preconditioner` ("jacobi" or "amg", see resolve_preconditioner) picks
+        the mixed-precision preconditioner.  `stol` is
         the relative residual of each linear solve.  `verbose` prints the
         Newton residuals and CG iteration counts.  `use_cached_solve` is
         accepted; the CG always starts from zero.
         """
         prec = resolve_precision(method, precision)
+        pc = resolve_preconditioner(preconditioner, prec, self.n_dof_per_node)
         if device is not None and torch.device(device).type != "cuda":
             raise RuntimeError("torchfem_gb300 solves on a CUDA device only")
         if alpha > 0.0:
@@ -225,6 +247,7 @@ class FEM:
             sc = SolveContext(dm, con_mask, mat_kind, prec, max_iter, rtol, atol, stol, cg_max_iter)
         sc.verbose = verbose
         sc.linear = "minres" if method == "minres" else "cg"
+        sc.precond = pc
         self.last_solve = sc
 
         shape_ip = (dm.nip, self.n_elem, *self.n_flux)

@@ -50,6 +50,10 @@ class SolveContext:
         self.verbose = False
         self.inner_rtol = 1e-6
         self.linear = "cg"  # or "minres" (FP64 path)
+        self.precond = "jacobi"  # or "amg" (mixed precision)
+        # FP64 replacement threshold of the multigrid CG: each V-cycle cuts the
+        # residual severalfold, so replacements are spaced by a deeper drop
+        self.amg_delta = 1e-4
 
     def structs(self, mat_data: Tensor, thickness: Tensor | None):
         from . import _lib
@@ -65,7 +69,8 @@ class SolveContext:
         if self.system is None or self.system_key != key:
             mesh, mat = self.structs(mat_data, thickness)
             self.system = self.dm.build_system(
-                mesh, mat, self.con_mask, self.precision, keep_refs=(mat_data, thickness, mesh, mat)
+                mesh, mat, self.con_mask, self.precision, keep_refs=(mat_data, thickness, mesh, mat),
+                precond=self.precond if self.precision == "mixed" else "jacobi",
             )
             self.system_key = key
         return self.system
@@ -78,13 +83,14 @@ class SolveContext:
         mixed precision the FP32 CG runs alone, the Newton iteration being its
         refinement.  Adjoint and linear-material solves use stol."""
         assert self.system is not None
+        delta = self.amg_delta if self.system.amg is not None else self.delta
         if inner and self.precision == "mixed":
             x = self.dm.solve(self.system, b, max(self.stol, self.inner_rtol), self.cg_max_iter, refine=False)
         elif inner:
-            x = self.dm.solve(self.system, b, max(self.stol, self.inner_rtol), self.cg_max_iter, self.delta,
+            x = self.dm.solve(self.system, b, max(self.stol, self.inner_rtol), self.cg_max_iter, delta,
                               linear=self.linear)
         else:
-            x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, self.delta, linear=self.linear)
+            x = self.dm.solve(self.system, b, self.stol, self.cg_max_iter, delta, linear=self.linear)
         self.iterations.append(self.system.stats.iterations)
         return x
 
