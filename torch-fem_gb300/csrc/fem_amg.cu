@@ -973,42 +973,93 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   }
 }
 
-// Coarser levels: block CSR (B x B blocks), warp per row; lane (u, r) takes
-// row r of every (32 / B)-th block.  Coarse operators are read evict_last so
-// they stay in L2 across the cycle.
+// Coarser levels: block CSR (B x B blocks), one warp per row; lane (u, r)
+// takes row r of every (32 / B)-th block, four blocks' loads in flight.
+// The epilogue runs on lanes r < B, one component each.  Coarse operators
+// are read evict_last so they stay in L2 across the cycle.
+template <int B, int MODE>
+__device__ __forceinline__ double csr_row(int64_t i, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                          const float* __restrict__ val, const OpArgs& a, uint64_t pol) {
+  constexpr int PB = 32 / B;
+  constexpr int U = 4;
+  const float* __restrict__ v = op_operand<MODE>(a);
+  const int lane = threadIdx.x & 31;
+  const int u = lane / B, r = lane % B;
+  float y = 0.f;
+  if (u < PB) {
+    const int64_t e1 = ptr[i + 1];
+    for (int64_t e = ptr[i] + u; e < e1; e += U * PB) {
+      int64_t c[U];
+#pragma unroll
+      for (int t = 0; t < U; ++t) c[t] = e + t * PB < e1 ? (int64_t)ld_l2(col + e + t * PB, pol) : -1;
+#pragma unroll
+      for (int t = 0; t < U; ++t) {
+        if (c[t] < 0) continue;
+        const float* m = val + (e + t * PB) * B * B + r * B;
+        const float* xv = v + c[t] * B;
+#pragma unroll
+        for (int q = 0; q < B; ++q) y = fmaf(ld_l2(m + q, pol), xv[q], y);
+      }
+    }
+  }
+  float yr = 0.f;
+#pragma unroll
+  for (int t = 0; t < PB; ++t) yr += __shfl_sync(0xffffffffu, y, r + t * B);
+  // lane r (< B) now holds component r of (A v)_i
+  const int64_t o = i * B + r;
+  const bool own = lane < B;
+  float rn = 0.f;
+  if constexpr (MODE == kOpS1 || MODE == kOpS3) rn = own ? a.f[o] - yr : 0.f;
+  else if constexpr (MODE == kOpS4 || MODE == kOpS4Dot) rn = own ? a.r[o] - yr : 0.f;
+  float t = 0.f;
+  if constexpr (MODE == kOpS1 || MODE == kOpS3 || MODE == kOpS4 || MODE == kOpS4Dot) {
+    const float* m = a.dinv + (i * B + r) * B;
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      const float rq = __shfl_sync(0xffffffffu, rn, q);
+      if (own) t = fmaf(m[q], rq, t);
+    }
+  }
+  double dot = 0.0;
+  if (own) {
+    if constexpr (MODE == kOpS1) {
+      const float dn = a.c1 * a.d[o] + a.c2 * t;
+      a.r[o] = rn;
+      a.db[o] = dn;
+      a.x[o] += dn;
+    } else if constexpr (MODE == kOpS2) {
+      a.r[o] -= yr;
+    } else if constexpr (MODE == kOpS3) {
+      const float dn = a.theta_inv * t;
+      a.r[o] = rn;
+      a.d[o] = dn;
+      a.xb[o] = a.x[o] + dn;
+    } else if constexpr (MODE == kOpS4 || MODE == kOpS4Dot) {
+      const float z = a.xb[o] + (a.c1 * a.d[o] + a.c2 * t);
+      a.xb[o] = z;
+      if constexpr (MODE == kOpS4Dot) dot = (double)a.f[o] * (double)z;
+    } else {
+      a.q[o] = yr;
+      dot = (double)a.p[o] * (double)yr;
+    }
+  }
+  if constexpr (op_has_dot<MODE>()) dot = warp_sum(dot);
+  return dot;
+}
+
 template <int B, int MODE>
 __global__ void __launch_bounds__(256) k_csr_op(int64_t n, const int64_t* __restrict__ ptr,
                                                 const int32_t* __restrict__ col, const float* __restrict__ val,
                                                 OpArgs a) {
-  constexpr int PB = 32 / B;
   __shared__ double red[32];
   if (amg_idle(a.ctrl)) return;
-  const float* __restrict__ v = op_operand<MODE>(a);
-  const int lane = threadIdx.x & 31;
-  const int u = lane / B, r = lane % B;
   const uint64_t pol = l2_policy(true);
   double dot = 0.0;
   const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw) {
-    float y = 0.f;
-    if (u < PB)
-      for (int64_t e = ptr[i] + u; e < ptr[i + 1]; e += PB) {
-        const int64_t c = ld_l2(col + e, pol);
-        const float* m = val + e * B * B + r * B;
-        const float* xv = v + c * B;
-#pragma unroll
-        for (int q = 0; q < B; ++q) y = fmaf(ld_l2(m + q, pol), xv[q], y);
-      }
-    float yt = 0.f;
-#pragma unroll
-    for (int t = 0; t < PB; ++t) yt += __shfl_sync(0xffffffffu, y, r + t * B);
-    float ys[B];
-#pragma unroll
-    for (int c = 0; c < B; ++c) ys[c] = __shfl_sync(0xffffffffu, yt, c);
-    if (lane == 0) dot += op_epilogue<B, MODE>(a, i, ys);
-  }
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw)
+    dot += csr_row<B, MODE>(i, ptr, col, val, a, pol);
   if constexpr (op_has_dot<MODE>()) {
-    const double bsum = block_sum(dot, red);
+    const double bsum = block_sum((threadIdx.x & 31) == 0 ? dot : 0.0, red);
     if (threadIdx.x == 0) a.partial[blockIdx.x] = bsum;
     if (arrive_last(&a.ctrl->counter)) {
       const double tot = sum_partials(a.partial, gridDim.x, 1, 0, red);
@@ -1020,24 +1071,23 @@ __global__ void __launch_bounds__(256) k_csr_op(int64_t n, const int64_t* __rest
   }
 }
 
-// Restriction f_c = P^T r, warp per coarse row, followed by the first
-// Chebyshev step of the coarse level: d = D^-1 f / theta, x = d.
-template <int BF, int K>
-__global__ void __launch_bounds__(256) k_restrict(int64_t n_c, const int64_t* __restrict__ pt_ptr,
-                                                  const int32_t* __restrict__ pt_row,
-                                                  const int64_t* __restrict__ pt_pos, const float* __restrict__ p_val,
-                                                  const float* __restrict__ rf, OpArgs c, const AmgCtrl* ctrl) {
-  if (amg_idle(ctrl)) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (I >= n_c) return;
+// Restriction f_c = P^T r of coarse row I by the threads of one CTA (P^T
+// values in transposed order, pt_val, so consecutive threads read
+// consecutive blocks), fixed-order reduction, then the first Chebyshev step
+// of the coarse level: d = D^-1 f / theta, x = d (the coarsest level, whose
+// OpArgs carry no dinv, only takes f).
+template <int BF, int K, int NT>
+__device__ __forceinline__ void restrict_row(int64_t I, const int64_t* __restrict__ pt_ptr,
+                                             const int32_t* __restrict__ pt_row, const float* __restrict__ pt_val,
+                                             const float* __restrict__ rf, float (&red)[NT / 32][K], float* fout) {
+  const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) % (NT / 32);
+  const int tid = threadIdx.x % NT;
   float acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = 0.f;
-  for (int64_t e = pt_ptr[I] + lane; e < pt_ptr[I + 1]; e += 32) {
+  for (int64_t e = pt_ptr[I] + tid; e < pt_ptr[I + 1]; e += NT) {
     const int64_t i = pt_row[e];
-    if (pt_pos[e] < 0) continue;
-    const float* pv = p_val + pt_pos[e] * BF * K;
+    const float* pv = pt_val + e * BF * K;
 #pragma unroll
     for (int q = 0; q < BF; ++q) {
       const float rv = rf[i * BF + q];
@@ -1047,89 +1097,209 @@ __global__ void __launch_bounds__(256) k_restrict(int64_t n_c, const int64_t* __
   }
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
-  if (lane < K) {
-    const float* m = c.dinv + (I * K + lane) * K;
-    float t = 0.f;
+  if (lane == 0)
 #pragma unroll
-    for (int q = 0; q < K; ++q) t = fmaf(m[q], acc[q], t);
-    const float dn = c.theta_inv * t;
-    float fv = 0.f;
+    for (int k = 0; k < K; ++k) red[w][k] = acc[k];
+  __syncthreads();
+  if (tid < K) {
+    float s = 0.f;
 #pragma unroll
-    for (int q = 0; q < K; ++q) fv = q == lane ? acc[q] : fv;
-    c.f[I * K + lane] = fv;
-    c.d[I * K + lane] = dn;
-    c.x[I * K + lane] = dn;
-  }
-}
-
-// Restriction onto the coarsest level and its dense solve, one CTA.
-template <int BF, int K>
-__global__ void __launch_bounds__(1024) k_restrict_solve(int64_t n_c, const int64_t* __restrict__ pt_ptr,
-                                                         const int32_t* __restrict__ pt_row,
-                                                         const int64_t* __restrict__ pt_pos,
-                                                         const float* __restrict__ p_val, const float* __restrict__ rf,
-                                                         const float* __restrict__ inv, float* __restrict__ xc,
-                                                         const AmgCtrl* ctrl) {
-  __shared__ float fs[kCoarseMaxDof];
-  if (amg_idle(ctrl)) return;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int64_t I = w; I < n_c; I += blockDim.x >> 5) {
-    float acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.f;
-    for (int64_t e = pt_ptr[I] + lane; e < pt_ptr[I + 1]; e += 32) {
-      const int64_t i = pt_row[e];
-      if (pt_pos[e] < 0) continue;
-      const float* pv = p_val + pt_pos[e] * BF * K;
-#pragma unroll
-      for (int q = 0; q < BF; ++q) {
-        const float rv = rf[i * BF + q];
-#pragma unroll
-        for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
-    if (lane == 0)
-#pragma unroll
-      for (int k = 0; k < K; ++k) fs[I * K + k] = acc[k];
+    for (int u = 0; u < NT / 32; ++u) s += red[u][tid];
+    fout[tid] = s;
   }
   __syncthreads();
-  const int m = (int)(n_c * K);
-  for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    float s = 0.f;
-    for (int j = 0; j < m; ++j) s = fmaf(inv[(int64_t)t * m + j], fs[j], s);
-    xc[t] = s;
+}
+
+template <int BF, int K>
+__global__ void __launch_bounds__(128) k_restrict(int64_t n_c, const int64_t* __restrict__ pt_ptr,
+                                                  const int32_t* __restrict__ pt_row, const float* __restrict__ pt_val,
+                                                  const float* __restrict__ rf, OpArgs c, const AmgCtrl* ctrl) {
+  __shared__ float red[4][K];
+  __shared__ float fs[K];
+  if (amg_idle(ctrl)) return;
+  for (int64_t I = blockIdx.x; I < n_c; I += gridDim.x) {
+    restrict_row<BF, K, 128>(I, pt_ptr, pt_row, pt_val, rf, red, fs);
+    if (threadIdx.x < K && !c.dinv) {
+      c.f[I * K + threadIdx.x] = fs[threadIdx.x];  // the coarsest level: right-hand side only
+    } else if (threadIdx.x < K) {
+      const int k = threadIdx.x;
+      const float* m = c.dinv + (I * K + k) * K;
+      float t = 0.f;
+#pragma unroll
+      for (int q = 0; q < K; ++q) t = fmaf(m[q], fs[q], t);
+      const float dn = c.theta_inv * t;
+      c.f[I * K + k] = fs[k];
+      c.d[I * K + k] = dn;
+      c.x[I * K + k] = dn;
+    }
   }
 }
 
-// Prolongation x += P x_c, thread per fine row.
+// Prolongation x += P x_c, one warp per fine row: the lanes read the row's
+// P blocks as one contiguous run of values (coalesced) and the B partial
+// sums are reduced across the warp.
+template <int BF, int K>
+__device__ __forceinline__ void prolong_row(int64_t i, const int64_t* __restrict__ p_ptr,
+                                            const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
+                                            const float* __restrict__ xc, float* __restrict__ x) {
+  constexpr int BK = BF * K;
+  const int lane = threadIdx.x & 31;
+  const int64_t e0 = p_ptr[i];
+  const int nv = (int)(p_ptr[i + 1] - e0) * BK;
+  if (nv == 0) return;
+  float part[BF];
+#pragma unroll
+  for (int q = 0; q < BF; ++q) part[q] = 0.f;
+  const float* pv = p_val + e0 * BK;
+  for (int v = lane; v < nv; v += 32) {
+    const int e = v / BK, rem = v - e * BK;
+    const int r = rem / K, k = rem - r * K;
+    const float t = pv[v] * xc[(int64_t)p_col[e0 + e] * K + k];
+#pragma unroll
+    for (int q = 0; q < BF; ++q)
+      if (q == r) part[q] += t;
+  }
+#pragma unroll
+  for (int q = 0; q < BF; ++q) part[q] = warp_sum(part[q]);
+  if (lane < BF) {
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < BF; ++q) s = q == lane ? part[q] : s;
+    x[i * BF + lane] += s;
+  }
+}
+
 template <int BF, int K>
 __global__ void __launch_bounds__(256) k_prolong(int64_t n, const int64_t* __restrict__ p_ptr,
                                                  const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
                                                  const float* __restrict__ xc, float* __restrict__ x,
                                                  const AmgCtrl* ctrl) {
   if (amg_idle(ctrl)) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int64_t e0 = p_ptr[i], e1 = p_ptr[i + 1];
-  if (e0 == e1) return;
-  float acc[BF];
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw)
+    prolong_row<BF, K>(i, p_ptr, p_col, p_val, xc, x);
+}
+
+// P^T values in transposed order: block e of P^T is block pt_pos[e] of P.
+__global__ void k_transpose_vals(int64_t n_e, int bk, const int64_t* __restrict__ pt_pos,
+                                 const float* __restrict__ p_val, float* __restrict__ pt_val) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_e * bk) return;
+  const int64_t e = t / bk;
+  const int c = (int)(t - e * bk);
+  const int64_t pos = pt_pos[e];
+  pt_val[t] = pos >= 0 ? p_val[pos * bk + c] : 0.f;
+}
+
+// --------------------------------------------------------- tail cycle ----
+// The small coarse levels (operator at most kTailBytes) run their whole
+// V-cycle inside one CTA: each phase is a loop over the level's rows by the
+// CTA's warps, phases separated by __syncthreads(), one launch instead of
+// six latency-bound ones per level.
+constexpr int64_t kTailBytes = 1 << 20;
+constexpr int kTailThreads = 1024;
+
+struct TailLevel {
+  int64_t n;
+  const int64_t* a_ptr;
+  const int32_t* a_col;
+  const float* a_val;
+  OpArgs args;  // f, x, xb, r, d, db, dinv, Chebyshev coefficients of the level
+  // transfer to the next level (absent on the coarsest)
+  int64_t n_c;
+  const int64_t* pt_ptr;
+  const int32_t* pt_row;
+  const float* pt_val;
+  const int64_t* p_ptr;
+  const int32_t* p_col;
+  const float* p_val;
+};
+
+struct TailParams {
+  int first, last;  // levels first .. last, last the coarsest
+  TailLevel lv[kMaxLevels];
+  const float* coarse_inv;
+  const AmgCtrl* ctrl;
+};
+
+template <int K, int MODE>
+__device__ __forceinline__ void tail_op(const TailLevel& L, uint64_t pol) {
+  const int nw = kTailThreads / 32;
+  for (int64_t i = threadIdx.x >> 5; i < L.n; i += nw) (void)csr_row<K, MODE>(i, L.a_ptr, L.a_col, L.a_val, L.args, pol);
+  __syncthreads();
+}
+
+template <int K>
+__global__ void __launch_bounds__(kTailThreads) k_tail(TailParams P) {
+  if (amg_idle(P.ctrl)) return;
+  const uint64_t pol = l2_policy(true);
+  const int nw = kTailThreads / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int l = P.first; l < P.last; ++l) {
+    const TailLevel& L = P.lv[l];
+    tail_op<K, kOpS1>(L, pol);
+    tail_op<K, kOpS2>(L, pol);
+    const TailLevel& C = P.lv[l + 1];
+    // restriction: warp per coarse row, reading P^T in transposed order
+    for (int64_t I = w; I < L.n_c; I += nw) {
+      float acc[K];
 #pragma unroll
-  for (int q = 0; q < BF; ++q) acc[q] = 0.f;
-  for (int64_t e = e0; e < e1; ++e) {
-    const float* pv = p_val + e * BF * K;
-    const float* cv = xc + (int64_t)p_col[e] * K;
-    float cx[K];
+      for (int k = 0; k < K; ++k) acc[k] = 0.f;
+      for (int64_t e = L.pt_ptr[I] + lane; e < L.pt_ptr[I + 1]; e += 32) {
+        const int64_t i = L.pt_row[e];
+        const float* pv = L.pt_val + e * K * K;
 #pragma unroll
-    for (int k = 0; k < K; ++k) cx[k] = cv[k];
+        for (int q = 0; q < K; ++q) {
+          const float rv = L.args.r[i * K + q];
 #pragma unroll
-    for (int q = 0; q < BF; ++q)
+          for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
+        }
+      }
 #pragma unroll
-      for (int k = 0; k < K; ++k) acc[q] = fmaf(pv[q * K + k], cx[k], acc[q]);
+      for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+      if (l + 1 == P.last) {
+        if (lane < K) {
+          float fv = 0.f;
+#pragma unroll
+          for (int q = 0; q < K; ++q) fv = q == lane ? acc[q] : fv;
+          C.args.f[I * K + lane] = fv;
+        }
+      } else if (lane < K) {
+        const float* m = C.args.dinv + (I * K + lane) * K;
+        float t = 0.f, fv = 0.f;
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+          t = fmaf(m[q], acc[q], t);
+          fv = q == lane ? acc[q] : fv;
+        }
+        const float dn = C.args.theta_inv * t;
+        C.args.f[I * K + lane] = fv;
+        C.args.d[I * K + lane] = dn;
+        C.args.x[I * K + lane] = dn;
+      }
+    }
+    __syncthreads();
   }
-#pragma unroll
-  for (int q = 0; q < BF; ++q) x[i * BF + q] += acc[q];
+  // coarsest: dense solve of the restricted residual (written by the loop
+  // above or, when the tail is the coarsest level alone, by k_restrict)
+  {
+    const TailLevel& C = P.lv[P.last];
+    const int m = (int)(C.n * K);
+    for (int t = threadIdx.x; t < m; t += kTailThreads) {
+      float s = 0.f;
+      for (int j = 0; j < m; ++j) s = fmaf(P.coarse_inv[(int64_t)t * m + j], C.args.f[j], s);
+      C.args.xb[t] = s;
+    }
+    __syncthreads();
+  }
+  for (int l = P.last - 1; l >= P.first; --l) {
+    const TailLevel& L = P.lv[l];
+    const TailLevel& C = P.lv[l + 1];
+    for (int64_t i = w; i < L.n; i += nw) prolong_row<K, K>(i, L.p_ptr, L.p_col, L.p_val, C.args.xb, L.args.x);
+    __syncthreads();
+    tail_op<K, kOpS3>(L, pol);
+    tail_op<K, kOpS4>(L, pol);
+  }
 }
 
 // ---------------------------------------------------------------- CG ------
@@ -1470,6 +1640,7 @@ struct AmgLevel {
   int64_t* pt_ptr = nullptr;
   int32_t* pt_row = nullptr;
   int64_t* pt_pos = nullptr;
+  float* pt_val = nullptr;  // P values in transposed order (restriction)
   int64_t* ap_ptr = nullptr;
   int32_t* ap_col = nullptr;
   float* ap_val = nullptr;
@@ -1489,6 +1660,8 @@ struct fem_amg {
   float* coarse_inv = nullptr;
   double* coarse_work = nullptr;
   int64_t m_coarse = 0;
+  int tail_first = 0;  // first level of the single-CTA tail cycle
+  tfg::TailParams tail{};
   uint8_t* active = nullptr;  // level 0: nodes with a free DOF
   // CG state
   float *xlo = nullptr, *rcg = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
@@ -1780,8 +1953,9 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
     const int64_t nv = L.n * L.b;
     if (k + 1 < h->n_levels) {
       L.p_val = h->alloc<float>(L.p_nnz * L.b * K, st);
+      L.pt_val = h->alloc<float>(L.p_nnz * L.b * K, st);
       L.ap_val = h->alloc<float>(L.ap_nnz * L.b * K, st);
-      if (!L.p_val || !L.ap_val) return check_cuda("AMG transfer storage");
+      if (!L.p_val || !L.pt_val || !L.ap_val) return check_cuda("AMG transfer storage");
     }
     if (k >= 1) {
       L.a_val = h->alloc<float>(L.a_nnz * K * K, st);
@@ -1811,6 +1985,13 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
   h->L[0].f = h->rcg;
   h->L[0].xb = h->z;
   cudaMemsetAsync(h->p, 0, sizeof(float) * n, st);
+  // the tail: the trailing levels >= 1 whose operators are small enough for
+  // one CTA (the coarsest level alone when there are none)
+  const int last = h->n_levels - 1;
+  h->tail_first = last;
+  while (h->tail_first - 1 >= 1 &&
+         h->L[h->tail_first - 1].a_nnz * K * K * (int64_t)sizeof(float) <= kTailBytes)
+    --h->tail_first;
   return read_status(h, st, "AMG create");
 }
 
@@ -1950,6 +2131,9 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
                                                          L.ap_col, L.ap_val, C.a_ptr, C.a_col, C.a_val);
       note_launch();
     }
+    k_transpose_vals<<<grid_for(L.p_nnz * L.b * K, kT), kT, 0, st>>>(L.p_nnz, L.b * K, L.pt_pos, L.p_val,
+                                                                     L.pt_val);
+    note_launch();
     k_block_inv<K><<<grid_for(C.n, kT), kT, 0, st>>>(C.n, C.a_ptr, C.a_col, C.a_val, C.dinv, h->status);
     note_launch();
     int rc2 = check_cuda("AMG setup");
@@ -1960,6 +2144,27 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
   note_launch();
   int rc = read_status(h, st, "AMG setup");
   if (rc) return rc;
+  TailParams& T = h->tail;
+  T.first = h->tail_first;
+  T.last = h->n_levels - 1;
+  T.coarse_inv = h->coarse_inv;
+  T.ctrl = h->ctrl;
+  for (int l = T.first; l <= T.last; ++l) {
+    const AmgLevel& L = h->L[l];
+    TailLevel& t = T.lv[l];
+    t.n = L.n;
+    t.a_ptr = L.a_ptr;
+    t.a_col = L.a_col;
+    t.a_val = L.a_val;
+    t.args = level_args<K>(h, l, h->ctrl);
+    t.n_c = l < T.last ? L.n_agg : 0;
+    t.pt_ptr = L.pt_ptr;
+    t.pt_row = L.pt_row;
+    t.pt_val = L.pt_val;
+    t.p_ptr = L.p_ptr;
+    t.p_col = L.p_col;
+    t.p_val = L.p_val;
+  }
   h->ready = true;
   return FEM_OK;
 }
@@ -1967,38 +2172,28 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
 // ------------------------------------------------------------------ solve --
 template <int B0, int K>
 void launch_vcycle(fem_amg* h, cudaStream_t st) {
-  const int nl = h->n_levels;
-  for (int l = 0; l + 1 < nl; ++l) {
+  const int tf = h->tail_first, last = h->n_levels - 1;
+  for (int l = 0; l < tf; ++l) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
     const OpArgs a = level_args<B0>(h, l, h->ctrl);
     launch_op<B0, K, kOpS1>(h, l, a, st);
     launch_op<B0, K, kOpS2>(h, l, a, st);
-    if (l + 2 == nl) {
-      if (l == 0)
-        k_restrict_solve<B0, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r, h->coarse_inv,
-                                                    C.xb, h->ctrl);
-      else
-        k_restrict_solve<K, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r, h->coarse_inv,
-                                                   C.xb, h->ctrl);
-    } else {
-      const OpArgs c = level_args<K>(h, l + 1, h->ctrl);
-      if (l == 0)
-        k_restrict<B0, K><<<grid_for(C.n * 32, 256), 256, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r,
-                                                                   c, h->ctrl);
-      else
-        k_restrict<K, K><<<grid_for(C.n * 32, 256), 256, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.r, c,
-                                                                  h->ctrl);
-    }
+    OpArgs c = level_args<K>(h, l + 1, h->ctrl);
+    if (l + 1 == last) c.dinv = nullptr;  // the coarsest level takes the right-hand side only
+    const unsigned g = capped(C.n, 64);
+    if (l == 0) k_restrict<B0, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
+    else k_restrict<K, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
     note_launch();
   }
-  for (int l = nl - 2; l >= 0; --l) {
+  k_tail<K><<<1, kTailThreads, 0, st>>>(h->tail);
+  note_launch();
+  for (int l = tf - 1; l >= 0; --l) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
-    if (l == 0)
-      k_prolong<B0, K><<<grid_for(L.n, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
-    else
-      k_prolong<K, K><<<grid_for(L.n, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+    const unsigned g = capped((L.n + 7) / 8, 16);
+    if (l == 0) k_prolong<B0, K><<<g, 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+    else k_prolong<K, K><<<g, 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
     note_launch();
     const OpArgs a = level_args<B0>(h, l, h->ctrl);
     launch_op<B0, K, kOpS3>(h, l, a, st);
