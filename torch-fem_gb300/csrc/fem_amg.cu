@@ -598,93 +598,177 @@ __global__ void __launch_bounds__(128) k_p_numeric(Graph g, OpView<B, kSell> A, 
   }
 }
 
-// A P, warp per fine row.
-template <int B, int K, bool kSell>
-__global__ void __launch_bounds__(64) k_ap_numeric(Graph g, OpView<B, kSell> A, const int64_t* __restrict__ p_ptr,
-                                                   const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
-                                                   const int64_t* __restrict__ ap_ptr,
-                                                   const int32_t* __restrict__ ap_col, float* __restrict__ ap_val) {
-  constexpr int BK = B * K;
-  __shared__ int32_t cols[2][kMaxAPRow];
-  __shared__ float acc[2][kMaxAPRow][BK];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t i = (int64_t)blockIdx.x * 2 + w;
+// Slot of v in the sorted list s[0..m) by binary search (v is present).
+__device__ __forceinline__ int bsearch_slot(const int32_t* s, int m, int32_t v) {
+  int lo = 0, hi = m - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (s[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return (m > 0 && s[lo] == v) ? lo : -1;
+}
+
+// A P by contribution lists: block (i, J) of W = A P is the sum over the
+// neighbours j of i (ascending) with J in their P row of A_ij P_jJ.  The
+// lists (neighbour slot, block of P) are built once with the pattern; here
+// a group of 8 lanes sums one block's list with all B x K products in
+// registers, then a fixed-order reduction within the group.
+template <bool kFill>
+__global__ void k_ap_lists(Graph g, const uint8_t* __restrict__ active, const int64_t* __restrict__ p_ptr,
+                           const int32_t* __restrict__ p_col, const int64_t* __restrict__ ap_ptr,
+                           const int32_t* __restrict__ ap_col, int64_t* __restrict__ cnt, int64_t* __restrict__ cursor,
+                           int32_t* __restrict__ cl_k, int32_t* __restrict__ cl_p, int32_t* __restrict__ row) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
-  const int64_t e0 = ap_ptr[i];
-  const int m = (int)(ap_ptr[i + 1] - e0);
-  if (m == 0) return;
-  for (int s = lane; s < m; s += 32) cols[w][s] = ap_col[e0 + s];
-  for (int t = lane; t < m * BK; t += 32) acc[w][t / BK][t % BK] = 0.f;
-  __syncwarp();
+  const int64_t a0 = ap_ptr[i];
+  const int m = (int)(ap_ptr[i + 1] - a0);
+  if (kFill)
+    for (int s = 0; s < m; ++s) row[a0 + s] = (int32_t)i;
+  if (m == 0 || (active && !active[i])) return;
   const int64_t nb = g.ptr[i];
   const int deg = (int)(g.ptr[i + 1] - nb);
   for (int kk = 0; kk < deg; ++kk) {
     const int32_t j = g.idx[nb + kk];
-    float a[B * B];
-#pragma unroll
-    for (int c = 0; c < B * B; ++c) a[c] = A.at(i, kk, c);
     for (int64_t pe = p_ptr[j]; pe < p_ptr[j + 1]; ++pe) {
-      const int s = find_slot(cols[w], m, p_col[pe]);
+      const int s = bsearch_slot(ap_col + a0, m, p_col[pe]);
       if (s < 0) continue;  // cannot happen: the row is the union of these columns
-      const float* pv = p_val + pe * BK;
-      for (int c = lane; c < BK; c += 32) {
-        const int r = c / K, k = c % K;
-        float v = acc[w][s][c];
-#pragma unroll
-        for (int q = 0; q < B; ++q) v = fmaf(a[r * B + q], pv[q * K + k], v);
-        acc[w][s][c] = v;
+      if (!kFill) {
+        cnt[a0 + s] += 1;
+      } else {
+        const int64_t pos = cursor[a0 + s]++;
+        cl_k[pos] = kk;
+        cl_p[pos] = (int32_t)pe;
       }
-      __syncwarp();
     }
   }
-  for (int t = lane; t < m * BK; t += 32) ap_val[e0 * BK + t] = acc[w][t / BK][t % BK];
 }
 
-// A_c = P^T (A P), warp per coarse row; decoupled coarse DOFs (a dropped
-// mode: zero row and column) get a unit diagonal.
-template <int B, int K>
-__global__ void __launch_bounds__(64) k_ac_numeric(int64_t n_c, const int64_t* __restrict__ pt_ptr,
-                                                   const int32_t* __restrict__ pt_row,
-                                                   const int64_t* __restrict__ pt_pos, const float* __restrict__ p_val,
-                                                   const int64_t* __restrict__ ap_ptr,
-                                                   const int32_t* __restrict__ ap_col, const float* __restrict__ ap_val,
-                                                   const int64_t* __restrict__ ac_ptr,
-                                                   const int32_t* __restrict__ ac_col, float* __restrict__ ac_val) {
-  constexpr int BK = B * K, KK = K * K;
-  __shared__ int32_t cols[2][kMaxCRow];
-  __shared__ float acc[2][kMaxCRow][KK];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t I = (int64_t)blockIdx.x * 2 + w;
-  if (I >= n_c) return;
-  const int64_t e0 = ac_ptr[I];
-  const int m = (int)(ac_ptr[I + 1] - e0);
-  for (int s = lane; s < m; s += 32) cols[w][s] = ac_col[e0 + s];
-  for (int t = lane; t < m * KK; t += 32) acc[w][t / KK][t % KK] = 0.f;
-  __syncwarp();
-  for (int64_t pe = pt_ptr[I]; pe < pt_ptr[I + 1]; ++pe) {
-    const int32_t i = pt_row[pe];
-    if (pt_pos[pe] < 0) continue;  // cannot happen: P^T lists entries of P
-    const float* pv = p_val + pt_pos[pe] * BK;
-    for (int64_t ae = ap_ptr[i]; ae < ap_ptr[i + 1]; ++ae) {
-      const int s = find_slot(cols[w], m, ap_col[ae]);
-      if (s < 0) continue;
-      const float* wv = ap_val + ae * BK;
-      for (int c = lane; c < KK; c += 32) {
-        const int k1 = c / K, k2 = c % K;
-        float v = acc[w][s][c];
+template <int B, int K, bool kSell>
+__global__ void __launch_bounds__(256) k_ap_numeric(int64_t n_slots, OpView<B, kSell> A,
+                                                    const int64_t* __restrict__ cl_ptr,
+                                                    const int32_t* __restrict__ cl_k, const int32_t* __restrict__ cl_p,
+                                                    const int32_t* __restrict__ row, const float* __restrict__ p_val,
+                                                    float* __restrict__ ap_val) {
+  constexpr int BK = B * K;
+  const int g8 = threadIdx.x & 7;
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const bool live = s < n_slots;
+  float acc[BK];
 #pragma unroll
-        for (int q = 0; q < B; ++q) v = fmaf(pv[q * K + k1], wv[q * K + k2], v);
-        acc[w][s][c] = v;
-      }
-      __syncwarp();
+  for (int c = 0; c < BK; ++c) acc[c] = 0.f;
+  if (live) {
+    const int64_t i = row[s];
+    for (int64_t e = cl_ptr[s] + g8; e < cl_ptr[s + 1]; e += 8) {
+      const int kk = cl_k[e];
+      const float* pv = p_val + (int64_t)cl_p[e] * BK;
+      float a[B * B], pr[BK];
+#pragma unroll
+      for (int c = 0; c < B * B; ++c) a[c] = A.at(i, kk, c);
+#pragma unroll
+      for (int c = 0; c < BK; ++c) pr[c] = pv[c];
+#pragma unroll
+      for (int r = 0; r < B; ++r)
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+#pragma unroll
+          for (int q = 0; q < B; ++q) acc[r * K + k] = fmaf(a[r * B + q], pr[q * K + k], acc[r * K + k]);
     }
   }
-  for (int t = lane; t < m * KK; t += 32) {
-    const int s = t / KK, c = t % KK;
-    float v = acc[w][s][c];
-    if (cols[w][s] == (int32_t)I && c / K == c % K && v == 0.f) v = 1.f;
-    ac_val[e0 * KK + t] = v;
+#pragma unroll
+  for (int c = 0; c < BK; ++c) {
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 4);
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 2);
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 1);
   }
+  if (live)
+    for (int c = g8; c < BK; c += 8) {
+      float v = 0.f;
+#pragma unroll
+      for (int q = 0; q < BK; ++q) v = q == c ? acc[q] : v;
+      ap_val[s * BK + c] = v;
+    }
+}
+
+// Galerkin product A_c = P^T (A P) by contribution lists: every block (I, J)
+// of A_c is the sum over the fine rows i of P^T row I (ascending) with J in
+// their A P row of P_iI^T W_iJ.  The lists (block of P, block of A P) are
+// built once with the pattern; here one warp sums one block's list, a lane
+// per contribution with all K x K products in registers, then a fixed-order
+// warp reduction.  Decoupled coarse DOFs (a dropped mode: zero row and
+// column) get a unit diagonal.
+template <bool kFill>
+__global__ void k_ac_lists(int64_t n_c, const int64_t* __restrict__ pt_ptr, const int32_t* __restrict__ pt_row,
+                           const int64_t* __restrict__ pt_pos, const int64_t* __restrict__ ap_ptr,
+                           const int32_t* __restrict__ ap_col, const int64_t* __restrict__ ac_ptr,
+                           const int32_t* __restrict__ ac_col, int64_t* __restrict__ cnt,
+                           int64_t* __restrict__ cursor, int32_t* __restrict__ cl_p, int32_t* __restrict__ cl_w) {
+  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n_c) return;
+  const int64_t a0 = ac_ptr[I];
+  const int m = (int)(ac_ptr[I + 1] - a0);
+  for (int64_t pe = pt_ptr[I]; pe < pt_ptr[I + 1]; ++pe) {
+    const int32_t i = pt_row[pe];
+    for (int64_t ae = ap_ptr[i]; ae < ap_ptr[i + 1]; ++ae) {
+      const int s = bsearch_slot(ac_col + a0, m, ap_col[ae]);
+      if (s < 0) continue;  // cannot happen: the row is the union of these columns
+      if (!kFill) {
+        cnt[a0 + s] += 1;
+      } else {
+        const int64_t pos = cursor[a0 + s]++;
+        cl_p[pos] = (int32_t)pt_pos[pe];
+        cl_w[pos] = (int32_t)ae;
+      }
+    }
+  }
+}
+
+template <int B, int K>
+__global__ void __launch_bounds__(256) k_ac_numeric(int64_t n_slots, const int64_t* __restrict__ cl_ptr,
+                                                    const int32_t* __restrict__ cl_p, const int32_t* __restrict__ cl_w,
+                                                    const float* __restrict__ p_val, const float* __restrict__ ap_val,
+                                                    const int32_t* __restrict__ slot_row,
+                                                    const int32_t* __restrict__ ac_col, float* __restrict__ ac_val) {
+  constexpr int BK = B * K, KK = K * K;
+  const int lane = threadIdx.x & 31;
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= n_slots) return;
+  float acc[KK];
+#pragma unroll
+  for (int c = 0; c < KK; ++c) acc[c] = 0.f;
+  for (int64_t e = cl_ptr[s] + lane; e < cl_ptr[s + 1]; e += 32) {
+    const float* pv = p_val + (int64_t)cl_p[e] * BK;
+    const float* wv = ap_val + (int64_t)cl_w[e] * BK;
+    float pr[BK], wr[BK];
+#pragma unroll
+    for (int c = 0; c < BK; ++c) {
+      pr[c] = pv[c];
+      wr[c] = wv[c];
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < K; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < K; ++k2)
+#pragma unroll
+        for (int q = 0; q < B; ++q) acc[k1 * K + k2] = fmaf(pr[q * K + k1], wr[q * K + k2], acc[k1 * K + k2]);
+  }
+#pragma unroll
+  for (int c = 0; c < KK; ++c) acc[c] = warp_sum(acc[c]);
+  const bool diag = ac_col[s] == slot_row[s];
+  for (int c = lane; c < KK; c += 32) {
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < KK; ++q) v = q == c ? acc[q] : v;
+    if (diag && c / K == c % K && v == 0.f) v = 1.f;
+    ac_val[s * KK + c] = v;
+  }
+}
+
+// Row of every block slot of a block CSR pattern.
+__global__ void k_slot_rows(int64_t n, const int64_t* __restrict__ ptr, int32_t* __restrict__ row) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) row[e] = (int32_t)i;
 }
 
 // Inverse of the diagonal block of every coarse row (Gauss-Jordan, partial
@@ -973,93 +1057,84 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   }
 }
 
-// Coarser levels: block CSR (B x B blocks), one warp per row; lane (u, r)
-// takes row r of every (32 / B)-th block, four blocks' loads in flight.
-// The epilogue runs on lanes r < B, one component each.  Coarse operators
-// are read evict_last so they stay in L2 across the cycle.
+// Coarser levels: block CSR (B x B blocks), one CTA of 128 threads per row;
+// thread t < 120 takes row t % B of every (120 / B)-th block, so every
+// thread keeps one component and the per-component sums run in a fixed
+// order.  The epilogue runs on threads t < B.  Coarse operators are read
+// evict_last so they stay in L2 across the cycle.
+constexpr int kRowT = 128;   // threads per coarse row
+constexpr int kRowItems = 120;  // of which hold (block, component) items: a multiple of 2, 3 and 6
+
 template <int B, int MODE>
-__device__ __forceinline__ double csr_row(int64_t i, const int64_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                                          const float* __restrict__ val, const OpArgs& a, uint64_t pol) {
-  constexpr int PB = 32 / B;
-  constexpr int U = 4;
+__global__ void __launch_bounds__(kRowT) k_csr_op(int64_t n, const int64_t* __restrict__ ptr,
+                                                  const int32_t* __restrict__ col, const float* __restrict__ val,
+                                                  OpArgs a) {
+  constexpr int PB = kRowItems / B;
+  __shared__ float part[kRowItems];
+  __shared__ float rs[B];
+  __shared__ double red[32];
+  if (amg_idle(a.ctrl)) return;
   const float* __restrict__ v = op_operand<MODE>(a);
-  const int lane = threadIdx.x & 31;
-  const int u = lane / B, r = lane % B;
-  float y = 0.f;
-  if (u < PB) {
-    const int64_t e1 = ptr[i + 1];
-    for (int64_t e = ptr[i] + u; e < e1; e += U * PB) {
-      int64_t c[U];
-#pragma unroll
-      for (int t = 0; t < U; ++t) c[t] = e + t * PB < e1 ? (int64_t)ld_l2(col + e + t * PB, pol) : -1;
-#pragma unroll
-      for (int t = 0; t < U; ++t) {
-        if (c[t] < 0) continue;
-        const float* m = val + (e + t * PB) * B * B + r * B;
-        const float* xv = v + c[t] * B;
+  const int t = threadIdx.x;
+  const int r = t % B, u = t / B;
+  const uint64_t pol = l2_policy(true);
+  double dot = 0.0;
+  for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+    if (t < kRowItems) {
+      float y = 0.f;
+      const int64_t e1 = ptr[i + 1];
+      for (int64_t e = ptr[i] + u; e < e1; e += PB) {
+        const int64_t c = ld_l2(col + e, pol);
+        const float* m = val + e * B * B + r * B;
+        const float* xv = v + c * B;
 #pragma unroll
         for (int q = 0; q < B; ++q) y = fmaf(ld_l2(m + q, pol), xv[q], y);
       }
+      part[t] = y;
     }
-  }
-  float yr = 0.f;
+    __syncthreads();
+    const int64_t o = i * B + t;
+    float yr = 0.f, rn = 0.f;
+    if (t < B) {
+#pragma unroll 4
+      for (int s = 0; s < PB; ++s) yr += part[t + s * B];
+      if constexpr (MODE == kOpS1 || MODE == kOpS3) rn = a.f[o] - yr;
+      else if constexpr (MODE == kOpS4 || MODE == kOpS4Dot) rn = a.r[o] - yr;
+      rs[t] = rn;
+    }
+    __syncthreads();
+    if (t < B) {
+      float tv = 0.f;
+      if constexpr (MODE == kOpS1 || MODE == kOpS3 || MODE == kOpS4 || MODE == kOpS4Dot) {
+        const float* m = a.dinv + o * B;
 #pragma unroll
-  for (int t = 0; t < PB; ++t) yr += __shfl_sync(0xffffffffu, y, r + t * B);
-  // lane r (< B) now holds component r of (A v)_i
-  const int64_t o = i * B + r;
-  const bool own = lane < B;
-  float rn = 0.f;
-  if constexpr (MODE == kOpS1 || MODE == kOpS3) rn = own ? a.f[o] - yr : 0.f;
-  else if constexpr (MODE == kOpS4 || MODE == kOpS4Dot) rn = own ? a.r[o] - yr : 0.f;
-  float t = 0.f;
-  if constexpr (MODE == kOpS1 || MODE == kOpS3 || MODE == kOpS4 || MODE == kOpS4Dot) {
-    const float* m = a.dinv + (i * B + r) * B;
-#pragma unroll
-    for (int q = 0; q < B; ++q) {
-      const float rq = __shfl_sync(0xffffffffu, rn, q);
-      if (own) t = fmaf(m[q], rq, t);
+        for (int q = 0; q < B; ++q) tv = fmaf(m[q], rs[q], tv);
+      }
+      if constexpr (MODE == kOpS1) {
+        const float dn = a.c1 * a.d[o] + a.c2 * tv;
+        a.r[o] = rn;
+        a.db[o] = dn;
+        a.x[o] += dn;
+      } else if constexpr (MODE == kOpS2) {
+        a.r[o] -= yr;
+      } else if constexpr (MODE == kOpS3) {
+        const float dn = a.theta_inv * tv;
+        a.r[o] = rn;
+        a.d[o] = dn;
+        a.xb[o] = a.x[o] + dn;
+      } else if constexpr (MODE == kOpS4 || MODE == kOpS4Dot) {
+        const float z = a.xb[o] + (a.c1 * a.d[o] + a.c2 * tv);
+        a.xb[o] = z;
+        if constexpr (MODE == kOpS4Dot) dot += (double)a.f[o] * (double)z;
+      } else {
+        a.q[o] = yr;
+        dot += (double)a.p[o] * (double)yr;
+      }
     }
+    __syncthreads();
   }
-  double dot = 0.0;
-  if (own) {
-    if constexpr (MODE == kOpS1) {
-      const float dn = a.c1 * a.d[o] + a.c2 * t;
-      a.r[o] = rn;
-      a.db[o] = dn;
-      a.x[o] += dn;
-    } else if constexpr (MODE == kOpS2) {
-      a.r[o] -= yr;
-    } else if constexpr (MODE == kOpS3) {
-      const float dn = a.theta_inv * t;
-      a.r[o] = rn;
-      a.d[o] = dn;
-      a.xb[o] = a.x[o] + dn;
-    } else if constexpr (MODE == kOpS4 || MODE == kOpS4Dot) {
-      const float z = a.xb[o] + (a.c1 * a.d[o] + a.c2 * t);
-      a.xb[o] = z;
-      if constexpr (MODE == kOpS4Dot) dot = (double)a.f[o] * (double)z;
-    } else {
-      a.q[o] = yr;
-      dot = (double)a.p[o] * (double)yr;
-    }
-  }
-  if constexpr (op_has_dot<MODE>()) dot = warp_sum(dot);
-  return dot;
-}
-
-template <int B, int MODE>
-__global__ void __launch_bounds__(256) k_csr_op(int64_t n, const int64_t* __restrict__ ptr,
-                                                const int32_t* __restrict__ col, const float* __restrict__ val,
-                                                OpArgs a) {
-  __shared__ double red[32];
-  if (amg_idle(a.ctrl)) return;
-  const uint64_t pol = l2_policy(true);
-  double dot = 0.0;
-  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw)
-    dot += csr_row<B, MODE>(i, ptr, col, val, a, pol);
   if constexpr (op_has_dot<MODE>()) {
-    const double bsum = block_sum((threadIdx.x & 31) == 0 ? dot : 0.0, red);
+    const double bsum = block_sum(dot, red);
     if (threadIdx.x == 0) a.partial[blockIdx.x] = bsum;
     if (arrive_last(&a.ctrl->counter)) {
       const double tot = sum_partials(a.partial, gridDim.x, 1, 0, red);
@@ -1074,8 +1149,7 @@ __global__ void __launch_bounds__(256) k_csr_op(int64_t n, const int64_t* __rest
 // Restriction f_c = P^T r of coarse row I by the threads of one CTA (P^T
 // values in transposed order, pt_val, so consecutive threads read
 // consecutive blocks), fixed-order reduction, then the first Chebyshev step
-// of the coarse level: d = D^-1 f / theta, x = d (the coarsest level, whose
-// OpArgs carry no dinv, only takes f).
+// of the coarse level: d = D^-1 f / theta, x = d.
 template <int BF, int K, int NT>
 __device__ __forceinline__ void restrict_row(int64_t I, const int64_t* __restrict__ pt_ptr,
                                              const int32_t* __restrict__ pt_row, const float* __restrict__ pt_val,
@@ -1119,9 +1193,7 @@ __global__ void __launch_bounds__(128) k_restrict(int64_t n_c, const int64_t* __
   if (amg_idle(ctrl)) return;
   for (int64_t I = blockIdx.x; I < n_c; I += gridDim.x) {
     restrict_row<BF, K, 128>(I, pt_ptr, pt_row, pt_val, rf, red, fs);
-    if (threadIdx.x < K && !c.dinv) {
-      c.f[I * K + threadIdx.x] = fs[threadIdx.x];  // the coarsest level: right-hand side only
-    } else if (threadIdx.x < K) {
+    if (threadIdx.x < K) {
       const int k = threadIdx.x;
       const float* m = c.dinv + (I * K + k) * K;
       float t = 0.f;
@@ -1135,49 +1207,26 @@ __global__ void __launch_bounds__(128) k_restrict(int64_t n_c, const int64_t* __
   }
 }
 
-// Prolongation x += P x_c, one warp per fine row: the lanes read the row's
-// P blocks as one contiguous run of values (coalesced) and the B partial
-// sums are reduced across the warp.
-template <int BF, int K>
-__device__ __forceinline__ void prolong_row(int64_t i, const int64_t* __restrict__ p_ptr,
-                                            const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
-                                            const float* __restrict__ xc, float* __restrict__ x) {
-  constexpr int BK = BF * K;
-  const int lane = threadIdx.x & 31;
-  const int64_t e0 = p_ptr[i];
-  const int nv = (int)(p_ptr[i + 1] - e0) * BK;
-  if (nv == 0) return;
-  float part[BF];
-#pragma unroll
-  for (int q = 0; q < BF; ++q) part[q] = 0.f;
-  const float* pv = p_val + e0 * BK;
-  for (int v = lane; v < nv; v += 32) {
-    const int e = v / BK, rem = v - e * BK;
-    const int r = rem / K, k = rem - r * K;
-    const float t = pv[v] * xc[(int64_t)p_col[e0 + e] * K + k];
-#pragma unroll
-    for (int q = 0; q < BF; ++q)
-      if (q == r) part[q] += t;
-  }
-#pragma unroll
-  for (int q = 0; q < BF; ++q) part[q] = warp_sum(part[q]);
-  if (lane < BF) {
-    float s = 0.f;
-#pragma unroll
-    for (int q = 0; q < BF; ++q) s = q == lane ? part[q] : s;
-    x[i * BF + lane] += s;
-  }
-}
-
+// Prolongation x += P x_c, one thread per (fine row, component): the
+// threads of a row read adjacent rows of its blocks.
 template <int BF, int K>
 __global__ void __launch_bounds__(256) k_prolong(int64_t n, const int64_t* __restrict__ p_ptr,
                                                  const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
                                                  const float* __restrict__ xc, float* __restrict__ x,
                                                  const AmgCtrl* ctrl) {
   if (amg_idle(ctrl)) return;
-  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw)
-    prolong_row<BF, K>(i, p_ptr, p_col, p_val, xc, x);
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * BF) return;
+  const int64_t i = t / BF;
+  const int r = (int)(t - i * BF);
+  float s = 0.f;
+  for (int64_t e = p_ptr[i]; e < p_ptr[i + 1]; ++e) {
+    const float* pv = p_val + e * BF * K + r * K;
+    const float* cv = xc + (int64_t)p_col[e] * K;
+#pragma unroll
+    for (int k = 0; k < K; ++k) s = fmaf(pv[k], cv[k], s);
+  }
+  x[t] += s;
 }
 
 // P^T values in transposed order: block e of P^T is block pt_pos[e] of P.
@@ -1191,114 +1240,43 @@ __global__ void k_transpose_vals(int64_t n_e, int bk, const int64_t* __restrict_
   pt_val[t] = pos >= 0 ? p_val[pos * bk + c] : 0.f;
 }
 
-// --------------------------------------------------------- tail cycle ----
-// The small coarse levels (operator at most kTailBytes) run their whole
-// V-cycle inside one CTA: each phase is a loop over the level's rows by the
-// CTA's warps, phases separated by __syncthreads(), one launch instead of
-// six latency-bound ones per level.
-constexpr int64_t kTailBytes = 1 << 20;
-constexpr int kTailThreads = 1024;
-
-struct TailLevel {
-  int64_t n;
-  const int64_t* a_ptr;
-  const int32_t* a_col;
-  const float* a_val;
-  OpArgs args;  // f, x, xb, r, d, db, dinv, Chebyshev coefficients of the level
-  // transfer to the next level (absent on the coarsest)
-  int64_t n_c;
-  const int64_t* pt_ptr;
-  const int32_t* pt_row;
-  const float* pt_val;
-  const int64_t* p_ptr;
-  const int32_t* p_col;
-  const float* p_val;
-};
-
-struct TailParams {
-  int first, last;  // levels first .. last, last the coarsest
-  TailLevel lv[kMaxLevels];
-  const float* coarse_inv;
-  const AmgCtrl* ctrl;
-};
-
-template <int K, int MODE>
-__device__ __forceinline__ void tail_op(const TailLevel& L, uint64_t pol) {
-  const int nw = kTailThreads / 32;
-  for (int64_t i = threadIdx.x >> 5; i < L.n; i += nw) (void)csr_row<K, MODE>(i, L.a_ptr, L.a_col, L.a_val, L.args, pol);
-  __syncthreads();
-}
-
-template <int K>
-__global__ void __launch_bounds__(kTailThreads) k_tail(TailParams P) {
-  if (amg_idle(P.ctrl)) return;
-  const uint64_t pol = l2_policy(true);
-  const int nw = kTailThreads / 32;
+// Restriction onto the coarsest level and its dense solve, one CTA: warps
+// over the coarse rows (P^T in transposed order), then x_c = A_c^-1 f_c.
+template <int BF, int K>
+__global__ void __launch_bounds__(1024) k_coarse_solve(int64_t n_c, const int64_t* __restrict__ pt_ptr,
+                                                       const int32_t* __restrict__ pt_row,
+                                                       const float* __restrict__ pt_val, const float* __restrict__ rf,
+                                                       const float* __restrict__ inv, float* __restrict__ xc,
+                                                       const AmgCtrl* ctrl) {
+  __shared__ float fs[kCoarseMaxDof];
+  if (amg_idle(ctrl)) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int l = P.first; l < P.last; ++l) {
-    const TailLevel& L = P.lv[l];
-    tail_op<K, kOpS1>(L, pol);
-    tail_op<K, kOpS2>(L, pol);
-    const TailLevel& C = P.lv[l + 1];
-    // restriction: warp per coarse row, reading P^T in transposed order
-    for (int64_t I = w; I < L.n_c; I += nw) {
-      float acc[K];
+  for (int64_t I = w; I < n_c; I += blockDim.x >> 5) {
+    float acc[K];
 #pragma unroll
-      for (int k = 0; k < K; ++k) acc[k] = 0.f;
-      for (int64_t e = L.pt_ptr[I] + lane; e < L.pt_ptr[I + 1]; e += 32) {
-        const int64_t i = L.pt_row[e];
-        const float* pv = L.pt_val + e * K * K;
+    for (int k = 0; k < K; ++k) acc[k] = 0.f;
+    for (int64_t e = pt_ptr[I] + lane; e < pt_ptr[I + 1]; e += 32) {
+      const int64_t i = pt_row[e];
+      const float* pv = pt_val + e * BF * K;
 #pragma unroll
-        for (int q = 0; q < K; ++q) {
-          const float rv = L.args.r[i * K + q];
+      for (int q = 0; q < BF; ++q) {
+        const float rv = rf[i * BF + q];
 #pragma unroll
-          for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
-      if (l + 1 == P.last) {
-        if (lane < K) {
-          float fv = 0.f;
-#pragma unroll
-          for (int q = 0; q < K; ++q) fv = q == lane ? acc[q] : fv;
-          C.args.f[I * K + lane] = fv;
-        }
-      } else if (lane < K) {
-        const float* m = C.args.dinv + (I * K + lane) * K;
-        float t = 0.f, fv = 0.f;
-#pragma unroll
-        for (int q = 0; q < K; ++q) {
-          t = fmaf(m[q], acc[q], t);
-          fv = q == lane ? acc[q] : fv;
-        }
-        const float dn = C.args.theta_inv * t;
-        C.args.f[I * K + lane] = fv;
-        C.args.d[I * K + lane] = dn;
-        C.args.x[I * K + lane] = dn;
+        for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
       }
     }
-    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < K; ++k) fs[I * K + k] = acc[k];
   }
-  // coarsest: dense solve of the restricted residual (written by the loop
-  // above or, when the tail is the coarsest level alone, by k_restrict)
-  {
-    const TailLevel& C = P.lv[P.last];
-    const int m = (int)(C.n * K);
-    for (int t = threadIdx.x; t < m; t += kTailThreads) {
-      float s = 0.f;
-      for (int j = 0; j < m; ++j) s = fmaf(P.coarse_inv[(int64_t)t * m + j], C.args.f[j], s);
-      C.args.xb[t] = s;
-    }
-    __syncthreads();
-  }
-  for (int l = P.last - 1; l >= P.first; --l) {
-    const TailLevel& L = P.lv[l];
-    const TailLevel& C = P.lv[l + 1];
-    for (int64_t i = w; i < L.n; i += nw) prolong_row<K, K>(i, L.p_ptr, L.p_col, L.p_val, C.args.xb, L.args.x);
-    __syncthreads();
-    tail_op<K, kOpS3>(L, pol);
-    tail_op<K, kOpS4>(L, pol);
+  __syncthreads();
+  const int m = (int)(n_c * K);
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    float s = 0.f;
+    for (int j = 0; j < m; ++j) s = fmaf(inv[(int64_t)t * m + j], fs[j], s);
+    xc[t] = s;
   }
 }
 
@@ -1645,6 +1623,16 @@ struct AmgLevel {
   int32_t* ap_col = nullptr;
   float* ap_val = nullptr;
   int64_t ap_nnz = 0;
+  // contribution lists of the blocks of A P
+  int64_t* wl_ptr = nullptr;  // [ap_nnz + 1]
+  int32_t* wl_k = nullptr;    // neighbour slot (block of A) of each contribution
+  int32_t* wl_p = nullptr;    // P block of each contribution
+  int32_t* ap_row = nullptr;  // [ap_nnz] fine row of each block
+  // Galerkin contribution lists of the next level's blocks
+  int64_t* cl_ptr = nullptr;  // [C.a_nnz + 1]
+  int32_t* cl_p = nullptr;    // P block of each contribution
+  int32_t* cl_w = nullptr;    // A P block of each contribution
+  int32_t* slot_row = nullptr;  // [C.a_nnz] coarse row of each block
   // smoother
   double rho = 0.0;
   float theta_inv = 0.f, c1 = 0.f, c2 = 0.f;
@@ -1660,8 +1648,6 @@ struct fem_amg {
   float* coarse_inv = nullptr;
   double* coarse_work = nullptr;
   int64_t m_coarse = 0;
-  int tail_first = 0;  // first level of the single-CTA tail cycle
-  tfg::TailParams tail{};
   uint8_t* active = nullptr;  // level 0: nodes with a free DOF
   // CG state
   float *xlo = nullptr, *rcg = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
@@ -1892,6 +1878,58 @@ int patterns(fem_amg* h, int l, cudaStream_t st) {
                                                                 L.ap_col, nullptr, C.a_ptr, C.a_col, h->status);
   note_launch();
   C.g = Graph{na, C.a_ptr, C.a_col};
+  // contribution lists of A P, in ascending neighbour per block
+  {
+    L.ap_row = h->alloc<int32_t>(L.ap_nnz, st);
+    int64_t* wcnt = h->alloc<int64_t>(L.ap_nnz + 1, st);
+    L.wl_ptr = h->alloc<int64_t>(L.ap_nnz + 1, st);
+    int64_t* wcur = h->alloc<int64_t>(L.ap_nnz + 1, st);
+    if (!L.ap_row || !wcnt || !L.wl_ptr || !wcur) return check_cuda("AMG A P lists");
+    cudaMemsetAsync(wcnt, 0, sizeof(int64_t) * (L.ap_nnz + 1), st);
+    k_ap_lists<false><<<gn, kT, 0, st>>>(L.g, active, L.p_ptr, L.p_col, L.ap_ptr, L.ap_col, wcnt, nullptr, nullptr,
+                                         nullptr, nullptr);
+    note_launch();
+    int64_t n_wl = 0;
+    rc = scan_total(h, wcnt, L.wl_ptr, L.ap_nnz, &n_wl, st);
+    if (rc) return rc;
+    if (n_wl >= ((int64_t)1 << 31)) {
+      set_last_error("AMG: A P of level %d too large for 32-bit block indices", l);
+      return FEM_BOUNDS;
+    }
+    L.wl_k = h->alloc<int32_t>(n_wl, st);
+    L.wl_p = h->alloc<int32_t>(n_wl, st);
+    if (!L.wl_k || !L.wl_p) return check_cuda("AMG A P lists");
+    cudaMemcpyAsync(wcur, L.wl_ptr, sizeof(int64_t) * (L.ap_nnz + 1), cudaMemcpyDeviceToDevice, st);
+    k_ap_lists<true><<<gn, kT, 0, st>>>(L.g, active, L.p_ptr, L.p_col, L.ap_ptr, L.ap_col, nullptr, wcur, L.wl_k,
+                                        L.wl_p, L.ap_row);
+    note_launch();
+  }
+  // contribution lists of the Galerkin product, in ascending fine row per block
+  L.slot_row = h->alloc<int32_t>(C.a_nnz, st);
+  int64_t* ccnt = h->alloc<int64_t>(C.a_nnz + 1, st);
+  L.cl_ptr = h->alloc<int64_t>(C.a_nnz + 1, st);
+  int64_t* ccur = h->alloc<int64_t>(C.a_nnz + 1, st);
+  if (!L.slot_row || !ccnt || !L.cl_ptr || !ccur) return check_cuda("AMG Galerkin lists");
+  k_slot_rows<<<grid_for(na, kT), kT, 0, st>>>(na, C.a_ptr, L.slot_row);
+  note_launch();
+  cudaMemsetAsync(ccnt, 0, sizeof(int64_t) * (C.a_nnz + 1), st);
+  k_ac_lists<false><<<grid_for(na, 128), 128, 0, st>>>(na, L.pt_ptr, L.pt_row, L.pt_pos, L.ap_ptr, L.ap_col, C.a_ptr,
+                                                       C.a_col, ccnt, nullptr, nullptr, nullptr);
+  note_launch();
+  int64_t n_cl = 0;
+  rc = scan_total(h, ccnt, L.cl_ptr, C.a_nnz, &n_cl, st);
+  if (rc) return rc;
+  if (n_cl >= ((int64_t)1 << 31) || L.p_nnz >= ((int64_t)1 << 31) || L.ap_nnz >= ((int64_t)1 << 31)) {
+    set_last_error("AMG: Galerkin product of level %d too large for 32-bit block indices", l);
+    return FEM_BOUNDS;
+  }
+  L.cl_p = h->alloc<int32_t>(n_cl, st);
+  L.cl_w = h->alloc<int32_t>(n_cl, st);
+  if (!L.cl_p || !L.cl_w) return check_cuda("AMG Galerkin lists");
+  cudaMemcpyAsync(ccur, L.cl_ptr, sizeof(int64_t) * (C.a_nnz + 1), cudaMemcpyDeviceToDevice, st);
+  k_ac_lists<true><<<grid_for(na, 128), 128, 0, st>>>(na, L.pt_ptr, L.pt_row, L.pt_pos, L.ap_ptr, L.ap_col, C.a_ptr,
+                                                      C.a_col, nullptr, ccur, L.cl_p, L.cl_w);
+  note_launch();
   return read_status(h, st, "AMG patterns");
 }
 
@@ -1985,13 +2023,6 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
   h->L[0].f = h->rcg;
   h->L[0].xb = h->z;
   cudaMemsetAsync(h->p, 0, sizeof(float) * n, st);
-  // the tail: the trailing levels >= 1 whose operators are small enough for
-  // one CTA (the coarsest level alone when there are none)
-  const int last = h->n_levels - 1;
-  h->tail_first = last;
-  while (h->tail_first - 1 >= 1 &&
-         h->L[h->tail_first - 1].a_nnz * K * K * (int64_t)sizeof(float) <= kTailBytes)
-    --h->tail_first;
   return read_status(h, st, "AMG create");
 }
 
@@ -2024,7 +2055,7 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
     const int64_t ns = (L.n + 31) / 32;
     k_sell_op<B0, MODE><<<capped(ns, 16), kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
   } else {
-    k_csr_op<K, MODE><<<capped((L.n + 7) / 8, 8), 256, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
+    k_csr_op<K, MODE><<<capped(L.n, 16), kRowT, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
   }
   note_launch();
 }
@@ -2053,7 +2084,7 @@ int lanczos_level(fem_amg* h, int l, int b0, cudaStream_t st, double* rho) {
       else
         k_sell_op<2, kOpLzQ><<<capped(ns, 16), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val, a);
     } else {
-      k_csr_op<B, kOpLzQ><<<capped((n + 7) / 8, 8), 256, 0, st>>>(n, L.a_ptr, L.a_col, L.a_val, a);
+      k_csr_op<B, kOpLzQ><<<capped(n, 16), kRowT, 0, st>>>(n, L.a_ptr, L.a_col, L.a_val, a);
     }
     note_launch();
     k_lz_update<B><<<g, kT, 0, st>>>(n, dinv, L.r, L.d, L.x, h->partial, h->lzc, h->lz);
@@ -2113,22 +2144,22 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
       k_p_numeric<B0, K, true><<<grid_for(L.n, 4), 128, 0, st>>>(L.g, Av, h->dinv0, L.agg, L.tval, L.p_ptr, L.p_col,
                                                                  L.p_val, omega);
       note_launch();
-      k_ap_numeric<B0, K, true><<<grid_for(L.n, 2), 64, 0, st>>>(L.g, Av, L.p_ptr, L.p_col, L.p_val, L.ap_ptr,
-                                                                 L.ap_col, L.ap_val);
+      k_ap_numeric<B0, K, true><<<grid_for(L.ap_nnz * 8, 256), 256, 0, st>>>(L.ap_nnz, Av, L.wl_ptr, L.wl_k, L.wl_p,
+                                                                            L.ap_row, L.p_val, L.ap_val);
       note_launch();
-      k_ac_numeric<B0, K><<<grid_for(C.n, 2), 64, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.ap_ptr,
-                                                          L.ap_col, L.ap_val, C.a_ptr, C.a_col, C.a_val);
+      k_ac_numeric<B0, K><<<grid_for(C.a_nnz * 32, 256), 256, 0, st>>>(C.a_nnz, L.cl_ptr, L.cl_p, L.cl_w, L.p_val,
+                                                                     L.ap_val, L.slot_row, C.a_col, C.a_val);
       note_launch();
     } else {
       OpView<K, false> Av{L.a_ptr, L.a_val};
       k_p_numeric<K, K, false><<<grid_for(L.n, 4), 128, 0, st>>>(L.g, Av, L.dinv, L.agg, L.tval, L.p_ptr, L.p_col,
                                                                  L.p_val, omega);
       note_launch();
-      k_ap_numeric<K, K, false><<<grid_for(L.n, 2), 64, 0, st>>>(L.g, Av, L.p_ptr, L.p_col, L.p_val, L.ap_ptr,
-                                                                 L.ap_col, L.ap_val);
+      k_ap_numeric<K, K, false><<<grid_for(L.ap_nnz * 8, 256), 256, 0, st>>>(L.ap_nnz, Av, L.wl_ptr, L.wl_k, L.wl_p,
+                                                                            L.ap_row, L.p_val, L.ap_val);
       note_launch();
-      k_ac_numeric<K, K><<<grid_for(C.n, 2), 64, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_pos, L.p_val, L.ap_ptr,
-                                                         L.ap_col, L.ap_val, C.a_ptr, C.a_col, C.a_val);
+      k_ac_numeric<K, K><<<grid_for(C.a_nnz * 32, 256), 256, 0, st>>>(C.a_nnz, L.cl_ptr, L.cl_p, L.cl_w, L.p_val,
+                                                                    L.ap_val, L.slot_row, C.a_col, C.a_val);
       note_launch();
     }
     k_transpose_vals<<<grid_for(L.p_nnz * L.b * K, kT), kT, 0, st>>>(L.p_nnz, L.b * K, L.pt_pos, L.p_val,
@@ -2144,27 +2175,6 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
   note_launch();
   int rc = read_status(h, st, "AMG setup");
   if (rc) return rc;
-  TailParams& T = h->tail;
-  T.first = h->tail_first;
-  T.last = h->n_levels - 1;
-  T.coarse_inv = h->coarse_inv;
-  T.ctrl = h->ctrl;
-  for (int l = T.first; l <= T.last; ++l) {
-    const AmgLevel& L = h->L[l];
-    TailLevel& t = T.lv[l];
-    t.n = L.n;
-    t.a_ptr = L.a_ptr;
-    t.a_col = L.a_col;
-    t.a_val = L.a_val;
-    t.args = level_args<K>(h, l, h->ctrl);
-    t.n_c = l < T.last ? L.n_agg : 0;
-    t.pt_ptr = L.pt_ptr;
-    t.pt_row = L.pt_row;
-    t.pt_val = L.pt_val;
-    t.p_ptr = L.p_ptr;
-    t.p_col = L.p_col;
-    t.p_val = L.p_val;
-  }
   h->ready = true;
   return FEM_OK;
 }
@@ -2172,28 +2182,35 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
 // ------------------------------------------------------------------ solve --
 template <int B0, int K>
 void launch_vcycle(fem_amg* h, cudaStream_t st) {
-  const int tf = h->tail_first, last = h->n_levels - 1;
-  for (int l = 0; l < tf; ++l) {
+  const int last = h->n_levels - 1;
+  for (int l = 0; l < last; ++l) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
     const OpArgs a = level_args<B0>(h, l, h->ctrl);
     launch_op<B0, K, kOpS1>(h, l, a, st);
     launch_op<B0, K, kOpS2>(h, l, a, st);
-    OpArgs c = level_args<K>(h, l + 1, h->ctrl);
-    if (l + 1 == last) c.dinv = nullptr;  // the coarsest level takes the right-hand side only
-    const unsigned g = capped(C.n, 64);
-    if (l == 0) k_restrict<B0, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
-    else k_restrict<K, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
+    if (l + 1 == last) {
+      if (l == 0)
+        k_coarse_solve<B0, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, h->coarse_inv, C.xb,
+                                                  h->ctrl);
+      else
+        k_coarse_solve<K, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, h->coarse_inv, C.xb,
+                                                 h->ctrl);
+    } else {
+      const OpArgs c = level_args<K>(h, l + 1, h->ctrl);
+      const unsigned g = capped(C.n, 64);
+      if (l == 0) k_restrict<B0, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
+      else k_restrict<K, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
+    }
     note_launch();
   }
-  k_tail<K><<<1, kTailThreads, 0, st>>>(h->tail);
-  note_launch();
-  for (int l = tf - 1; l >= 0; --l) {
+  for (int l = last - 1; l >= 0; --l) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
-    const unsigned g = capped((L.n + 7) / 8, 16);
-    if (l == 0) k_prolong<B0, K><<<g, 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
-    else k_prolong<K, K><<<g, 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+    if (l == 0)
+      k_prolong<B0, K><<<grid_for(L.n * B0, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+    else
+      k_prolong<K, K><<<grid_for(L.n * K, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
     note_launch();
     const OpArgs a = level_args<B0>(h, l, h->ctrl);
     launch_op<B0, K, kOpS3>(h, l, a, st);
