@@ -8,12 +8,17 @@ residual 1e-10 plus the gradient of sum(u) with respect to the nodal forces
 through the hand-written adjoint (the reference benchmark's loss,
 benchmarks/cubes.py:31-37).  Synthetic seeded data; no dataset.
 
-value      mixed precision (FP32 K + FP32 CG with FP64 residual replacement),
-           inputs resident in HBM, CUDA events on the launching stream.
+value      mixed precision: FP32 K and FP32 CG with FP64 residual
+           replacement, preconditioned by the smoothed-aggregation multigrid
+           V-cycle (--precond amg, the library default) or block Jacobi
+           (--precond jacobi); inputs resident in HBM, CUDA events on the
+           launching stream.
 e2e        the same through the public API from host tensors: the model is
            built from CPU tensors, so every step copies its inputs to the
            device and its results (u, f, sigma, F, grad) back.
 plain_fp64 the FP64 Jacobi-CG path (scalar CSR in the reference pattern).
+mixed_block_jacobi  the mixed path with block Jacobi (the persistent CG
+           kernel), reported beside the headline.
 
 `--impl reference` times the CPU oracle (a restatement of torch-fem's CPU
 path: numpy assembly + scipy Jacobi-CG) on a bounded sample of the same
@@ -242,7 +247,8 @@ def run_profile(args):
     mesh_s = dm.make_mesh(None)
     mat = _lib.FemMaterial(kind, data.data_ptr())
     con = m.constraints.reshape(-1).to(dev, torch.uint8).contiguous()
-    sysm = dm.build_system(mesh_s, mat, con, args.profile, keep_refs=(data, mesh_s, mat))
+    sysm = dm.build_system(mesh_s, mat, con, args.profile, keep_refs=(data, mesh_s, mat),
+                           precond=args.precond if args.profile == "mixed" else "jacobi")
     b = torch.where(con.bool(), torch.zeros_like(forces.reshape(-1)), forces.reshape(-1)).contiguous()
     try:
         dm.solve(sysm, b, 1e-30, max_iter=args.profile_iters)
@@ -267,6 +273,8 @@ def main():
                     help="profiling mode: assemble one system and run --profile-iters CG iterations")
     ap.add_argument("--profile-iters", type=int, default=20)
     ap.add_argument("--cg-path", choices=["persistent", "persistent-regs", "kernels"], default="persistent")
+    ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
+                    help="preconditioner of the mixed-precision headline")
     args = ap.parse_args()
     torch.set_default_dtype(torch.float64)
     if args.impl == "reference":
@@ -289,8 +297,9 @@ def main():
     stream = torch.cuda.current_stream(dev)
 
     # warm-up (W untimed steps), then K timed steps of the mixed path
+    pc = args.precond
     for _ in range(max(args.warmup, 0)):
-        out = step(m, forces, "mixed", args.stol)
+        out = step(m, forces, "mixed", args.stol, pc)
     torch.cuda.synchronize()
     lib.fem_set_timing(1)
     spmv_ms, spmv_n, iters = 0.0, 0, []
@@ -302,7 +311,7 @@ def main():
         torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
-            out = step(m, forces, "mixed", args.stol)
+            out = step(m, forces, "mixed", args.stol, pc)
             st = m.last_solve
             iters.append(st.iterations)
             spmv_ms += st.system.stats.spmv_ms
@@ -319,11 +328,11 @@ def main():
     m_host, forces_host = cube_workload(args.n, torch.device("cpu"))
     forces_host = forces_host.pin_memory()
     _ = m_host.device_mesh  # setup (pattern, geometry) outside the timed region
-    e2e_out = step(m_host, forces_host, "mixed", args.stol)
+    e2e_out = step(m_host, forces_host, "mixed", args.stol, pc)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        e2e_out = step(m_host, forces_host, "mixed", args.stol)
+        e2e_out = step(m_host, forces_host, "mixed", args.stol, pc)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     e2e_ms = reduce_max(dist, e2e_ms, dev)
@@ -349,10 +358,36 @@ def main():
                                  "cg_iterations": m.last_solve.iterations},
                   "mixed_speedup_vs_plain": plain_ms / ms,
                   "rel_err_mixed_vs_fp64": {"u": err_u, "sigma": err_s, "grad": err_g}}
+        if pc != "jacobi":
+            # the mixed path with block Jacobi, same workload
+            step(m, forces, "mixed", args.stol, "jacobi")
+            torch.cuda.synchronize()
+            j0, j1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            j0.record(stream)
+            step(m, forces, "mixed", args.stol, "jacobi")
+            j1.record(stream)
+            torch.cuda.synchronize()
+            bj_ms = reduce_max(dist, j0.elapsed_time(j1), dev)
+            result["mixed_block_jacobi"] = {"value": bj_ms / 1e3 / (n_dofs / 1e6), "ms_per_step": bj_ms,
+                                            "cg_iterations": m.last_solve.iterations,
+                                            "speedup_vs_plain": plain_ms / bj_ms}
 
     peak, peak_kind = measured_peak_hbm()
-    persistent = lib.fem_get_cg_path() in (1, 2)
-    if persistent:
+    persistent = lib.fem_get_cg_path() in (1, 2) and pc == "jacobi"
+    traffic = None
+    if pc == "amg":
+        # CUDA events around every level-0 SpMV launch of the multigrid CG
+        # (four Chebyshev passes and q = A p per iteration)
+        unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
+        sb = spmv_bytes(dm)
+        kernel_name = "k_sell_op<3,*> (level-0 FP32 block SpMV of the multigrid CG, fused smoothing epilogue)"
+        traffic_file = ROOT / "profiles" / "amg_sell_op_traffic.json"
+        if traffic_file.exists():
+            try:
+                traffic = json.loads(traffic_file.read_text())["dram_bytes_per_block_per_launch"] * dm.n_blocks
+            except (KeyError, ValueError):
+                traffic = None
+    elif persistent:
         # CUDA events around each persistent CG launch; spmv_n counts the
         # iterations those launches ran
         unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
@@ -368,7 +403,6 @@ def main():
     # (dram__bytes_read.sum + dram__bytes_write.sum over a 20-iteration launch),
     # per stored block so that it scales to this workload's matrix
     traffic_file = ROOT / "profiles" / "pcg_persistent_traffic.json"
-    traffic = None
     if persistent and traffic_file.exists():
         try:
             tj = json.loads(traffic_file.read_text())
@@ -391,6 +425,7 @@ def main():
             "dtype": "f32+f64",
             "data": "synthetic (seeded jittered cube)",
             "config": {"workload": f"hexa1_cube_{args.n}^3_jittered_linear_elastic_solve+adjoint",
+                       "preconditioner": "smoothed-aggregation multigrid" if pc == "amg" else "block Jacobi",
                        "dofs": n_dofs, "nnz": dm.nnz, "n_elem": n_elem, "stol": args.stol,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (FP32 K = %.0f MB)" % (dm.n_blocks * 40 / 1e6)},

@@ -80,8 +80,8 @@ def test_element_stiffness_vs_reference(cuda, golden):
     assert rel(ke, torch.tensor(g["ke"])) <= 1e-13
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_hexa2_vs_reference(cuda, golden, precision):
+@pytest.mark.parametrize("precision,precond", [("fp64", None), ("mixed", "jacobi"), ("mixed", "amg")])
+def test_hexa2_vs_reference(cuda, golden, precision, precond):
     """Hexa2 (20-node serendipity): pattern, element matrices and the solution
     of the reference's jittered quadratic cube."""
     g = golden("hexa2_jitter2.npz")
@@ -98,7 +98,7 @@ def test_hexa2_vs_reference(cuda, golden, precision):
     assert rel(ke, torch.tensor(g["ke"])) <= 1e-13
     m.constraints[nodes[:, 0] == 0.0, :] = True
     m.forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
-    u, f, s, _, _ = m.solve(stol=1e-12, precision=precision)
+    u, f, s, _, _ = m.solve(stol=1e-12, precision=precision, preconditioner=precond)
     assert rel(u, g["u"]) <= RTOL
     assert rel(f, g["f"]) <= RTOL
     assert rel(s, g["sigma"]) <= RTOL
@@ -121,14 +121,15 @@ def test_c1_forward_and_adjoint(cuda, golden):
     assert rel(gf, g["grad_forces"]) <= RTOL
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_jittered_cube_gradients(cuda, golden, precision):
+@pytest.mark.parametrize("precision,precond", [("fp64", None), ("mixed", "jacobi"), ("mixed", "amg")])
+def test_jittered_cube_gradients(cuda, golden, precision, precond):
     g = golden("hexa_jitter3.npz")
     E = torch.tensor(g["E"], requires_grad=True)
     m = cube_model(g, E)
     forces = m.forces.clone().requires_grad_(True)
     m.forces = forces
-    u, f, s, gr, _ = m.solve(stol=1e-12, precision=precision, differentiable_parameters=(forces, E))
+    u, f, s, gr, _ = m.solve(stol=1e-12, precision=precision, preconditioner=precond,
+                             differentiable_parameters=(forces, E))
     assert rel(u, g["u"]) <= RTOL
     assert rel(f, g["f"]) <= RTOL
     assert rel(s, g["sigma"]) <= RTOL
@@ -337,7 +338,7 @@ def test_persistent_and_kernel_cg_paths_agree(cuda, precision):
             m = Solid(nodes, el, IsotropicElasticity3D(1000.0, 0.3))
             m.constraints[nodes[:, 0] == 0.0, :] = True
             m.forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
-            out[path] = m.solve(precision=precision, stol=1e-12)[0]
+            out[path] = m.solve(precision=precision, stol=1e-12, preconditioner="jacobi")[0]
             iters[path] = m.last_solve.iterations
     finally:
         lib.fem_set_cg_path(1)
@@ -374,15 +375,16 @@ def _hyper_model(g):
     return m, E, right
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_neo_hookean_tetra2_vs_reference(cuda, golden, precision):
+@pytest.mark.parametrize("precision,precond", [("fp64", None), ("mixed", "jacobi"), ("mixed", "amg")])
+def test_neo_hookean_tetra2_vs_reference(cuda, golden, precision, precond):
     """Config 4 at small size: Tetra2, Neo-Hookean, nlgeom, 10 increments;
     tip reaction and its gradient w.r.t. per-element E against the reference."""
     g = golden("hyper_tet2_6x2x2.npz")
     m, E, right = _hyper_model(g)
     # Newton to 1e-10 relative: 1e-12 is at this problem's FP64 residual floor
     u, f, s, F, _ = m.solve(increments=torch.linspace(0.0, 1.0, 11), nlgeom=True, rtol=1e-10, atol=1e-10,
-                            max_iter=20, stol=1e-13, precision=precision, differentiable_parameters=E)
+                            max_iter=20, stol=1e-13, precision=precision, preconditioner=precond,
+                            differentiable_parameters=E)
     assert rel(u, g["u"]) <= 1e-8
     assert rel(f, g["f"]) <= 1e-8
     assert rel(s, g["sigma"]) <= 1e-8
@@ -425,15 +427,15 @@ def _plastic_model(g):
     return m, t, right
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_plane_strain_plasticity_vs_reference(cuda, golden, precision):
+@pytest.mark.parametrize("precision,precond", [("fp64", None), ("mixed", "jacobi"), ("mixed", "amg")])
+def test_plane_strain_plasticity_vs_reference(cuda, golden, precision, precond):
     """Config 5 at small size: O-grid plate with hole, J2 plane strain,
     20 increments; reaction and its gradient w.r.t. element thickness through
     the per-increment checkpointed adjoint, against the reference."""
     g = golden("plastic_ogrid_32x8.npz")
     m, t, right = _plastic_model(g)
     u, f, s, _, st = m.solve(increments=torch.linspace(0.0, 1.0, 21), rtol=1e-12, atol=1e-12, max_iter=80,
-                             stol=1e-13, precision=precision, differentiable_parameters=t)
+                             stol=1e-13, precision=precision, preconditioner=precond, differentiable_parameters=t)
     assert float(st[:, 0].max()) > 0.0  # the plate yields
     assert rel(u, g["u"]) <= 1e-8
     assert rel(f, g["f"]) <= 1e-8
@@ -491,12 +493,12 @@ def test_simp_full_size_central_differences(cuda, golden):
 # ------------------------------------------------------------ full sizes ---
 def test_config2_full_size_mixed_matches_fp64(cuda):
     """Config 2 at full size (70^3 jittered Hexa1, 1,073,733 DOF): the mixed
-    path (FP32 storage and CG inside FP64 residual replacement) against the
-    FP64 path: u, sigma and d(sum u)/d(forces) to 1e-8 relative."""
+    path with block Jacobi (FP32 storage and CG inside FP64 residual
+    replacement) against the FP64 path: u, sigma and d(sum u)/d(forces) to 1e-8 relative."""
     import bench
 
     m, forces = bench.cube_workload(70, cuda)
-    um, fm, sm, _, _, gm = bench.step(m, forces, "mixed", 1e-10)
+    um, fm, sm, _, _, gm = bench.step(m, forces, "mixed", 1e-10, precond="jacobi")
     up, fp, sp, _, _, gp = bench.step(m, forces, "fp64", 1e-10)
     assert m.n_dofs == 1_073_733
     assert rel(um, up) <= RTOL

@@ -134,3 +134,20 @@ def test_shell_constructor_validates_like_reference():
     f = 1000.0 / (1 - 0.09)
     assert torch.allclose(data[0, :9], torch.tensor([f, 0.3 * f, 0, 0.3 * f, f, 0, 0, 0, f * 0.35]))
     assert torch.allclose(data[0, 9:], mat.G * torch.ones(2))
+
+
+def test_preconditioner_resolution(monkeypatch):
+    from torchfem_gb300.base import resolve_preconditioner
+
+    monkeypatch.delenv("TORCHFEM_GB300_PRECOND", raising=False)
+    assert resolve_preconditioner(None, "mixed", 3) == "amg"
+    assert resolve_preconditioner(None, "mixed", 2) == "amg"
+    assert resolve_preconditioner(None, "fp64", 3) == "jacobi"
+    assert resolve_preconditioner(None, "mixed", 6) == "jacobi"  # shells
+    assert resolve_preconditioner("jacobi", "mixed", 3) == "jacobi"
+    with pytest.raises(ValueError):
+        resolve_preconditioner("amg", "fp64", 3)
+    with pytest.raises(ValueError):
+        resolve_preconditioner("ilu", "mixed", 3)
+    monkeypatch.setenv("TORCHFEM_GB300_PRECOND", "jacobi")
+    assert resolve_preconditioner(None, "mixed", 3) == "jacobi"

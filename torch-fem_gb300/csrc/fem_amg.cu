@@ -39,6 +39,7 @@
 namespace tfg {
 
 int etype_info(int etype, int* ne, int* d, int* nip);
+extern int g_timing;  // fem_set_timing
 size_t scan_workspace_bytes(int64_t n);
 int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
 
@@ -1660,6 +1661,13 @@ struct fem_amg {
   std::vector<void*> mem;
   int64_t dropped = 0;
   bool ready = false;
+  // CUDA events around the level-0 SpMV launches of a chunk (timing on)
+  static constexpr int kTimed = 32;
+  cudaEvent_t ev[2 * kTimed];
+  bool ev_ready = false;
+  int ev_used = kTimed;  // events are recorded only inside a timed chunk
+  double timed_ms = 0.0;
+  long long timed_n = 0;
   // level-0 operator captured at setup
   const int64_t* sell_base = nullptr;
   const int32_t* sell_col = nullptr;
@@ -2053,7 +2061,10 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
   AmgLevel& L = h->L[l];
   if (l == 0) {
     const int64_t ns = (L.n + 31) / 32;
+    const bool timed = h->ev_ready && h->ev_used < fem_amg::kTimed;
+    if (timed) cudaEventRecord(h->ev[2 * h->ev_used], st);
     k_sell_op<B0, MODE><<<capped(ns, 16), kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
+    if (timed) cudaEventRecord(h->ev[2 * h->ev_used++ + 1], st);
   } else {
     k_csr_op<K, MODE><<<capped(L.n, 16), kRowT, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
   }
@@ -2291,6 +2302,16 @@ int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, d
   double best = -1.0;
   int stalled = 0;
   int chunk = 2;
+  h->timed_ms = 0.0;
+  h->timed_n = 0;
+  if (g_timing && !h->ev_ready) {
+    bool ok = true;
+    for (int k = 0; k < 2 * fem_amg::kTimed && ok; ++k) ok = cudaEventCreate(&h->ev[k]) == cudaSuccess;
+    if (!ok) return check_cuda("AMG timing events");
+    h->ev_ready = true;
+  }
+  const bool timing = g_timing && h->ev_ready;
+  constexpr int kFinePerIter = 5;  // level-0 SpMVs per iteration: S1, S2, S3, S4, q = A p
   while (c.done == kRun) {
     if (c.replace) {
       k_cg_fold<<<grid_for(n, kT), kT, 0, st>>>(n, x, h->xlo, h->ctrl);
@@ -2324,11 +2345,27 @@ int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, d
       }
       continue;
     }
+    const long long before = c.iters;
+    h->ev_used = 0;
+    if (!timing) h->ev_used = fem_amg::kTimed;  // no events recorded
     for (int k = 0; k < chunk; ++k) launch_iteration<B0, K>(h, st);
     rc = check_cuda("AMG CG iteration");
     if (rc) return rc;
     rc = read_ctrl(h, &c, st);
     if (rc) return rc;
+    if (timing) {
+      // the launches of iterations that ran (the ones after convergence or a
+      // pending replacement return at once and are not counted)
+      const int active = (int)std::min<long long>(c.iters - before, chunk) * kFinePerIter;
+      for (int k = 0; k < active && k < h->ev_used; ++k) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, h->ev[2 * k], h->ev[2 * k + 1]) == cudaSuccess) {
+          h->timed_ms += t;
+          h->timed_n += 1;
+        }
+      }
+    }
+    h->ev_used = fem_amg::kTimed;
     chunk = std::min(chunk + 1, 4);
   }
   if (op) {
@@ -2345,8 +2382,8 @@ int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, d
     info->replacements = c.replacements;
     info->rel_residual = rel;
     info->status = status_code(c.done);
-    info->spmv_ms = 0.0;
-    info->spmv_timed = 0;
+    info->spmv_ms = h->timed_ms;
+    info->spmv_timed = h->timed_n;
   }
   if (c.done != kConverged)
     set_last_error("multigrid CG did not converge: %lld iterations, relative residual %.3e, code %d", c.iters, rel,
@@ -2387,6 +2424,8 @@ int fem_amg_create(const fem_blocks* B, const double* coords, const uint8_t* con
 
 void fem_amg_destroy(fem_amg* h) {
   if (!h) return;
+  if (h->ev_ready)
+    for (int k = 0; k < 2 * fem_amg::kTimed; ++k) cudaEventDestroy(h->ev[k]);
   for (void* p : h->mem) cudaFree(p);
   delete h;
 }

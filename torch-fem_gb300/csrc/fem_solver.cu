@@ -1600,7 +1600,7 @@ static int validate_matrix(const fem_matrix* A) {
 
 // Optional CUDA-event timing of the SpMV launches (fem_set_timing).
 constexpr int kMaxChunk = 64;
-static int g_timing = 0;
+int g_timing = 0;  // CUDA-event timing of the CG (fem_set_timing), read by the multigrid CG too
 
 struct SpmvTimer {
   cudaEvent_t ev[2 * kMaxChunk];

@@ -27,11 +27,12 @@ _PRECONDITIONERS = ("jacobi", "amg")
 def resolve_preconditioner(preconditioner: str | None, precision: str, n_dof_per_node: int) -> str:
     """'jacobi' (block Jacobi in mixed precision, Jacobi in FP64) or 'amg'
     (smoothed-aggregation multigrid, the counterpart of the reference's
-    pyamg / AmgX preconditioners; mixed precision, 2 or 3 DOFs per node).
-    None picks the default: TORCHFEM_GB300_PRECOND if set, else 'jacobi'."""
+    default pyamg / AmgX preconditioners; mixed precision, 2 or 3 DOFs per
+    node).  None picks the default: TORCHFEM_GB300_PRECOND if set, else 'amg'
+    where it applies and 'jacobi' elsewhere (FP64, shells)."""
     import os
 
-    p = preconditioner if preconditioner is not None else os.environ.get("TORCHFEM_GB300_PRECOND", "jacobi")
+    p = preconditioner if preconditioner is not None else os.environ.get("TORCHFEM_GB300_PRECOND", "amg")
     if p not in _PRECONDITIONERS:
         raise ValueError(f"preconditioner must be one of {_PRECONDITIONERS}")
     if p == "amg" and (precision != "mixed" or n_dof_per_node not in (2, 3)):
