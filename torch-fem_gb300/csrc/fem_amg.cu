@@ -987,9 +987,11 @@ __host__ __device__ constexpr bool op_has_dot() {
   return MODE == kOpS4Dot || MODE == kOpQ || MODE == kOpLzQ;
 }
 
-// Level 0: the sliced FP32 matrix, thread per row, kSellW warps sharing each
-// slice's slots (the layout of fem_assemble_sell).  The matrix streams with
-// L2 evict_first; the vectors stay in L2.
+// Level 0: the sliced FP32 matrix (the layout of fem_assemble_sell): one CTA
+// per slice of 32 rows, thread per row, the kSellW warps sharing the slice's
+// slots (short dependent chains), partial rows summed in shared memory in a
+// fixed order.  The grid covers every slice, so the hardware balances the
+// tail.  The matrix streams with L2 evict_first; the vectors stay in L2.
 template <int D, int MODE>
 __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const int64_t* __restrict__ sell_base,
                                                          const int32_t* __restrict__ col,
@@ -1000,50 +1002,47 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   if (amg_idle(a.ctrl)) return;
   const float* __restrict__ v = op_operand<MODE>(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t n_slices = (n_rows + 31) >> 5;
+  const int64_t s = blockIdx.x;
   const uint64_t pol = l2_policy(false);
-  double dot = 0.0;
-  for (int64_t s = blockIdx.x; s < n_slices; s += gridDim.x) {
-    const int64_t b0 = sell_base[s];
-    const int len = (int)((sell_base[s + 1] - b0) >> 5);
-    const int32_t* cp = col + b0 + lane;
-    const float* vp = sval + b0 * DD + lane;
-    float y[D];
+  const int64_t b0 = sell_base[s];
+  const int len = (int)((sell_base[s + 1] - b0) >> 5);
+  const int32_t* cp = col + b0 + lane;
+  const float* vp = sval + b0 * DD + lane;
+  float y[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) y[c] = 0.f;
+  for (int c = 0; c < D; ++c) y[c] = 0.f;
 #pragma unroll 2
-    for (int k = w; k < len; k += kSellW) {
-      const int64_t cc = ld_l2(cp + (int64_t)k * 32, pol);
-      const float* vk = vp + (int64_t)k * DD * 32;
-      float m[DD];
+  for (int k = w; k < len; k += kSellW) {
+    const int64_t cc = ld_l2(cp + (int64_t)k * 32, pol);
+    const float* vk = vp + (int64_t)k * DD * 32;
+    float m[DD];
 #pragma unroll
-      for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, pol);
-      float xv[D];
+    for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, pol);
+    float xv[D];
 #pragma unroll
-      for (int j = 0; j < D; ++j) xv[j] = v[cc * D + j];
+    for (int j = 0; j < D; ++j) xv[j] = v[cc * D + j];
 #pragma unroll
-      for (int r = 0; r < D; ++r)
+    for (int r = 0; r < D; ++r)
 #pragma unroll
-        for (int j = 0; j < D; ++j) y[r] = fmaf(m[r * D + j], xv[j], y[r]);
-    }
+      for (int j = 0; j < D; ++j) y[r] = fmaf(m[r * D + j], xv[j], y[r]);
+  }
 #pragma unroll
-    for (int c = 0; c < D; ++c) ys[w][c][lane] = y[c];
-    __syncthreads();
-    if (w == 0) {
-      const int64_t i = s * 32 + lane;
-      if (i < n_rows) {
-        float yt[D];
+  for (int c = 0; c < D; ++c) ys[w][c][lane] = y[c];
+  __syncthreads();
+  double dot = 0.0;
+  if (w == 0) {
+    const int64_t i = s * 32 + lane;
+    if (i < n_rows) {
+      float yt[D];
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-          float t = ys[0][c][lane];
+      for (int c = 0; c < D; ++c) {
+        float t = ys[0][c][lane];
 #pragma unroll
-          for (int u = 1; u < kSellW; ++u) t += ys[u][c][lane];
-          yt[c] = t;
-        }
-        dot += op_epilogue<D, MODE>(a, i, yt);
+        for (int u = 1; u < kSellW; ++u) t += ys[u][c][lane];
+        yt[c] = t;
       }
+      dot = op_epilogue<D, MODE>(a, i, yt);
     }
-    __syncthreads();
   }
   if constexpr (op_has_dot<MODE>()) {
     const double bsum = block_sum(dot, red);
@@ -1082,14 +1081,25 @@ __global__ void __launch_bounds__(kRowT) k_csr_op(int64_t n, const int64_t* __re
   double dot = 0.0;
   for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
     if (t < kRowItems) {
+      constexpr int U = 4;  // passes whose loads are in flight together
       float y = 0.f;
       const int64_t e1 = ptr[i + 1];
-      for (int64_t e = ptr[i] + u; e < e1; e += PB) {
-        const int64_t c = ld_l2(col + e, pol);
-        const float* m = val + e * B * B + r * B;
-        const float* xv = v + c * B;
+      for (int64_t e = ptr[i] + u; e < e1; e += U * PB) {
+        int64_t c[U];
 #pragma unroll
-        for (int q = 0; q < B; ++q) y = fmaf(ld_l2(m + q, pol), xv[q], y);
+        for (int w = 0; w < U; ++w) c[w] = e + w * PB < e1 ? (int64_t)ld_l2(col + e + w * PB, pol) : -1;
+        float m[U][B], xv[U][B];
+#pragma unroll
+        for (int w = 0; w < U; ++w)
+#pragma unroll
+          for (int q = 0; q < B; ++q) {
+            m[w][q] = c[w] >= 0 ? ld_l2(val + (e + w * PB) * B * B + r * B + q, pol) : 0.f;
+            xv[w][q] = c[w] >= 0 ? v[c[w] * B + q] : 0.f;
+          }
+#pragma unroll
+        for (int w = 0; w < U; ++w)
+#pragma unroll
+          for (int q = 0; q < B; ++q) y = fmaf(m[w][q], xv[w][q], y);
       }
       part[t] = y;
     }
@@ -1162,7 +1172,19 @@ __device__ __forceinline__ void restrict_row(int64_t I, const int64_t* __restric
   for (int k = 0; k < K; ++k) acc[k] = 0.f;
   for (int64_t e = pt_ptr[I] + tid; e < pt_ptr[I + 1]; e += NT) {
     const int64_t i = pt_row[e];
-    const float* pv = pt_val + e * BF * K;
+    float pv[BF * K];
+    if constexpr ((BF * K) % 2 == 0) {  // BF K even: the block start is 8-byte aligned
+      const float2* pv2 = reinterpret_cast<const float2*>(pt_val + e * BF * K);
+#pragma unroll
+      for (int c = 0; c < BF * K / 2; ++c) {
+        const float2 t2 = pv2[c];
+        pv[2 * c] = t2.x;
+        pv[2 * c + 1] = t2.y;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < BF * K; ++c) pv[c] = pt_val[e * BF * K + c];
+    }
 #pragma unroll
     for (int q = 0; q < BF; ++q) {
       const float rv = rf[i * BF + q];
@@ -1224,8 +1246,19 @@ __global__ void __launch_bounds__(256) k_prolong(int64_t n, const int64_t* __res
   for (int64_t e = p_ptr[i]; e < p_ptr[i + 1]; ++e) {
     const float* pv = p_val + e * BF * K + r * K;
     const float* cv = xc + (int64_t)p_col[e] * K;
+    if constexpr (K % 2 == 0) {  // K even: the row start (e BF K + r K floats) is 8-byte aligned
+      const float2* p2 = reinterpret_cast<const float2*>(pv);
+      const float2* c2 = reinterpret_cast<const float2*>(cv);
 #pragma unroll
-    for (int k = 0; k < K; ++k) s = fmaf(pv[k], cv[k], s);
+      for (int k = 0; k < K / 2; ++k) {
+        const float2 a2 = p2[k], b2 = c2[k];
+        s = fmaf(a2.x, b2.x, s);
+        s = fmaf(a2.y, b2.y, s);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < K; ++k) s = fmaf(pv[k], cv[k], s);
+    }
   }
   x[t] += s;
 }
@@ -1953,7 +1986,9 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
   h->ctrl = h->alloc<AmgCtrl>(1, st);
   h->lzc = h->alloc<AmgCtrl>(1, st);
   h->lz = h->alloc<double>(2 * kLanczos + 2, st);
-  h->partial = h->alloc<double>(2 * kPartialLen, st);
+  // per-CTA partial sums: the level-0 SpMV grid has one CTA per slice
+  const int64_t n_partial = std::max<int64_t>(kPartialLen, (n0 + 31) / 32 + 1);
+  h->partial = h->alloc<double>(2 * n_partial, st);
   double* origin = h->alloc<double>(3, st);
   if (!h->active || !h->status || !h->counter || !h->ctrl || !h->lzc || !h->lz || !h->partial || !origin)
     return check_cuda("AMG buffers");
@@ -2063,7 +2098,7 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
     const int64_t ns = (L.n + 31) / 32;
     const bool timed = h->ev_ready && h->ev_used < fem_amg::kTimed;
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used], st);
-    k_sell_op<B0, MODE><<<capped(ns, 16), kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
+    k_sell_op<B0, MODE><<<(unsigned)ns, kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used++ + 1], st);
   } else {
     k_csr_op<K, MODE><<<capped(L.n, 16), kRowT, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
@@ -2091,9 +2126,11 @@ int lanczos_level(fem_amg* h, int l, int b0, cudaStream_t st, double* rho) {
     if (l == 0) {
       const int64_t ns = (n + 31) / 32;
       if (b0 == 3)
-        k_sell_op<3, kOpLzQ><<<capped(ns, 16), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val, a);
+        k_sell_op<3, kOpLzQ><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
+                                                                          a);
       else
-        k_sell_op<2, kOpLzQ><<<capped(ns, 16), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val, a);
+        k_sell_op<2, kOpLzQ><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
+                                                                          a);
     } else {
       k_csr_op<B, kOpLzQ><<<capped(n, 16), kRowT, 0, st>>>(n, L.a_ptr, L.a_col, L.a_val, a);
     }
