@@ -987,11 +987,18 @@ __host__ __device__ constexpr bool op_has_dot() {
   return MODE == kOpS4Dot || MODE == kOpQ || MODE == kOpLzQ;
 }
 
-// Level 0: the sliced FP32 matrix (the layout of fem_assemble_sell): one CTA
-// per slice of 32 rows, thread per row, the kSellW warps sharing the slice's
-// slots (short dependent chains), partial rows summed in shared memory in a
-// fixed order.  The grid covers every slice, so the hardware balances the
-// tail.  The matrix streams with L2 evict_first; the vectors stay in L2.
+// Level 0: the sliced FP32 matrix (the layout of fem_assemble_sell): a CTA
+// takes kSellSpc<MODE> consecutive slices of 32 rows, thread per row, the
+// kSellW warps sharing each slice's slots (short dependent chains), partial
+// rows summed in shared memory in a fixed order.  The grid covers every
+// slice, so the hardware balances the tail; the modes that end in a grid
+// reduction take several slices per CTA so that few CTAs arrive at it.  The
+// matrix streams with L2 evict_first; the vectors stay in L2.
+template <int MODE>
+__host__ __device__ constexpr int kSellSpc() {
+  return op_has_dot<MODE>() ? 8 : 1;
+}
+
 template <int D, int MODE>
 __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const int64_t* __restrict__ sell_base,
                                                          const int32_t* __restrict__ col,
@@ -1002,8 +1009,11 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   if (amg_idle(a.ctrl)) return;
   const float* __restrict__ v = op_operand<MODE>(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t s = blockIdx.x;
+  const int64_t n_slices = (n_rows + 31) >> 5;
   const uint64_t pol = l2_policy(false);
+  double dot = 0.0;
+  const int64_t s_end = ((int64_t)blockIdx.x + 1) * kSellSpc<MODE>();
+  for (int64_t s = (int64_t)blockIdx.x * kSellSpc<MODE>(); s < (s_end < n_slices ? s_end : n_slices); ++s) {
   const int64_t b0 = sell_base[s];
   const int len = (int)((sell_base[s + 1] - b0) >> 5);
   const int32_t* cp = col + b0 + lane;
@@ -1029,7 +1039,6 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
 #pragma unroll
   for (int c = 0; c < D; ++c) ys[w][c][lane] = y[c];
   __syncthreads();
-  double dot = 0.0;
   if (w == 0) {
     const int64_t i = s * 32 + lane;
     if (i < n_rows) {
@@ -1041,8 +1050,10 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
         for (int u = 1; u < kSellW; ++u) t += ys[u][c][lane];
         yt[c] = t;
       }
-      dot = op_epilogue<D, MODE>(a, i, yt);
+      dot += op_epilogue<D, MODE>(a, i, yt);
     }
+  }
+  __syncthreads();
   }
   if constexpr (op_has_dot<MODE>()) {
     const double bsum = block_sum(dot, red);
@@ -2098,7 +2109,8 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
     const int64_t ns = (L.n + 31) / 32;
     const bool timed = h->ev_ready && h->ev_used < fem_amg::kTimed;
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used], st);
-    k_sell_op<B0, MODE><<<(unsigned)ns, kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
+    k_sell_op<B0, MODE><<<grid_for(ns, kSellSpc<MODE>()), kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col,
+                                                                                 h->sell_val, a);
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used++ + 1], st);
   } else {
     k_csr_op<K, MODE><<<capped(L.n, 16), kRowT, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
@@ -2126,10 +2138,10 @@ int lanczos_level(fem_amg* h, int l, int b0, cudaStream_t st, double* rho) {
     if (l == 0) {
       const int64_t ns = (n + 31) / 32;
       if (b0 == 3)
-        k_sell_op<3, kOpLzQ><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
+        k_sell_op<3, kOpLzQ><<<grid_for(ns, kSellSpc<kOpLzQ>()), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
                                                                           a);
       else
-        k_sell_op<2, kOpLzQ><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
+        k_sell_op<2, kOpLzQ><<<grid_for(ns, kSellSpc<kOpLzQ>()), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
                                                                           a);
     } else {
       k_csr_op<B, kOpLzQ><<<capped(n, 16), kRowT, 0, st>>>(n, L.a_ptr, L.a_col, L.a_val, a);
