@@ -233,6 +233,18 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_profile_step(args):
+    """For a launch list: the cube's set-up, --warmup mixed steps, then
+    exactly one more (the one a summary describes)."""
+    dev = torch.device("cuda", 0)
+    m, forces = cube_workload(args.n, dev)
+    for _ in range(max(args.warmup, 0) + 1):
+        step(m, forces, "mixed", args.stol, args.precond)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "step", "n": args.n, "warmup": args.warmup, "preconditioner": args.precond,
+                      "cg_iterations": m.last_solve.iterations}))
+
+
 def run_profile(args):
     """A short, fixed launch sequence for ncu: setup, one assembly, then
     exactly --profile-iters CG iterations of the chosen precision."""
@@ -269,8 +281,9 @@ def main():
     ap.add_argument("--stol", type=float, default=1e-10)
     ap.add_argument("--cpu-n", type=int, default=24, help="cube size of the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
-    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
-                    help="profiling mode: assemble one system and run --profile-iters CG iterations")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "step"], default=None,
+                    help="profiling mode: assemble one system and run --profile-iters CG iterations "
+                         "(mixed, fp64), or --warmup steps and then exactly one step (step)")
     ap.add_argument("--profile-iters", type=int, default=20)
     ap.add_argument("--cg-path", choices=["persistent", "persistent-regs", "kernels"], default="persistent")
     ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
@@ -279,6 +292,9 @@ def main():
     torch.set_default_dtype(torch.float64)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile == "step":
+        run_profile_step(args)
         return
     if args.profile:
         run_profile(args)
