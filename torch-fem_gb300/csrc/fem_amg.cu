@@ -30,6 +30,8 @@
 // Determinism: no floating-point atomics; every sum runs in a fixed order and
 // the aggregation priorities are fixed, so hierarchy and iterates are identical
 // run to run.
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -131,6 +133,24 @@ __device__ __forceinline__ void block_mv(const float* __restrict__ m, const floa
 #pragma unroll
     for (int c = 0; c < B; ++c) s = fmaf(m[a * B + c], v[c], s);
     out[a] = s;
+  }
+}
+
+// N FP16 values to FP32 (4-byte loads when N is even: callers keep the start
+// 4-byte aligned).
+template <int N>
+__device__ __forceinline__ void load_half(const __half* __restrict__ src, float (&dst)[N]) {
+  if constexpr (N % 2 == 0) {
+    const __half2* s2 = reinterpret_cast<const __half2*>(src);
+#pragma unroll
+    for (int c = 0; c < N / 2; ++c) {
+      const float2 f = __half22float2(s2[c]);
+      dst[2 * c] = f.x;
+      dst[2 * c + 1] = f.y;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < N; ++c) dst[c] = __half2float(src[c]);
   }
 }
 
@@ -540,65 +560,6 @@ struct OpView {
   }
 };
 
-// Slot of v in the warp's sorted list s[0..m) (v is present).
-__device__ __forceinline__ int find_slot(const int32_t* s, int m, int32_t v) {
-  const int lane = threadIdx.x & 31;
-  for (int b0 = 0; b0 < m; b0 += 32) {
-    const bool hit = b0 + lane < m && s[b0 + lane] == v;
-    const unsigned bal = __ballot_sync(0xffffffffu, hit);
-    if (bal) return b0 + __ffs(bal) - 1;
-  }
-  return -1;
-}
-
-// P = T - w D^-1 A T, warp per fine row, accumulators in shared memory.
-template <int B, int K, bool kSell>
-__global__ void __launch_bounds__(128) k_p_numeric(Graph g, OpView<B, kSell> A, const float* __restrict__ dinv,
-                                                   const int32_t* __restrict__ agg, const float* __restrict__ tval,
-                                                   const int64_t* __restrict__ p_ptr, const int32_t* __restrict__ p_col,
-                                                   float* __restrict__ p_val, float omega) {
-  constexpr int BK = B * K;
-  __shared__ int32_t cols[4][kMaxPRow];
-  __shared__ float acc[4][kMaxPRow][BK];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t i = (int64_t)blockIdx.x * 4 + w;
-  if (i >= g.n) return;
-  const int64_t e0 = p_ptr[i];
-  const int m = (int)(p_ptr[i + 1] - e0);
-  if (m == 0) return;
-  for (int s = lane; s < m; s += 32) cols[w][s] = p_col[e0 + s];
-  for (int t = lane; t < m * BK; t += 32) acc[w][t / BK][t % BK] = 0.f;
-  __syncwarp();
-  const int64_t nb = g.ptr[i];
-  const int deg = (int)(g.ptr[i + 1] - nb);
-  for (int kk = 0; kk < deg; ++kk) {
-    const int32_t j = g.idx[nb + kk];
-    const int32_t aj = agg[j];
-    if (aj < 0) continue;
-    const int s = find_slot(cols[w], m, aj);
-    if (s < 0) continue;  // cannot happen: the row lists every neighbour's aggregate
-    for (int c = lane; c < BK; c += 32) {
-      const int r = c / K, k = c % K;
-      float v = acc[w][s][c];
-#pragma unroll
-      for (int q = 0; q < B; ++q) v = fmaf(A.at(i, kk, r * B + q), tval[((int64_t)j * B + q) * K + k], v);
-      acc[w][s][c] = v;
-    }
-    __syncwarp();
-  }
-  const int32_t ai = agg[i];
-  for (int s = 0; s < m; ++s) {
-    for (int c = lane; c < BK; c += 32) {
-      const int r = c / K, k = c % K;
-      float v = 0.f;
-#pragma unroll
-      for (int q = 0; q < B; ++q) v = fmaf(dinv[(i * B + r) * B + q], acc[w][s][q * K + k], v);
-      const float t = cols[w][s] == ai ? tval[(i * B + r) * K + k] : 0.f;
-      p_val[(e0 + s) * BK + c] = t - omega * v;
-    }
-  }
-}
-
 // Slot of v in the sorted list s[0..m) by binary search (v is present).
 __device__ __forceinline__ int bsearch_slot(const int32_t* s, int m, int32_t v) {
   int lo = 0, hi = m - 1;
@@ -608,6 +569,93 @@ __device__ __forceinline__ int bsearch_slot(const int32_t* s, int m, int32_t v) 
     else hi = mid;
   }
   return (m > 0 && s[lo] == v) ? lo : -1;
+}
+
+// P = T - w D^-1 A T by contribution lists: block (i, J) of A T is the sum
+// over the neighbours j of i (ascending) with aggregate J of A_ij T_j.  The
+// lists (neighbour slots) are built once with the pattern; a group of 8 lanes
+// sums one block's list in registers, reduces in a fixed order, then applies
+// D_i^-1 and subtracts from T (T_iJ is nonzero only for J = agg(i)).
+template <bool kFill>
+__global__ void k_p_lists(Graph g, const int32_t* __restrict__ agg, const int64_t* __restrict__ p_ptr,
+                          const int32_t* __restrict__ p_col, int64_t* __restrict__ cnt, int64_t* __restrict__ cursor,
+                          int32_t* __restrict__ cl_k, int32_t* __restrict__ row) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const int64_t p0 = p_ptr[i];
+  const int m = (int)(p_ptr[i + 1] - p0);
+  if (kFill)
+    for (int s = 0; s < m; ++s) row[p0 + s] = (int32_t)i;
+  if (m == 0) return;
+  const int64_t nb = g.ptr[i];
+  const int deg = (int)(g.ptr[i + 1] - nb);
+  for (int kk = 0; kk < deg; ++kk) {
+    const int32_t a = agg[g.idx[nb + kk]];
+    if (a < 0) continue;
+    const int s = bsearch_slot(p_col + p0, m, a);
+    if (s < 0) continue;  // cannot happen: the row lists every neighbour's aggregate
+    if (!kFill) cnt[p0 + s] += 1;
+    else cl_k[cursor[p0 + s]++] = kk;
+  }
+}
+
+template <int B, int K, bool kSell>
+__global__ void __launch_bounds__(256) k_p_numeric(int64_t n_slots, Graph g, OpView<B, kSell> A,
+                                                   const float* __restrict__ dinv, const int32_t* __restrict__ agg,
+                                                   const float* __restrict__ tval, const int64_t* __restrict__ cl_ptr,
+                                                   const int32_t* __restrict__ cl_k, const int32_t* __restrict__ row,
+                                                   const int32_t* __restrict__ p_col, float* __restrict__ p_val,
+                                                   float omega) {
+  constexpr int BK = B * K;
+  const int g8 = threadIdx.x & 7;
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const bool live = s < n_slots;
+  float acc[BK];
+#pragma unroll
+  for (int c = 0; c < BK; ++c) acc[c] = 0.f;
+  int64_t i = 0;
+  if (live) {
+    i = row[s];
+    const int64_t nb = g.ptr[i];
+    for (int64_t e = cl_ptr[s] + g8; e < cl_ptr[s + 1]; e += 8) {
+      const int kk = cl_k[e];
+      const int64_t j = g.idx[nb + kk];
+      const float* tv = tval + j * BK;
+      float a[B * B], tr[BK];
+#pragma unroll
+      for (int c = 0; c < B * B; ++c) a[c] = A.at(i, kk, c);
+#pragma unroll
+      for (int c = 0; c < BK; ++c) tr[c] = tv[c];
+#pragma unroll
+      for (int r = 0; r < B; ++r)
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+#pragma unroll
+          for (int q = 0; q < B; ++q) acc[r * K + k] = fmaf(a[r * B + q], tr[q * K + k], acc[r * K + k]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < BK; ++c) {
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 4);
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 2);
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 1);
+  }
+  if (live) {
+    const bool own = p_col[s] == agg[i];
+    for (int c = g8; c < BK; c += 8) {
+      const int r = c / K, k = c % K;
+      float v = 0.f;
+#pragma unroll
+      for (int q = 0; q < B; ++q) {
+        float aq = 0.f;
+#pragma unroll
+        for (int t = 0; t < BK; ++t) aq = t == q * K + k ? acc[t] : aq;
+        v = fmaf(dinv[(i * B + r) * B + q], aq, v);
+      }
+      const float t0 = own ? tval[i * BK + c] : 0.f;
+      p_val[s * BK + c] = t0 - omega * v;
+    }
+  }
 }
 
 // A P by contribution lists: block (i, J) of W = A P is the sum over the
@@ -878,7 +926,7 @@ __global__ void __launch_bounds__(1024) k_coarse_inverse(int64_t n, int K, const
 }
 
 // ================================================================== solve ==
-enum { kOpS1 = 1, kOpS2, kOpS3, kOpS4, kOpS4Dot, kOpQ, kOpLzQ };
+enum { kOpS1 = 1, kOpS2, kOpS3, kOpS4, kOpS4Dot, kOpQ, kOpLzQ, kOpQc };
 
 // Level vectors of the V-cycle and the CG scalars the fused kernels touch.
 struct OpArgs {
@@ -890,7 +938,7 @@ struct OpArgs {
   float* db;
   const float* dinv;
   float theta_inv, c1, c2;
-  const float* p;  // kOpQ / kOpLzQ operand
+  float* p;        // kOpQ / kOpLzQ operand; kOpQc updates it
   float* q;
   double* partial;
   AmgCtrl* ctrl;
@@ -902,6 +950,7 @@ __device__ __forceinline__ const float* op_operand(const OpArgs& a) {
   if constexpr (MODE == kOpS1 || MODE == kOpS4 || MODE == kOpS4Dot) return a.d;
   else if constexpr (MODE == kOpS2) return a.db;
   else if constexpr (MODE == kOpS3) return a.x;
+  else if constexpr (MODE == kOpQc) return a.xb;  // z, the preconditioned residual
   else return a.p;
 }
 
@@ -947,6 +996,18 @@ __device__ __forceinline__ double op_epilogue(const OpArgs& a, int64_t i, const 
       a.xb[o + c] = z;
       if constexpr (MODE == kOpS4Dot) dot += (double)a.f[o + c] * (double)z;
     }
+  } else if constexpr (MODE == kOpQc) {
+    // direction update folded into the product: p = z + beta p and
+    // q = A z + beta q, which carries A p by recurrence between restarts
+    const float beta = (float)a.ctrl->beta;
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+      const float pn = a.xb[o + c] + beta * a.p[o + c];
+      const float qn = y[c] + beta * a.q[o + c];
+      a.p[o + c] = pn;
+      a.q[o + c] = qn;
+      dot += (double)pn * (double)qn;
+    }
   } else {
 #pragma unroll
     for (int c = 0; c < B; ++c) {
@@ -972,7 +1033,7 @@ __device__ __forceinline__ void op_finish(const OpArgs& a, double tot) {
       c->rz = tot;
       c->pscale = 1.0;
     }
-  } else if constexpr (MODE == kOpQ || MODE == kOpLzQ) {
+  } else if constexpr (MODE == kOpQ || MODE == kOpLzQ || MODE == kOpQc) {
     if (!isfinite(tot)) c->done = kNonFinite;
     else if (tot == 0.0 || (MODE == kOpLzQ && tot < 0.0)) c->done = kBreakdown;
     else {
@@ -984,7 +1045,7 @@ __device__ __forceinline__ void op_finish(const OpArgs& a, double tot) {
 
 template <int MODE>
 __host__ __device__ constexpr bool op_has_dot() {
-  return MODE == kOpS4Dot || MODE == kOpQ || MODE == kOpLzQ;
+  return MODE == kOpS4Dot || MODE == kOpQ || MODE == kOpLzQ || MODE == kOpQc;
 }
 
 // Level 0: the sliced FP32 matrix (the layout of fem_assemble_sell): a CTA
@@ -1174,7 +1235,7 @@ __global__ void __launch_bounds__(kRowT) k_csr_op(int64_t n, const int64_t* __re
 // of the coarse level: d = D^-1 f / theta, x = d.
 template <int BF, int K, int NT>
 __device__ __forceinline__ void restrict_row(int64_t I, const int64_t* __restrict__ pt_ptr,
-                                             const int32_t* __restrict__ pt_row, const float* __restrict__ pt_val,
+                                             const int32_t* __restrict__ pt_row, const __half* __restrict__ pt_val,
                                              const float* __restrict__ rf, float (&red)[NT / 32][K], float* fout) {
   const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) % (NT / 32);
   const int tid = threadIdx.x % NT;
@@ -1184,18 +1245,7 @@ __device__ __forceinline__ void restrict_row(int64_t I, const int64_t* __restric
   for (int64_t e = pt_ptr[I] + tid; e < pt_ptr[I + 1]; e += NT) {
     const int64_t i = pt_row[e];
     float pv[BF * K];
-    if constexpr ((BF * K) % 2 == 0) {  // BF K even: the block start is 8-byte aligned
-      const float2* pv2 = reinterpret_cast<const float2*>(pt_val + e * BF * K);
-#pragma unroll
-      for (int c = 0; c < BF * K / 2; ++c) {
-        const float2 t2 = pv2[c];
-        pv[2 * c] = t2.x;
-        pv[2 * c + 1] = t2.y;
-      }
-    } else {
-#pragma unroll
-      for (int c = 0; c < BF * K; ++c) pv[c] = pt_val[e * BF * K + c];
-    }
+    load_half<BF * K>(pt_val + e * BF * K, pv);
 #pragma unroll
     for (int q = 0; q < BF; ++q) {
       const float rv = rf[i * BF + q];
@@ -1220,7 +1270,7 @@ __device__ __forceinline__ void restrict_row(int64_t I, const int64_t* __restric
 
 template <int BF, int K>
 __global__ void __launch_bounds__(128) k_restrict(int64_t n_c, const int64_t* __restrict__ pt_ptr,
-                                                  const int32_t* __restrict__ pt_row, const float* __restrict__ pt_val,
+                                                  const int32_t* __restrict__ pt_row, const __half* __restrict__ pt_val,
                                                   const float* __restrict__ rf, OpArgs c, const AmgCtrl* ctrl) {
   __shared__ float red[4][K];
   __shared__ float fs[K];
@@ -1242,10 +1292,10 @@ __global__ void __launch_bounds__(128) k_restrict(int64_t n_c, const int64_t* __
 }
 
 // Prolongation x += P x_c, one thread per (fine row, component): the
-// threads of a row read adjacent rows of its blocks.
+// threads of a row read adjacent rows of its blocks (the FP16 copy of P).
 template <int BF, int K>
 __global__ void __launch_bounds__(256) k_prolong(int64_t n, const int64_t* __restrict__ p_ptr,
-                                                 const int32_t* __restrict__ p_col, const float* __restrict__ p_val,
+                                                 const int32_t* __restrict__ p_col, const __half* __restrict__ p_val,
                                                  const float* __restrict__ xc, float* __restrict__ x,
                                                  const AmgCtrl* ctrl) {
   if (amg_idle(ctrl)) return;
@@ -1255,34 +1305,29 @@ __global__ void __launch_bounds__(256) k_prolong(int64_t n, const int64_t* __res
   const int r = (int)(t - i * BF);
   float s = 0.f;
   for (int64_t e = p_ptr[i]; e < p_ptr[i + 1]; ++e) {
-    const float* pv = p_val + e * BF * K + r * K;
+    float pv[K];
+    load_half<K>(p_val + e * BF * K + r * K, pv);  // 4-byte aligned when K is even
     const float* cv = xc + (int64_t)p_col[e] * K;
-    if constexpr (K % 2 == 0) {  // K even: the row start (e BF K + r K floats) is 8-byte aligned
-      const float2* p2 = reinterpret_cast<const float2*>(pv);
-      const float2* c2 = reinterpret_cast<const float2*>(cv);
 #pragma unroll
-      for (int k = 0; k < K / 2; ++k) {
-        const float2 a2 = p2[k], b2 = c2[k];
-        s = fmaf(a2.x, b2.x, s);
-        s = fmaf(a2.y, b2.y, s);
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < K; ++k) s = fmaf(pv[k], cv[k], s);
-    }
+    for (int k = 0; k < K; ++k) s = fmaf(pv[k], cv[k], s);
   }
   x[t] += s;
 }
 
-// P^T values in transposed order: block e of P^T is block pt_pos[e] of P.
-__global__ void k_transpose_vals(int64_t n_e, int bk, const int64_t* __restrict__ pt_pos,
-                                 const float* __restrict__ p_val, float* __restrict__ pt_val) {
+// FP16 copies of P for the V-cycle's transfers: p_h in P order (the
+// prolongation) and pt_h in transposed order (block e of P^T is block
+// pt_pos[e] of P, the restriction).  Both transfers use the same rounded P,
+// so the V-cycle stays symmetric; the Galerkin product uses the FP32 P.
+__global__ void k_transfer_copies(int64_t n_e, int bk, const int64_t* __restrict__ pt_pos,
+                                  const float* __restrict__ p_val, __half* __restrict__ p_h,
+                                  __half* __restrict__ pt_h) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_e * bk) return;
   const int64_t e = t / bk;
   const int c = (int)(t - e * bk);
   const int64_t pos = pt_pos[e];
-  pt_val[t] = pos >= 0 ? p_val[pos * bk + c] : 0.f;
+  pt_h[t] = __float2half_rn(pos >= 0 ? p_val[pos * bk + c] : 0.f);
+  p_h[t] = __float2half_rn(p_val[t]);
 }
 
 // Restriction onto the coarsest level and its dense solve, one CTA: warps
@@ -1290,7 +1335,7 @@ __global__ void k_transpose_vals(int64_t n_e, int bk, const int64_t* __restrict_
 template <int BF, int K>
 __global__ void __launch_bounds__(1024) k_coarse_solve(int64_t n_c, const int64_t* __restrict__ pt_ptr,
                                                        const int32_t* __restrict__ pt_row,
-                                                       const float* __restrict__ pt_val, const float* __restrict__ rf,
+                                                       const __half* __restrict__ pt_val, const float* __restrict__ rf,
                                                        const float* __restrict__ inv, float* __restrict__ xc,
                                                        const AmgCtrl* ctrl) {
   __shared__ float fs[kCoarseMaxDof];
@@ -1302,7 +1347,8 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(int64_t n_c, const int64_
     for (int k = 0; k < K; ++k) acc[k] = 0.f;
     for (int64_t e = pt_ptr[I] + lane; e < pt_ptr[I + 1]; e += 32) {
       const int64_t i = pt_row[e];
-      const float* pv = pt_val + e * BF * K;
+      float pv[BF * K];
+      load_half<BF * K>(pt_val + e * BF * K, pv);
 #pragma unroll
       for (int q = 0; q < BF; ++q) {
         const float rv = rf[i * BF + q];
@@ -1663,7 +1709,8 @@ struct AmgLevel {
   int64_t* pt_ptr = nullptr;
   int32_t* pt_row = nullptr;
   int64_t* pt_pos = nullptr;
-  float* pt_val = nullptr;  // P values in transposed order (restriction)
+  __half* pt_val = nullptr;  // FP16 P values in transposed order (restriction)
+  __half* p_h = nullptr;     // FP16 P values in P order (prolongation)
   int64_t* ap_ptr = nullptr;
   int32_t* ap_col = nullptr;
   float* ap_val = nullptr;
@@ -1678,6 +1725,10 @@ struct AmgLevel {
   int32_t* cl_p = nullptr;    // P block of each contribution
   int32_t* cl_w = nullptr;    // A P block of each contribution
   int32_t* slot_row = nullptr;  // [C.a_nnz] coarse row of each block
+  // contribution lists of the blocks of A T (smoothed prolongator)
+  int64_t* tl_ptr = nullptr;  // [p_nnz + 1]
+  int32_t* tl_k = nullptr;    // neighbour slot of each contribution
+  int32_t* p_row = nullptr;   // [p_nnz] fine row of each block
   // smoother
   double rho = 0.0;
   float theta_inv = 0.f, c1 = 0.f, c2 = 0.f;
@@ -1880,6 +1931,24 @@ int patterns(fem_amg* h, int l, cudaStream_t st) {
   if (!L.p_col) return check_cuda("AMG P pattern");
   k_p_rows<true><<<gn, kT, 0, st>>>(L.g, active, L.agg, nullptr, L.p_ptr, L.p_col, h->status);
   note_launch();
+  {  // contribution lists of A T, in ascending neighbour per block
+    L.p_row = h->alloc<int32_t>(L.p_nnz, st);
+    int64_t* tcnt = h->alloc<int64_t>(L.p_nnz + 1, st);
+    L.tl_ptr = h->alloc<int64_t>(L.p_nnz + 1, st);
+    int64_t* tcur = h->alloc<int64_t>(L.p_nnz + 1, st);
+    if (!L.p_row || !tcnt || !L.tl_ptr || !tcur) return check_cuda("AMG A T lists");
+    cudaMemsetAsync(tcnt, 0, sizeof(int64_t) * (L.p_nnz + 1), st);
+    k_p_lists<false><<<gn, kT, 0, st>>>(L.g, L.agg, L.p_ptr, L.p_col, tcnt, nullptr, nullptr, nullptr);
+    note_launch();
+    int64_t n_tl = 0;
+    rc = scan_total(h, tcnt, L.tl_ptr, L.p_nnz, &n_tl, st);
+    if (rc) return rc;
+    L.tl_k = h->alloc<int32_t>(n_tl, st);
+    if (!L.tl_k) return check_cuda("AMG A T lists");
+    cudaMemcpyAsync(tcur, L.tl_ptr, sizeof(int64_t) * (L.p_nnz + 1), cudaMemcpyDeviceToDevice, st);
+    k_p_lists<true><<<gn, kT, 0, st>>>(L.g, L.agg, L.p_ptr, L.p_col, nullptr, tcur, L.tl_k, L.p_row);
+    note_launch();
+  }
   // P^T
   L.pt_ptr = h->alloc<int64_t>(na + 1, st);
   int64_t* cur = h->alloc<int64_t>(na + 1, st);
@@ -2045,9 +2114,10 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
     const int64_t nv = L.n * L.b;
     if (k + 1 < h->n_levels) {
       L.p_val = h->alloc<float>(L.p_nnz * L.b * K, st);
-      L.pt_val = h->alloc<float>(L.p_nnz * L.b * K, st);
+      L.pt_val = h->alloc<__half>(L.p_nnz * L.b * K, st);
+      L.p_h = h->alloc<__half>(L.p_nnz * L.b * K, st);
       L.ap_val = h->alloc<float>(L.ap_nnz * L.b * K, st);
-      if (!L.p_val || !L.pt_val || !L.ap_val) return check_cuda("AMG transfer storage");
+      if (!L.p_val || !L.pt_val || !L.p_h || !L.ap_val) return check_cuda("AMG transfer storage");
     }
     if (k >= 1) {
       L.a_val = h->alloc<float>(L.a_nnz * K * K, st);
@@ -2081,7 +2151,7 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
 }
 
 // ---------------------------------------------------------------- numeric --
-template <int B>
+// The V-cycle vectors, block inverse and Chebyshev coefficients of level l.
 OpArgs level_args(fem_amg* h, int l, AmgCtrl* ctrl) {
   AmgLevel& L = h->L[l];
   OpArgs a{};
@@ -2118,8 +2188,10 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
   note_launch();
 }
 
+// Spectral estimate of D^-1 A on level l (block size B) by kLanczos CG-Lanczos
+// steps; the level's V-cycle vectors serve as scratch.
 template <int B>
-int lanczos_level(fem_amg* h, int l, int b0, cudaStream_t st, double* rho) {
+int lanczos_level(fem_amg* h, int l, cudaStream_t st, double* rho) {
   AmgLevel& L = h->L[l];
   const int64_t n = L.n;
   const float* dinv = l == 0 ? h->dinv0 : L.dinv;
@@ -2127,7 +2199,6 @@ int lanczos_level(fem_amg* h, int l, int b0, cudaStream_t st, double* rho) {
   const unsigned g = capped(grid_for(n, kT), 8);
   k_lz_init<B><<<g, kT, 0, st>>>(n, dinv, L.r, L.d, L.db, h->partial, h->lzc);
   note_launch();
-  (void)b0;
   OpArgs a{};
   a.p = L.db;
   a.q = L.x;
@@ -2135,17 +2206,16 @@ int lanczos_level(fem_amg* h, int l, int b0, cudaStream_t st, double* rho) {
   a.ctrl = h->lzc;
   a.lz = h->lz;
   for (int j = 0; j < kLanczos; ++j) {
-    if (l == 0) {
-      const int64_t ns = (n + 31) / 32;
-      if (b0 == 3)
-        k_sell_op<3, kOpLzQ><<<grid_for(ns, kSellSpc<kOpLzQ>()), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
-                                                                          a);
-      else
-        k_sell_op<2, kOpLzQ><<<grid_for(ns, kSellSpc<kOpLzQ>()), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
-                                                                          a);
-    } else {
-      k_csr_op<B, kOpLzQ><<<capped(n, 16), kRowT, 0, st>>>(n, L.a_ptr, L.a_col, L.a_val, a);
+    bool sliced = false;
+    if constexpr (B <= 3) {  // level 0 (B = dim) holds the sliced matrix
+      if (l == 0) {
+        const int64_t ns = (n + 31) / 32;
+        k_sell_op<B, kOpLzQ><<<grid_for(ns, kSellSpc<kOpLzQ>()), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col,
+                                                                                      h->sell_val, a);
+        sliced = true;
+      }
     }
+    if (!sliced) k_csr_op<B, kOpLzQ><<<capped(n, 16), kRowT, 0, st>>>(n, L.a_ptr, L.a_col, L.a_val, a);
     note_launch();
     k_lz_update<B><<<g, kT, 0, st>>>(n, dinv, L.r, L.d, L.x, h->partial, h->lzc, h->lz);
     note_launch();
@@ -2189,7 +2259,7 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
     double rho = 0.0;
-    int rc = l == 0 ? lanczos_level<B0>(h, l, B0, st, &rho) : lanczos_level<K>(h, l, B0, st, &rho);
+    int rc = l == 0 ? lanczos_level<B0>(h, l, st, &rho) : lanczos_level<K>(h, l, st, &rho);
     if (rc) return rc;
     L.rho = rho;
     const double lo = kChebLo * rho, hi = kChebHi * rho;
@@ -2201,8 +2271,9 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
     const float omega = (float)(kOmega / rho);
     if (l == 0) {
       OpView<B0, true> Av{h->sell_base, h->sell_val};
-      k_p_numeric<B0, K, true><<<grid_for(L.n, 4), 128, 0, st>>>(L.g, Av, h->dinv0, L.agg, L.tval, L.p_ptr, L.p_col,
-                                                                 L.p_val, omega);
+      k_p_numeric<B0, K, true><<<grid_for(L.p_nnz * 8, 256), 256, 0, st>>>(L.p_nnz, L.g, Av, h->dinv0, L.agg, L.tval,
+                                                                            L.tl_ptr, L.tl_k, L.p_row, L.p_col,
+                                                                            L.p_val, omega);
       note_launch();
       k_ap_numeric<B0, K, true><<<grid_for(L.ap_nnz * 8, 256), 256, 0, st>>>(L.ap_nnz, Av, L.wl_ptr, L.wl_k, L.wl_p,
                                                                             L.ap_row, L.p_val, L.ap_val);
@@ -2212,8 +2283,9 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
       note_launch();
     } else {
       OpView<K, false> Av{L.a_ptr, L.a_val};
-      k_p_numeric<K, K, false><<<grid_for(L.n, 4), 128, 0, st>>>(L.g, Av, L.dinv, L.agg, L.tval, L.p_ptr, L.p_col,
-                                                                 L.p_val, omega);
+      k_p_numeric<K, K, false><<<grid_for(L.p_nnz * 8, 256), 256, 0, st>>>(L.p_nnz, L.g, Av, L.dinv, L.agg, L.tval,
+                                                                            L.tl_ptr, L.tl_k, L.p_row, L.p_col,
+                                                                            L.p_val, omega);
       note_launch();
       k_ap_numeric<K, K, false><<<grid_for(L.ap_nnz * 8, 256), 256, 0, st>>>(L.ap_nnz, Av, L.wl_ptr, L.wl_k, L.wl_p,
                                                                             L.ap_row, L.p_val, L.ap_val);
@@ -2222,8 +2294,8 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
                                                                     L.ap_val, L.slot_row, C.a_col, C.a_val);
       note_launch();
     }
-    k_transpose_vals<<<grid_for(L.p_nnz * L.b * K, kT), kT, 0, st>>>(L.p_nnz, L.b * K, L.pt_pos, L.p_val,
-                                                                     L.pt_val);
+    k_transfer_copies<<<grid_for(L.p_nnz * L.b * K, kT), kT, 0, st>>>(L.p_nnz, L.b * K, L.pt_pos, L.p_val, L.p_h,
+                                                                      L.pt_val);
     note_launch();
     k_block_inv<K><<<grid_for(C.n, kT), kT, 0, st>>>(C.n, C.a_ptr, C.a_col, C.a_val, C.dinv, h->status);
     note_launch();
@@ -2246,7 +2318,7 @@ void launch_vcycle(fem_amg* h, cudaStream_t st) {
   for (int l = 0; l < last; ++l) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
-    const OpArgs a = level_args<B0>(h, l, h->ctrl);
+    const OpArgs a = level_args(h, l, h->ctrl);
     launch_op<B0, K, kOpS1>(h, l, a, st);
     launch_op<B0, K, kOpS2>(h, l, a, st);
     if (l + 1 == last) {
@@ -2257,7 +2329,7 @@ void launch_vcycle(fem_amg* h, cudaStream_t st) {
         k_coarse_solve<K, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, h->coarse_inv, C.xb,
                                                  h->ctrl);
     } else {
-      const OpArgs c = level_args<K>(h, l + 1, h->ctrl);
+      const OpArgs c = level_args(h, l + 1, h->ctrl);
       const unsigned g = capped(C.n, 64);
       if (l == 0) k_restrict<B0, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
       else k_restrict<K, K><<<g, 128, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, c, h->ctrl);
@@ -2268,11 +2340,11 @@ void launch_vcycle(fem_amg* h, cudaStream_t st) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
     if (l == 0)
-      k_prolong<B0, K><<<grid_for(L.n * B0, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+      k_prolong<B0, K><<<grid_for(L.n * B0, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_h, C.xb, L.x, h->ctrl);
     else
-      k_prolong<K, K><<<grid_for(L.n * K, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_val, C.xb, L.x, h->ctrl);
+      k_prolong<K, K><<<grid_for(L.n * K, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_h, C.xb, L.x, h->ctrl);
     note_launch();
-    const OpArgs a = level_args<B0>(h, l, h->ctrl);
+    const OpArgs a = level_args(h, l, h->ctrl);
     launch_op<B0, K, kOpS3>(h, l, a, st);
     if (l == 0) launch_op<B0, K, kOpS4Dot>(h, l, a, st);
     else launch_op<B0, K, kOpS4>(h, l, a, st);
@@ -2281,16 +2353,14 @@ void launch_vcycle(fem_amg* h, cudaStream_t st) {
 
 template <int B0, int K>
 void launch_iteration(fem_amg* h, cudaStream_t st) {
-  const int64_t n = h->L[0].n * B0;
   launch_vcycle<B0, K>(h, st);
-  k_pup<<<capped(grid_for(n, kT), 8), kT, 0, st>>>(n, h->z, h->p, h->ctrl);
-  note_launch();
   OpArgs a{};
   a.p = h->p;
   a.q = h->q;
+  a.xb = h->z;
   a.partial = h->partial;
   a.ctrl = h->ctrl;
-  launch_op<B0, K, kOpQ>(h, 0, a, st);
+  launch_op<B0, K, kOpQc>(h, 0, a, st);
   k_cg_update<B0><<<capped(grid_for(h->L[0].n, kT), 8), kT, 0, st>>>(h->L[0].n, h->xlo, h->rcg, h->p, h->q, h->dinv0,
                                                                       h->L[0].theta_inv, h->L[0].d, h->L[0].x,
                                                                       h->partial, h->ctrl);
@@ -2333,6 +2403,7 @@ int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, d
   cudaMemsetAsync(x, 0, sizeof(double) * n, st);
   cudaMemsetAsync(h->xlo, 0, sizeof(float) * n, st);
   cudaMemsetAsync(h->p, 0, sizeof(float) * n, st);
+  cudaMemsetAsync(h->q, 0, sizeof(float) * n, st);  // q carries A p: finite before the first beta = 0 update
   const unsigned gv = capped(grid_for(nn, kT), 8);
   k_cg_bnorm<<<capped(grid_for(n, kT), 8), kT, 0, st>>>(n, b, rtol * rtol, h->partial, h->ctrl);
   note_launch();
