@@ -151,3 +151,35 @@ def test_preconditioner_resolution(monkeypatch):
         resolve_preconditioner("ilu", "mixed", 3)
     monkeypatch.setenv("TORCHFEM_GB300_PRECOND", "jacobi")
     assert resolve_preconditioner(None, "mixed", 3) == "jacobi"
+
+
+def test_default_multigrid_falls_back_to_block_jacobi():
+    """A hierarchy that cannot be built (here: a fake device mesh that refuses
+    it) falls back to block Jacobi when the preconditioner was the default,
+    and raises when it was asked for by name."""
+    import torch
+
+    from torchfem_gb300 import _lib
+    from torchfem_gb300.sparse import SolveContext
+
+    class FakeMesh:
+        def __init__(self):
+            self.calls = []
+
+        def build_system(self, mesh, mat, con_mask, precision, keep_refs=(), precond="jacobi"):
+            self.calls.append(precond)
+            if precond == "amg":
+                raise _lib.FemError(_lib.FEM_BOUNDS, "fem_amg_create: a row exceeds its size limit")
+            return "system-" + precond
+
+    con = torch.zeros(6, dtype=torch.uint8)
+    sc = SolveContext(FakeMesh(), con, 1, "mixed", 10, 1e-8, 1e-6, 1e-10, None)
+    sc.precond = "amg"
+    with pytest.warns(RuntimeWarning, match="block Jacobi"):
+        assert sc.build_system(None, None, ()) == "system-jacobi"
+    assert sc.precond == "jacobi" and sc.dm.calls == ["amg", "jacobi"]
+
+    sc = SolveContext(FakeMesh(), con, 1, "mixed", 10, 1e-8, 1e-6, 1e-10, None)
+    sc.precond, sc.precond_explicit = "amg", True
+    with pytest.raises(_lib.FemError):
+        sc.build_system(None, None, ())

@@ -55,9 +55,7 @@ class NLContext(SolveContext):
     def tangent_system(self, tangent, thickness):
         mesh = self.dm.make_mesh(thickness)
         mat = _lib.FemMaterial(_lib.FEM_MAT_TANGENT_IP, tangent.data_ptr())
-        self.system = self.dm.build_system(mesh, mat, self.con_mask, self.precision,
-                                           keep_refs=(tangent, thickness, mesh, mat),
-                                           precond=self.precond if self.precision == "mixed" else "jacobi")
+        self.system = self.build_system(mesh, mat, keep_refs=(tangent, thickness, mesh, mat))
         self.system_key = None
         return self.system
 

@@ -249,6 +249,7 @@ class FEM:
         sc.verbose = verbose
         sc.linear = "minres" if method == "minres" else "cg"
         sc.precond = pc
+        sc.precond_explicit = preconditioner is not None
         self.last_solve = sc
 
         shape_ip = (dm.nip, self.n_elem, *self.n_flux)

@@ -19,6 +19,7 @@ increment, with its own kernel-based backward.
 from __future__ import annotations
 
 import ctypes as C
+import warnings
 
 import torch
 from torch import Tensor
@@ -51,6 +52,7 @@ class SolveContext:
         self.inner_rtol = 1e-6
         self.linear = "cg"  # or "minres" (FP64 path)
         self.precond = "jacobi"  # or "amg" (mixed precision)
+        self.precond_explicit = False  # the caller asked for this preconditioner by name
         # FP64 replacement threshold of the multigrid CG: each V-cycle cuts the
         # residual severalfold, so replacements are spaced by a deeper drop
         self.amg_delta = 1e-4
@@ -62,16 +64,34 @@ class SolveContext:
         mat = _lib.FemMaterial(self.mat_kind, mat_data.data_ptr())
         return mesh, mat
 
+    def build_system(self, mesh, mat, keep_refs) -> LinearSystem:
+        """The device system of one tangent with this context's preconditioner.
+        A multigrid hierarchy that cannot be built for this mesh (a row over its
+        size caps, a coarsening that stalls, a singular coarse block) falls back
+        to block Jacobi with a warning when the preconditioner was the default;
+        a preconditioner asked for by name raises instead."""
+        from . import _lib
+
+        precond = self.precond if self.precision == "mixed" else "jacobi"
+        try:
+            return self.dm.build_system(mesh, mat, self.con_mask, self.precision, keep_refs=keep_refs,
+                                        precond=precond)
+        except (_lib.FemError, ValueError) as err:
+            if precond != "amg" or self.precond_explicit:
+                raise
+            warnings.warn(f"multigrid preconditioner unavailable for this mesh ({err}); using block Jacobi",
+                          RuntimeWarning, stacklevel=2)
+            self.precond = "jacobi"
+            return self.dm.build_system(mesh, mat, self.con_mask, self.precision, keep_refs=keep_refs,
+                                        precond="jacobi")
+
     def get_system(self, mat_data: Tensor, thickness: Tensor | None) -> LinearSystem:
         """The condensed tangent for these material data (built once per solve,
         as the reference keeps self.K for a constant-tangent material)."""
         key = (mat_data.data_ptr(), None if thickness is None else thickness.data_ptr())
         if self.system is None or self.system_key != key:
             mesh, mat = self.structs(mat_data, thickness)
-            self.system = self.dm.build_system(
-                mesh, mat, self.con_mask, self.precision, keep_refs=(mat_data, thickness, mesh, mat),
-                precond=self.precond if self.precision == "mixed" else "jacobi",
-            )
+            self.system = self.build_system(mesh, mat, keep_refs=(mat_data, thickness, mesh, mat))
             self.system_key = key
         return self.system
 
