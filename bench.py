@@ -20,6 +20,10 @@ plain_fp64 the FP64 Jacobi-CG path (scalar CSR in the reference pattern).
 mixed_block_jacobi  the mixed path with block Jacobi (the persistent CG
            kernel), reported beside the headline.
 
+`--workload heat` times the heat-conduction path instead (SolidHeat,
+steady FP64 solve + adjoint gradient w.r.t. the per-element conductivity)
+and prints its own line; the headline is the elastic cube.
+
 `--impl reference` times the CPU oracle (a restatement of torch-fem's CPU
 path: numpy assembly + scipy Jacobi-CG) on a bounded sample of the same
 workload, because torch-fem itself is Python that cannot be run where the
@@ -233,6 +237,131 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+HEAT_METRIC = "heat solve+grad s per 1M DOF (FP64 Jacobi-CG + adjoint)"
+
+
+def heat_workload(n: int, device):
+    """SolidHeat on the jittered n^3 Hexa1 cube: conductivity U(1, 2) per
+    element (seed 1), T = 0 on the x = 0 face, uniform source 1/n_nodes."""
+    from torchfem_gb300 import SolidHeat, mesh
+    from torchfem_gb300.materials import IsotropicConductivity3D
+
+    nodes, el = mesh.cube_hexa(n + 1, n + 1, n + 1)
+    gen = torch.Generator().manual_seed(0)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen, dtype=torch.float64) * 2 - 1) * (0.1 / n)
+    kappa = 1.0 + torch.rand(len(el), generator=torch.Generator().manual_seed(1), dtype=torch.float64)
+    x0 = nodes[:, 0] == 0.0
+    m = SolidHeat(nodes.to(device), el.to(device), IsotropicConductivity3D(kappa.to(device)))
+    m.constraints[x0.to(device)] = True
+    q = torch.full((len(nodes), 1), 1.0 / len(nodes), dtype=torch.float64, device=device)
+    return m, kappa.to(device), q, (nodes.numpy(), el.numpy(), kappa.numpy(), x0.numpy())
+
+
+def heat_step(m, kappa0, q, stol):
+    from torchfem_gb300.materials import IsotropicConductivity3D
+
+    kappa = kappa0.detach().requires_grad_(True)
+    m.material = IsotropicConductivity3D(kappa)
+    m.heat_flux = q
+    T, f, flux, _, _ = m.solve(stol=stol, differentiable_parameters=kappa)
+    (g,) = torch.autograd.grad(T.sum(), kappa)
+    return T, f, flux, g
+
+
+def heat_cpu_baseline(n_sample: int):
+    """The heat oracle's solve + adjoint (numpy assembly, scipy Jacobi-CG to
+    1e-10) on a smaller cube of the same kind, scaled linearly to 1M DOF."""
+    from oracle import heat_oracle as H
+
+    _, _, _, (nodes, el, kappa, x0) = heat_workload_host(n_sample)
+    t0 = time.perf_counter()
+    om = H.HeatModel(nodes, el, kappa[:, None, None] * np.eye(3))
+    om.solve(np.full(len(nodes), 1.0 / len(nodes)), x0, method="cg", rtol=1e-10)
+    om.adjoint(np.ones(len(nodes)), method="cg", rtol=1e-10)
+    t = time.perf_counter() - t0
+    return {"value": t / (len(nodes) / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"heat oracle (numpy assembly + scipy Jacobi-CG, rtol 1e-10, solve + adjoint) on the {n_sample}^3 "
+                      f"jittered Hexa1 cube ({len(nodes)} DOF), scaled linearly to 1M DOF"}
+
+
+def heat_workload_host(n: int):
+    """The inputs of heat_workload(n) as numpy arrays (no device)."""
+    from torchfem_gb300 import mesh
+
+    nodes_t, el_t = mesh.cube_hexa(n + 1, n + 1, n + 1)
+    gen = torch.Generator().manual_seed(0)
+    inner = ((nodes_t > 0) & (nodes_t < 1)).all(1)
+    nodes_t = nodes_t + inner[:, None] * (torch.rand(nodes_t.shape, generator=gen, dtype=torch.float64) * 2 - 1) * (0.1 / n)
+    kappa = 1.0 + torch.rand(len(el_t), generator=torch.Generator().manual_seed(1), dtype=torch.float64)
+    return None, None, None, (nodes_t.numpy(), el_t.numpy(), kappa.numpy(), (nodes_t[:, 0] == 0.0).numpy())
+
+
+def run_heat(args):
+    """Steady heat conduction: --warmup untimed and --steps timed steps of
+    solve + adjoint on the n^3 cube (n = --heat-n), CUDA events on the
+    launching stream; roofline of the FP64 CSR SpMV inside the CG."""
+    from torchfem_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    lib = _lib.load()
+    m, kappa, q, _ = heat_workload(args.heat_n, dev)
+    for _ in range(max(args.warmup, 0)):
+        heat_step(m, kappa, q, args.stol)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    lib.fem_set_timing(1)
+    spmv_ms, spmv_n, iters = 0.0, 0, []
+    launches0 = lib.fem_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            heat_step(m, kappa, q, args.stol)
+            st = m.last_solve
+            iters.append(st.iterations)
+            spmv_ms += st.system.stats.spmv_ms
+            spmv_n += st.system.stats.spmv_timed
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.fem_launch_count() - launches0
+    lib.fem_set_timing(0)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    dm = m.device_mesh
+    n_dofs = m.n_dofs
+    if lib.fem_get_cg_path() in (1, 2):
+        # events around each persistent CG launch, spmv_n its iterations: one
+        # FP64 Jacobi-CG iteration reads the CSR matrix once (8-byte value and
+        # int32 column per entry, int64 row pointers), twelve FP64 vector
+        # streams and the inverse diagonal
+        sb = dm.nnz * 12 + (n_dofs + 1) * 8 + 13 * 8 * n_dofs
+        kernel_name = "persistent FP64 Jacobi-CG kernel (one iteration)"
+    else:
+        # scalar FP64 CSR SpMV: values and int32 columns once, row pointers, x read once, y written
+        sb = dm.nnz * 12 + (n_dofs + 1) * 8 + 2 * n_dofs * 8
+        kernel_name = "k_spmv_csr (FP64 CSR SpMV of the Jacobi CG)"
+    unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
+    achieved = sb / unit_s / 1e9 if unit_s else None
+    peak, peak_kind = measured_peak_hbm()
+    line = {
+        "metric": HEAT_METRIC, "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered cube)",
+        "config": {"workload": f"solidheat_hexa1_cube_{args.heat_n}^3_jittered_steady_solve+adjoint",
+                   "dofs": n_dofs, "nnz": dm.nnz, "n_elem": m.n_elem, "stol": args.stol,
+                   "l2": "inputs larger than L2 (FP64 K = %.0f MB)" % (dm.nnz * 12 / 1e6)},
+        "cg_iterations": iters, "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": None, "algorithmic_bytes": sb,
+                     "avg_unit_us": unit_s * 1e6 if unit_s else None, "peak_source": peak_kind},
+        "clocks": clocks.summary(),
+        "cpu_baseline": heat_cpu_baseline(args.heat_cpu_n),
+    }
+    print(json.dumps(line))
+
+
 def run_profile_step(args):
     """For a launch list: the cube's set-up, --warmup mixed steps, then
     exactly one more (the one a summary describes)."""
@@ -288,10 +417,16 @@ def main():
     ap.add_argument("--cg-path", choices=["persistent", "persistent-regs", "kernels"], default="persistent")
     ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
                     help="preconditioner of the mixed-precision headline")
+    ap.add_argument("--workload", choices=["elastic", "heat"], default="elastic")
+    ap.add_argument("--heat-n", type=int, default=100, help="elements per cube edge of the heat workload")
+    ap.add_argument("--heat-cpu-n", type=int, default=30, help="cube size of the heat CPU baseline sample")
     args = ap.parse_args()
     torch.set_default_dtype(torch.float64)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "heat":
+        run_heat(args)
         return
     if args.profile == "step":
         run_profile_step(args)

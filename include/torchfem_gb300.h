@@ -73,7 +73,9 @@ enum {
                              Covers IsotropicElasticity3D / PlaneStrain and, with effective
                              constants, PlaneStress (materials/elasticity.py:44-241). */
   FEM_MAT_GENERAL = 2,    /* [n_elem][dim^4] full tangent C_iJkL per element. */
-  FEM_MAT_TANGENT_IP = 3  /* [nip][n_elem][dim^4] tangent per integration point. */
+  FEM_MAT_TANGENT_IP = 3, /* [nip][n_elem][dim^4] tangent per integration point. */
+  FEM_MAT_CONDUCTIVITY = 16 /* [n_elem][dim][dim] conductivity (heat conduction); the
+                               fem_heat_* kernels take the array itself. */
 };
 
 enum { FEM_F64 = 0, FEM_F32 = 1 };
@@ -155,6 +157,8 @@ typedef struct fem_mesh {
   const int64_t* inc_ptr;  /* [n_nod+1] node->element incidence */
   const int32_t* inc;      /* [n_elem*n_e] */
   const double* thickness; /* [n_elem] planar thickness, NULL for solids */
+  int dof_per_node;        /* DOFs per node of the field (0: the element's dimension; 1 for
+                              heat conduction) */
 } fem_mesh;
 
 typedef struct fem_material {
@@ -213,6 +217,50 @@ int fem_element_vjp(const fem_mesh* mesh, const fem_material* mat, const double*
                     const double* sigma_prev, const double* de0, const double* g,
                     const double* gflux, const double* ghgrad, double* gsig, double* gmat,
                     double* gthick, double* gde0, double* gve, int32_t* status, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Heat conduction: one temperature DOF per node (mesh->dof_per_node = 1).  */
+/* ------------------------------------------------------------------------ */
+/* kappa [n_elem][dim][dim] is the conductivity tensor of the Fourier law of
+ * materials/conductivity.py:80-99 (flux = flux_prev + kappa (grad_inc -
+ * de0), tangent kappa).  Point arrays (flux_prev, flux, hgrad, gflux, ...)
+ * are [nip][n_elem][dim], the reference's [n_int][n_elem][1][dim]. */
+
+/* Element conductivity matrices k_ab = sum_ip w detJ t B_a . kappa B_b
+ * [n_elem][n_e][n_e] in out_dtype: the stiffness part of
+ * Heat.integrate_material (base.py:1177-1286) with compute_k
+ * (solid.py:52-54, planar.py:86-88); also Heat.k0 (base.py:228-245). */
+int fem_heat_stiffness(const fem_mesh* mesh, const double* kappa, int out_dtype, void* ke,
+                       int32_t* status, void* stream);
+
+/* Nodal heat fluxes of a temperature increment v [n_nod] (constrained
+ * entries replaced per con_mode as in fem_element_force): f_a = sum_ip w
+ * detJ t B_a . flux (compute_f, solid.py:56-58, planar.py:90-92), with the
+ * updated point fluxes (flux) and the gradient increments (hgrad) as
+ * optional outputs (base.py:1236-1262).  de0 [n_elem][dim] may be NULL. */
+int fem_heat_force(const fem_mesh* mesh, const double* kappa, const double* v,
+                   const uint8_t* con_mask, const double* con_values, int con_mode,
+                   const double* flux_prev, const double* de0, double* fe, double* flux,
+                   double* hgrad, int32_t* status, void* stream);
+
+/* Vector-Jacobian product of fem_heat_force: cotangents g (assembled heat
+ * fluxes [n_nod]), gflux and ghgrad (point outputs) pulled back to flux_prev
+ * (gflux_prev), kappa (gkappa [n_elem][dim][dim]), the thickness (gthick),
+ * de0 (gde0 [n_elem][dim]) and the element temperatures (gve [n_elem][n_e],
+ * gather with fem_gather_nodal).  Every output is nullable. */
+int fem_heat_vjp(const fem_mesh* mesh, const double* kappa, const double* v,
+                 const uint8_t* con_mask, const double* con_values, int con_mode,
+                 const double* flux_prev, const double* de0, const double* g, const double* gflux,
+                 const double* ghgrad, double* gflux_prev, double* gkappa, double* gthick,
+                 double* gde0, double* gve, void* stream);
+
+/* Element capacity (mass) matrices m_ab = sum_ip w detJ t rho N_a N_b
+ * [n_elem][n_e][n_e] of FEM.integrate_mass (base.py:376-396) with compute_m
+ * (solid.py:60-62, planar.py:94-96) for one DOF per node; rho [n_elem],
+ * nval [nip][n_e] the shape-function values at the integration points. */
+int fem_heat_mass(const fem_mesh* mesh, const double* rho, const double* nval, int out_dtype,
+                  void* me, int32_t* status, void* stream);
+
 
 /* ------------------------------------------------------------------------ */
 /* Nonlinear material points fused with element integration.                */
@@ -341,6 +389,24 @@ typedef struct fem_solve_info {
   double spmv_ms;          /* summed CUDA-event time of the SpMV launches (timing on) */
   int64_t spmv_timed;      /* number of SpMV launches in spmv_ms */
 } fem_solve_info;
+
+/* out = a x + b y over nnz stored values of two matrices with one pattern:
+ * the Crank-Nicolson system M + dt/2 K of Heat.time_integration
+ * (base.py:1519-1521) from the assembled capacity and conductivity values. */
+int fem_csr_combine(int64_t nnz, double a, const double* x, double b, const double* y,
+                    double* out, void* stream);
+
+/* Crank-Nicolson residual of one time-step Newton iteration
+ * (base.py:1486-1495): res = M du + half_dt (f_old + f_int + f_ext), zero
+ * where con_mask is set, and sumsq = ||res||^2 (fixed summation order).  M is
+ * the assembled FP64 CSR capacity matrix (fem_matrix of format
+ * FEM_FMT_CSR_F64); f_old and f_ext are nullable (zero).  ws holds
+ * fem_heat_cn_workspace_bytes(M->n) bytes. */
+size_t fem_heat_cn_workspace_bytes(int64_t n);
+int fem_heat_cn_residual(const fem_matrix* M, const double* du, const double* f_old,
+                         const double* f_int, const double* f_ext, double half_dt,
+                         const uint8_t* con_mask, double* res, double* sumsq, void* ws,
+                         size_t ws_bytes, void* stream);
 
 /* Turns CUDA-event timing of the CG on (1) or off (0).  With the persistent
  * CG (default) spmv_ms covers whole iterations and spmv_timed counts them;

@@ -411,6 +411,99 @@ def make_hexa2(tf):
     )
 
 
+def make_heat(tf):
+    """Heat conduction: a jittered 4^3 SolidHeat with per-element
+    conductivity, a PlanarHeat with thickness rho^3 and a rotated orthotropic
+    PlanarHeat (temperatures, heat fluxes, element conductivity matrices and
+    gradients of the thermal compliance f.T), and the Crank-Nicolson time
+    integration of the heated plate of tests/test_time_integration.py."""
+    from torchfem import PlanarHeat, SolidHeat
+    from torchfem.materials import (IsotropicConductivity2D, IsotropicConductivity3D,
+                                    OrthotropicConductivity2D)
+    from torchfem.mesh import cube_hexa, rect_quad
+
+    out = {}
+    # (a) SolidHeat, Hexa1, kappa per element, T = 0 on x = 0, uniform source
+    nodes, elements = cube_hexa(5, 5, 5)
+    nodes = jitter(nodes, 0.25, seed=3)
+    kappa = 400.0 * (1.0 + 0.5 * torch.rand(len(elements), generator=torch.Generator().manual_seed(4)))
+    kappa.requires_grad_(True)
+    model = SolidHeat(nodes, elements, IsotropicConductivity3D(kappa))
+    model.constraints[nodes[:, 0] == 0.0] = True
+    model.temperatures[nodes[:, 0] == 0.0, 0] = 1.0
+    q = torch.full((len(nodes), 1), 10.0 / len(nodes)).requires_grad_(True)
+    model.heat_flux = q
+    T, f, flux, grad, _ = model.solve(differentiable_parameters=(kappa, q))
+    L = torch.inner(f.ravel(), T.ravel())
+    g_kappa, g_q = torch.autograd.grad(L, (kappa, q))
+    with torch.no_grad():
+        k0 = model.k0()
+    out.update(solid_nodes=nodes.numpy(), solid_elements=elements.numpy(), solid_kappa=kappa.detach().numpy(),
+               solid_con=model.constraints.numpy(), solid_temp=model.temperatures.numpy(),
+               solid_q=q.detach().numpy(), solid_T=T.detach().numpy(), solid_f=f.detach().numpy(),
+               solid_flux=flux.detach().numpy(), solid_grad=grad.detach().numpy(), solid_L=L.detach().numpy(),
+               solid_g_kappa=g_kappa.numpy(), solid_g_q=g_q.numpy(), solid_k0=k0.numpy())
+
+    # (b) PlanarHeat, Quad1, thickness rho^3 per element, T = 0 west and north
+    nodes, elements = rect_quad(7, 5, 1.5, 1.0)
+    rho = 0.3 + 0.7 * torch.rand(len(elements), generator=torch.Generator().manual_seed(5), dtype=torch.float64)
+    rho.requires_grad_(True)
+    model = PlanarHeat(nodes, elements, IsotropicConductivity2D(kappa=400.0))
+    model.thickness = rho**3
+    west = torch.isclose(nodes[:, 0], nodes[:, 0].min())
+    north = torch.isclose(nodes[:, 1], nodes[:, 1].max())
+    model.constraints[west | north] = True
+    model.heat_flux[:, 0] = 1000.0 / len(nodes)
+    T, f, flux, grad, _ = model.solve(differentiable_parameters=rho)
+    L = torch.inner(f.ravel(), T.ravel())
+    (g_rho,) = torch.autograd.grad(L, rho)
+    out.update(planar_nodes=nodes.numpy(), planar_elements=elements.numpy(), planar_rho=rho.detach().numpy(),
+               planar_con=model.constraints.numpy(), planar_q=model.heat_flux.numpy(),
+               planar_T=T.detach().numpy(), planar_f=f.detach().numpy(), planar_flux=flux.detach().numpy(),
+               planar_L=L.detach().numpy(), planar_g_rho=g_rho.numpy())
+
+    # (c) rotated orthotropic conductivity on the same mesh, T prescribed on x = 0 and x = 1.5
+    c = torch.cos(torch.tensor(0.5)), torch.sin(torch.tensor(0.5))
+    R = torch.stack([torch.stack([c[0], -c[1]]), torch.stack([c[1], c[0]])])
+    mat = OrthotropicConductivity2D(50.0, 5.0).rotate(R)
+    model = PlanarHeat(nodes, elements, mat, thickness=0.1)
+    east = torch.isclose(nodes[:, 0], nodes[:, 0].max())
+    model.constraints[west | east] = True
+    model.temperatures[west, 0] = 10.0
+    model.temperatures[east, 0] = -5.0
+    T, f, flux, grad, _ = model.solve()
+    with torch.no_grad():
+        k0 = model.k0()
+    out.update(ortho_kappa=mat.KAPPA.numpy(), ortho_con=model.constraints.numpy(),
+               ortho_temp=model.temperatures.numpy(), ortho_T=T.numpy(), ortho_f=f.numpy(),
+               ortho_flux=flux.numpy(), ortho_grad=grad.numpy(), ortho_k0=k0.numpy())
+
+    # (d) transient: heated plate, Crank-Nicolson with dt = 1 to t = 24, and a
+    # late-starting output grid with dt = 0.5
+    def plate():
+        m = PlanarHeat(*rect_quad(5, 5, 1.0, 1.0), IsotropicConductivity2D(kappa=400.0, rho=1.0e5))
+        w = torch.isclose(m.nodes[:, 0], m.nodes[:, 0].min())
+        e = torch.isclose(m.nodes[:, 0], m.nodes[:, 0].max())
+        m.constraints[w | e] = True
+        m.temperatures[w, 0] = 5.0
+        m.temperatures[e, 0] = 20.0
+        return m
+
+    m = plate()
+    with torch.no_grad():
+        me = m.integrate_mass()
+    t_out = torch.tensor([0.0, 6.0, 12.0, 18.0, 24.0])
+    temp, rfl, flux, grad, _ = m.time_integration(t_out, delta_t=1.0)
+    out.update(plate_mass=me.numpy(), plate_t=t_out.numpy(), plate_temp=temp.numpy(), plate_f=rfl.numpy(),
+               plate_flux=flux.numpy(), plate_grad=grad.numpy())
+    m = plate()
+    t_late = torch.tensor([2.5, 5.0])
+    temp, rfl, flux, grad, _ = m.time_integration(t_late, delta_t=0.5, aggregate_integration_points=False)
+    out.update(late_t=t_late.numpy(), late_temp=temp.numpy(), late_f=rfl.numpy(), late_flux=flux.numpy(),
+               late_grad=grad.numpy())
+    np.savez_compressed(OUT / "heat_cases.npz", **out)
+
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
@@ -418,7 +511,7 @@ MAKERS = {
     "simp_full": lambda tf: make_simp(tf, 400, 200, "simp_400x200.npz", sample=20),
     "hyper": make_hyper, "plastic": make_plastic, "shell": make_shell,
     "plastic_full": lambda tf: make_plastic(tf, 256, 64, "plastic_ogrid_256x64.npz"),
-    "hexa2": make_hexa2,
+    "hexa2": make_hexa2, "heat": make_heat,
 }
 
 

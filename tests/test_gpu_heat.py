@@ -1,0 +1,149 @@
+"""GPU tests of the heat-conduction path (SolidHeat / PlanarHeat).
+
+Steady solves, their adjoint gradients and the Crank-Nicolson time
+integration against golden vectors produced by the reference itself
+(tests/golden/heat_cases.npz) and against the CPU oracle
+(oracle/heat_oracle.py) on a larger mesh.  FP64 throughout: temperatures,
+heat fluxes and gradients agree to 1e-8 relative (CG stopped at 1e-12).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import heat_oracle as H
+from torchfem_gb300 import PlanarHeat, SolidHeat, mesh
+from torchfem_gb300.materials import (IsotropicConductivity2D, IsotropicConductivity3D,
+                                      OrthotropicConductivity2D)
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-8
+
+
+def rel(a, b):
+    a = a.detach().cpu().double().numpy() if torch.is_tensor(a) else np.asarray(a)
+    b = np.asarray(b)
+    return float(np.abs(a.reshape(b.shape) - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_solid_heat_solve_and_gradients(cuda, golden):
+    g = golden("heat_cases.npz")
+    nodes = torch.tensor(g["solid_nodes"], device=cuda)
+    el = torch.tensor(g["solid_elements"], device=cuda)
+    kappa = torch.tensor(g["solid_kappa"], device=cuda, requires_grad=True)
+    model = SolidHeat(nodes, el, IsotropicConductivity3D(kappa))
+    model.constraints = torch.tensor(g["solid_con"], device=cuda)
+    model.temperatures = torch.tensor(g["solid_temp"], device=cuda)
+    q = torch.tensor(g["solid_q"], device=cuda, requires_grad=True)
+    model.heat_flux = q
+    T, f, flux, grad, state = model.solve(stol=1e-12, differentiable_parameters=(kappa, q))
+    assert T.shape == (len(nodes), 1) and flux.shape == (len(el), 3) and state.shape == (len(el), 0)
+    for name, out in (("T", T), ("f", f), ("flux", flux), ("grad", grad)):
+        assert rel(out, g[f"solid_{name}"]) < RTOL, name
+    L = torch.inner(f.ravel(), T.ravel())
+    assert rel(L, g["solid_L"]) < RTOL
+    gk, gq = torch.autograd.grad(L, (kappa, q))
+    assert rel(gk, g["solid_g_kappa"]) < RTOL
+    assert rel(gq, g["solid_g_q"]) < RTOL
+    assert rel(model.k0(), g["solid_k0"]) < 1e-13
+
+
+def test_planar_heat_thickness_gradient(cuda, golden):
+    g = golden("heat_cases.npz")
+    nodes = torch.tensor(g["planar_nodes"], device=cuda)
+    el = torch.tensor(g["planar_elements"], device=cuda)
+    rho = torch.tensor(g["planar_rho"], device=cuda, requires_grad=True)
+    model = PlanarHeat(nodes, el, IsotropicConductivity2D(kappa=400.0))
+    model.thickness = rho**3
+    model.constraints = torch.tensor(g["planar_con"], device=cuda)
+    model.heat_flux = torch.tensor(g["planar_q"], device=cuda)
+    T, f, flux, _, _ = model.solve(stol=1e-12, differentiable_parameters=rho)
+    assert rel(T, g["planar_T"]) < RTOL and rel(f, g["planar_f"]) < RTOL and rel(flux, g["planar_flux"]) < RTOL
+    L = torch.inner(f.ravel(), T.ravel())
+    (g_rho,) = torch.autograd.grad(L, rho)
+    assert rel(L, g["planar_L"]) < RTOL
+    assert rel(g_rho, g["planar_g_rho"]) < RTOL
+
+
+def test_planar_heat_rotated_orthotropic(cuda, golden):
+    g = golden("heat_cases.npz")
+    nodes = torch.tensor(g["planar_nodes"])
+    el = torch.tensor(g["planar_elements"])
+    c, s = np.cos(0.5), np.sin(0.5)
+    R = torch.tensor([[c, -s], [s, c]])
+    model = PlanarHeat(nodes, el, OrthotropicConductivity2D(50.0, 5.0).rotate(R), thickness=0.1)
+    model.constraints = torch.tensor(g["ortho_con"])
+    model.temperatures = torch.tensor(g["ortho_temp"])
+    T, f, flux, grad, _ = model.solve(stol=1e-12)
+    assert T.device.type == "cpu"  # results come back on the device of the nodes
+    for name, out in (("T", T), ("f", f), ("flux", flux), ("grad", grad), ("k0", model.k0())):
+        assert rel(out, g[f"ortho_{name}"]) < RTOL, name
+
+
+def _plate():
+    model = PlanarHeat(*mesh.rect_quad(5, 5, 1.0, 1.0), IsotropicConductivity2D(kappa=400.0, rho=1.0e5))
+    west = torch.isclose(model.nodes[:, 0], model.nodes[:, 0].min())
+    east = torch.isclose(model.nodes[:, 0], model.nodes[:, 0].max())
+    model.constraints[west | east] = True
+    model.temperatures[west, 0] = 5.0
+    model.temperatures[east, 0] = 20.0
+    return model
+
+
+def test_time_integration_heated_plate(cuda, golden):
+    g = golden("heat_cases.npz")
+    model = _plate()
+    assert rel(model.integrate_mass(), g["plate_mass"]) < 1e-13
+    temp, rfl, flux, grad, state = model.time_integration(torch.tensor(g["plate_t"]), delta_t=1.0, stol=1e-12)
+    assert temp.shape == (5, 25, 1) and flux.shape == (5, 16, 2) and state.shape == (5, 16, 0)
+    assert rel(temp, g["plate_temp"]) < RTOL
+    assert rel(rfl, g["plate_f"]) < RTOL
+    assert rel(flux, g["plate_flux"]) < RTOL
+    assert rel(grad, g["plate_grad"]) < RTOL
+    # late start, per-point outputs: integration still starts at t = 0
+    temp, rfl, flux, grad, _ = _plate().time_integration(torch.tensor(g["late_t"]), delta_t=0.5, stol=1e-12,
+                                                         aggregate_integration_points=False)
+    assert flux.shape == (2, 4, 16, 2)
+    for name, out in (("temp", temp), ("f", rfl), ("flux", flux), ("grad", grad)):
+        assert rel(out, g[f"late_{name}"]) < RTOL, name
+
+
+def test_time_integration_sparse_output_matches_dense(cuda):
+    """Fewer output times do not change the internal stepping
+    (tests/test_time_integration.py of the reference)."""
+    dense_t = torch.arange(0.0, 3.0 + 0.25, 0.25)
+    dense, *_ = _plate().time_integration(dense_t, 0.25, stol=1e-12)
+    sparse_t = torch.tensor([0.0, 0.5, 2.0, 3.0])
+    sparse, *_ = _plate().time_integration(sparse_t, 0.25, stol=1e-12)
+    rows = torch.searchsorted(dense_t.contiguous(), sparse_t)
+    assert torch.allclose(sparse, dense[rows], atol=1e-9)
+
+
+def test_solid_heat_larger_mesh_against_oracle(cuda):
+    """16^3 jittered Hexa1 cube, conductivity varying per element: temperatures
+    and the compliance gradient against the oracle."""
+    n = 16
+    nodes, el = mesh.cube_hexa(n + 1, n + 1, n + 1)
+    gen = torch.Generator().manual_seed(7)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen, dtype=torch.float64) * 2 - 1) * 0.1 / n
+    kappa = 1.0 + torch.rand(len(el), generator=gen, dtype=torch.float64)
+    kappa_g = kappa.clone().to(cuda).requires_grad_(True)
+    model = SolidHeat(nodes.to(cuda), el.to(cuda), IsotropicConductivity3D(kappa_g))
+    model.constraints[(nodes[:, 0] == 0.0).to(cuda)] = True
+    model.heat_flux[:] = 1.0 / len(nodes)
+    T, f, _, _, _ = model.solve(stol=1e-12, differentiable_parameters=kappa_g)
+    L = torch.inner(f.ravel(), T.ravel())
+    (gk,) = torch.autograd.grad(L, kappa_g)
+    om = H.HeatModel(nodes.numpy(), el.numpy(), kappa.numpy()[:, None, None] * np.eye(3))
+    To, fo, _, _ = om.solve(np.full(len(nodes), 1.0 / len(nodes)), (nodes[:, 0] == 0.0).numpy())
+    gko, _, _ = om.compliance_grads(To, fo)
+    assert rel(T, To) < RTOL and rel(f, fo) < RTOL
+    assert rel(gk, np.einsum("Eaa->E", gko)) < RTOL
+
+
+def test_heat_rejects_mixed_precision(cuda):
+    model = _plate()
+    with pytest.raises(NotImplementedError, match="FP64"):
+        model.solve(precision="mixed")

@@ -183,3 +183,58 @@ def test_default_multigrid_falls_back_to_block_jacobi():
     sc.precond, sc.precond_explicit = "amg", True
     with pytest.raises(_lib.FemError):
         sc.build_system(None, None, ())
+
+
+def test_heat_models_and_setters_like_reference():
+    """Heat boundary conditions validate like the reference
+    (tests/test_base.py TestHeatBoundaryConditions)."""
+    from torchfem_gb300 import PlanarHeat, SolidHeat
+    from torchfem_gb300.materials import IsotropicConductivity2D, IsotropicConductivity3D
+
+    model = PlanarHeat(*mesh.rect_quad(3, 3), IsotropicConductivity2D(kappa=400.0))
+    assert model.n_dof_per_node == 1 and model.n_flux == [1, 2]
+    assert model.constraints.shape == (9, 1)
+    for prop in ("heat_flux", "temperatures"):
+        value = torch.randn(model.n_nod, 1)
+        setattr(model, prop, value)
+        assert torch.equal(getattr(model, prop), value)
+        with pytest.raises(ValueError, match="same shape as nodes"):
+            setattr(model, prop, torch.zeros(model.n_nod, 2))
+        with pytest.raises(TypeError, match="floating-point"):
+            setattr(model, prop, torch.zeros(model.n_nod, 1, dtype=torch.int64))
+    solid = SolidHeat(*mesh.cube_hexa(3, 3, 3), IsotropicConductivity3D(400.0))
+    assert solid.n_flux == [1, 3] and solid.material.KAPPA.shape == (8, 3, 3)
+
+
+def test_heat_time_integration_validates_t_output():
+    from torchfem_gb300 import PlanarHeat
+    from torchfem_gb300.materials import IsotropicConductivity2D
+
+    model = PlanarHeat(*mesh.rect_quad(3, 3), IsotropicConductivity2D(kappa=400.0))
+    with pytest.raises(ValueError, match="at least one time"):
+        model.time_integration(torch.tensor([]))
+    with pytest.raises(ValueError, match="negative"):
+        model.time_integration(torch.tensor([-1.0, 1.0]))
+    with pytest.raises(ValueError, match="strictly increasing"):
+        model.time_integration(torch.tensor([0.0, 2.0, 2.0]))
+    kappa = torch.tensor(400.0, requires_grad=True)
+    with pytest.raises(NotImplementedError, match="gradients"):
+        PlanarHeat(*mesh.rect_quad(3, 3), IsotropicConductivity2D(kappa)).time_integration(
+            differentiable_parameters=kappa)
+
+
+def test_conductivity_kernel_data():
+    from torchfem_gb300 import _lib
+    from torchfem_gb300.materials import OrthotropicConductivity2D, OrthotropicConductivity3D
+
+    c, s = np.cos(0.3), np.sin(0.3)
+    R = torch.tensor([[c, -s], [s, c]])
+    mat = OrthotropicConductivity2D(3.0, 1.0).rotate(R).vectorize(4)
+    kind, data = mat.kernel_data(4)
+    assert kind == _lib.FEM_MAT_CONDUCTIVITY and data.shape == (4, 4)
+    expect = R @ torch.diag(torch.tensor([3.0, 1.0])) @ R.T
+    assert torch.allclose(data[2].view(2, 2), expect, rtol=1e-14, atol=0)
+    k3 = OrthotropicConductivity3D(1.0, 2.0, 3.0)
+    assert torch.equal(k3.KAPPA, torch.diag(torch.tensor([1.0, 2.0, 3.0])))
+    flux, _, tangent = k3.step(torch.ones(1, 3), None, torch.zeros(1, 3), None, torch.zeros(1, 3), None, 0)
+    assert torch.equal(flux, torch.tensor([[1.0, 2.0, 3.0]])) and tangent is k3.KAPPA

@@ -232,3 +232,60 @@ def test_amg_oracle_vcycle_symmetric_and_converges():
     x, it = AO.pcg(K, rhs, levels, rtol=1e-10)
     assert np.linalg.norm(rhs - K @ x) <= 1e-10 * np.linalg.norm(rhs)
     assert it <= 25
+
+
+# ------------------------------------------------------------ heat conduction --
+def _heat_rel(a, b):
+    return float(np.abs(np.asarray(a) - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_heat_oracle_steady(golden):
+    """Conductivity matrices, temperatures, heat fluxes and compliance
+    gradients of the heat oracle against the reference (heat_cases.npz)."""
+    from oracle import heat_oracle as H
+
+    g = golden("heat_cases.npz")
+    m = H.HeatModel(g["solid_nodes"], g["solid_elements"], g["solid_kappa"][:, None, None] * np.eye(3))
+    assert _heat_rel(m.conductivity(), g["solid_k0"]) < 1e-13
+    T, f, flux, gr = m.solve(g["solid_q"], g["solid_con"], g["solid_temp"])
+    for a, b in ((T, g["solid_T"]), (f, g["solid_f"]), (flux.mean(0), g["solid_flux"]), (gr.mean(0), g["solid_grad"])):
+        assert _heat_rel(a, b.reshape(a.shape)) < 1e-11
+    gk, _, gq = m.compliance_grads(T, f)
+    assert _heat_rel(np.einsum("Eaa->E", gk), g["solid_g_kappa"]) < 1e-9
+    assert _heat_rel(gq, g["solid_g_q"].ravel()) < 1e-11
+
+    rho = g["planar_rho"]
+    m = H.HeatModel(g["planar_nodes"], g["planar_elements"], 400.0 * np.eye(2), thickness=rho**3)
+    T, f, flux, _ = m.solve(g["planar_q"], g["planar_con"])
+    assert _heat_rel(T, g["planar_T"].ravel()) < 1e-12
+    assert _heat_rel(flux.mean(0), g["planar_flux"]) < 1e-12
+    _, gt, _ = m.compliance_grads(T, f)
+    assert _heat_rel(gt * 3 * rho**2, g["planar_g_rho"]) < 1e-11
+
+    m = H.HeatModel(g["planar_nodes"], g["planar_elements"], g["ortho_kappa"], thickness=0.1)
+    assert _heat_rel(m.conductivity(), g["ortho_k0"]) < 1e-13
+    T, f, flux, gr = m.solve(np.zeros(m.n_nod), g["ortho_con"], g["ortho_temp"])
+    assert _heat_rel(T, g["ortho_T"].ravel()) < 1e-12
+    assert _heat_rel(f, g["ortho_f"].ravel()) < 1e-12
+
+
+def test_heat_oracle_transient(golden):
+    """Capacity matrices and Crank-Nicolson time integration of the heat
+    oracle against the reference's heated plate."""
+    from oracle import heat_oracle as H
+
+    g = golden("heat_cases.npz")
+    nodes, el = O.rect_quad(5, 5, 1.0, 1.0)
+    m = H.HeatModel(nodes, el, 400.0 * np.eye(2), rho=1e5)
+    assert _heat_rel(m.capacity(), g["plate_mass"]) < 1e-13
+    w, e = np.isclose(nodes[:, 0], 0.0), np.isclose(nodes[:, 0], 1.0)
+    temp = np.where(w, 5.0, np.where(e, 20.0, 0.0))
+    T, f, flux, gr = H.time_integration(m, w | e, temp, np.zeros(len(nodes)), g["plate_t"], 1.0)
+    assert _heat_rel(T, g["plate_temp"][..., 0]) < 1e-12
+    assert _heat_rel(f, g["plate_f"][..., 0]) < 1e-12
+    assert _heat_rel(flux.mean(1), g["plate_flux"]) < 1e-12
+    times, rows = H.time_grid(g["late_t"], 0.5)
+    assert times[0] == 0.0 and list(rows) == [5, 10]
+    T, f, flux, gr = H.time_integration(m, w | e, temp, np.zeros(len(nodes)), g["late_t"], 0.5)
+    assert _heat_rel(T, g["late_temp"][..., 0]) < 1e-12
+    assert _heat_rel(flux, g["late_flux"]) < 1e-12

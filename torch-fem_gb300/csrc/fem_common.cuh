@@ -130,3 +130,29 @@ __device__ __forceinline__ double unit_scale(double norm2) {
     int _rc = ::tfg::check_cuda(where);              \
     if (_rc != FEM_OK) return _rc;                   \
   } while (0)
+
+// Element-type dispatch: TFG_BODY runs with NE (nodes), D (dimension) and
+// NIP (integration points) as compile-time constants.
+#define TFG_ETYPE_CASE(ID, NE_, D_, NIP_) \
+  case ID: {                              \
+    constexpr int NE = NE_;               \
+    constexpr int D = D_;                 \
+    constexpr int NIP = NIP_;             \
+    TFG_BODY;                             \
+  } break;
+
+#define TFG_DISPATCH_ETYPE(etype)                        \
+  switch (etype) {                                       \
+    TFG_ETYPE_CASE(FEM_QUAD1, 4, 2, 4)                   \
+    TFG_ETYPE_CASE(FEM_HEXA1, 8, 3, 8)                   \
+    TFG_ETYPE_CASE(FEM_TETRA2, 10, 3, 4)                 \
+    TFG_ETYPE_CASE(FEM_TETRA1, 4, 3, 1)                  \
+    TFG_ETYPE_CASE(FEM_TRIA1, 3, 2, 1)                   \
+    TFG_ETYPE_CASE(FEM_QUAD2, 8, 2, 4)                   \
+    TFG_ETYPE_CASE(FEM_TRIA2, 6, 2, 3)                   \
+    TFG_ETYPE_CASE(FEM_HEXA2, 20, 3, 8)                  \
+    default:                                             \
+      set_last_error("unsupported element type %d", etype); \
+      return FEM_INVALID;                                \
+  }
+

@@ -14,30 +14,6 @@
 
 namespace tfg {
 
-// ---------------------------------------------------------------- dispatch --
-#define TFG_ETYPE_CASE(ID, NE_, D_, NIP_) \
-  case ID: {                              \
-    constexpr int NE = NE_;               \
-    constexpr int D = D_;                 \
-    constexpr int NIP = NIP_;             \
-    TFG_BODY;                             \
-  } break;
-
-#define TFG_DISPATCH_ETYPE(etype)                        \
-  switch (etype) {                                       \
-    TFG_ETYPE_CASE(FEM_QUAD1, 4, 2, 4)                   \
-    TFG_ETYPE_CASE(FEM_HEXA1, 8, 3, 8)                   \
-    TFG_ETYPE_CASE(FEM_TETRA2, 10, 3, 4)                 \
-    TFG_ETYPE_CASE(FEM_TETRA1, 4, 3, 1)                  \
-    TFG_ETYPE_CASE(FEM_TRIA1, 3, 2, 1)                   \
-    TFG_ETYPE_CASE(FEM_QUAD2, 8, 2, 4)                   \
-    TFG_ETYPE_CASE(FEM_TRIA2, 6, 2, 3)                   \
-    TFG_ETYPE_CASE(FEM_HEXA2, 20, 3, 8)                  \
-    default:                                             \
-      set_last_error("unsupported element type %d", etype); \
-      return FEM_INVALID;                                \
-  }
-
 int etype_info(int etype, int* ne, int* d, int* nip) {
   switch (etype) {
     case FEM_QUAD1: *ne = 4; *d = 2; *nip = 4; return FEM_OK;
@@ -685,6 +661,7 @@ int fem_gather_nodal(const fem_mesh* m, const double* fe, const double* sub, con
     set_last_error("fem_gather_nodal: unsupported element type %d", m->etype);
     return FEM_INVALID;
   }
+  if (m->dof_per_node > 0) d = m->dof_per_node;
   const int64_t n = m->n_nod * d;
   double* partial = nullptr;
   if (sumsq) {

@@ -118,8 +118,12 @@ class DeviceMesh:
         self.n_e = etype.nodes
         self.dim = nodes.shape[1]
         self.d = dof_per_node
-        if geometry and self.d != self.dim:
-            raise NotImplementedError("only mechanics with one DOF per spatial dimension")
+        # heat conduction: one temperature per node, flux [1, dim] per point
+        self.heat = geometry and self.d == 1
+        if geometry and self.d != self.dim and not self.heat:
+            raise NotImplementedError("continua carry one DOF per spatial dimension or one temperature")
+        self.flux_shape = (1, self.dim) if self.heat else (self.d, self.d)
+        self.flux_n = self.flux_shape[0] * self.flux_shape[1]
         self.n_nod = nodes.shape[0]
         self.n_elem = elements.shape[0]
         self.n_dofs = self.n_nod * self.d
@@ -282,7 +286,7 @@ class DeviceMesh:
         return _lib.FemMesh(
             self.etype.etype_id, self.n_nod, self.n_elem, ptr(self.nodes), ptr(self.elements),
             ptr(self.weights), ptr(getattr(self, "bt", None)), ptr(getattr(self, "detj", None)),
-            ptr(self.inc_ptr), ptr(self.inc), ptr(thickness),
+            ptr(self.inc_ptr), ptr(self.inc), ptr(thickness), self.d,
         )
 
     # ------------------------------------------------------------ elements --
@@ -290,6 +294,10 @@ class DeviceMesh:
         nd = self.n_e * self.d
         ke = self._empty(self.n_elem * nd * nd, dtype)
         code = _lib.FEM_F64 if dtype == torch.float64 else _lib.FEM_F32
+        if self.heat:
+            check(self.lib.fem_heat_stiffness(C.byref(mesh), mat.data, code, ptr(ke), ptr(self.status), self.stream),
+                  "fem_heat_stiffness")
+            return ke.view(self.n_elem, nd, nd)
         check(
             self.lib.fem_element_stiffness(
                 C.byref(mesh), C.byref(mat), code, ptr(ke), ptr(self.status), self.stream
@@ -301,8 +309,17 @@ class DeviceMesh:
     def element_force(self, mesh, mat, v, con_mask=None, con_values=None, con_mode=0,
                       sigma_prev=None, de0=None, want_flux=False, want_h=False):
         fe = self._empty(self.n_elem * self.n_e * self.d, torch.float64)
-        flux = self._empty(self.nip * self.n_elem * self.d * self.d, torch.float64) if want_flux else None
-        hg = self._empty(self.nip * self.n_elem * self.d * self.d, torch.float64) if want_h else None
+        flux = self._empty(self.nip * self.n_elem * self.flux_n, torch.float64) if want_flux else None
+        hg = self._empty(self.nip * self.n_elem * self.flux_n, torch.float64) if want_h else None
+        if self.heat:
+            check(
+                self.lib.fem_heat_force(
+                    C.byref(mesh), mat.data, ptr(v), ptr(con_mask), ptr(con_values), con_mode, ptr(sigma_prev),
+                    ptr(de0), ptr(fe), ptr(flux), ptr(hg), ptr(self.status), self.stream,
+                ),
+                "fem_heat_force",
+            )
+            return fe, flux, hg
         check(
             self.lib.fem_element_force(
                 C.byref(mesh), C.byref(mat), ptr(v), ptr(con_mask), ptr(con_values), con_mode,
@@ -331,20 +348,30 @@ class DeviceMesh:
     def vjp(self, mesh, mat, v, g, con_mask=None, con_values=None, con_mode=0, sigma_prev=None,
             de0=None, gflux=None, gh=None, want_sig=False, want_mat=False, want_thick=False,
             want_de0=False, want_v=False, mat_numel=0):
-        n_ip_e = self.nip * self.n_elem * self.d * self.d
+        n_ip_e = self.nip * self.n_elem * self.flux_n
         gsig = self._empty(n_ip_e, torch.float64) if want_sig else None
         gmat = self._empty(mat_numel, torch.float64) if want_mat else None
         gthick = self._empty(self.n_elem, torch.float64) if want_thick else None
-        gde0 = self._empty(self.n_elem * self.d * self.d, torch.float64) if want_de0 else None
+        gde0 = self._empty(self.n_elem * self.flux_n, torch.float64) if want_de0 else None
         gve = self._empty(self.n_elem * self.n_e * self.d, torch.float64) if want_v else None
-        check(
-            self.lib.fem_element_vjp(
-                C.byref(mesh), C.byref(mat), ptr(v), ptr(con_mask), ptr(con_values), con_mode,
-                ptr(sigma_prev), ptr(de0), ptr(g), ptr(gflux), ptr(gh), ptr(gsig), ptr(gmat),
-                ptr(gthick), ptr(gde0), ptr(gve), ptr(self.status), self.stream,
-            ),
-            "fem_element_vjp",
-        )
+        if self.heat:
+            check(
+                self.lib.fem_heat_vjp(
+                    C.byref(mesh), mat.data, ptr(v), ptr(con_mask), ptr(con_values), con_mode, ptr(sigma_prev),
+                    ptr(de0), ptr(g), ptr(gflux), ptr(gh), ptr(gsig), ptr(gmat), ptr(gthick), ptr(gde0),
+                    ptr(gve), self.stream,
+                ),
+                "fem_heat_vjp",
+            )
+        else:
+            check(
+                self.lib.fem_element_vjp(
+                    C.byref(mesh), C.byref(mat), ptr(v), ptr(con_mask), ptr(con_values), con_mode,
+                    ptr(sigma_prev), ptr(de0), ptr(g), ptr(gflux), ptr(gh), ptr(gsig), ptr(gmat),
+                    ptr(gthick), ptr(gde0), ptr(gve), ptr(self.status), self.stream,
+                ),
+                "fem_element_vjp",
+            )
         gv = None
         if want_v:
             gv, _ = self.gather(gve)
@@ -395,19 +422,9 @@ class DeviceMesh:
         L, st = self.lib, self.stream
         if precision == "fp64":
             ke = self.element_stiffness(mesh, mat, torch.float64)
-            sysm.val = self.assemble_csr(ke, con_mask)
+            val = self.assemble_csr(ke, con_mask)
             del ke
-            sysm.precond = self._empty(self.n_dofs, torch.float64)
-            check(
-                L.fem_jacobi(ptr(sysm.val), ptr(self.diag_map), self.n_dofs, ptr(sysm.precond),
-                             ptr(self.status), st),
-                "fem_jacobi",
-            )
-            sysm.matrix = _lib.FemMatrix(
-                _lib.FEM_FMT_CSR_F64, 1, self.n_dofs, self.n_dofs, ptr(self.row_ptr), ptr(self.col),
-                ptr(sysm.val), ptr(sysm.precond),
-            )
-            ws_bytes = L.fem_pcg_workspace_bytes(C.byref(sysm.matrix))
+            ws_bytes = self._set_csr(sysm, val)
         elif precision == "mixed":
             ke = self.element_stiffness(mesh, mat, torch.float32)
             sysm.bval = self.assemble_sell(ke, con_mask)
@@ -438,6 +455,63 @@ class DeviceMesh:
         sysm.ws = self._ws(ws_bytes)
         self.check_status("assembly")
         return sysm
+
+    def _set_csr(self, sysm: LinearSystem, val: Tensor) -> int:
+        """FP64 CSR values plus their Jacobi preconditioner into sysm; returns
+        the CG workspace size."""
+        sysm.val = val
+        sysm.precond = self._empty(self.n_dofs, torch.float64)
+        check(
+            self.lib.fem_jacobi(ptr(val), ptr(self.diag_map), self.n_dofs, ptr(sysm.precond), ptr(self.status),
+                                self.stream),
+            "fem_jacobi",
+        )
+        sysm.matrix = _lib.FemMatrix(
+            _lib.FEM_FMT_CSR_F64, 1, self.n_dofs, self.n_dofs, ptr(self.row_ptr), ptr(self.col), ptr(val),
+            ptr(sysm.precond),
+        )
+        return self.lib.fem_pcg_workspace_bytes(C.byref(sysm.matrix))
+
+    def csr_system(self, val: Tensor, con_mask: Tensor) -> LinearSystem:
+        """FP64 system (Jacobi CG) over already assembled CSR values."""
+        sysm = LinearSystem(self, "fp64")
+        sysm.ws = self._ws(self._set_csr(sysm, val))
+        sysm.con_mask = con_mask
+        self.check_status("assembly")
+        return sysm
+
+    # -------------------------------------------------------- heat transient --
+    def heat_mass(self, mesh, rho: Tensor) -> Tensor:
+        """Element capacity matrices [n_elem, n_e, n_e] (fem_heat_mass)."""
+        nval = self.etype.N(self.etype.ipoints().to(torch.float64)).to(self.device, torch.float64).contiguous()
+        me = self._empty(self.n_elem * self.n_e * self.n_e, torch.float64)
+        check(
+            self.lib.fem_heat_mass(C.byref(mesh), ptr(rho), ptr(nval), _lib.FEM_F64, ptr(me), ptr(self.status),
+                                   self.stream),
+            "fem_heat_mass",
+        )
+        return me.view(self.n_elem, self.n_e, self.n_e)
+
+    def csr_combine(self, a: float, x: Tensor, b: float, y: Tensor) -> Tensor:
+        out = self._empty(x.numel(), torch.float64)
+        check(self.lib.fem_csr_combine(x.numel(), a, ptr(x), b, ptr(y), ptr(out), self.stream), "fem_csr_combine")
+        return out
+
+    def cn_residual(self, mass: LinearSystem, du: Tensor, f_old: Tensor | None, f_int: Tensor,
+                    f_ext: Tensor | None, half_dt: float, con_mask: Tensor) -> tuple[Tensor, Tensor]:
+        """M du + half_dt (f_old + f_int + f_ext), zero on constrained rows,
+        and its squared norm (device scalar)."""
+        res = self._empty(self.n_dofs, torch.float64)
+        sumsq = self._empty(1, torch.float64)
+        ws = self._ws(self.lib.fem_heat_cn_workspace_bytes(self.n_dofs))
+        check(
+            self.lib.fem_heat_cn_residual(
+                C.byref(mass.matrix), ptr(du), ptr(f_old), ptr(f_int), ptr(f_ext), half_dt, ptr(con_mask),
+                ptr(res), ptr(sumsq), ptr(ws), ws.numel(), self.stream,
+            ),
+            "fem_heat_cn_residual",
+        )
+        return res, sumsq
 
     def solve(self, sysm: LinearSystem, b: Tensor, rtol: float, max_iter: int | None = None,
               delta: float = 0.1, refine: bool = True, linear: str = "cg") -> Tensor:

@@ -24,6 +24,8 @@ FEM_BREAKDOWN = 7
 
 FEM_QUAD1, FEM_HEXA1, FEM_TETRA2, FEM_TETRA1, FEM_TRIA1, FEM_QUAD2, FEM_TRIA2, FEM_SHELL3, FEM_HEXA2 = range(1, 10)
 FEM_MAT_ISO, FEM_MAT_GENERAL, FEM_MAT_TANGENT_IP = 1, 2, 3
+# conductivity tensor [n_elem][dim][dim] of the heat kernels (fem_heat_*)
+FEM_MAT_CONDUCTIVITY = 16
 FEM_F64, FEM_F32 = 0, 1
 FEM_FMT_CSR_F64, FEM_FMT_SELL_F32 = 1, 2
 
@@ -44,6 +46,7 @@ class FemMesh(C.Structure):
         ("inc_ptr", vp),
         ("inc", vp),
         ("thickness", vp),
+        ("dof_per_node", C.c_int),
     ]
 
 
@@ -192,6 +195,19 @@ _SIGNATURES = {
         C.c_int,
         [_P(FemMesh), _P(FemMaterial), vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
          vp, vp],
+    ),
+    "fem_heat_stiffness": (C.c_int, [_P(FemMesh), vp, C.c_int, vp, vp, vp]),
+    "fem_heat_force": (
+        C.c_int, [_P(FemMesh), vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp]
+    ),
+    "fem_heat_vjp": (
+        C.c_int, [_P(FemMesh), vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    ),
+    "fem_heat_mass": (C.c_int, [_P(FemMesh), vp, vp, C.c_int, vp, vp, vp]),
+    "fem_csr_combine": (C.c_int, [i64, C.c_double, vp, C.c_double, vp, vp, vp]),
+    "fem_heat_cn_workspace_bytes": (C.c_size_t, [i64]),
+    "fem_heat_cn_residual": (
+        C.c_int, [_P(FemMatrix), vp, vp, vp, vp, C.c_double, vp, vp, vp, vp, C.c_size_t, vp]
     ),
     "fem_hyper_force": (
         C.c_int, [_P(FemMesh), vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]

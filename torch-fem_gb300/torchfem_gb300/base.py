@@ -113,6 +113,10 @@ class FEM:
         raise NotImplementedError
 
     @property
+    def initial_grad(self) -> Tensor:
+        raise NotImplementedError
+
+    @property
     def n_state(self) -> int:
         assert self.material is not None
         return self.material.n_state
@@ -160,6 +164,30 @@ class FEM:
             raise TypeError("Constraints must be a boolean tensor.")
         self._constraints = value.to(self.nodes.device)
 
+    # ---------------------------------------------------- element matrices --
+    def _device_material(self):
+        """(mesh struct, material struct, keep-alive refs) on the device."""
+        dm = self.device_mesh
+        assert self.material is not None
+        kind, data = self.material.kernel_data(self.n_elem)
+        if isinstance(kind, str):
+            raise NotImplementedError(f"{type(self.material).__name__} has a state-dependent tangent")
+        data = data.detach().to(dm.device, torch.float64).contiguous()
+        thickness = self._thickness()
+        if thickness is not None:
+            thickness = thickness.detach().to(dm.device, torch.float64).contiguous()
+        mesh = dm.make_mesh(thickness)
+        return mesh, _lib.FemMaterial(kind, data.data_ptr()), (data, thickness)
+
+    def k0(self) -> Tensor:
+        """Element stiffness (mechanics) or conductivity (heat) matrices of the
+        reference state, [n_elem, n_dof_elem, n_dof_elem] (base.py:228-245),
+        for materials with a constant tangent."""
+        mesh, mat, refs = self._device_material()
+        ke = self.device_mesh.element_stiffness(mesh, mat, torch.float64)
+        del refs
+        return ke.to(self.nodes.device, self.nodes.dtype)
+
     # -------------------------------------------------------------- solve --
     def solve(
         self,
@@ -196,6 +224,8 @@ class FEM:
         accepted; the CG always starts from zero.
         """
         prec = resolve_precision(method, precision)
+        if self.n_dof_per_node == 1 and prec != "fp64":
+            raise NotImplementedError("heat conduction solves in FP64 (precision 'fp64')")
         pc = resolve_preconditioner(preconditioner, prec, self.n_dof_per_node)
         if device is not None and torch.device(device).type != "cuda":
             raise RuntimeError("torchfem_gb300 solves on a CUDA device only")
@@ -256,7 +286,8 @@ class FEM:
         u_cur = torch.zeros(self.n_dofs, dtype=torch.float64, device=dev)
         f_cur = torch.zeros(self.n_dofs, dtype=torch.float64, device=dev)
         flux_cur = torch.zeros(shape_ip, dtype=torch.float64, device=dev)
-        grad_cur = torch.eye(self.n_flux[0], dtype=torch.float64, device=dev).expand(shape_ip).clone()
+        grad_cur = torch.zeros(shape_ip, dtype=torch.float64, device=dev)
+        grad_cur[:] = self.initial_grad.to(dev, torch.float64)
         state_cur = torch.zeros(dm.nip, self.n_elem, self.n_state, dtype=torch.float64, device=dev)
         du = torch.zeros(self.n_dofs, dtype=torch.float64, device=dev)
 
@@ -399,3 +430,205 @@ class Mechanics(FEM):
             raise TypeError("External strain must be a floating-point tensor.")
         self._external_gradient = value.to(self.nodes.device)
         self._external_gradient_set = True
+
+
+class Heat(FEM):
+    """Steady and transient heat conduction (base.py:1132-1553): one
+    temperature per node, heat flux [1, dim] per integration point."""
+
+    @property
+    def n_dof_per_node(self) -> int:
+        return 1
+
+    @property
+    def n_flux(self) -> list[int]:
+        return [1, self.n_dim]
+
+    @property
+    def initial_grad(self) -> Tensor:
+        return torch.zeros(1)
+
+    @property
+    def heat_flux(self) -> Tensor:
+        return self._neumann
+
+    @heat_flux.setter
+    def heat_flux(self, value: Tensor):
+        if not value.shape == (self.n_nod, 1):
+            raise ValueError("Heat flux must have the same shape as nodes.")
+        if not torch.is_floating_point(value):
+            raise TypeError("Heat flux must be a floating-point tensor.")
+        self._neumann = value.to(self.nodes.device)
+
+    @property
+    def temperatures(self) -> Tensor:
+        return self._dirichlet
+
+    @temperatures.setter
+    def temperatures(self, value: Tensor):
+        if not value.shape == (self.n_nod, self.n_dof_per_node):
+            raise ValueError("Temperatures must have the same shape as nodes.")
+        if not torch.is_floating_point(value):
+            raise TypeError("Temperatures must be a floating-point tensor.")
+        self._dirichlet = value.to(self.nodes.device)
+
+    def integrate_mass(self) -> Tensor:
+        """Element capacity matrices sum_ip w detJ t rho N N^T,
+        [n_elem, n_e, n_e] (base.py:376-396)."""
+        mesh, _, refs = self._device_material()
+        dm = self.device_mesh
+        rho = torch.as_tensor(self.material.rho).detach().to(dm.device, torch.float64).expand(self.n_elem)
+        me = dm.heat_mass(mesh, rho.contiguous())
+        del refs
+        return me.to(self.nodes.device, self.nodes.dtype)
+
+    def time_integration(
+        self,
+        t_output: Tensor | None = None,
+        delta_t: float = 1.0e-1,
+        max_iter: int = 100,
+        verbose: bool = False,
+        rtol: float = 1e-8,
+        atol: float = 1e-6,
+        stol: float = 1e-10,
+        device: str | None = None,
+        method: str | None = None,
+        aggregate_integration_points: bool = True,
+        use_cached_solve: bool = False,
+        differentiable_parameters: Tensor | Iterable[Tensor] | None = None,
+    ) -> tuple[Tensor, Tensor, Tensor, Tensor, Tensor]:
+        """Crank-Nicolson time integration (base.py:1288-1553), same arguments
+        and results as the reference.
+
+        The equilibrium at t = 0 under the prescribed temperatures comes from
+        `solve` with every DOF constrained; each later time step runs Newton
+        iterations on r = M du + dt/2 (f_old + f_int + f_ext) (r = 0 on
+        constrained DOFs) with (M + dt/2 K) du = -r solved by the GPU CG to
+        `stol`.  As in the reference, the internal heat flux of the first
+        step's f_old is zero.  Gradients through the time integration are not
+        implemented on this path.
+        """
+        if differentiable_parameters is not None:
+            params = (differentiable_parameters,) if isinstance(differentiable_parameters, Tensor) \
+                else tuple(differentiable_parameters)
+            if any(p.requires_grad for p in params):
+                raise NotImplementedError("gradients through time_integration are not implemented on the GPU path")
+        resolve_precision(method, None)
+        if device is not None and torch.device(device).type != "cuda":
+            raise RuntimeError("torchfem_gb300 solves on a CUDA device only")
+        t_output = torch.tensor([0.0, 1.0]) if t_output is None else t_output
+        if t_output.numel() == 0:
+            raise ValueError("t_output must contain at least one time.")
+        if t_output.min() < 0.0:
+            raise ValueError("t_output must not contain negative times.")
+        if (t_output[1:] <= t_output[:-1]).any():
+            raise ValueError("t_output must be strictly increasing.")
+
+        # equilibrium at t = 0 with the temperatures imposed everywhere
+        bc_constraints = self.constraints.clone()
+        self.constraints[:] = True
+        try:
+            temp_eq, _, flux_eq, grad_eq, state_eq = self.solve(aggregate_integration_points=False, stol=stol)
+        finally:
+            self.constraints[:] = bc_constraints
+
+        # internal time grid: every knot interval in steps of at most delta_t
+        t_output = t_output.detach().cpu().to(torch.float64)
+        knots = t_output
+        if knots[0] > 0.0:
+            knots = torch.cat((knots.new_zeros(1), knots))
+        chunks = [knots[0:1]]
+        output_rows = [] if t_output[0] > 0.0 else [0]
+        row = 0
+        for t_start, t_end in zip(knots[:-1], knots[1:]):
+            ratio = float((t_end - t_start) / delta_t)
+            n_sub = max(1, math.ceil(ratio - 1e-9 * max(1.0, ratio)))
+            sub = torch.linspace(float(t_start), float(t_end), n_sub + 1, dtype=torch.float64)[1:]
+            sub[-1] = t_end
+            chunks.append(sub)
+            row += n_sub
+            output_rows.append(row)
+        increments = torch.cat(chunks)
+        t_rows = torch.tensor(output_rows)
+        dts = (increments[1:] - increments[:-1]).tolist()
+        n_out = len(increments)
+
+        dm = self.device_mesh
+        dev = dm.device
+        con_mask = self._constraints.reshape(-1).to(dev).to(torch.uint8).contiguous()
+        con = con_mask.bool()
+        mesh, mat, refs = self._device_material()
+        rho = torch.as_tensor(self.material.rho).detach().to(dev, torch.float64).expand(self.n_elem).contiguous()
+        nip, fs = dm.nip, dm.flux_shape
+        u = torch.zeros(n_out, self.n_dofs, dtype=torch.float64, device=dev)
+        f = torch.zeros(n_out, self.n_dofs, dtype=torch.float64, device=dev)
+        flux = torch.zeros(n_out, nip, self.n_elem, *fs, dtype=torch.float64, device=dev)
+        grad = torch.zeros_like(flux)
+        state = torch.zeros(n_out, nip, self.n_elem, self.n_state, dtype=torch.float64, device=dev)
+        u[0] = temp_eq.reshape(-1).to(dev, torch.float64)
+        flux[0] = flux_eq.to(dev, torch.float64).reshape(nip, self.n_elem, *fs)
+        grad[0] = grad_eq.to(dev, torch.float64).reshape(nip, self.n_elem, *fs)
+        state[0] = state_eq.to(dev, torch.float64).reshape(nip, self.n_elem, self.n_state)
+        dirichlet = self._dirichlet.reshape(-1).to(dev, torch.float64)
+        u[0] = torch.where(con, dirichlet, u[0])
+        f_ext = self._neumann.reshape(-1).to(dev, torch.float64).contiguous()
+
+        # constant conductivity and capacity: both assembled once
+        kval = dm.assemble_csr(dm.element_stiffness(mesh, mat, torch.float64), con_mask)
+        mval = dm.assemble_csr(dm.heat_mass(mesh, rho), con_mask)
+        mass = dm.csr_system(mval, con_mask)
+        systems: dict[float, object] = {}
+        self.iterations: list[int] = []
+
+        for n in range(1, n_out):
+            dt_n = dts[n - 1]
+            u_prev = u[n - 1]
+            u_guess = u_prev.clone()
+            f_old = f[n - 1]
+            flux_prev = flux[n - 1].contiguous()
+            res0 = None
+            res_norm = float("inf")
+            f_int = f_old
+            if verbose:
+                print(f"time step {n}: t = {float(increments[n]):.6g}")
+            for it in range(max_iter):
+                du = (u_guess - u_prev).contiguous()
+                fe, flux_n, h_inc = dm.element_force(mesh, mat, du, None, None, 0, flux_prev, None,
+                                                     want_flux=True, want_h=True)
+                f_int, _ = dm.gather(fe)
+                flux[n] = flux_n.view(nip, self.n_elem, *fs)
+                grad[n] = grad[n - 1] + h_inc.view(nip, self.n_elem, *fs)
+                res, sumsq = dm.cn_residual(mass, du, f_old, f_int, f_ext, 0.5 * dt_n, con_mask)
+                res_norm = math.sqrt(float(sumsq.item()))
+                if it == 0:
+                    res0 = res_norm
+                if verbose:
+                    print(f"  newton {it:2d}  |res| = {res_norm:.6e}")
+                if res_norm < rtol * res0 or res_norm < atol:
+                    break
+                sysm = systems.get(dt_n)
+                if sysm is None:
+                    sysm = dm.csr_system(dm.csr_combine(1.0, mval, 0.5 * dt_n, kval), con_mask)
+                    systems[dt_n] = sysm
+                x = dm.solve(sysm, (-res).contiguous(), stol)
+                self.iterations.append(sysm.stats.iterations)
+                u_guess = u_guess + x
+            if res_norm > rtol * res0 and res_norm > atol:
+                raise RuntimeError("Newton-Raphson iteration did not converge.")
+            u[n] = u_guess
+            f[n] = f_int
+        del refs
+
+        out_u = u[t_rows].reshape(-1, self.n_nod, 1)
+        out_f = f[t_rows].reshape(-1, self.n_nod, 1)
+        out_flux, out_grad, out_state = flux[t_rows], grad[t_rows], state[t_rows]
+        if aggregate_integration_points:
+            out_grad = out_grad.mean(dim=1)
+            out_flux = out_flux.mean(dim=1)
+            out_state = out_state.mean(dim=1)
+        out_flux = out_flux.squeeze((-2, -1))
+        out_grad = out_grad.squeeze((-2, -1))
+        dt = self.nodes.dtype
+        out_dev = self.nodes.device
+        return tuple(t.to(out_dev, dt) for t in (out_u, out_f, out_flux, out_grad, out_state))
+

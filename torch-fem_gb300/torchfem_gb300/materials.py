@@ -336,3 +336,97 @@ class IsotropicPlasticityPlaneStrain(IsotropicElasticityPlaneStrain):
             ddsdde[fm] = d
         state_new = torch.stack([q, ez], dim=-1)
         return stress_new, state_new, ddsdde
+
+
+# ------------------------------------------------------------ heat conduction ---
+class IsotropicConductivity3D(Material):
+    """Fourier heat conduction in 3D (materials/conductivity.py:11-99):
+    conductivity tensor KAPPA = kappa I, heat flux update
+    q_new = q + KAPPA (grad_inc - de0), tangent KAPPA.  The GPU kernels take
+    KAPPA per element, so any symmetric or rotated tensor is exact."""
+
+    dim = 3
+
+    def __init__(self, kappa, rho=1.0):
+        self.kappa = torch.as_tensor(kappa)
+        self.rho = torch.as_tensor(rho)
+        self.n_state = 0
+        self.is_vectorized = self.kappa.dim() > 0
+        self.KAPPA = self.kappa[..., None, None] * torch.eye(3, device=self.kappa.device)
+
+    def step(self, H_inc, F, stress, state, de0, cl, iter):
+        """q_new = q + KAPPA (grad_inc - de0) (conductivity.py:80-99)."""
+        flux = stress + torch.einsum("...ij,...kj->...ki", self.KAPPA, H_inc - de0)
+        return flux, state, self.KAPPA
+
+    def kernel_data(self, n_elem: int) -> tuple[int, Tensor]:
+        d = self.KAPPA.shape[-1]
+        k = self.KAPPA.reshape(-1, d * d).to(torch.float64)
+        if k.shape[0] != n_elem:
+            k = k.expand(n_elem, d * d)
+        return _lib.FEM_MAT_CONDUCTIVITY, k.contiguous()
+
+
+class IsotropicConductivity2D(IsotropicConductivity3D):
+    """In-plane 2x2 block of the 3D conductivity (conductivity.py:102-121)."""
+
+    dim = 2
+
+    def __init__(self, kappa, rho=1.0):
+        super().__init__(kappa, rho)
+        self.KAPPA = self.KAPPA[..., :2, :2]
+
+
+class IsotropicConductivity1D(IsotropicConductivity2D):
+    """Scalar 1x1 conductivity (conductivity.py:124-142); no 1D element is part
+    of the GPU path, so it is kept for the material interface only."""
+
+    dim = 1
+
+    def __init__(self, kappa, rho=1.0):
+        super().__init__(kappa, rho)
+        self.KAPPA = self.KAPPA[..., :1, :1]
+
+
+class OrthotropicConductivity3D(IsotropicConductivity3D):
+    """Principal conductivities along the material axes, rotated into the
+    global frame by `rotate` (conductivity.py:145-191)."""
+
+    def __init__(self, kappa_1, kappa_2, kappa_3, rho=1.0):
+        self.kappa_1 = torch.as_tensor(kappa_1)
+        self.kappa_2 = torch.as_tensor(kappa_2)
+        self.kappa_3 = torch.as_tensor(kappa_3)
+        self.rho = torch.as_tensor(rho)
+        self.n_state = 0
+        self.is_vectorized = self.kappa_1.dim() > 0
+        e = torch.eye(3, device=self.kappa_1.device)
+        self.KAPPA = sum(k[..., None, None] * torch.outer(e[i], e[i])
+                         for i, k in enumerate((self.kappa_1, self.kappa_2, self.kappa_3)))
+
+    def rotate(self, R: Tensor) -> "OrthotropicConductivity3D":
+        if R.shape[-2] != 3 or R.shape[-1] != 3:
+            raise ValueError("Rotation matrix must be a 3x3 tensor.")
+        new = copy.copy(self)
+        new.KAPPA = torch.einsum("...ik,...jl,...kl->...ij", R, R, self.KAPPA)
+        return new
+
+
+class OrthotropicConductivity2D(IsotropicConductivity2D):
+    """Two principal in-plane conductivities (conductivity.py:194-237)."""
+
+    def __init__(self, kappa_1, kappa_2, rho=1.0):
+        self.kappa_1 = torch.as_tensor(kappa_1)
+        self.kappa_2 = torch.as_tensor(kappa_2)
+        self.rho = torch.as_tensor(rho)
+        self.n_state = 0
+        self.is_vectorized = self.kappa_1.dim() > 0
+        e = torch.eye(2, device=self.kappa_1.device)
+        self.KAPPA = (self.kappa_1[..., None, None] * torch.outer(e[0], e[0])
+                      + self.kappa_2[..., None, None] * torch.outer(e[1], e[1]))
+
+    def rotate(self, R: Tensor) -> "OrthotropicConductivity2D":
+        if R.shape[-2] != 2 or R.shape[-1] != 2:
+            raise ValueError("Rotation matrix must be a 2x2 tensor.")
+        new = copy.copy(self)
+        new.KAPPA = torch.einsum("...ik,...jl,...kl->...ij", R, R, self.KAPPA)
+        return new

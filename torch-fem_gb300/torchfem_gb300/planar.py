@@ -1,7 +1,7 @@
-"""Planar continuum model (src/torchfem/planar.py:17-92, :306-322).
+"""Planar continuum models (src/torchfem/planar.py:17-96, :306-340).
 
-Element forces and stiffness carry the element thickness t_e as a factor
-(planar.py:86-92), which the kernels apply per element.
+Element forces, stiffness and capacity carry the element thickness t_e as a
+factor (planar.py:86-96), which the kernels apply per element.
 """
 
 from __future__ import annotations
@@ -9,12 +9,12 @@ from __future__ import annotations
 import torch
 from torch import Tensor
 
-from .base import Mechanics
+from .base import FEM, Heat, Mechanics
 from .elements import PLANAR_TYPES
 
 
-class Planar(Mechanics):
-    """Plane-stress / plane-strain model: Tria1, Quad1, Tria2 or Quad2."""
+class PlanarGeometry(FEM):
+    """Tria1, Quad1, Tria2 or Quad2 connectivity with a thickness per element."""
 
     def __init__(self, nodes: Tensor, elements: Tensor, material, thickness: Tensor | float = 1.0):
         super().__init__(nodes, elements, material)
@@ -31,10 +31,6 @@ class Planar(Mechanics):
         return PLANAR_TYPES[n]
 
     @property
-    def n_flux(self) -> list[int]:
-        return [2, 2]
-
-    @property
     def volume_scale(self) -> Tensor:
         return self.thickness
 
@@ -44,5 +40,20 @@ class Planar(Mechanics):
             t = t.expand(self.n_elem)
         return t
 
+
+class Planar(PlanarGeometry, Mechanics):
+    """Plane-stress / plane-strain model (planar.py:306-322)."""
+
+    @property
+    def n_flux(self) -> list[int]:
+        return [2, 2]
+
     def __repr__(self) -> str:
         return f"<torch-fem planar ({self.n_nod} nodes, {self.n_elem} {self.etype.__name__} elements)>"
+
+
+class PlanarHeat(PlanarGeometry, Heat):
+    """Planar heat conduction model: one temperature per node (planar.py:325-340)."""
+
+    def __repr__(self) -> str:
+        return f"<torch-fem planar heat ({self.n_nod} nodes, {self.n_elem} {self.etype.__name__} elements)>"

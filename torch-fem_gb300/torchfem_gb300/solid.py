@@ -1,15 +1,15 @@
-"""Three-dimensional continuum model (src/torchfem/solid.py:15-62, :240-255)."""
+"""Three-dimensional continuum models (src/torchfem/solid.py:15-62, :240-270)."""
 
 from __future__ import annotations
 
-from .base import Mechanics
+from .base import FEM, Heat, Mechanics
 from .elements import SOLID_TYPES
 
 
-class Solid(Mechanics):
-    """Solid mechanics model: Hexa1, Hexa2, Tetra1 or Tetra2 connectivity, picked by
-    the number of nodes per element (solid.py:32-44).  Plotting is not part of
-    this library."""
+class SolidGeometry(FEM):
+    """Hexa1, Hexa2, Tetra1 or Tetra2 connectivity, picked by the number of
+    nodes per element (solid.py:32-44).  Plotting is not part of this
+    library."""
 
     @property
     def etype(self):
@@ -18,9 +18,20 @@ class Solid(Mechanics):
             raise ValueError("Element type not supported.")
         return SOLID_TYPES[n]
 
+
+class Solid(SolidGeometry, Mechanics):
+    """Solid mechanics model (solid.py:240-255)."""
+
     @property
     def n_flux(self) -> list[int]:
         return [3, 3]
 
     def __repr__(self) -> str:
         return f"<torch-fem solid ({self.n_nod} nodes, {self.n_elem} {self.etype.__name__} elements)>"
+
+
+class SolidHeat(SolidGeometry, Heat):
+    """Solid heat conduction model: one temperature per node (solid.py:258-270)."""
+
+    def __repr__(self) -> str:
+        return f"<torch-fem solid heat ({self.n_nod} nodes, {self.n_elem} {self.etype.__name__} elements)>"

@@ -196,7 +196,7 @@ class IntegrateMaterial(torch.autograd.Function):
             mesh, mat, du_eval, None, None, 0, sigma_prev, de0, want_flux=True, want_h=True
         )
         f_int, _ = dm.gather(fe)
-        shape = (dm.nip, dm.n_elem, dm.d, dm.d)
+        shape = (dm.nip, dm.n_elem, *dm.flux_shape)
         ctx.sc = sc
         ctx.save_for_backward(du_eval, sigma_prev, de0, mat_data, thickness)
         return f_int, flux.view(shape), hg.view(shape)
