@@ -21,8 +21,11 @@ mixed_block_jacobi  the mixed path with block Jacobi (the persistent CG
            kernel), reported beside the headline.
 
 `--workload heat` times the heat-conduction path instead (SolidHeat,
-steady FP64 solve + adjoint gradient w.r.t. the per-element conductivity)
-and prints its own line; the headline is the elastic cube.
+steady solve + adjoint gradient w.r.t. the per-element conductivity, FP64
+Jacobi CG or mixed multigrid) and `--workload thermal` the reference's own
+thermal benchmark (benchmarks/thermal.py: SIMP slab, thermal compliance
+gradient w.r.t. the densities); each prints its own line.  The headline is
+the elastic cube.
 
 `--impl reference` times the CPU oracle (a restatement of torch-fem's CPU
 path: numpy assembly + scipy Jacobi-CG) on a bounded sample of the same
@@ -237,7 +240,91 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-HEAT_METRIC = "heat solve+grad s per 1M DOF (FP64 Jacobi-CG + adjoint)"
+HEAT_METRIC = "heat solve+grad s per 1M DOF"
+THERMAL_METRIC = "thermal SIMP slab fwd+bwd s per 1M DOF (benchmarks/thermal.py)"
+
+
+def thermal_slab(N: int, device):
+    """The slab of the reference's thermal benchmark (benchmarks/thermal.py:
+    get_slab): one Hexa1 layer of N x N/2 elements on [0,2]x[0,1], thickness
+    2/N, conductivity k = k_max (1e-3 + (1 - 1e-3) rho^3) with rho = 0.5 per
+    element, T = 0 on x = 0, unit heat flux per area on x = 2 lumped to the
+    nodes with trapezoidal weights."""
+    from torchfem_gb300 import SolidHeat, mesh
+    from torchfem_gb300.materials import IsotropicConductivity3D
+
+    lx, ly = 2.0, 1.0
+    nx, ny, nz = N, N // 2, 1
+    lz = lx / nx
+    nodes, elements = mesh.cube_hexa(nx + 1, ny + 1, nz + 1, lx, ly, lz)
+    right = nodes[:, 0] == lx
+    wy = torch.full((len(nodes),), ly / ny, dtype=torch.float64)
+    wy[(nodes[:, 1] == 0.0) | (nodes[:, 1] == ly)] /= 2.0
+    wz = torch.full((len(nodes),), lz / nz, dtype=torch.float64)
+    wz[(nodes[:, 2] == 0.0) | (nodes[:, 2] == lz)] /= 2.0
+    q = torch.zeros(len(nodes), 1, dtype=torch.float64)
+    q[right, 0] = wy[right] * wz[right]
+    left = nodes[:, 0] == 0.0
+    model = SolidHeat(nodes.to(device), elements.to(device), IsotropicConductivity3D(1.0))
+    model.constraints[left.to(device)] = True
+    model.heat_flux = q.to(device)
+    rho = torch.full((model.n_elem,), 0.5, dtype=torch.float64, device=device)
+    base = model.material.KAPPA.detach().to(device)
+    return model, rho, base
+
+
+def thermal_step(model, base_kappa, rho0, precision, stol):
+    """One benchmark repetition: SIMP conductivity of the densities, forward
+    solve with them as differentiable parameters, then the backward of the
+    thermal compliance q . T."""
+    rho = rho0.detach().requires_grad_(True)
+    model.material.KAPPA = (1e-3 + (1.0 - 1e-3) * rho**3.0)[:, None, None] * base_kappa
+    u, *_ = model.solve(differentiable_parameters=rho, stol=stol, precision=precision)
+    compliance = torch.inner(model.heat_flux.ravel(), u.ravel())
+    compliance.backward()
+    return u, rho.grad
+
+
+def run_thermal(args):
+    """--warmup untimed and --steps timed repetitions of the thermal slab
+    benchmark at N = --thermal-n, mixed precision (multigrid) as the value and
+    the FP64 Jacobi CG beside it; CUDA events on the launching stream."""
+    from torchfem_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    lib = _lib.load()
+    model, rho, base = thermal_slab(args.thermal_n, dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 0)):
+        thermal_step(model, base, rho, "mixed", args.stol)
+    torch.cuda.synchronize()
+    ms, iters, u_ms, u_n, launches, clocks, (u_m, g_m) = timed_steps(
+        lib, lambda: (thermal_step(model, base, rho, "mixed", args.stol), model), args.steps, stream)
+    thermal_step(model, base, rho, "fp64", args.stol)
+    p_ms, p_iters, p_ums, p_un, _, _, (u_p, g_p) = timed_steps(
+        lib, lambda: (thermal_step(model, base, rho, "fp64", args.stol), model), 1, stream)
+    dm = model.device_mesh
+    n_dofs = model.n_dofs
+    roof, roof_plain = scalar_rooflines(lib, dm, n_dofs, (u_ms / u_n) / 1e3 if u_n else None,
+                                        (p_ums / p_un) / 1e3 if p_un else None)
+    line = {
+        "metric": THERMAL_METRIC, "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (the benchmark's slab)",
+        "config": {"workload": f"thermal_slab_simp N={args.thermal_n} (benchmarks/thermal.py)",
+                   "dofs": n_dofs, "nnz": dm.nnz, "n_elem": model.n_elem, "stol": args.stol,
+                   "preconditioner": "smoothed-aggregation multigrid (constant near-null vector)",
+                   "l2": "inputs larger than L2 (FP64 element data %.0f MB)" % (model.n_elem * 8 * 8 * 4 * 8 / 1e6)},
+        "cg_iterations": iters, "gpu_launches": launches,
+        "roofline": roof,
+        "plain_fp64": {"value": p_ms / 1e3 / (n_dofs / 1e6), "ms_per_step": p_ms, "cg_iterations": p_iters,
+                       "roofline": roof_plain},
+        "mixed_speedup_vs_plain": p_ms / ms,
+        "rel_err_mixed_vs_fp64": {"u": float((u_m - u_p).abs().max() / u_p.abs().max()),
+                                  "grad": float((g_m - g_p).abs().max() / g_p.abs().max())},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
 
 
 def heat_workload(n: int, device):
@@ -258,15 +345,15 @@ def heat_workload(n: int, device):
     return m, kappa.to(device), q, (nodes.numpy(), el.numpy(), kappa.numpy(), x0.numpy())
 
 
-def heat_step(m, kappa0, q, stol):
+def heat_step(m, kappa0, q, stol, precision="mixed"):
     from torchfem_gb300.materials import IsotropicConductivity3D
 
     kappa = kappa0.detach().requires_grad_(True)
     m.material = IsotropicConductivity3D(kappa)
     m.heat_flux = q
-    T, f, flux, _, _ = m.solve(stol=stol, differentiable_parameters=kappa)
+    T, f, flux, _, _ = m.solve(stol=stol, precision=precision, differentiable_parameters=kappa)
     (g,) = torch.autograd.grad(T.sum(), kappa)
-    return T, f, flux, g
+    return T, g
 
 
 def heat_cpu_baseline(n_sample: int):
@@ -297,29 +384,21 @@ def heat_workload_host(n: int):
     return None, None, None, (nodes_t.numpy(), el_t.numpy(), kappa.numpy(), (nodes_t[:, 0] == 0.0).numpy())
 
 
-def run_heat(args):
-    """Steady heat conduction: --warmup untimed and --steps timed steps of
-    solve + adjoint on the n^3 cube (n = --heat-n), CUDA events on the
-    launching stream; roofline of the FP64 CSR SpMV inside the CG."""
-    from torchfem_gb300 import _lib
-
-    dev = torch.device("cuda", 0)
-    lib = _lib.load()
-    m, kappa, q, _ = heat_workload(args.heat_n, dev)
-    for _ in range(max(args.warmup, 0)):
-        heat_step(m, kappa, q, args.stol)
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream(dev)
+def timed_steps(lib, fn, steps, stream):
+    """Runs fn() `steps` times between CUDA events on `stream` with the
+    library's CG timing on; returns (ms per step, CG iterations per step,
+    summed CG unit time in ms, timed units, kernel launches, clock summary,
+    the last result)."""
     lib.fem_set_timing(1)
-    spmv_ms, spmv_n, iters = 0.0, 0, []
+    spmv_ms, spmv_n, iters, out = 0.0, 0, [], None
     launches0 = lib.fem_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clocks:
+    with ClockSampler(stream.device.index or 0) as clocks:
         torch.cuda.synchronize()
         ev0.record(stream)
-        for _ in range(args.steps):
-            heat_step(m, kappa, q, args.stol)
-            st = m.last_solve
+        for _ in range(steps):
+            out, model = fn()
+            st = model.last_solve
             iters.append(st.iterations)
             spmv_ms += st.system.stats.spmv_ms
             spmv_n += st.system.stats.spmv_timed
@@ -327,36 +406,73 @@ def run_heat(args):
         torch.cuda.synchronize()
     launches = lib.fem_launch_count() - launches0
     lib.fem_set_timing(0)
-    ms = ev0.elapsed_time(ev1) / args.steps
+    return ev0.elapsed_time(ev1) / steps, iters, spmv_ms, spmv_n, launches, clocks.summary(), out
+
+
+def scalar_rooflines(lib, dm, n_dofs, mixed_unit, plain_unit):
+    """Roofline objects of the two heat paths: the level-0 FP32 SpMV of the
+    multigrid CG (4-byte value and int32 column per stored entry, x read
+    once, y written once) and one FP64 Jacobi-CG iteration of the persistent
+    kernel (8-byte value and int32 column per entry, int64 row pointers,
+    twelve FP64 vector streams and the inverse diagonal)."""
+    peak, peak_kind = measured_peak_hbm()
+
+    def obj(kernel, sb, unit_s):
+        achieved = sb / unit_s / 1e9 if unit_s else None
+        return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": None, "algorithmic_bytes": sb,
+                "avg_unit_us": unit_s * 1e6 if unit_s else None, "peak_source": peak_kind}
+
+    mixed = obj("k_sell_op<1,*> (level-0 FP32 SpMV of the multigrid CG)", dm.n_blocks * 8 + 8 * n_dofs, mixed_unit)
+    if lib.fem_get_cg_path() in (1, 2):
+        plain = obj("persistent FP64 Jacobi-CG kernel (one iteration)",
+                    dm.nnz * 12 + (n_dofs + 1) * 8 + 13 * 8 * n_dofs, plain_unit)
+    else:
+        plain = obj("k_spmv_csr (FP64 CSR SpMV of the Jacobi CG)",
+                    dm.nnz * 12 + (n_dofs + 1) * 8 + 2 * n_dofs * 8, plain_unit)
+    return mixed, plain
+
+
+def run_heat(args):
+    """Steady heat conduction on the n^3 cube (n = --heat-n): --warmup
+    untimed and --steps timed steps of solve + adjoint in mixed precision
+    (multigrid), then the FP64 Jacobi CG on the same problem; CUDA events
+    on the launching stream."""
+    from torchfem_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    lib = _lib.load()
+    m, kappa, q, _ = heat_workload(args.heat_n, dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 0)):
+        heat_step(m, kappa, q, args.stol, "mixed")
+    torch.cuda.synchronize()
+    ms, iters, u_ms, u_n, launches, clocks, (T_m, g_m) = timed_steps(
+        lib, lambda: (heat_step(m, kappa, q, args.stol, "mixed"), m), args.steps, stream)
+    heat_step(m, kappa, q, args.stol, "fp64")
+    p_ms, p_iters, p_ums, p_un, _, _, (T_p, g_p) = timed_steps(
+        lib, lambda: (heat_step(m, kappa, q, args.stol, "fp64"), m), 1, stream)
     dm = m.device_mesh
     n_dofs = m.n_dofs
-    if lib.fem_get_cg_path() in (1, 2):
-        # events around each persistent CG launch, spmv_n its iterations: one
-        # FP64 Jacobi-CG iteration reads the CSR matrix once (8-byte value and
-        # int32 column per entry, int64 row pointers), twelve FP64 vector
-        # streams and the inverse diagonal
-        sb = dm.nnz * 12 + (n_dofs + 1) * 8 + 13 * 8 * n_dofs
-        kernel_name = "persistent FP64 Jacobi-CG kernel (one iteration)"
-    else:
-        # scalar FP64 CSR SpMV: values and int32 columns once, row pointers, x read once, y written
-        sb = dm.nnz * 12 + (n_dofs + 1) * 8 + 2 * n_dofs * 8
-        kernel_name = "k_spmv_csr (FP64 CSR SpMV of the Jacobi CG)"
-    unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
-    achieved = sb / unit_s / 1e9 if unit_s else None
-    peak, peak_kind = measured_peak_hbm()
+    roof, roof_plain = scalar_rooflines(lib, dm, n_dofs, (u_ms / u_n) / 1e3 if u_n else None,
+                                        (p_ums / p_un) / 1e3 if p_un else None)
     line = {
-        "metric": HEAT_METRIC, "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
+        "metric": HEAT_METRIC + " (FP32 multigrid CG + FP64 refinement + adjoint)",
+        "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered cube)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded jittered cube)",
         "config": {"workload": f"solidheat_hexa1_cube_{args.heat_n}^3_jittered_steady_solve+adjoint",
                    "dofs": n_dofs, "nnz": dm.nnz, "n_elem": m.n_elem, "stol": args.stol,
+                   "preconditioner": "smoothed-aggregation multigrid (constant near-null vector)",
                    "l2": "inputs larger than L2 (FP64 K = %.0f MB)" % (dm.nnz * 12 / 1e6)},
         "cg_iterations": iters, "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": None, "algorithmic_bytes": sb,
-                     "avg_unit_us": unit_s * 1e6 if unit_s else None, "peak_source": peak_kind},
-        "clocks": clocks.summary(),
+        "roofline": roof,
+        "plain_fp64": {"value": p_ms / 1e3 / (n_dofs / 1e6), "ms_per_step": p_ms, "cg_iterations": p_iters,
+                       "roofline": roof_plain},
+        "mixed_speedup_vs_plain": p_ms / ms,
+        "rel_err_mixed_vs_fp64": {"T": float((T_m - T_p).abs().max() / T_p.abs().max()),
+                                  "grad": float((g_m - g_p).abs().max() / g_p.abs().max())},
+        "clocks": clocks,
         "cpu_baseline": heat_cpu_baseline(args.heat_cpu_n),
     }
     print(json.dumps(line))
@@ -417,7 +533,8 @@ def main():
     ap.add_argument("--cg-path", choices=["persistent", "persistent-regs", "kernels"], default="persistent")
     ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
                     help="preconditioner of the mixed-precision headline")
-    ap.add_argument("--workload", choices=["elastic", "heat"], default="elastic")
+    ap.add_argument("--workload", choices=["elastic", "heat", "thermal"], default="elastic")
+    ap.add_argument("--thermal-n", type=int, default=1024, help="N of the thermal slab (N x N/2 x 1 elements)")
     ap.add_argument("--heat-n", type=int, default=100, help="elements per cube edge of the heat workload")
     ap.add_argument("--heat-cpu-n", type=int, default=30, help="cube size of the heat CPU baseline sample")
     args = ap.parse_args()
@@ -427,6 +544,9 @@ def main():
         return
     if args.workload == "heat":
         run_heat(args)
+        return
+    if args.workload == "thermal":
+        run_thermal(args)
         return
     if args.profile == "step":
         run_profile_step(args)

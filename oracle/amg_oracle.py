@@ -93,7 +93,8 @@ def aggregate(ptr, idx, active):
 
 
 def null_rows(coords, con, b, K, center):
-    """Near-null rows [n, b, K] about `center` (FEM.compute_B's modes)."""
+    """Near-null rows [n, b, K] about `center` (FEM.compute_B's modes; the
+    constant field for one DOF per node)."""
     n = coords.shape[0]
     B = np.zeros((n, b, K))
     for r in range(b):
@@ -104,7 +105,7 @@ def null_rows(coords, con, b, K, center):
         B[:, 0, 4], B[:, 0, 5] = z, -y
         B[:, 1, 3], B[:, 1, 5] = -z, x
         B[:, 2, 3], B[:, 2, 4] = y, -x
-    else:
+    elif b == 2:
         B[:, 0, 2], B[:, 1, 2] = p[:, 1], -p[:, 0]
     if con is not None:
         B[con.reshape(n, b)] = 0.0
@@ -142,7 +143,7 @@ def tentative(agg, n_agg, b, K, coords=None, con=None, bn=None):
                 Q[:, k] = (M[:, k] - Q[:, :k] @ R[:k, k]) / R[k, k]
         T[mem] = Q.reshape(len(mem), b, K)
         S = np.eye(K)
-        if bn is None:
+        if bn is None and b > 1:
             cx, cy = c[0] - origin[0], c[1] - origin[1]
             if b == 3:
                 cz = c[2] - origin[2]
@@ -208,7 +209,7 @@ class Level:
 def hierarchy(A, coords, con, dim, rhos=None):
     """Levels of the multigrid hierarchy of the condensed matrix A (scipy,
     FP64).  rhos: spectral estimates per level (default: power iteration)."""
-    K = 6 if dim == 3 else 3
+    K = 6 if dim == 3 else (3 if dim == 2 else 1)
     b = dim
     n = A.shape[0] // b
     ptr, idx, _ = block_pattern(A, b)

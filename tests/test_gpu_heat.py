@@ -3,8 +3,10 @@
 Steady solves, their adjoint gradients and the Crank-Nicolson time
 integration against golden vectors produced by the reference itself
 (tests/golden/heat_cases.npz) and against the CPU oracle
-(oracle/heat_oracle.py) on a larger mesh.  FP64 throughout: temperatures,
-heat fluxes and gradients agree to 1e-8 relative (CG stopped at 1e-12).
+(oracle/heat_oracle.py) on a larger mesh, in FP64 and in mixed precision
+(FP32 multigrid-preconditioned CG with FP64 residual replacement; one DOF per
+node, the constant near-null vector): temperatures, heat fluxes and
+gradients agree to 1e-8 relative (CG stopped at 1e-12).
 """
 
 import numpy as np
@@ -143,7 +145,91 @@ def test_solid_heat_larger_mesh_against_oracle(cuda):
     assert rel(gk, np.einsum("Eaa->E", gko)) < RTOL
 
 
-def test_heat_rejects_mixed_precision(cuda):
+def _jittered_heat_cube(n, seed=7):
+    nodes, el = mesh.cube_hexa(n + 1, n + 1, n + 1)
+    gen = torch.Generator().manual_seed(seed)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen, dtype=torch.float64) * 2 - 1) * 0.1 / n
+    kappa = 1.0 + torch.rand(len(el), generator=gen, dtype=torch.float64)
+    return nodes, el, kappa
+
+
+def test_solid_heat_mixed_multigrid_vs_reference(cuda, golden):
+    """The reference's SolidHeat case through FP32 multigrid-preconditioned CG
+    with FP64 residual replacement: temperatures, fluxes and gradients to
+    1e-8 of the reference's FP64 results."""
+    g = golden("heat_cases.npz")
+    kappa = torch.tensor(g["solid_kappa"], device=cuda, requires_grad=True)
+    model = SolidHeat(torch.tensor(g["solid_nodes"], device=cuda), torch.tensor(g["solid_elements"], device=cuda),
+                      IsotropicConductivity3D(kappa))
+    model.constraints = torch.tensor(g["solid_con"], device=cuda)
+    model.temperatures = torch.tensor(g["solid_temp"], device=cuda)
+    q = torch.tensor(g["solid_q"], device=cuda, requires_grad=True)
+    model.heat_flux = q
+    T, f, flux, grad, _ = model.solve(stol=1e-12, precision="mixed", differentiable_parameters=(kappa, q))
+    assert model.last_solve.system.amg is not None
+    for name, out in (("T", T), ("f", f), ("flux", flux), ("grad", grad)):
+        assert rel(out, g[f"solid_{name}"]) < RTOL, name
+    L = torch.inner(f.ravel(), T.ravel())
+    gk, gq = torch.autograd.grad(L, (kappa, q))
+    assert rel(gk, g["solid_g_kappa"]) < RTOL
+    assert rel(gq, g["solid_g_q"]) < RTOL
+
+
+def test_planar_heat_mixed_thickness_gradient(cuda, golden):
+    g = golden("heat_cases.npz")
+    rho = torch.tensor(g["planar_rho"], device=cuda, requires_grad=True)
+    model = PlanarHeat(torch.tensor(g["planar_nodes"], device=cuda), torch.tensor(g["planar_elements"], device=cuda),
+                       IsotropicConductivity2D(kappa=400.0))
+    model.thickness = rho**3
+    model.constraints = torch.tensor(g["planar_con"], device=cuda)
+    model.heat_flux = torch.tensor(g["planar_q"], device=cuda)
+    T, f, _, _, _ = model.solve(stol=1e-12, precision="mixed", differentiable_parameters=rho)
+    L = torch.inner(f.ravel(), T.ravel())
+    (g_rho,) = torch.autograd.grad(L, rho)
+    assert rel(T, g["planar_T"]) < RTOL
+    assert rel(g_rho, g["planar_g_rho"]) < RTOL
+
+
+def test_heat_multigrid_hierarchy_matches_oracle(cuda):
+    """One DOF per node: the constant near-null vector, aggregation bit for
+    bit and the tentative prolongator against the oracle, level sizes of the
+    oracle's hierarchy, and the solution against the oracle's FP64 solve."""
+    from test_gpu_amg import fetch
+
+    from oracle import amg_oracle as AO
+
+    nodes, el, kappa = _jittered_heat_cube(14)
+    model = SolidHeat(nodes, el, IsotropicConductivity3D(kappa))
+    x0 = nodes[:, 0] == 0.0
+    model.constraints[x0] = True
+    model.heat_flux[:] = 1.0 / len(nodes)
+    T, f, _, _, _ = model.solve(stol=1e-12, precision="mixed")
+    assert max(model.last_solve.iterations) <= 40
+    om = H.HeatModel(nodes.numpy(), el.numpy(), kappa.numpy()[:, None, None] * np.eye(3))
+    To, fo, _, _ = om.solve(np.full(len(nodes), 1.0 / len(nodes)), x0.numpy())
+    assert rel(T, To) < RTOL and rel(f, fo) < RTOL
+
+    amg = model.last_solve.system.amg
+    levels = amg.levels()
+    assert levels[0].block == 1 and levels[1].block == 1
+    dm = model.device_mesh
+    n = len(nodes)
+    con = x0.numpy()
+    ptr = dm.nbr_ptr.cpu().numpy()
+    idx = dm.nbr.cpu().numpy().astype(np.int64)
+    agg = fetch(amg.lib, levels[0].agg, n, torch.int32)
+    agg_o, na_o = AO.aggregate(ptr, idx, ~con)
+    assert levels[0].n_agg == na_o and np.array_equal(agg, agg_o)
+    T_o, _ = AO.tentative(agg_o, na_o, 1, 1, coords=nodes.numpy(), con=con)
+    Tg = fetch(amg.lib, levels[0].tval, n, torch.float32).reshape(n, 1, 1)
+    assert np.abs(Tg - T_o).max() <= 1e-6 * np.abs(T_o).max()
+    K = om.matrix(np.nonzero(con)[0]).tocsr()
+    lo = AO.hierarchy(K, nodes.numpy(), con, 1, rhos=[lv.rho for lv in levels[:-1]])
+    assert [lv.n for lv in levels] == [x.A.shape[0] // x.b for x in lo]
+
+
+def test_heat_mixed_needs_multigrid(cuda):
     model = _plate()
-    with pytest.raises(NotImplementedError, match="FP64"):
-        model.solve(precision="mixed")
+    with pytest.raises(NotImplementedError, match="multigrid"):
+        model.solve(precision="mixed", preconditioner="jacobi")

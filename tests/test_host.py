@@ -149,6 +149,11 @@ def test_preconditioner_resolution(monkeypatch):
         resolve_preconditioner("amg", "fp64", 3)
     with pytest.raises(ValueError):
         resolve_preconditioner("ilu", "mixed", 3)
+    # one DOF per node (heat): multigrid in mixed precision, Jacobi in FP64
+    assert resolve_preconditioner(None, "mixed", 1) == "amg"
+    assert resolve_preconditioner(None, "fp64", 1) == "jacobi"
+    with pytest.raises(NotImplementedError):
+        resolve_preconditioner("jacobi", "mixed", 1)
     monkeypatch.setenv("TORCHFEM_GB300_PRECOND", "jacobi")
     assert resolve_preconditioner(None, "mixed", 3) == "jacobi"
 
@@ -163,21 +168,28 @@ def test_default_multigrid_falls_back_to_block_jacobi():
     from torchfem_gb300.sparse import SolveContext
 
     class FakeMesh:
-        def __init__(self):
+        def __init__(self, d=3):
             self.calls = []
+            self.d = d
 
         def build_system(self, mesh, mat, con_mask, precision, keep_refs=(), precond="jacobi"):
             self.calls.append(precond)
             if precond == "amg":
                 raise _lib.FemError(_lib.FEM_BOUNDS, "fem_amg_create: a row exceeds its size limit")
-            return "system-" + precond
+            return f"system-{precision}-{precond}"
 
     con = torch.zeros(6, dtype=torch.uint8)
     sc = SolveContext(FakeMesh(), con, 1, "mixed", 10, 1e-8, 1e-6, 1e-10, None)
     sc.precond = "amg"
     with pytest.warns(RuntimeWarning, match="block Jacobi"):
-        assert sc.build_system(None, None, ()) == "system-jacobi"
+        assert sc.build_system(None, None, ()) == "system-mixed-jacobi"
     assert sc.precond == "jacobi" and sc.dm.calls == ["amg", "jacobi"]
+
+    # one DOF per node (heat conduction): the fallback is the FP64 Jacobi CG
+    sc = SolveContext(FakeMesh(d=1), con, 16, "mixed", 10, 1e-8, 1e-6, 1e-10, None)
+    sc.precond = "amg"
+    with pytest.warns(RuntimeWarning, match="FP64 Jacobi CG"):
+        assert sc.build_system(None, None, ()) == "system-fp64-jacobi"
 
     sc = SolveContext(FakeMesh(), con, 1, "mixed", 10, 1e-8, 1e-6, 1e-10, None)
     sc.precond, sc.precond_explicit = "amg", True

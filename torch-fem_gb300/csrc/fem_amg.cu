@@ -2386,6 +2386,7 @@ int status_code(int done) {
 int64_t op_fe_len(const fem_operator64* op) {
   int ne, d, nip;
   if (!op || etype_info(op->mesh->etype, &ne, &d, &nip) != FEM_OK) return -1;
+  if (op->mesh->dof_per_node > 0) d = op->mesh->dof_per_node;
   return op->mesh->n_elem * ne * d;
 }
 
@@ -2520,8 +2521,8 @@ extern "C" {
 
 int fem_amg_create(const fem_blocks* B, const double* coords, const uint8_t* con_mask, fem_amg** out,
                    void* stream) {
-  if (!B || !coords || !out || B->n_nod <= 0 || !(B->dim == 2 || B->dim == 3)) {
-    set_last_error("fem_amg_create: needs the node graph, coordinates and 2 or 3 DOFs per node");
+  if (!B || !coords || !out || B->n_nod <= 0 || !(B->dim >= 1 && B->dim <= 3)) {
+    set_last_error("fem_amg_create: needs the node graph, coordinates and 1, 2 or 3 DOFs per node");
     return FEM_INVALID;
   }
   if (B->n_nod >= (int64_t)1 << 31) {
@@ -2531,8 +2532,12 @@ int fem_amg_create(const fem_blocks* B, const double* coords, const uint8_t* con
   cudaStream_t st = as_stream(stream);
   fem_amg* h = new fem_amg();
   h->dim = B->dim;
-  h->K = B->dim == 3 ? 6 : 3;
-  const int rc = B->dim == 3 ? create_impl<3, 6>(h, B, coords, con_mask, st) : create_impl<2, 3>(h, B, coords, con_mask, st);
+  // near-null space: rigid-body modes (6 in 3D, 3 in 2D) or, for one DOF per
+  // node (heat conduction), the constant field
+  h->K = B->dim == 3 ? 6 : (B->dim == 2 ? 3 : 1);
+  const int rc = B->dim == 3   ? create_impl<3, 6>(h, B, coords, con_mask, st)
+                 : B->dim == 2 ? create_impl<2, 3>(h, B, coords, con_mask, st)
+                               : create_impl<1, 1>(h, B, coords, con_mask, st);
   if (rc) {
     fem_amg_destroy(h);
     *out = nullptr;
@@ -2558,7 +2563,7 @@ int fem_amg_setup(fem_amg* h, const fem_matrix* A, void* stream) {
   }
   cudaStream_t st = as_stream(stream);
   h->ready = false;
-  return h->dim == 3 ? setup_impl<3, 6>(h, A, st) : setup_impl<2, 3>(h, A, st);
+  return h->dim == 3 ? setup_impl<3, 6>(h, A, st) : h->dim == 2 ? setup_impl<2, 3>(h, A, st) : setup_impl<1, 1>(h, A, st);
 }
 
 size_t fem_amg_pcg_workspace_bytes(const fem_amg* h, const fem_operator64* op) {
@@ -2589,8 +2594,9 @@ int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const
     return FEM_INVALID;
   }
   cudaStream_t st = as_stream(stream);
-  return h->dim == 3 ? pcg_impl<3, 6>(h, op, b, x, rtol, delta, max_iter, ws, info, st)
-                     : pcg_impl<2, 3>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
+  if (h->dim == 3) return pcg_impl<3, 6>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
+  if (h->dim == 2) return pcg_impl<2, 3>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
+  return pcg_impl<1, 1>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
 }
 
 int fem_amg_levels(const fem_amg* h) { return h ? h->n_levels : 0; }

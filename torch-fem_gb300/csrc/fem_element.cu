@@ -586,6 +586,7 @@ int fem_element_stiffness(const fem_mesh* m, const fem_material* mat, int out_dt
   (void)status;
   cudaStream_t st = as_stream(stream);
   if (m->n_elem == 0) return FEM_OK;
+  if (mat->kind == FEM_MAT_CONDUCTIVITY) return fem_heat_stiffness(m, mat->data, out_dtype, ke, status, stream);
   if (mat->kind != FEM_MAT_ISO && mat->kind != FEM_MAT_GENERAL && mat->kind != FEM_MAT_TANGENT_IP) {
     set_last_error("fem_element_stiffness: unknown material kind %d", mat->kind);
     return FEM_INVALID;
@@ -617,6 +618,9 @@ int fem_element_force(const fem_mesh* m, const fem_material* mat, const double* 
                       double* hgrad, int32_t* status, void* stream) {
   cudaStream_t st = as_stream(stream);
   if (m->n_elem == 0) return FEM_OK;
+  if (mat->kind == FEM_MAT_CONDUCTIVITY)
+    return fem_heat_force(m, mat->data, v, con_mask, con_values, con_mode, sigma_prev, de0, fe, flux, hgrad,
+                          status, stream);
   if (con_mode != 0 && !con_mask) {
     set_last_error("fem_element_force: con_mode needs con_mask");
     return FEM_INVALID;
@@ -639,6 +643,9 @@ int fem_element_vjp(const fem_mesh* m, const fem_material* mat, const double* v,
   (void)status;
   cudaStream_t st = as_stream(stream);
   if (m->n_elem == 0) return FEM_OK;
+  if (mat->kind == FEM_MAT_CONDUCTIVITY)
+    return fem_heat_vjp(m, mat->data, v, con_mask, con_values, con_mode, sigma_prev, de0, g, gflux, ghgrad, gsig,
+                        gmat, gthick, gde0, gve, stream);
 #define TFG_BODY                                                                                 \
   k_vjp<NE, D, NIP><<<grid_for(m->n_elem, 128), 128, 0, st>>>(                                   \
       m->bt, m->detj, m->weights, m->thickness, m->elements, mat->kind, mat->data, m->n_elem, v,   \

@@ -1965,6 +1965,7 @@ int fem_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_
 static int64_t op_fe_len(const fem_operator64* op) {
   int ne, d, nip;
   if (etype_info(op->mesh->etype, &ne, &d, &nip) != FEM_OK) return -1;
+  if (op->mesh->dof_per_node > 0) d = op->mesh->dof_per_node;
   return op->mesh->n_elem * ne * d;
 }
 

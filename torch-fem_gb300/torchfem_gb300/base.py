@@ -27,7 +27,7 @@ _PRECONDITIONERS = ("jacobi", "amg")
 def resolve_preconditioner(preconditioner: str | None, precision: str, n_dof_per_node: int) -> str:
     """'jacobi' (block Jacobi in mixed precision, Jacobi in FP64) or 'amg'
     (smoothed-aggregation multigrid, the counterpart of the reference's
-    default pyamg / AmgX preconditioners; mixed precision, 2 or 3 DOFs per
+    default pyamg / AmgX preconditioners; mixed precision, 1, 2 or 3 DOFs per
     node).  None picks the default: TORCHFEM_GB300_PRECOND if set, else 'amg'
     where it applies and 'jacobi' elsewhere (FP64, shells)."""
     import os
@@ -35,10 +35,12 @@ def resolve_preconditioner(preconditioner: str | None, precision: str, n_dof_per
     p = preconditioner if preconditioner is not None else os.environ.get("TORCHFEM_GB300_PRECOND", "amg")
     if p not in _PRECONDITIONERS:
         raise ValueError(f"preconditioner must be one of {_PRECONDITIONERS}")
-    if p == "amg" and (precision != "mixed" or n_dof_per_node not in (2, 3)):
+    if p == "amg" and (precision != "mixed" or n_dof_per_node not in (1, 2, 3)):
         if preconditioner is not None:
-            raise ValueError("the multigrid preconditioner runs with precision 'mixed' on 2 or 3 DOFs per node")
+            raise ValueError("the multigrid preconditioner runs with precision 'mixed' on 1, 2 or 3 DOFs per node")
         p = "jacobi"
+    if precision == "mixed" and n_dof_per_node == 1 and p != "amg":
+        raise NotImplementedError("mixed precision with one DOF per node runs with the multigrid preconditioner")
     return p
 
 
@@ -224,8 +226,6 @@ class FEM:
         accepted; the CG always starts from zero.
         """
         prec = resolve_precision(method, precision)
-        if self.n_dof_per_node == 1 and prec != "fp64":
-            raise NotImplementedError("heat conduction solves in FP64 (precision 'fp64')")
         pc = resolve_preconditioner(preconditioner, prec, self.n_dof_per_node)
         if device is not None and torch.device(device).type != "cuda":
             raise RuntimeError("torchfem_gb300 solves on a CUDA device only")

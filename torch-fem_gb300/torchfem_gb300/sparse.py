@@ -79,11 +79,13 @@ class SolveContext:
         except (_lib.FemError, ValueError) as err:
             if precond != "amg" or self.precond_explicit:
                 raise
-            warnings.warn(f"multigrid preconditioner unavailable for this mesh ({err}); using block Jacobi",
-                          RuntimeWarning, stacklevel=2)
+            # one DOF per node has no FP32 block-Jacobi CG: fall back to FP64
+            scalar = self.dm.d == 1
+            warnings.warn(f"multigrid preconditioner unavailable for this mesh ({err}); using "
+                          f"{'the FP64 Jacobi CG' if scalar else 'block Jacobi'}", RuntimeWarning, stacklevel=2)
             self.precond = "jacobi"
-            return self.dm.build_system(mesh, mat, self.con_mask, self.precision, keep_refs=keep_refs,
-                                        precond="jacobi")
+            return self.dm.build_system(mesh, mat, self.con_mask, "fp64" if scalar else self.precision,
+                                        keep_refs=keep_refs, precond="jacobi")
 
     def get_system(self, mat_data: Tensor, thickness: Tensor | None) -> LinearSystem:
         """The condensed tangent for these material data (built once per solve,
