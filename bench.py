@@ -320,7 +320,7 @@ def run_thermal(args):
         "plain_fp64": {"value": p_ms / 1e3 / (n_dofs / 1e6), "ms_per_step": p_ms, "cg_iterations": p_iters,
                        "roofline": roof_plain},
         "mixed_speedup_vs_plain": p_ms / ms,
-        "rel_err_mixed_vs_fp64": {"u": float((u_m - u_p).abs().max() / u_p.abs().max()),
+        "rel_err_mixed_vs_fp64": {"u": float((u_m - u_p).detach().abs().max() / u_p.detach().abs().max()),
                                   "grad": float((g_m - g_p).abs().max() / g_p.abs().max())},
         "clocks": clocks,
     }
@@ -470,7 +470,7 @@ def run_heat(args):
         "plain_fp64": {"value": p_ms / 1e3 / (n_dofs / 1e6), "ms_per_step": p_ms, "cg_iterations": p_iters,
                        "roofline": roof_plain},
         "mixed_speedup_vs_plain": p_ms / ms,
-        "rel_err_mixed_vs_fp64": {"T": float((T_m - T_p).abs().max() / T_p.abs().max()),
+        "rel_err_mixed_vs_fp64": {"T": float((T_m - T_p).detach().abs().max() / T_p.detach().abs().max()),
                                   "grad": float((g_m - g_p).abs().max() / g_p.abs().max())},
         "clocks": clocks,
         "cpu_baseline": heat_cpu_baseline(args.heat_cpu_n),

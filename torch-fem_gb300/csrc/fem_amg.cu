@@ -1082,8 +1082,24 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   float y[D];
 #pragma unroll
   for (int c = 0; c < D; ++c) y[c] = 0.f;
+  int k0 = w;
+  if constexpr (D == 1) {
+    // one value per slot: eight slots' loads in flight per thread before the
+    // gathers (same summation order as the loop below)
+    for (; k0 + 7 * kSellW < len; k0 += 8 * kSellW) {
+      int64_t cc[8];
+      float mv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        cc[u] = ld_l2(cp + (int64_t)(k0 + u * kSellW) * 32, pol);
+        mv[u] = ld_l2(vp + (int64_t)(k0 + u * kSellW) * 32, pol);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[0] = fmaf(mv[u], v[cc[u]], y[0]);
+    }
+  }
 #pragma unroll 2
-  for (int k = w; k < len; k += kSellW) {
+  for (int k = k0; k < len; k += kSellW) {
     const int64_t cc = ld_l2(cp + (int64_t)k * 32, pol);
     const float* vk = vp + (int64_t)k * DD * 32;
     float m[DD];
