@@ -74,8 +74,9 @@ enum {
                              constants, PlaneStress (materials/elasticity.py:44-241). */
   FEM_MAT_GENERAL = 2,    /* [n_elem][dim^4] full tangent C_iJkL per element. */
   FEM_MAT_TANGENT_IP = 3, /* [nip][n_elem][dim^4] tangent per integration point. */
-  FEM_MAT_CONDUCTIVITY = 16 /* [n_elem][dim][dim] conductivity (heat conduction); the
-                               fem_heat_* kernels take the array itself. */
+  FEM_MAT_CONDUCTIVITY = 16 /* [n_elem][dim][dim] conductivity (heat conduction, one DOF
+                               per node): fem_element_stiffness / _force / _vjp forward
+                               this kind to fem_heat_*, which take the array itself. */
 };
 
 enum { FEM_F64 = 0, FEM_F32 = 1 };
