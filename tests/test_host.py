@@ -250,3 +250,30 @@ def test_conductivity_kernel_data():
     assert torch.equal(k3.KAPPA, torch.diag(torch.tensor([1.0, 2.0, 3.0])))
     flux, _, tangent = k3.step(torch.ones(1, 3), None, torch.zeros(1, 3), None, torch.zeros(1, 3), None, 0)
     assert torch.equal(flux, torch.tensor([[1.0, 2.0, 3.0]])) and tangent is k3.KAPPA
+
+
+def test_heat_time_grid_matches_oracle():
+    """The internal time grid of time_integration: starts at t = 0, steps of
+    at most delta_t per knot interval, exact multiples take no extra step,
+    knots are kept exactly; the same grid as the oracle's restatement."""
+    from oracle import heat_oracle as H
+    from torchfem_gb300.base import time_grid
+
+    cases = [
+        (torch.tensor([0.0, 6.0, 12.0, 18.0, 24.0]), 1.0),
+        (torch.tensor([2.5, 5.0]), 0.5),
+        (torch.tensor([0.0, 1.0]), 99.0),
+        (torch.tensor([0.0, 0.3, 1.0]), 0.1),
+        (torch.tensor([10.0]), 1.0),
+        (torch.arange(0.0, 3.0 + 0.25, 0.25), 0.25),
+    ]
+    for t_out, dt in cases:
+        times, rows = time_grid(t_out, dt)
+        times_o, rows_o = H.time_grid(t_out.numpy(), dt)
+        # torch.linspace (as in the reference) and numpy's may differ in the last bit
+        assert np.allclose(times.numpy(), times_o, rtol=1e-15, atol=1e-15) and np.array_equal(rows.numpy(), rows_o)
+        assert times[0] == 0.0 and torch.equal(times[rows], t_out.to(torch.float64))
+        assert ((times[1:] - times[:-1]) <= dt * (1 + 1e-9)).all()
+    times, rows = time_grid(torch.tensor([0.0, 0.3, 1.0]), 0.1)
+    assert len(times) == 11 and rows.tolist() == [0, 3, 10]
+    assert len(time_grid(torch.tensor([0.0, 1.0]), 99.0)[0]) == 2  # clamped to one step

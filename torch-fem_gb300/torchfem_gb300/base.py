@@ -432,6 +432,31 @@ class Mechanics(FEM):
         self._external_gradient_set = True
 
 
+def time_grid(t_output: Tensor, delta_t: float) -> tuple[Tensor, Tensor]:
+    """Internal times of `Heat.time_integration` and the rows that hold the
+    output times (base.py:1387-1411): integration starts at t = 0 even when
+    it is not an output time, and every interval between consecutive knots
+    is cut into the fewest equal steps of at most delta_t; a ratio within
+    1e-9 (relative) of an integer takes no extra step, and each knot is kept
+    exactly."""
+    t_output = t_output.detach().cpu().to(torch.float64)
+    knots = t_output
+    if knots[0] > 0.0:
+        knots = torch.cat((knots.new_zeros(1), knots))
+    chunks = [knots[0:1]]
+    output_rows = [] if t_output[0] > 0.0 else [0]
+    row = 0
+    for t_start, t_end in zip(knots[:-1], knots[1:]):
+        ratio = float((t_end - t_start) / delta_t)
+        n_sub = max(1, math.ceil(ratio - 1e-9 * max(1.0, ratio)))
+        sub = torch.linspace(float(t_start), float(t_end), n_sub + 1, dtype=torch.float64)[1:]
+        sub[-1] = t_end
+        chunks.append(sub)
+        row += n_sub
+        output_rows.append(row)
+    return torch.cat(chunks), torch.tensor(output_rows)
+
+
 class Heat(FEM):
     """Steady and transient heat conduction (base.py:1132-1553): one
     temperature per node, heat flux [1, dim] per integration point."""
@@ -532,24 +557,7 @@ class Heat(FEM):
         finally:
             self.constraints[:] = bc_constraints
 
-        # internal time grid: every knot interval in steps of at most delta_t
-        t_output = t_output.detach().cpu().to(torch.float64)
-        knots = t_output
-        if knots[0] > 0.0:
-            knots = torch.cat((knots.new_zeros(1), knots))
-        chunks = [knots[0:1]]
-        output_rows = [] if t_output[0] > 0.0 else [0]
-        row = 0
-        for t_start, t_end in zip(knots[:-1], knots[1:]):
-            ratio = float((t_end - t_start) / delta_t)
-            n_sub = max(1, math.ceil(ratio - 1e-9 * max(1.0, ratio)))
-            sub = torch.linspace(float(t_start), float(t_end), n_sub + 1, dtype=torch.float64)[1:]
-            sub[-1] = t_end
-            chunks.append(sub)
-            row += n_sub
-            output_rows.append(row)
-        increments = torch.cat(chunks)
-        t_rows = torch.tensor(output_rows)
+        increments, t_rows = time_grid(t_output, delta_t)
         dts = (increments[1:] - increments[:-1]).tolist()
         n_out = len(increments)
 
