@@ -327,22 +327,31 @@ def run_thermal(args):
     print(json.dumps(line))
 
 
-def heat_workload(n: int, device):
-    """SolidHeat on the jittered n^3 Hexa1 cube: conductivity U(1, 2) per
-    element (seed 1), T = 0 on the x = 0 face, uniform source 1/n_nodes."""
-    from torchfem_gb300 import SolidHeat, mesh
-    from torchfem_gb300.materials import IsotropicConductivity3D
+def heat_inputs(n: int):
+    """The heat cube's inputs: the jittered n^3 Hexa1 mesh (interior nodes
+    moved by U(-0.1h, 0.1h), seed 0), conductivity U(1, 2) per element
+    (seed 1) and the x = 0 face, as CPU tensors."""
+    from torchfem_gb300 import mesh
 
     nodes, el = mesh.cube_hexa(n + 1, n + 1, n + 1)
     gen = torch.Generator().manual_seed(0)
     inner = ((nodes > 0) & (nodes < 1)).all(1)
     nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen, dtype=torch.float64) * 2 - 1) * (0.1 / n)
     kappa = 1.0 + torch.rand(len(el), generator=torch.Generator().manual_seed(1), dtype=torch.float64)
-    x0 = nodes[:, 0] == 0.0
+    return nodes, el, kappa, nodes[:, 0] == 0.0
+
+
+def heat_workload(n: int, device):
+    """SolidHeat on the heat cube (heat_inputs), T = 0 on the x = 0 face,
+    uniform source 1/n_nodes."""
+    from torchfem_gb300 import SolidHeat
+    from torchfem_gb300.materials import IsotropicConductivity3D
+
+    nodes, el, kappa, x0 = heat_inputs(n)
     m = SolidHeat(nodes.to(device), el.to(device), IsotropicConductivity3D(kappa.to(device)))
     m.constraints[x0.to(device)] = True
     q = torch.full((len(nodes), 1), 1.0 / len(nodes), dtype=torch.float64, device=device)
-    return m, kappa.to(device), q, (nodes.numpy(), el.numpy(), kappa.numpy(), x0.numpy())
+    return m, kappa.to(device), q
 
 
 def heat_step(m, kappa0, q, stol, precision="mixed"):
@@ -361,7 +370,7 @@ def heat_cpu_baseline(n_sample: int):
     1e-10) on a smaller cube of the same kind, scaled linearly to 1M DOF."""
     from oracle import heat_oracle as H
 
-    _, _, _, (nodes, el, kappa, x0) = heat_workload_host(n_sample)
+    nodes, el, kappa, x0 = (t.numpy() for t in heat_inputs(n_sample))
     t0 = time.perf_counter()
     om = H.HeatModel(nodes, el, kappa[:, None, None] * np.eye(3))
     om.solve(np.full(len(nodes), 1.0 / len(nodes)), x0, method="cg", rtol=1e-10)
@@ -370,18 +379,6 @@ def heat_cpu_baseline(n_sample: int):
     return {"value": t / (len(nodes) / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
             "sample": f"heat oracle (numpy assembly + scipy Jacobi-CG, rtol 1e-10, solve + adjoint) on the {n_sample}^3 "
                       f"jittered Hexa1 cube ({len(nodes)} DOF), scaled linearly to 1M DOF"}
-
-
-def heat_workload_host(n: int):
-    """The inputs of heat_workload(n) as numpy arrays (no device)."""
-    from torchfem_gb300 import mesh
-
-    nodes_t, el_t = mesh.cube_hexa(n + 1, n + 1, n + 1)
-    gen = torch.Generator().manual_seed(0)
-    inner = ((nodes_t > 0) & (nodes_t < 1)).all(1)
-    nodes_t = nodes_t + inner[:, None] * (torch.rand(nodes_t.shape, generator=gen, dtype=torch.float64) * 2 - 1) * (0.1 / n)
-    kappa = 1.0 + torch.rand(len(el_t), generator=torch.Generator().manual_seed(1), dtype=torch.float64)
-    return None, None, None, (nodes_t.numpy(), el_t.numpy(), kappa.numpy(), (nodes_t[:, 0] == 0.0).numpy())
 
 
 def timed_steps(lib, fn, steps, stream):
@@ -442,7 +439,7 @@ def run_heat(args):
 
     dev = torch.device("cuda", 0)
     lib = _lib.load()
-    m, kappa, q, _ = heat_workload(args.heat_n, dev)
+    m, kappa, q = heat_workload(args.heat_n, dev)
     stream = torch.cuda.current_stream(dev)
     for _ in range(max(args.warmup, 0)):
         heat_step(m, kappa, q, args.stol, "mixed")
