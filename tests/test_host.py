@@ -277,3 +277,22 @@ def test_heat_time_grid_matches_oracle():
     times, rows = time_grid(torch.tensor([0.0, 0.3, 1.0]), 0.1)
     assert len(times) == 11 and rows.tolist() == [0, 3, 10]
     assert len(time_grid(torch.tensor([0.0, 1.0]), 99.0)[0]) == 2  # clamped to one step
+
+
+def test_conductivity_kernel_data_carries_gradients():
+    """kernel_data is differentiable: the adjoint's gradient for the per-element
+    conductivity reaches kappa, and the SIMP pattern of the reference's thermal
+    benchmark (KAPPA replaced by a scaled copy) reaches the densities."""
+    from torchfem_gb300.materials import IsotropicConductivity2D, IsotropicConductivity3D
+
+    kappa = torch.tensor([1.0, 2.0, 3.0], requires_grad=True)
+    _, data = IsotropicConductivity2D(kappa).kernel_data(3)
+    data.sum().backward()
+    assert torch.equal(kappa.grad, torch.full((3,), 2.0))
+
+    mat = IsotropicConductivity3D(1.0).vectorize(4)
+    rho = torch.full((4,), 0.5, requires_grad=True)
+    mat.KAPPA = (1e-3 + (1 - 1e-3) * rho**3)[:, None, None] * mat.KAPPA
+    _, data = mat.kernel_data(4)
+    data.view(4, 3, 3)[:, 0, 0].sum().backward()
+    assert torch.allclose(rho.grad, 3 * (1 - 1e-3) * rho.detach() ** 2, rtol=1e-15, atol=0)
