@@ -17,6 +17,8 @@ Restated reference code (paths relative to the torch-fem repository):
   solve (linear)           src/torchfem/base.py:597-923
   adjoint                  src/torchfem/sparse.py:641-724
   time_integration         src/torchfem/base.py:1288-1553 (Crank-Nicolson)
+  its gradients            the reverse sweep of those steps, pinned to the
+                           reference's autograd (heat_transient_grad.npz)
 """
 
 from __future__ import annotations
@@ -216,3 +218,79 @@ def time_integration(model: HeatModel, constraints, temperatures, q, t_output, d
             guess = guess + spla.spsolve((M + 0.5 * dt * K).tocsc(), -r)
         T[k], f[k] = guess, f_int
     return T[rows], f[rows], flux[rows], grad[rows]
+
+
+def time_integration_adjoint(model: HeatModel, constraints, temperatures, q, t_output, delta_t, c):
+    """Gradients of L = sum_k c_k . T(t_k) through the Crank-Nicolson
+    integration of `time_integration` (base.py:1288-1553) for a linear
+    conductivity, by reverse sweep of the discrete steps.
+
+    With g_n the assembled B^T flux_n (g_0 = K u_0, u_0 the prescribed
+    temperatures), h = dt_n / 2, P the projection on the free DOFs and
+    A_n = P (M + h K) P, each step is one Newton correction (exact solve):
+        s_n  = g_0 + q (n = 1; the reference's f_old of the first step is 0)
+             = 2 g_{n-1} + q (n > 1; f_old = f_int of the previous step = g_{n-1})
+        du_n = -A_n^-1 P h s_n,   g_n = g_{n-1} + K du_n,   u_n = u_{n-1} + du_n.
+    Returns (L, dL/dkappa [E, dim, dim], dL/drho [E], dL/dq [n])."""
+    n = model.n_nod
+    con = np.asarray(constraints).ravel().astype(bool)
+    free = ~con
+    u0 = np.asarray(temperatures, float).ravel().copy()
+    q = np.asarray(q, float).ravel()
+    times, rows = time_grid(t_output, delta_t)
+    c = np.asarray(c, float).reshape(len(rows), n)
+    kel = model.conductivity()
+    mel = model.capacity()
+    K = model.matrix(np.array([], dtype=np.int64), kel).toarray()
+    M = model.matrix(np.array([], dtype=np.int64), mel).toarray()
+    Kff, Mff = K[np.ix_(free, free)], M[np.ix_(free, free)]
+    # forward
+    us, dus, gs, hs = [u0], [], [K @ u0], []
+    for k in range(1, len(times)):
+        h = 0.5 * (times[k] - times[k - 1])
+        s = (gs[0] if k == 1 else 2.0 * gs[-1]) + q
+        du = np.zeros(n)
+        du[free] = -np.linalg.solve(Mff + h * Kff, h * s[free])
+        dus.append(du)
+        hs.append(h)
+        gs.append(gs[-1] + K @ du)
+        us.append(us[-1] + du)
+    L = float(sum(c[j] @ us[r] for j, r in enumerate(rows)))
+    # reverse
+    cbar = np.zeros((len(times), n))
+    for j, r in enumerate(rows):
+        cbar[r] += c[j]
+    ubar = cbar[-1].copy()
+    gbar = np.zeros(n)
+    Kbar = np.zeros((n, n))
+    Mbar = np.zeros((n, n))
+    qbar = np.zeros(n)
+    for k in range(len(times) - 1, 0, -1):
+        du, h = dus[k - 1], hs[k - 1]
+        dubar = ubar.copy()
+        # g_k = g_{k-1} + K du
+        dubar += K.T @ gbar
+        Kbar += np.outer(gbar, du)
+        # du = -A^-1 P h s
+        lam = np.zeros(n)
+        lam[free] = np.linalg.solve((Mff + h * Kff).T, dubar[free])
+        Af = np.outer(lam[free], du[free])
+        Mbar[np.ix_(free, free)] -= Af
+        Kbar[np.ix_(free, free)] -= h * Af
+        sbar = -h * lam
+        qbar += sbar
+        if k == 1:
+            gbar = gbar + sbar  # s_1 = g_0 + q
+        else:
+            gbar = gbar + 2.0 * sbar
+        ubar = ubar + cbar[k - 1]
+    # g_0 = K u_0 (u_0 prescribed, not a parameter)
+    Kbar += np.outer(gbar, u0)
+    # element parameters: K = sum_e kappa-contractions, M = sum_e rho_e m_e
+    el = model.elements
+    Kb_e = Kbar[el[:, :, None], el[:, None, :]]
+    Mb_e = Mbar[el[:, :, None], el[:, None, :]]
+    wj = model.w[:, None] * model.detJ * model.t[None]
+    g_kappa = np.einsum("ENM,iE,iEaN,iEbM->Eab", Kb_e, wj, model.B, model.B)
+    g_rho = np.einsum("ENM,ENM->E", Mb_e, mel / model.rho[:, None, None])
+    return L, g_kappa, g_rho, qbar

@@ -504,6 +504,41 @@ def make_heat(tf):
     np.savez_compressed(OUT / "heat_cases.npz", **out)
 
 
+def make_heat_transient_grad(tf):
+    """Gradients through Heat.time_integration: the heated plate with
+    per-element conductivity and density and nodal heat sources as
+    differentiable parameters, loss sum_k c_k . T(t_k) with seeded weights c,
+    on a grid with unequal steps (knots 0, 2, 5 and delta_t 0.8)."""
+    from torchfem import PlanarHeat
+    from torchfem.materials import IsotropicConductivity2D
+    from torchfem.mesh import rect_quad
+
+    nodes, elements = rect_quad(6, 5, 1.0, 0.8)
+    g = torch.Generator().manual_seed(11)
+    kappa = (400.0 * (1.0 + torch.rand(len(elements), generator=g))).requires_grad_(True)
+    rho = (1.0e5 * (1.0 + torch.rand(len(elements), generator=g))).requires_grad_(True)
+    q = (50.0 * torch.rand(len(nodes), 1, generator=g)).requires_grad_(True)
+    model = PlanarHeat(nodes, elements, IsotropicConductivity2D(kappa, rho))
+    west = torch.isclose(nodes[:, 0], nodes[:, 0].min())
+    east = torch.isclose(nodes[:, 0], nodes[:, 0].max())
+    model.constraints[west | east] = True
+    model.temperatures[west, 0] = 5.0
+    model.temperatures[east, 0] = 20.0
+    model.heat_flux = q
+    t_out = torch.tensor([0.0, 2.0, 5.0])
+    temp, rfl, flux, grad, _ = model.time_integration(t_out, delta_t=0.8, differentiable_parameters=(kappa, rho, q))
+    c = torch.rand(temp.shape, generator=g)
+    L = (c * temp).sum()
+    gk, gr, gq = torch.autograd.grad(L, (kappa, rho, q))
+    np.savez_compressed(
+        OUT / "heat_transient_grad.npz", nodes=nodes.numpy(), elements=elements.numpy(),
+        kappa=kappa.detach().numpy(), rho=rho.detach().numpy(), q=q.detach().numpy(),
+        con=model.constraints.numpy(), temp_bc=model.temperatures.numpy(), t_out=t_out.numpy(), delta_t=0.8,
+        temp=temp.detach().numpy(), c=c.numpy(), L=L.detach().numpy(), g_kappa=gk.numpy(), g_rho=gr.numpy(),
+        g_q=gq.numpy(),
+    )
+
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
@@ -511,7 +546,7 @@ MAKERS = {
     "simp_full": lambda tf: make_simp(tf, 400, 200, "simp_400x200.npz", sample=20),
     "hyper": make_hyper, "plastic": make_plastic, "shell": make_shell,
     "plastic_full": lambda tf: make_plastic(tf, 256, 64, "plastic_ogrid_256x64.npz"),
-    "hexa2": make_hexa2, "heat": make_heat,
+    "hexa2": make_hexa2, "heat": make_heat, "heat_transient_grad": make_heat_transient_grad,
 }
 
 

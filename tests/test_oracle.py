@@ -289,3 +289,19 @@ def test_heat_oracle_transient(golden):
     T, f, flux, gr = H.time_integration(m, w | e, temp, np.zeros(len(nodes)), g["late_t"], 0.5)
     assert _heat_rel(T, g["late_temp"][..., 0]) < 1e-12
     assert _heat_rel(flux, g["late_flux"]) < 1e-12
+
+
+def test_heat_oracle_transient_adjoint(golden):
+    """The discrete adjoint of the Crank-Nicolson steps against the
+    reference's autograd through time_integration (unequal steps, per-element
+    conductivity and density, nodal sources)."""
+    from oracle import heat_oracle as H
+
+    g = golden("heat_transient_grad.npz")
+    m = H.HeatModel(g["nodes"], g["elements"], g["kappa"][:, None, None] * np.eye(2), rho=g["rho"])
+    L, gk, gr, gq = H.time_integration_adjoint(m, g["con"], g["temp_bc"], g["q"], g["t_out"], float(g["delta_t"]),
+                                               g["c"])
+    assert abs(L - float(g["L"])) <= 1e-13 * abs(float(g["L"]))
+    assert _heat_rel(np.einsum("Eaa->E", gk), g["g_kappa"]) < 1e-12
+    assert _heat_rel(gr, g["g_rho"]) < 1e-12
+    assert _heat_rel(gq, g["g_q"].ravel()) < 1e-12
