@@ -539,6 +539,29 @@ def make_heat_transient_grad(tf):
     )
 
 
+def make_modes(tf):
+    """Modal analysis (FEM.solve_modes): the six lowest squared angular
+    frequencies of a jittered 3^3 Hexa1 cube clamped on x = 0, with
+    per-element E and rho, and d(sum omega^2)/d(E, rho)."""
+    from torchfem import Solid
+    from torchfem.materials import IsotropicElasticity3D
+
+    base = cube_problem(tf, 3, jit=True)
+    nodes, elements = base.nodes, base.elements
+    g = torch.Generator().manual_seed(21)
+    E = (1000.0 * (1.0 + 0.5 * torch.rand(len(elements), generator=g))).requires_grad_(True)
+    rho = (1.0 + torch.rand(len(elements), generator=g)).requires_grad_(True)
+    model = Solid(nodes, elements, IsotropicElasticity3D(E, 0.3, rho))
+    model.constraints[nodes[:, 0] == 0.0, :] = True
+    omega_sq, modes = model.solve_modes(6)
+    gE, gr = torch.autograd.grad(omega_sq.sum(), (E, rho))
+    np.savez_compressed(
+        OUT / "modes_hexa_jitter3.npz", nodes=nodes.numpy(), elements=elements.numpy(), E=E.detach().numpy(),
+        rho=rho.detach().numpy(), con=model.constraints.numpy(), omega_sq=omega_sq.detach().numpy(),
+        modes=modes.numpy(), g_E=gE.numpy(), g_rho=gr.numpy(),
+    )
+
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
@@ -547,6 +570,7 @@ MAKERS = {
     "hyper": make_hyper, "plastic": make_plastic, "shell": make_shell,
     "plastic_full": lambda tf: make_plastic(tf, 256, 64, "plastic_ogrid_256x64.npz"),
     "hexa2": make_hexa2, "heat": make_heat, "heat_transient_grad": make_heat_transient_grad,
+    "modes": make_modes,
 }
 
 

@@ -305,3 +305,17 @@ def test_heat_oracle_transient_adjoint(golden):
     assert _heat_rel(np.einsum("Eaa->E", gk), g["g_kappa"]) < 1e-12
     assert _heat_rel(gr, g["g_rho"]) < 1e-12
     assert _heat_rel(gq, g["g_q"].ravel()) < 1e-12
+
+
+def test_modal_oracle(golden):
+    """FEM.solve_modes: the lowest squared angular frequencies, mode shapes
+    (up to sign) and d(sum omega^2)/d(E, rho) against the reference."""
+    from oracle import modal_oracle as MO
+
+    g = golden("modes_hexa_jitter3.npz")
+    lam, modes, gE, gr = MO.solve_modes(g["nodes"], g["elements"], g["E"], 0.3, g["rho"], g["con"], 6)
+    assert _heat_rel(lam, g["omega_sq"]) < 1e-12
+    sign = np.sign(np.einsum("mnd,mnd->m", modes, g["modes"]))
+    assert _heat_rel(modes * sign[:, None, None], g["modes"]) < 1e-10
+    assert _heat_rel(gE, g["g_E"]) < 1e-12
+    assert _heat_rel(gr, g["g_rho"]) < 1e-12
