@@ -1,8 +1,10 @@
 """Generates the golden fixtures in this folder by running torch-fem itself.
 
-Run in a container that has the reference checkout at /root/reference:
+Run where a torch-fem checkout is available, naming its `src` folder:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference <torch-fem checkout>/src [target ...]
+
+(or set TORCHFEM_REFERENCE_SRC instead of passing --reference).
 
 The reference's optional plotting / AMG / IO dependencies (pyvista,
 matplotlib, meshio, pyamg) are replaced by inert stub modules so that
@@ -13,16 +15,19 @@ unmodified.  Outputs are small .npz files; nothing here runs on the GPU machine.
 
 from __future__ import annotations
 
+import contextlib
+import hashlib
 import importlib.abc
 import importlib.machinery
+import os
 import sys
+import time
 import types
 from pathlib import Path
 
 import numpy as np
 import torch
 
-REFERENCE_SRC = "/root/reference/src"
 OUT = Path(__file__).resolve().parent
 STUB_ROOTS = ("pyamg", "pyvista", "meshio", "matplotlib", "mpl_toolkits")
 
@@ -74,9 +79,9 @@ class _StubFinder(importlib.abc.MetaPathFinder):
         return None
 
 
-def import_reference():
+def import_reference(src: str):
     sys.meta_path.insert(0, _StubFinder())
-    sys.path.insert(0, REFERENCE_SRC)
+    sys.path.insert(0, src)
     import torchfem  # noqa: F401
 
     return torchfem
@@ -106,15 +111,20 @@ def cube_problem(tf, N: int, jit: bool):
 
 
 def make_c1(tf):
-    """10^3 Hexa1 cube: u, f, sigma and d(sum u)/d(forces)."""
+    """10^3 Hexa1 cube: u, f, sigma and d(sum u)/d(forces), and the
+    reference's element matrices (k0) and condensed assembled values
+    (assemble_matrix, base.py:398-426) of the configuration."""
     model = cube_problem(tf, 10, jit=False)
+    con = torch.nonzero(model.constraints.ravel()).ravel()
+    ke = model.k0()
+    kval = model.assemble_matrix(ke, con)._values()
     forces = model.forces.clone().requires_grad_(True)
     model.forces = forces
     u, f, s, _, _ = model.solve(method="spsolve", differentiable_parameters=forces)
     (g,) = torch.autograd.grad(u.sum(), forces)
     np.savez_compressed(
         OUT / "c1_cube10.npz", u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(),
-        grad_forces=g.numpy(), torch_version=torch.__version__,
+        grad_forces=g.numpy(), ke=ke.numpy(), kval=kval.numpy(), torch_version=torch.__version__,
     )
 
 
@@ -562,6 +572,182 @@ def make_modes(tf):
     )
 
 
+class _JacobiAMG:
+    """Stand-in for pyamg on the reference's iterative CPU route.
+
+    `_solve_cpu` (sparse.py:477-512) builds its CG/MINRES preconditioner with
+    `pyamg.smoothed_aggregation_solver(A, B, smooth="jacobi").aspreconditioner()`.
+    pyamg is not installed here, so this object answers that call with the
+    Jacobi operator diag(A)^-1, the preconditioner the reference's GPU CG branch
+    builds (sparse.py:406-421).  Each operator counts its applications, which
+    is the CG iteration count plus one.
+    """
+
+    applications = 0
+
+    @classmethod
+    def smoothed_aggregation_solver(cls, A, B=None, smooth=None):
+        from scipy.sparse.linalg import LinearOperator
+
+        dinv = 1.0 / A.diagonal()
+
+        def matvec(x):
+            cls.applications += 1
+            return dinv * x.ravel()
+
+        class _Hierarchy:
+            def aspreconditioner(self):
+                return LinearOperator(A.shape, matvec=matvec, dtype=A.dtype)
+
+        return _Hierarchy()
+
+
+@contextlib.contextmanager
+def jacobi_cg_route(tf):
+    """The reference's `sparse_solve(method="cg")` with the Jacobi stand-in."""
+    old = tf.sparse.pyamg
+    tf.sparse.pyamg = _JacobiAMG
+    try:
+        yield _JacobiAMG
+    finally:
+        tf.sparse.pyamg = old
+
+
+def c2_problem(n: int):
+    """Config 2 geometry: Hexa1 cube of n^3 elements, interior nodes jittered
+    by U(-0.1, 0.1)/n per coordinate from torch seed 0, E = 1000, nu = 0.3,
+    x = 0 clamped, z-force -1/n_nodes on every node of x = 1."""
+    from torchfem import Solid
+    from torchfem.materials import IsotropicElasticity3D
+    from torchfem.mesh import cube_hexa
+
+    nodes, elements = cube_hexa(n + 1, n + 1, n + 1)
+    gen = torch.Generator().manual_seed(0)
+    inner = ((nodes > 0) & (nodes < 1)).all(1)
+    nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen, dtype=torch.float64) * 2 - 1) * (0.1 / n)
+    model = Solid(nodes, elements, IsotropicElasticity3D(1000.0, 0.3))
+    model.constraints[nodes[:, 0] == 0.0, :] = True
+    forces = torch.zeros_like(nodes)
+    forces[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
+    forces.requires_grad_(True)
+    model.forces = forces
+    return model, forces, nodes, elements
+
+
+def c2_solve(tf, n: int, method: str, stol: float):
+    """The reference's solve + d(sum u)/d(forces) on the config-2 cube."""
+    model, forces, nodes, elements = c2_problem(n)
+    with jacobi_cg_route(tf) as amg:
+        amg.applications = 0
+        t0 = time.perf_counter()
+        u, f, s, _, _ = model.solve(method=method, stol=stol, differentiable_parameters=forces)
+        t1 = time.perf_counter()
+        fwd_apps = amg.applications
+        (g,) = torch.autograd.grad(u.sum(), forces)
+        t2 = time.perf_counter()
+        adj_apps = amg.applications - fwd_apps
+    return dict(nodes=nodes, elements=elements, u=u.detach().numpy(), f=f.detach().numpy(),
+                sigma=s.detach().numpy(), grad=g.numpy(), t_fwd=t1 - t0, t_adj=t2 - t1,
+                cg_fwd=fwd_apps - 1, cg_adj=adj_apps - 1)
+
+
+def _sample(rng, n, k):
+    return np.sort(rng.choice(n, size=min(k, n), replace=False)).astype(np.int64)
+
+
+def _projection_weights(n):
+    """Deterministic weights for full-field checksums <w, x>."""
+    return np.cos(np.arange(n, dtype=np.float64) * 0.6180339887498949)
+
+
+def make_c2(tf, n=70, stol=1e-13, name="c2_cube70_sample.npz"):
+    """Config 2 at full size (70^3 jittered Hexa1, 1,073,733 DOF) by the
+    reference's own pattern, k0, assembly and autograd, with its CG route
+    (`sparse_solve(method="cg")`, Jacobi, stol 1e-13) for the forward and the
+    adjoint of sum(u).  SuperLU cannot factor this size.  Stored: seeded
+    samples of u, f, sigma and the gradient, their max-abs and 2-norms, and
+    full-field checksums <w, x> with the weights of `_projection_weights`."""
+    r = c2_solve(tf, n, "cg", stol)
+    rng = np.random.default_rng(20261204)
+    u, f, s, g = r["u"].ravel(), r["f"].ravel(), r["sigma"].ravel(), r["grad"].ravel()
+    out = dict(n=n, stol=stol, n_dofs=u.size,
+               nodes_sha256=hashlib.sha256(np.ascontiguousarray(r["nodes"].numpy())).hexdigest(),
+               t_fwd=r["t_fwd"], t_adj=r["t_adj"], cg_fwd=r["cg_fwd"], cg_adj=r["cg_adj"],
+               torch_version=torch.__version__, host_threads=torch.get_num_threads(), cpu_count=os.cpu_count())
+    for key, x in (("u", u), ("f", f), ("sigma", s), ("grad", g)):
+        idx = _sample(rng, x.size, 10000)
+        out[f"{key}_idx"] = idx
+        out[f"{key}_sample"] = x[idx]
+        out[f"{key}_maxabs"] = float(np.abs(x).max())
+        out[f"{key}_norm"] = float(np.linalg.norm(x))
+        w = _projection_weights(x.size)
+        out[f"{key}_proj"] = float(w @ x)
+        out[f"{key}_projscale"] = float(np.abs(w) @ np.abs(x))
+    np.savez_compressed(OUT / name, **out)
+    print(f"c2 n={n}: fwd {r['t_fwd']:.1f} s ({r['cg_fwd']} CG its), adjoint {r['t_adj']:.1f} s ({r['cg_adj']} its)")
+
+
+def make_c2_crosscheck(tf, sizes=(20, 30), stol=1e-13, name="c2_route_crosscheck.npz"):
+    """Shows that the CG route of `make_c2` reproduces the reference's direct
+    solve (SuperLU, method="spsolve") on smaller cubes of the same kind: the
+    max-abs relative differences of u, sigma and the gradient."""
+    out = {}
+    for n in sizes:
+        a = c2_solve(tf, n, "spsolve", stol)
+        b = c2_solve(tf, n, "cg", stol)
+        for key in ("u", "sigma", "grad"):
+            d = float(np.abs(a[key] - b[key]).max() / np.abs(a[key]).max())
+            out[f"n{n}_{key}"] = d
+        out[f"n{n}_t_spsolve"] = a["t_fwd"] + a["t_adj"]
+        out[f"n{n}_t_cg"] = b["t_fwd"] + b["t_adj"]
+        out[f"n{n}_cg_its"] = np.array([b["cg_fwd"], b["cg_adj"]])
+        print(n, {k: v for k, v in out.items() if k.startswith(f"n{n}_")})
+    np.savez_compressed(OUT / name, sizes=np.array(sizes), stol=stol, **out)
+
+
+def make_hyper_full(tf, name="hyper_tet2_30x10x10.npz", counts=(10, 20, 40)):
+    """Config 4 at full size (30 x 10 x 10 box, 6 Tetra2 per hex, 80,703 DOF,
+    Neo-Hookean, nlgeom, x = 3 face pulled to +0.5) by the reference's own
+    solve and autograd, with the CG route of `jacobi_cg_route` (SuperLU needs
+    minutes per Newton step at this size).  The load is first applied in 10
+    increments as the configuration states; when the reference's own solve
+    raises there, its message is stored and the next count of `counts` is
+    tried.  Stored: u, f, the tip reaction and its gradient w.r.t. the
+    per-element E of the first count that completes, a seeded sample of the
+    element stresses, and the wall times and CG iteration counts."""
+    out = {"counts_tried": np.array(counts)}
+    for n_inc in counts:
+        model, E, right, nodes, elements = hyper_problem(30, 10, 10)
+        inc = torch.linspace(0.0, 1.0, n_inc + 1)
+        with jacobi_cg_route(tf) as amg:
+            amg.applications = 0
+            t0 = time.perf_counter()
+            try:
+                u, f, s, F, _ = model.solve(increments=inc, nlgeom=True, method="cg", rtol=1e-10, atol=1e-10,
+                                            max_iter=20, stol=1e-12, differentiable_parameters=E, verbose=True)
+            except RuntimeError as err:
+                out[f"inc{n_inc}_error"] = str(err)
+                out[f"inc{n_inc}_seconds"] = time.perf_counter() - t0
+                print(f"{n_inc} increments: the reference raised: {err}", flush=True)
+                continue
+            t1 = time.perf_counter()
+            fwd_apps = amg.applications
+            R = f[right, 0].sum()
+            (gE,) = torch.autograd.grad(R, E)
+            t2 = time.perf_counter()
+        rng = np.random.default_rng(4)
+        sig = s.detach().numpy().ravel()
+        idx = _sample(rng, sig.size, 10000)
+        out.update(increments=n_inc, nodes=nodes.numpy(), elements=elements.numpy(), E=E.detach().numpy(),
+                   u=u.detach().numpy(), f=f.detach().numpy(), sigma_idx=idx, sigma_sample=sig[idx],
+                   sigma_maxabs=float(np.abs(sig).max()), reaction=R.detach().numpy(), grad_E=gE.numpy(),
+                   t_fwd=t1 - t0, t_adj=t2 - t1, precond_applications_fwd=fwd_apps,
+                   precond_applications_adj=amg.applications - fwd_apps, torch_version=torch.__version__)
+        print(f"{n_inc} increments: fwd {t1 - t0:.1f} s, adjoint {t2 - t1:.1f} s", flush=True)
+        break
+    np.savez_compressed(OUT / name, **out)
+
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
@@ -571,13 +757,26 @@ MAKERS = {
     "plastic_full": lambda tf: make_plastic(tf, 256, 64, "plastic_ogrid_256x64.npz"),
     "hexa2": make_hexa2, "heat": make_heat, "heat_transient_grad": make_heat_transient_grad,
     "modes": make_modes,
+    "c2": make_c2, "c2_crosscheck": make_c2_crosscheck, "hyper_full": make_hyper_full,
 }
+# targets that take minutes to an hour of CPU; run only when named
+SLOW = {"c2", "c2_crosscheck", "hyper_full", "plastic_full", "simp_full"}
 
 
 def main():
+    import argparse
+    import os
+
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", default=os.environ.get("TORCHFEM_REFERENCE_SRC"),
+                    help="the src folder of a torch-fem checkout (or TORCHFEM_REFERENCE_SRC)")
+    ap.add_argument("targets", nargs="*")
+    args = ap.parse_args()
+    if not args.reference:
+        ap.error("name the torch-fem src folder with --reference or TORCHFEM_REFERENCE_SRC")
     torch.set_default_dtype(torch.float64)
-    tf = import_reference()
-    names = sys.argv[1:] or list(MAKERS)
+    tf = import_reference(args.reference)
+    names = args.targets or [n for n in MAKERS if n not in SLOW]
     for name in names:
         MAKERS[name](tf)
     print("fixtures written to", OUT, names)

@@ -47,6 +47,21 @@ def test_c1_solution(golden):
         assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max()
     gf = m.grad_forces(np.ones(m.n_dofs))
     assert np.abs(gf - g["grad_forces"]).max() <= 1e-10 * np.abs(g["grad_forces"]).max()
+    # the oracle's element matrices and serial-order assembly against the
+    # reference's k0 and assemble_matrix at config 1 (268,119 values)
+    assert np.abs(m.stiffness() - g["ke"]).max() <= 1e-13 * np.abs(g["ke"]).max()
+    val = O.assemble_matrix(g["ke"], m.k_map, m.glob_idx.shape[1], m.glob_idx, m.diag_map, np.flatnonzero(con))
+    assert np.array_equal(val, g["kval"])  # bit for bit
+
+
+def test_c2_route_reproduces_direct_solve(golden):
+    """The reference's CG route that generated the config-2 fixture (Jacobi
+    CG to 1e-13) agrees with its direct solve on the 20^3 and 30^3 cubes of
+    the same kind far below the 1e-8 target."""
+    g = golden("c2_route_crosscheck.npz")
+    for n in g["sizes"]:
+        for key in ("u", "sigma", "grad"):
+            assert float(g[f"n{n}_{key}"]) < 1e-12, (n, key)
 
 
 def test_hexa_jitter_gradients(golden):
