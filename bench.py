@@ -37,6 +37,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -57,14 +58,25 @@ METRIC = "solve+grad s per 1M DOF: FP32-CG+FP64-refine+adjoint vs plain FP64 @ r
 UNIT = "s/1M DOF"
 
 
-def cube_workload(n: int, device):
-    from torchfem_gb300 import Solid, mesh
-    from torchfem_gb300.materials import IsotropicElasticity3D
+def cube_nodes(n: int):
+    """Nodes and elements of the n^3 Hexa1 cube, interior nodes jittered by
+    U(-0.1, 0.1)/n per coordinate from torch seed 0."""
+    from torchfem_gb300 import mesh
 
     nodes, el = mesh.cube_hexa(n + 1, n + 1, n + 1)
     gen = torch.Generator().manual_seed(0)
     inner = ((nodes > 0) & (nodes < 1)).all(1)
     nodes = nodes + inner[:, None] * (torch.rand(nodes.shape, generator=gen, dtype=torch.float64) * 2 - 1) * (0.1 / n)
+    return nodes, el
+
+
+def cube_workload(n: int, device):
+    """The jittered cube with E = 1000, nu = 0.3, x = 0 clamped and the
+    z-force -1/n_nodes on every node of x = 1 (forces returned separately)."""
+    from torchfem_gb300 import Solid
+    from torchfem_gb300.materials import IsotropicElasticity3D
+
+    nodes, el = cube_nodes(n)
     x0 = nodes[:, 0] == 0.0
     x1 = nodes[:, 0] == 1.0
     nodes, el = nodes.to(device), el.to(device)
@@ -103,8 +115,12 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.first = threading.Event()
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # nvidia-smi's own start-up (driver and NVML initialisation) stays
+            # outside the timed region: wait for its first sample
+            self.first.wait(timeout=10.0)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -112,6 +128,8 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
+        self.first.set()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -160,40 +178,70 @@ def cg_iteration_bytes(dm) -> float:
     return dm.n_blocks * 40 + 8 * (n_slices + 1) + 48 * dm.n_dofs + 12 * dm.n_dofs
 
 
-def spmv_bytes(dm) -> float:
-    """Algorithmic bytes of one FP32 block SpMV: 4*9 value bytes and one
+def spmv_bytes(dm, value_bytes: int = 4) -> float:
+    """Algorithmic bytes of one level-0 block SpMV: d*d values of
+    `value_bytes` (4: the FP32 matrix, 2: the FP16 smoothing copy) and one
     int32 column per stored block, x read once, y written once (the padding
     slots of the sliced layout are not counted)."""
     d = dm.d
-    return dm.n_blocks * (4 * d * d + 4) + 2 * 4 * dm.n_dofs
+    return dm.n_blocks * (value_bytes * d * d + 4) + 2 * 4 * dm.n_dofs
 
 
-def cpu_baseline(n_sample: int, steps: int = 1):
-    """The oracle's CPU solve + adjoint on a smaller cube of the same kind."""
+def level0_launch_bytes(dm, smoother: str) -> float:
+    """Mean algorithmic bytes of the timed level-0 launches of one multigrid
+    CG iteration: the four Chebyshev passes (FP16 copy with --smoother fp16)
+    and CG's q = A p (always the FP32 matrix)."""
+    smooth = spmv_bytes(dm, 2 if smoother == "fp16" else 4)
+    return (4 * smooth + spmv_bytes(dm, 4)) / 5
+
+
+def _port_step(n: int):
+    """One solve + adjoint of the oracle port on the jittered n^3 cube:
+    (seconds, of which CG seconds, DOF, CG iterations of both solves)."""
     from oracle import fem_oracle as O
 
-    nodes, el = O.cube_hexa(n_sample + 1, n_sample + 1, n_sample + 1)
+    nodes, el = O.cube_hexa(n + 1, n + 1, n + 1)
     rng = torch.Generator().manual_seed(0)
     inner = ((nodes > 0) & (nodes < 1)).all(1)
-    jit = (torch.rand(nodes.shape, generator=rng, dtype=torch.float64).numpy() * 2 - 1) * (0.1 / n_sample)
+    jit = (torch.rand(nodes.shape, generator=rng, dtype=torch.float64).numpy() * 2 - 1) * (0.1 / n)
     nodes = nodes + inner[:, None] * jit
     con = np.zeros(nodes.shape, dtype=bool)
     con[nodes[:, 0] == 0.0, :] = True
     F = np.zeros(nodes.shape)
     F[nodes[:, 0] == 1.0, 2] = -1.0 / len(nodes)
-    times = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        m = O.LinearModel(nodes, el, O.elastic_c("3d", 1000.0, 0.3, len(el)))
-        m.solve(F, con, method="cg", rtol=1e-10)
-        m.adjoint(np.ones(m.n_dofs), method="cg", rtol=1e-10)
-        times.append(time.perf_counter() - t0)
-    t = min(times)
-    dofs = nodes.size
-    return {"value": t / (dofs / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-            "sample": f"oracle (numpy assembly + scipy Jacobi-CG, rtol 1e-10, solve + adjoint) on the "
-                      f"{n_sample}^3 jittered Hexa1 cube ({dofs} DOF), best of {steps}, "
-                      f"scaled linearly to 1M DOF; numpy/BLAS may use every host thread, scipy SpMV runs on one"}
+    O.LinearModel.cg_iterations.clear()
+    O.LinearModel.cg_seconds.clear()
+    t0 = time.perf_counter()
+    m = O.LinearModel(nodes, el, O.elastic_c("3d", 1000.0, 0.3, len(el)))
+    m.solve(F, con, method="cg", rtol=1e-10)
+    m.adjoint(np.ones(m.n_dofs), method="cg", rtol=1e-10)
+    t = time.perf_counter() - t0
+    return t, sum(O.LinearModel.cg_seconds), nodes.size, sum(O.LinearModel.cg_iterations)
+
+
+def cpu_baseline(n_sample: int, n_target: int = 70):
+    """The oracle port (the reference's CPU path restated: numpy assembly,
+    scipy Jacobi CG to rtol 1e-10, forward + adjoint) timed on two cubes,
+    (2 n_sample / 3)^3 and n_sample^3, then extrapolated to the n_target^3
+    workload: set-up (integration, assembly, stresses) by DOF, the CG by
+    DOF x iterations, with the iteration growth measured between the two
+    samples (Jacobi-CG iterations grow like a power of n, about n^1)."""
+    n_small = max(4, (2 * n_sample) // 3)
+    t_s, cg_s, dofs_s, it_s = _port_step(n_small)
+    t_l, cg_l, dofs_l, it_l = _port_step(n_sample)
+    alpha = math.log(it_l / it_s) / math.log(n_sample / n_small) if it_s > 0 and it_l > 0 else 1.0
+    dofs_t = 3 * (n_target + 1) ** 3
+    it_t = it_l * (n_target / n_sample) ** alpha
+    t_t = (t_l - cg_l) * (dofs_t / dofs_l) + cg_l * (dofs_t / dofs_l) * (it_t / it_l)
+    return {"value": t_t / (dofs_t / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"oracle port (numpy assembly + scipy Jacobi-CG, rtol 1e-10, solve + adjoint) on the "
+                      f"{n_small}^3 and {n_sample}^3 jittered Hexa1 cubes ({dofs_s} and {dofs_l} DOF: "
+                      f"{t_s:.2f} s and {t_l:.2f} s, of which CG {cg_s:.2f} s and {cg_l:.2f} s over {it_s} and "
+                      f"{it_l} iterations), extrapolated to {n_target}^3 ({dofs_t} DOF): set-up by DOF, CG by "
+                      f"DOF x iterations with iterations ~ n^{alpha:.2f} ({it_t:.0f} predicted); scipy's SpMV "
+                      f"runs on one thread, numpy may use every core",
+            "samples": {"n": [n_small, n_sample], "seconds": [t_s, t_l], "cg_seconds": [cg_s, cg_l],
+                        "cg_iterations": [it_s, it_l], "iteration_exponent": alpha, "predicted_seconds": t_t}}
 
 
 def dist_setup():
@@ -221,12 +269,10 @@ def run_reference(args):
     dist, rank, world, _ = dist_setup()
     if rank != 0:
         return
-    times = []
-    for _ in range(args.warmup + args.steps):
-        times.append(cpu_baseline(args.cpu_n)["value"])
-    timed = times[args.warmup:] or times
-    v = sum(timed) / len(timed)
-    cb = cpu_baseline(args.cpu_n)
+    runs = [cpu_baseline(args.cpu_n, args.n) for _ in range(max(args.warmup, 0) + max(args.steps, 1))]
+    timed = runs[args.warmup:] or runs
+    v = sum(r["value"] for r in timed) / len(timed)
+    cb = dict(timed[-1])
     cb["value"] = v
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
@@ -532,6 +578,8 @@ def main():
     ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
                     help="preconditioner of the mixed-precision headline")
     ap.add_argument("--workload", choices=["elastic", "heat", "thermal"], default="elastic")
+    ap.add_argument("--smoother", choices=["fp16", "fp32"], default="fp16",
+                    help="level-0 smoothing passes of the multigrid V-cycle: FP16 copy or the FP32 matrix")
     ap.add_argument("--thermal-n", type=int, default=1024, help="N of the thermal slab (N x N/2 x 1 elements)")
     ap.add_argument("--heat-n", type=int, default=100, help="elements per cube edge of the heat workload")
     ap.add_argument("--heat-cpu-n", type=int, default=30, help="cube size of the heat CPU baseline sample")
@@ -540,6 +588,10 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if torch.cuda.is_available():
+        from torchfem_gb300 import _lib
+
+        _lib.load().fem_amg_set_half_smoother(1 if args.smoother == "fp16" else 0)
     if args.workload == "heat":
         run_heat(args)
         return
@@ -561,12 +613,26 @@ def main():
     lib = _lib.load()
     lib.fem_set_cg_path({"persistent": 1, "persistent-regs": 2, "kernels": 0}[args.cg_path])
     m, forces = cube_workload(args.n, dev)
+    # set-up kept out of the timed steps (once per mesh, and once per mesh and
+    # constraint set): the pattern and geometry cache, and the symbolic
+    # multigrid hierarchy (aggregation, tentative prolongator, patterns)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     dm = m.device_mesh
+    torch.cuda.synchronize()
+    setup_mesh_ms = (time.perf_counter() - t0) * 1e3
     n_dofs = m.n_dofs
     stream = torch.cuda.current_stream(dev)
+    pc = args.precond
+    amg_symbolic_ms = None
+    if pc == "amg":
+        con_mask = m.constraints.reshape(-1).to(dev).to(torch.uint8).contiguous()
+        t0 = time.perf_counter()
+        dm.amg_hierarchy(con_mask)
+        torch.cuda.synchronize()
+        amg_symbolic_ms = (time.perf_counter() - t0) * 1e3
 
     # warm-up (W untimed steps), then K timed steps of the mixed path
-    pc = args.precond
     for _ in range(max(args.warmup, 0)):
         out = step(m, forces, "mixed", args.stol, pc)
     torch.cuda.synchronize()
@@ -648,8 +714,10 @@ def main():
         # CUDA events around every level-0 SpMV launch of the multigrid CG
         # (four Chebyshev passes and q = A p per iteration)
         unit_s = (spmv_ms / spmv_n) / 1e3 if spmv_n else None
-        sb = spmv_bytes(dm)
-        kernel_name = "k_sell_op<3,*> (level-0 FP32 block SpMV of the multigrid CG, fused smoothing epilogue)"
+        sb = level0_launch_bytes(dm, args.smoother)
+        kernel_name = ("k_sell_op<3,*> (level-0 block SpMV of the multigrid CG: four Chebyshev passes on the "
+                       "%s matrix, q = A p on the FP32 matrix; fused epilogues)"
+                       % ("FP16 smoothing copy of the" if args.smoother == "fp16" else "FP32"))
         traffic_file = ROOT / "profiles" / "amg_sell_op_traffic.json"
         if traffic_file.exists():
             try:
@@ -695,11 +763,13 @@ def main():
             "data": "synthetic (seeded jittered cube)",
             "config": {"workload": f"hexa1_cube_{args.n}^3_jittered_linear_elastic_solve+adjoint",
                        "preconditioner": "smoothed-aggregation multigrid" if pc == "amg" else "block Jacobi",
+                       "level0_smoothing": args.smoother if pc == "amg" else None,
                        "dofs": n_dofs, "nnz": dm.nnz, "n_elem": n_elem, "stol": args.stol,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (FP32 K = %.0f MB)" % (dm.n_blocks * 40 / 1e6)},
             "cg_iterations": iters,
             "gpu_launches": launches,
+            "setup_excluded_ms": {"mesh_pattern_and_geometry": setup_mesh_ms, "amg_symbolic": amg_symbolic_ms},
             "e2e": {"value": e2e_ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak,
@@ -710,7 +780,7 @@ def main():
             **result,
         }
         if world == 1:
-            line["cpu_baseline"] = cpu_baseline(args.cpu_n)
+            line["cpu_baseline"] = cpu_baseline(args.cpu_n, args.n)
         print(json.dumps(line))
     if dist is not None:
         dist.barrier()

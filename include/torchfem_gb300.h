@@ -262,6 +262,15 @@ int fem_heat_vjp(const fem_mesh* mesh, const double* kappa, const double* v,
 int fem_heat_mass(const fem_mesh* mesh, const double* rho, const double* nval, int out_dtype,
                   void* me, int32_t* status, void* stream);
 
+/* Vector-Jacobian product of the capacity matrices: out[e] = sum_ip w detJ
+ * (N . a_e)(N . b_e) for nodal vectors a, b [n_nod], i.e. a_e^T m_e b_e /
+ * (rho_e t_e).  The caller scales it into d/d rho_e and d/d t_e of a^T M b:
+ * the parameter pull-back of the capacity term M du of the Crank-Nicolson
+ * residual that the reference's time_integration differentiates by autograd
+ * (base.py:376-396 with solid.py:60-62 / planar.py:94-96, base.py:1288-1553). */
+int fem_heat_mass_vjp(const fem_mesh* mesh, const double* nval, const double* a, const double* b, double* out,
+                      void* stream);
+
 
 /* ------------------------------------------------------------------------ */
 /* Nonlinear material points fused with element integration.                */
@@ -441,9 +450,13 @@ int fem_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_
  * exits, so A->n may be at most fem_pcg_static_max_unknowns() (131072);
  * larger systems return FEM_BOUNDS with a message.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) and
- * should come before any stream capture on that device.  All calls share
+ * should come before any stream capture on that device; the address is
+ * kept for the life of the process, so the entry point must not be used on
+ * a device after cudaDeviceReset re-creates its context.  All calls share
  * the array: calls that overlap on the GPU race and must be serialised by
- * the caller.  Nothing from a previous call is reused. */
+ * the caller.  Nothing from a previous call is reused.  No SpMV event
+ * timing (fem_set_timing) is done here, and the timing switch is left as
+ * it is. */
 int64_t fem_pcg_static_max_unknowns(void);
 int fem_pcg_static(const fem_matrix* A, const double* b, double* x, double rtol,
                    int64_t max_iter, fem_solve_info* info, void* stream);
@@ -501,6 +514,16 @@ int fem_amg_create(const fem_blocks* blocks, const double* coords, const uint8_t
  * unchanged until the next setup. */
 int fem_amg_setup(fem_amg* amg, const fem_matrix* A32, void* stream);
 
+/* Precision of the level-0 smoothing passes for the setups that follow
+ * (process-wide; default 1).  1: the four Chebyshev passes of every V-cycle
+ * read an FP16 copy of the level-0 matrix, scaled by a power of two and
+ * built by fem_amg_setup (2 bytes per value instead of 4); CG's own product
+ * q = A p keeps the FP32 matrix.  The same copy serves pre- and
+ * post-smoothing, so the V-cycle stays a fixed symmetric operator.  0: the
+ * smoothing passes read the FP32 matrix.  A preconditioner choice with no
+ * counterpart in the reference (its AMG runs in FP64). */
+void fem_amg_set_half_smoother(int enable);
+
 /* CG preconditioned by one V-cycle (Chebyshev smoothing) on the matrix of
  * the last fem_amg_setup, from x = 0.  With op != NULL: FP64 residual
  * replacement as in fem_pcg_mixed (threshold delta), stopping at
@@ -557,6 +580,26 @@ int fem_minres(const fem_matrix* A, const double* b, double* x, double rtol, int
  * ws: fem_diag_workspace_bytes() bytes of device memory. */
 size_t fem_diag_workspace_bytes(void);
 int fem_diag_barrier_timeout(void* ws, size_t ws_bytes, long long spin_limit, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Modal analysis (FEM.solve_modes, base.py:1097-1129; eigen-solve          */
+/* sparse.py:798-1011).                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Element mass matrices me [n_elem][n_e d][n_e d] of a mechanics model:
+ * sum_ip w detJ rho t N N^T expanded to the d DOFs of each node (Kronecker
+ * product with I_d), rho [n_elem], t the mesh thickness (1 when NULL), nval
+ * [nip][n_e] the shape-function values at the integration points.  Replaces
+ * FEM.integrate_mass (base.py:376-396) with compute_m (solid.py:60-62,
+ * planar.py:94-96). */
+int fem_mass_matrices(const fem_mesh* mesh, const double* rho, const double* nval, int d, double* me,
+                      void* stream);
+
+/* Y = A X for a scalar FP64 CSR matrix and row-major blocks X, Y
+ * [n][nvec] of device memory: the operator applications of the block
+ * eigensolver that replaces the reference's shift-invert eigsh on the free
+ * DOFs (sparse.py:798-827). */
+int fem_csr_spmm(const fem_matrix* A, int nvec, const double* X, double* Y, void* stream);
 
 /* ---------------------------------------------------------------- shell --
  * Tria1 flat-facet shell, homogeneous linear-elastic section (the reference's

@@ -30,6 +30,7 @@ Restated reference code (paths relative to the torch-fem repository):
 from __future__ import annotations
 
 from math import sqrt
+import time
 
 import numpy as np
 import scipy.sparse as sp
@@ -285,12 +286,23 @@ class LinearModel:
         self.K, self.con = K, con
         return du.reshape(self.n_nod, self.d), F_int.reshape(self.n_nod, self.d), sig.mean(axis=0)
 
+    cg_iterations: list = []  # iterations of every Jacobi-CG solve (appended per solve)
+    cg_seconds: list = []  # wall time of every Jacobi-CG solve
+
     @staticmethod
     def linear_solve(K, b, method="spsolve", rtol=1e-12):
         if method == "spsolve":
             return spla.spsolve(K.tocsc(), b)
         M = sp.diags(1.0 / K.diagonal())
-        x, info = spla.cg(K, b, rtol=rtol, atol=0.0, M=M, maxiter=20 * K.shape[0])
+        count = [0]
+
+        def tick(_):
+            count[0] += 1
+
+        t0 = time.perf_counter()
+        x, info = spla.cg(K, b, rtol=rtol, atol=0.0, M=M, maxiter=20 * K.shape[0], callback=tick)
+        LinearModel.cg_seconds.append(time.perf_counter() - t0)
+        LinearModel.cg_iterations.append(count[0])
         if info != 0:
             raise RuntimeError(f"CG failed with exit code {info}")
         return x

@@ -613,6 +613,58 @@ def jacobi_cg_route(tf):
         tf.sparse.pyamg = old
 
 
+class _OracleAMG:
+    """Stand-in for pyamg on the reference's iterative CPU route, with a
+    multigrid preconditioner: `smoothed_aggregation_solver(A, B, smooth)`
+    answers with one V-cycle of the oracle's smoothed-aggregation hierarchy
+    (oracle/amg_oracle.py, the algorithm family of pyamg's solver) of the
+    condensed matrix A.  The node coordinates come from the rotation columns
+    of the reference's rigid-body modes B (FEM.compute_B, base.py:316-344)
+    and the constrained DOFs are the rows the reference's condensation made
+    unit rows (base.py:414-419).  CG still stops at the reference's stol, so
+    the preconditioner changes only how fast the reference's solves get
+    there.  3D models only."""
+
+    applications = 0
+
+    @classmethod
+    def smoothed_aggregation_solver(cls, A, B=None, smooth=None):
+        import scipy.sparse as sp
+        from scipy.sparse.linalg import LinearOperator
+
+        sys.path.insert(0, str(OUT.parents[1]))
+        from oracle import amg_oracle as AO
+
+        A = sp.csr_matrix(A)
+        B = np.asarray(B)
+        coords = np.stack([B[1::3, 5], B[2::3, 3], B[0::3, 4]], axis=1)
+        diag = A.diagonal()
+        off = np.asarray(abs(A).sum(axis=1)).ravel() - np.abs(diag)
+        con = ((off == 0.0) & (diag == 1.0)).reshape(-1, 3)
+        levels = AO.hierarchy(A, coords, con, 3)
+
+        def matvec(x):
+            cls.applications += 1
+            return AO.vcycle(levels, np.asarray(x, dtype=np.float64).ravel())
+
+        class _Hierarchy:
+            def aspreconditioner(self):
+                return LinearOperator(A.shape, matvec=matvec, dtype=A.dtype)
+
+        return _Hierarchy()
+
+
+@contextlib.contextmanager
+def oracle_amg_cg_route(tf):
+    """The reference's `sparse_solve(method="cg")` with the multigrid stand-in."""
+    old = tf.sparse.pyamg
+    tf.sparse.pyamg = _OracleAMG
+    try:
+        yield _OracleAMG
+    finally:
+        tf.sparse.pyamg = old
+
+
 def c2_problem(n: int):
     """Config 2 geometry: Hexa1 cube of n^3 elements, interior nodes jittered
     by U(-0.1, 0.1)/n per coordinate from torch seed 0, E = 1000, nu = 0.3,
@@ -708,8 +760,9 @@ def make_c2_crosscheck(tf, sizes=(20, 30), stol=1e-13, name="c2_route_crosscheck
 def make_hyper_full(tf, name="hyper_tet2_30x10x10.npz", counts=(10, 20, 40)):
     """Config 4 at full size (30 x 10 x 10 box, 6 Tetra2 per hex, 80,703 DOF,
     Neo-Hookean, nlgeom, x = 3 face pulled to +0.5) by the reference's own
-    solve and autograd, with the CG route of `jacobi_cg_route` (SuperLU needs
-    minutes per Newton step at this size).  The load is first applied in 10
+    solve and autograd, with the CG route of `oracle_amg_cg_route` (SuperLU
+    needs minutes per Newton step at this size, Jacobi CG about 2,500
+    iterations per solve).  The load is first applied in 10
     increments as the configuration states; when the reference's own solve
     raises there, its message is stored and the next count of `counts` is
     tried.  Stored: u, f, the tip reaction and its gradient w.r.t. the
@@ -719,7 +772,7 @@ def make_hyper_full(tf, name="hyper_tet2_30x10x10.npz", counts=(10, 20, 40)):
     for n_inc in counts:
         model, E, right, nodes, elements = hyper_problem(30, 10, 10)
         inc = torch.linspace(0.0, 1.0, n_inc + 1)
-        with jacobi_cg_route(tf) as amg:
+        with oracle_amg_cg_route(tf) as amg:
             amg.applications = 0
             t0 = time.perf_counter()
             try:

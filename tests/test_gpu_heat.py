@@ -122,6 +122,76 @@ def test_time_integration_sparse_output_matches_dense(cuda):
     assert torch.allclose(sparse, dense[rows], atol=1e-9)
 
 
+def _transient_grad_model(g, cuda, kappa, rho, q):
+    nodes = torch.tensor(g["nodes"], device=cuda)
+    el = torch.tensor(g["elements"], device=cuda)
+    model = PlanarHeat(nodes, el, IsotropicConductivity2D(kappa, rho))
+    model.constraints = torch.tensor(g["con"], device=cuda)
+    model.temperatures = torch.tensor(g["temp_bc"], device=cuda)
+    model.heat_flux = q
+    return model
+
+
+def test_time_integration_gradients_vs_reference(cuda, golden):
+    """Gradients through Heat.time_integration: per-element conductivity and
+    density and the nodal heat sources, loss sum_k c_k . T(t_k) on a grid of
+    unequal steps, against the reference's autograd through its own
+    integration (heat_transient_grad.npz), to 1e-8."""
+    g = golden("heat_transient_grad.npz")
+    kappa = torch.tensor(g["kappa"], device=cuda, requires_grad=True)
+    rho = torch.tensor(g["rho"], device=cuda, requires_grad=True)
+    q = torch.tensor(g["q"], device=cuda, requires_grad=True)
+    model = _transient_grad_model(g, cuda, kappa, rho, q)
+    temp, *_ = model.time_integration(torch.tensor(g["t_out"]), delta_t=float(g["delta_t"]), stol=1e-13,
+                                      differentiable_parameters=(kappa, rho, q))
+    assert rel(temp, g["temp"]) < RTOL
+    L = (torch.tensor(g["c"], device=cuda) * temp).sum()
+    assert rel(L, g["L"]) < RTOL
+    gk, gr, gq = torch.autograd.grad(L, (kappa, rho, q))
+    assert rel(gk, g["g_kappa"]) < RTOL
+    assert rel(gr, g["g_rho"]) < RTOL
+    assert rel(gq, g["g_q"]) < RTOL
+
+
+def test_time_integration_flux_and_thickness_gradients_central_differences(cuda, golden):
+    """A loss on every output of time_integration (temperatures, internal
+    heat fluxes and element fluxes) differentiated w.r.t. conductivity,
+    density and thickness, against central differences of the GPU path on
+    the three most sensitive elements of each parameter."""
+    g = golden("heat_transient_grad.npz")
+    gen = torch.Generator().manual_seed(5)
+    k0 = torch.tensor(g["kappa"])
+    r0 = torch.tensor(g["rho"])
+    t0 = 0.5 + torch.rand(len(k0), generator=gen, dtype=torch.float64)
+    q = torch.tensor(g["q"], device=cuda)
+    t_out = torch.tensor(g["t_out"])
+    w = []
+
+    def loss(kappa, rho, th, track):
+        model = _transient_grad_model(g, cuda, kappa, rho, q)
+        model.thickness = th
+        temp, rfl, flux, _, _ = model.time_integration(t_out, delta_t=float(g["delta_t"]), stol=1e-13,
+                                                       differentiable_parameters=(kappa, rho, th) if track else None)
+        if not w:
+            w.extend(torch.rand(x.shape, generator=gen, dtype=torch.float64).to(cuda) for x in (temp, rfl, flux))
+        return (w[0] * temp).sum() + 1e-3 * (w[1] * rfl).sum() + 1e-3 * (w[2] * flux).sum()
+
+    kappa, rho, th = (x.to(cuda).clone().requires_grad_(True) for x in (k0, r0, t0))
+    grads = torch.autograd.grad(loss(kappa, rho, th, True), (kappa, rho, th))
+    base = (k0, r0, t0)
+    for which, gvec in enumerate(grads):
+        for e in torch.argsort(gvec.abs(), descending=True)[:3].tolist():
+            h = 1e-5 * float(base[which][e])
+            vals = []
+            for sgn in (1.0, -1.0):
+                args = [b.clone() for b in base]
+                args[which][e] += sgn * h
+                with torch.no_grad():
+                    vals.append(float(loss(*(a.to(cuda) for a in args), False)))
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - float(gvec[e])) <= 1e-6 * abs(float(gvec[e])), (which, e, fd, float(gvec[e]))
+
+
 def test_solid_heat_larger_mesh_against_oracle(cuda):
     """16^3 jittered Hexa1 cube, conductivity varying per element: temperatures
     and the compliance gradient against the oracle."""

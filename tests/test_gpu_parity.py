@@ -491,21 +491,6 @@ def test_simp_full_size_central_differences(cuda, golden):
 
 
 # ------------------------------------------------------------ full sizes ---
-def test_config2_full_size_mixed_matches_fp64(cuda):
-    """Config 2 at full size (70^3 jittered Hexa1, 1,073,733 DOF): the mixed
-    path with block Jacobi (FP32 storage and CG inside FP64 residual
-    replacement) against the FP64 path: u, sigma and d(sum u)/d(forces) to 1e-8 relative."""
-    import bench
-
-    m, forces = bench.cube_workload(70, cuda)
-    um, fm, sm, _, _, gm = bench.step(m, forces, "mixed", 1e-10, precond="jacobi")
-    up, fp, sp, _, _, gp = bench.step(m, forces, "fp64", 1e-10)
-    assert m.n_dofs == 1_073_733
-    assert rel(um, up) <= RTOL
-    assert rel(sm, sp) <= RTOL
-    assert rel(gm, gp) <= RTOL
-
-
 def test_config4_full_size_gradient_central_differences(cuda):
     """Config 4 at full size (30 x 10 x 10 box, 6 Tetra2 per hex, 80,703 DOF,
     Neo-Hookean, nlgeom, x = 3 face pulled to +0.5): d(tip reaction)/dE_e

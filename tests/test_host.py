@@ -229,10 +229,12 @@ def test_heat_time_integration_validates_t_output():
         model.time_integration(torch.tensor([-1.0, 1.0]))
     with pytest.raises(ValueError, match="strictly increasing"):
         model.time_integration(torch.tensor([0.0, 2.0, 2.0]))
-    kappa = torch.tensor(400.0, requires_grad=True)
-    with pytest.raises(NotImplementedError, match="gradients"):
-        PlanarHeat(*mesh.rect_quad(3, 3), IsotropicConductivity2D(kappa)).time_integration(
-            differentiable_parameters=kappa)
+    # prescribed temperatures are the one input the GPU adjoint does not differentiate
+    model = PlanarHeat(*mesh.rect_quad(3, 3), IsotropicConductivity2D(kappa=400.0))
+    temps = torch.zeros(model.n_nod, 1, requires_grad=True)
+    model.temperatures = temps
+    with pytest.raises(NotImplementedError, match="prescribed temperatures"):
+        model.time_integration(differentiable_parameters=temps)
 
 
 def test_conductivity_kernel_data():

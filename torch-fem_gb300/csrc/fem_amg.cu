@@ -42,6 +42,7 @@ namespace tfg {
 
 int etype_info(int etype, int* ne, int* d, int* nip);
 extern int g_timing;  // fem_set_timing
+int g_amg_half = 1;   // FP16 smoothing copy of the level-0 matrix (fem_amg_set_half_smoother)
 size_t scan_workspace_bytes(int64_t n);
 int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
 
@@ -943,6 +944,9 @@ struct OpArgs {
   double* partial;
   AmgCtrl* ctrl;
   double* lz;      // Lanczos coefficients (kOpLzQ)
+  unsigned int* gcount;  // arrival counters of the level-0 reduction groups (grid_sum2)
+  const __half* sv16;    // level 0: FP16 smoothing copy of the sliced matrix (scaled by 1 / *s16inv)
+  const float* s16inv;
 };
 
 template <int MODE>
@@ -1048,19 +1052,111 @@ __host__ __device__ constexpr bool op_has_dot() {
   return MODE == kOpS4Dot || MODE == kOpQ || MODE == kOpLzQ || MODE == kOpQc;
 }
 
-// Level 0: the sliced FP32 matrix (the layout of fem_assemble_sell): a CTA
-// takes kSellSpc<MODE> consecutive slices of 32 rows, thread per row, the
-// kSellW warps sharing each slice's slots (short dependent chains), partial
-// rows summed in shared memory in a fixed order.  The grid covers every
-// slice, so the hardware balances the tail; the modes that end in a grid
-// reduction take several slices per CTA so that few CTAs arrive at it.  The
-// matrix streams with L2 evict_first; the vectors stay in L2.
-template <int MODE>
-__host__ __device__ constexpr int kSellSpc() {
-  return op_has_dot<MODE>() ? 8 : 1;
+// Level 0: the sliced FP32 matrix (the layout of fem_assemble_sell): one CTA
+// per slice of 32 rows, thread per row, the kSellW warps sharing the slice's
+// slots (short dependent chains), partial rows summed in shared memory in a
+// fixed order.  The grid covers every slice, so the hardware balances the
+// tail.  The matrix streams with L2 evict_first; the vectors stay in L2.
+//
+// The smoothing passes (S1..S4) may read an FP16 copy of the same matrix
+// instead (sv16, built by k_sell_to_half): Chebyshev smoothing only has to
+// damp the rough error, and one consistent copy in all four passes keeps the
+// V-cycle a fixed symmetric operator (pre- and post-smoothing are adjoint),
+// so CG still applies; CG's own q = A p always uses the FP32 matrix.
+constexpr int kDotGroup = 64;  // CTAs whose partial sums one arriving CTA adds first
+
+// True in every thread of the CTA that arrives last of n at `counter`.
+__device__ __forceinline__ bool arrive_last_of(unsigned int* counter, unsigned int n) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == n - 1;
+  __syncthreads();
+  return last;
 }
 
-template <int D, int MODE>
+// Deterministic sum of v over the grid in two levels: each CTA writes its
+// sum to partial[b]; the last CTA to arrive in its group of kDotGroup
+// consecutive CTAs adds the group's partials in a fixed order into
+// partial[gridDim.x + g]; the last group to finish adds the group sums in a
+// fixed order.  The CTA that does that returns true with the total in *tot
+// (thread 0).  Every sum has a fixed order, whichever CTA computes it, so
+// the result does not depend on the arrival order.  Needs blockDim.x >=
+// kDotGroup, partial[gridDim.x + ceil(gridDim.x / kDotGroup)] and zeroed
+// counters.
+__device__ __forceinline__ bool grid_sum2(double v, double* partial, unsigned int* gcount, unsigned int* counter,
+                                          double* red, double* tot) {
+  const unsigned int n = gridDim.x, b = blockIdx.x;
+  const double s = block_sum(v, red);
+  if (threadIdx.x == 0) partial[b] = s;
+  const unsigned int g = b / kDotGroup, g0 = g * kDotGroup;
+  const unsigned int gn = min((unsigned int)kDotGroup, n - g0);
+  const unsigned int n_groups = (n + kDotGroup - 1) / kDotGroup;
+  if (!arrive_last_of(&gcount[g], gn)) return false;
+  const double gs = block_sum(threadIdx.x < gn ? __ldcg(partial + g0 + threadIdx.x) : 0.0, red);
+  if (threadIdx.x == 0) {
+    partial[n + g] = gs;
+    gcount[g] = 0;
+  }
+  if (!arrive_last_of(counter, n_groups)) return false;
+  const double t = sum_partials(partial + n, (int)n_groups, 1, 0, red);
+  if (threadIdx.x == 0) *counter = 0;
+  *tot = t;
+  return true;
+}
+
+__device__ __forceinline__ uint32_t ld_l2_b32(const void* ptr, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+__device__ __forceinline__ uint16_t ld_l2_b16(const void* ptr, uint64_t pol) {
+  uint16_t v;
+  asm("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
+// The DD values of slot-row entry `lane` of the FP16 copy.  Layout of one
+// slot-row (32 rows, DD values each, DD * 64 bytes): the value pairs (0,1),
+// (2,3), ... as [pair][lane] half2 words, then an odd last value as [lane]
+// halves.  base16 points at the slot-row.
+template <int DD>
+__device__ __forceinline__ void load_slot16(const __half* __restrict__ base16, int lane, uint64_t pol,
+                                            float (&m)[DD]) {
+#pragma unroll
+  for (int p = 0; p < DD / 2; ++p) {
+    const uint32_t w = ld_l2_b32(base16 + p * 64 + 2 * lane, pol);
+    const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w));
+    m[2 * p] = f.x;
+    m[2 * p + 1] = f.y;
+  }
+  if constexpr (DD % 2 == 1) {
+    const uint16_t hv = ld_l2_b16(base16 + (DD / 2) * 64 + lane, pol);
+    m[DD - 1] = __half2float(*reinterpret_cast<const __half*>(&hv));
+  }
+}
+
+// The smoothing modes, which may read the FP16 copy.
+template <int MODE>
+__host__ __device__ constexpr bool op_smoothing() {
+  return MODE == kOpS1 || MODE == kOpS2 || MODE == kOpS3 || MODE == kOpS4 || MODE == kOpS4Dot;
+}
+
+// Values of slot k of this thread's row: FP32 matrix, or the FP16 copy (H).
+template <int DD, bool H>
+__device__ __forceinline__ void load_slot(const float* __restrict__ vp, const __half* __restrict__ hp, int k,
+                                          int lane, uint64_t pol, float (&m)[DD]) {
+  if constexpr (H) {
+    load_slot16<DD>(hp + (int64_t)k * DD * 32, lane, pol, m);
+  } else {
+    const float* vk = vp + (int64_t)k * DD * 32;
+#pragma unroll
+    for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, pol);
+  }
+}
+
+template <int D, int MODE, bool H>
 __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const int64_t* __restrict__ sell_base,
                                                          const int32_t* __restrict__ col,
                                                          const float* __restrict__ sval, OpArgs a) {
@@ -1070,15 +1166,14 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   if (amg_idle(a.ctrl)) return;
   const float* __restrict__ v = op_operand<MODE>(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t n_slices = (n_rows + 31) >> 5;
   const uint64_t pol = l2_policy(false);
   double dot = 0.0;
-  const int64_t s_end = ((int64_t)blockIdx.x + 1) * kSellSpc<MODE>();
-  for (int64_t s = (int64_t)blockIdx.x * kSellSpc<MODE>(); s < (s_end < n_slices ? s_end : n_slices); ++s) {
+  const int64_t s = blockIdx.x;
   const int64_t b0 = sell_base[s];
   const int len = (int)((sell_base[s + 1] - b0) >> 5);
   const int32_t* cp = col + b0 + lane;
   const float* vp = sval + b0 * DD + lane;
+  const __half* hp = H ? a.sv16 + b0 * DD : nullptr;
   float y[D];
 #pragma unroll
   for (int c = 0; c < D; ++c) y[c] = 0.f;
@@ -1088,23 +1183,21 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
     // gathers (same summation order as the loop below)
     for (; k0 + 7 * kSellW < len; k0 += 8 * kSellW) {
       int64_t cc[8];
-      float mv[8];
+      float mv[8][1];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         cc[u] = ld_l2(cp + (int64_t)(k0 + u * kSellW) * 32, pol);
-        mv[u] = ld_l2(vp + (int64_t)(k0 + u * kSellW) * 32, pol);
+        load_slot<1, H>(vp, hp, k0 + u * kSellW, lane, pol, mv[u]);
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) y[0] = fmaf(mv[u], v[cc[u]], y[0]);
+      for (int u = 0; u < 8; ++u) y[0] = fmaf(mv[u][0], v[cc[u]], y[0]);
     }
   }
 #pragma unroll 2
   for (int k = k0; k < len; k += kSellW) {
     const int64_t cc = ld_l2(cp + (int64_t)k * 32, pol);
-    const float* vk = vp + (int64_t)k * DD * 32;
     float m[DD];
-#pragma unroll
-    for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, pol);
+    load_slot<DD, H>(vp, hp, k, lane, pol, m);
     float xv[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) xv[j] = v[cc * D + j];
@@ -1119,29 +1212,67 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   if (w == 0) {
     const int64_t i = s * 32 + lane;
     if (i < n_rows) {
+      const float sc = H ? *a.s16inv : 1.f;  // a power of two: exact
       float yt[D];
 #pragma unroll
       for (int c = 0; c < D; ++c) {
         float t = ys[0][c][lane];
 #pragma unroll
         for (int u = 1; u < kSellW; ++u) t += ys[u][c][lane];
-        yt[c] = t;
+        yt[c] = H ? t * sc : t;
       }
       dot += op_epilogue<D, MODE>(a, i, yt);
     }
   }
-  __syncthreads();
-  }
   if constexpr (op_has_dot<MODE>()) {
-    const double bsum = block_sum(dot, red);
-    if (threadIdx.x == 0) a.partial[blockIdx.x] = bsum;
-    if (arrive_last(&a.ctrl->counter)) {
-      const double tot = sum_partials(a.partial, gridDim.x, 1, 0, red);
-      if (threadIdx.x == 0) {
-        a.ctrl->counter = 0;
-        op_finish<MODE>(a, tot);
-      }
-    }
+    double tot = 0.0;
+    if (grid_sum2(dot, a.partial, a.gcount, &a.ctrl->counter, red, &tot) && threadIdx.x == 0)
+      op_finish<MODE>(a, tot);
+  }
+}
+
+// The FP16 smoothing copy: max |a_ij| over the sliced FP32 values (as the
+// bit pattern of a non-negative float, whose integer order is the float
+// order; a max is exact and order-independent).
+__global__ void k_abs_max(int64_t n, const float* __restrict__ v, unsigned int* __restrict__ out) {
+  float m = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(v[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// Power-of-two scale that maps max |a_ij| into [2^13, 2^14): every value
+// keeps FP16's 11-bit significand down to 2^-24 of the largest one, far from
+// FP16's maximum 65504.
+__device__ __forceinline__ float half_scale(unsigned int maxbits, bool inverse) {
+  const float mx = __uint_as_float(maxbits);
+  if (!(mx > 0.f) || !isfinite(mx)) return 1.f;
+  int e;
+  frexpf(mx, &e);
+  return ldexpf(1.f, inverse ? e - 14 : 14 - e);
+}
+
+// FP16 copy of the sliced matrix in the slot-row layout of load_slot16, a
+// thread per (slot-row, row).
+template <int DD>
+__global__ void k_sell_to_half(int64_t n_blocks, const float* __restrict__ sval,
+                               const unsigned int* __restrict__ maxbits, __half* __restrict__ sv16,
+                               float* __restrict__ s16inv) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) *s16inv = half_scale(*maxbits, true);
+  if (t >= n_blocks) return;
+  const float sc = half_scale(*maxbits, false);
+  const int64_t sr = t >> 5;
+  const int lane = (int)(t & 31);
+  const float* src = sval + sr * 32 * DD + lane;
+  __half* dst = sv16 + sr * 32 * DD;
+#pragma unroll
+  for (int e = 0; e < DD; ++e) {
+    const __half hv = __float2half_rn(src[e * 32] * sc);
+    if (DD % 2 == 1 && e == DD - 1) dst[(DD / 2) * 64 + lane] = hv;
+    else dst[(e / 2) * 64 + 2 * lane + (e & 1)] = hv;
   }
 }
 
@@ -1767,6 +1898,7 @@ struct fem_amg {
   tfg::AmgCtrl* lzc = nullptr;
   double* lz = nullptr;
   double* partial = nullptr;
+  unsigned int* gcount = nullptr;  // arrival counters of the level-0 reduction groups
   int32_t* status = nullptr;
   unsigned long long* counter = nullptr;
   std::vector<void*> mem;
@@ -1784,6 +1916,11 @@ struct fem_amg {
   const int32_t* sell_col = nullptr;
   const float* sell_val = nullptr;
   const float* dinv0 = nullptr;
+  // FP16 smoothing copy of the level-0 matrix (allocated at the first setup)
+  __half* sv16 = nullptr;
+  int64_t sv16_len = 0;
+  float* s16inv = nullptr;
+  unsigned int* absmax = nullptr;
 
   template <typename T>
   T* alloc(int64_t count, cudaStream_t st) {
@@ -2085,9 +2222,15 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
   // per-CTA partial sums: the level-0 SpMV grid has one CTA per slice
   const int64_t n_partial = std::max<int64_t>(kPartialLen, (n0 + 31) / 32 + 1);
   h->partial = h->alloc<double>(2 * n_partial, st);
+  const int64_t n_groups = n_partial / kDotGroup + 2;
+  h->gcount = h->alloc<unsigned int>(n_groups, st);
+  h->s16inv = h->alloc<float>(1, st);
+  h->absmax = h->alloc<unsigned int>(1, st);
   double* origin = h->alloc<double>(3, st);
-  if (!h->active || !h->status || !h->counter || !h->ctrl || !h->lzc || !h->lz || !h->partial || !origin)
+  if (!h->active || !h->status || !h->counter || !h->ctrl || !h->lzc || !h->lz || !h->partial || !h->gcount ||
+      !h->s16inv || !h->absmax || !origin)
     return check_cuda("AMG buffers");
+  cudaMemsetAsync(h->gcount, 0, sizeof(unsigned int) * n_groups, st);
   cudaMemsetAsync(h->status, 0, sizeof(int32_t), st);
   cudaMemsetAsync(h->ctrl, 0, sizeof(AmgCtrl), st);
   cudaMemsetAsync(h->lzc, 0, sizeof(AmgCtrl), st);
@@ -2184,6 +2327,9 @@ OpArgs level_args(fem_amg* h, int l, AmgCtrl* ctrl) {
   a.partial = h->partial;
   a.ctrl = ctrl;
   a.lz = h->lz;
+  a.gcount = h->gcount;
+  a.sv16 = h->sv16;
+  a.s16inv = h->s16inv;
   return a;
 }
 
@@ -2195,8 +2341,11 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
     const int64_t ns = (L.n + 31) / 32;
     const bool timed = h->ev_ready && h->ev_used < fem_amg::kTimed;
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used], st);
-    k_sell_op<B0, MODE><<<grid_for(ns, kSellSpc<MODE>()), kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col,
-                                                                                 h->sell_val, a);
+    if (op_smoothing<MODE>() && h->sv16 && g_amg_half)
+      k_sell_op<B0, MODE, true><<<(unsigned)ns, kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
+    else
+      k_sell_op<B0, MODE, false><<<(unsigned)ns, kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val,
+                                                                        a);
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used++ + 1], st);
   } else {
     k_csr_op<K, MODE><<<capped(L.n, 16), kRowT, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
@@ -2221,13 +2370,14 @@ int lanczos_level(fem_amg* h, int l, cudaStream_t st, double* rho) {
   a.partial = h->partial;
   a.ctrl = h->lzc;
   a.lz = h->lz;
+  a.gcount = h->gcount;
   for (int j = 0; j < kLanczos; ++j) {
     bool sliced = false;
     if constexpr (B <= 3) {  // level 0 (B = dim) holds the sliced matrix
       if (l == 0) {
         const int64_t ns = (n + 31) / 32;
-        k_sell_op<B, kOpLzQ><<<grid_for(ns, kSellSpc<kOpLzQ>()), kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col,
-                                                                                      h->sell_val, a);
+        k_sell_op<B, kOpLzQ, false><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
+                                                                           a);
         sliced = true;
       }
     }
@@ -2271,6 +2421,31 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
   h->sell_val = static_cast<const float*>(A->val);
   h->dinv0 = static_cast<const float*>(A->precond);
   cudaMemsetAsync(h->status, 0, sizeof(int32_t), st);
+  {
+    // the FP16 smoothing copy, sized from the sliced layout at the first setup
+    const int64_t ns = (h->L[0].n + 31) / 32;
+    int64_t slots = 0;
+    if (cudaMemcpyAsync(&slots, A->row_ptr + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return check_cuda("AMG setup");
+    const int64_t len = slots * B0 * B0;
+    if (len != h->sv16_len) {
+      if (h->sv16) {
+        cudaFree(h->sv16);
+        h->mem.erase(std::remove(h->mem.begin(), h->mem.end(), (void*)h->sv16), h->mem.end());
+        h->sv16 = nullptr;
+        h->sv16_len = 0;
+      }
+      h->sv16 = h->alloc<__half>(len, st);
+      if (!h->sv16) return check_cuda("AMG FP16 smoothing copy");
+      h->sv16_len = len;
+    }
+    cudaMemsetAsync(h->absmax, 0, sizeof(unsigned int), st);
+    k_abs_max<<<capped(grid_for(len, kT), 8), kT, 0, st>>>(len, h->sell_val, h->absmax);
+    note_launch();
+    k_sell_to_half<B0 * B0><<<grid_for(slots, kT), kT, 0, st>>>(slots, h->sell_val, h->absmax, h->sv16, h->s16inv);
+    note_launch();
+  }
   for (int l = 0; l + 1 < h->n_levels; ++l) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
@@ -2376,6 +2551,7 @@ void launch_iteration(fem_amg* h, cudaStream_t st) {
   a.xb = h->z;
   a.partial = h->partial;
   a.ctrl = h->ctrl;
+  a.gcount = h->gcount;
   launch_op<B0, K, kOpQc>(h, 0, a, st);
   k_cg_update<B0><<<capped(grid_for(h->L[0].n, kT), 8), kT, 0, st>>>(h->L[0].n, h->xlo, h->rcg, h->p, h->q, h->dinv0,
                                                                       h->L[0].theta_inv, h->L[0].d, h->L[0].x,
@@ -2614,6 +2790,8 @@ int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const
   if (h->dim == 2) return pcg_impl<2, 3>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
   return pcg_impl<1, 1>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
 }
+
+void fem_amg_set_half_smoother(int enable) { g_amg_half = enable ? 1 : 0; }
 
 int fem_amg_levels(const fem_amg* h) { return h ? h->n_levels : 0; }
 

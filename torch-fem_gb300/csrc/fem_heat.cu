@@ -258,6 +258,35 @@ __global__ void k_heat_mass(int64_t n_elem, const double* __restrict__ detj, con
   for (int b = 0; b < NE; ++b) me[(e * NE + a) * NE + b] = (T)row[b];
 }
 
+// Capacity vector-Jacobian product, a thread per element:
+// out_e = sum_ip w detJ (N . a_e)(N . b_e), i.e. a_e^T m_e b_e / (rho_e t_e)
+// for the capacity matrix m_e of k_heat_mass.
+template <int NE, int D, int NIP>
+__global__ void k_heat_mass_vjp(int64_t n_elem, const int32_t* __restrict__ conn, const double* __restrict__ detj,
+                                const double* __restrict__ w, const double* __restrict__ nval,
+                                const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elem) return;
+  double av[NE], bv[NE];
+#pragma unroll
+  for (int k = 0; k < NE; ++k) {
+    const int64_t nd = conn[e * NE + k];
+    av[k] = a[nd];
+    bv[k] = b[nd];
+  }
+  double s = 0.0;
+  for (int ip = 0; ip < NIP; ++ip) {
+    double na = 0.0, nb = 0.0;
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+      na += nval[ip * NE + k] * av[k];
+      nb += nval[ip * NE + k] * bv[k];
+    }
+    s += w[ip] * detj[(int64_t)ip * n_elem + e] * na * nb;
+  }
+  out[e] = s;
+}
+
 // out = a x + b y over the stored entries of two matrices of one pattern.
 __global__ void k_csr_combine(int64_t nnz, double a, const double* __restrict__ x, double b,
                               const double* __restrict__ y, double* __restrict__ out) {
@@ -400,6 +429,26 @@ int fem_heat_mass(const fem_mesh* m, const double* rho, const double* nval, int 
   TFG_DISPATCH_ETYPE(m->etype)
 #undef TFG_BODY
   return check_cuda("fem_heat_mass");
+}
+
+int fem_heat_mass_vjp(const fem_mesh* m, const double* nval, const double* a, const double* b, double* out,
+                      void* stream) {
+  int rc = check_heat_mesh(m, "fem_heat_mass_vjp");
+  if (rc) return rc;
+  if (!nval || !a || !b || !out) {
+    set_last_error("fem_heat_mass_vjp: nval, a, b and out are required");
+    return FEM_INVALID;
+  }
+  cudaStream_t st = as_stream(stream);
+#define TFG_BODY                                                                                         \
+  {                                                                                                      \
+    k_heat_mass_vjp<NE, D, NIP><<<grid_for(m->n_elem, 128), 128, 0, st>>>(m->n_elem, m->elements, m->detj, \
+                                                                         m->weights, nval, a, b, out);  \
+    ::tfg::note_launch();                                                                                \
+  }
+  TFG_DISPATCH_ETYPE(m->etype)
+#undef TFG_BODY
+  return check_cuda("fem_heat_mass_vjp");
 }
 
 int fem_csr_combine(int64_t nnz, double a, const double* x, double b, const double* y, double* out,

@@ -1772,7 +1772,7 @@ static size_t layout(const fem_matrix* A, int64_t fe_len, Vecs* v, void* ws) {
 
 template <int G, typename VT>
 static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_t max_iter,
-                   const Vecs& v, fem_solve_info* info, cudaStream_t st) {
+                   const Vecs& v, fem_solve_info* info, cudaStream_t st, bool timing_on) {
   Ctrl h;
   memset(&h, 0, sizeof(h));
   h.max_iter = max_iter;
@@ -1793,9 +1793,11 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
   TFG_CHECK_LAUNCH("fem_pcg init");
   int rc = read_ctrl(v.ctrl, &h, st);
   if (rc) return rc;
-  const bool timing = g_timing && g_timer.init() == FEM_OK;
-  g_timer.ms = 0.0;
-  g_timer.timed = 0;
+  const bool timing = timing_on && g_timer.init() == FEM_OK;
+  if (timing) {
+    g_timer.ms = 0.0;
+    g_timer.timed = 0;
+  }
   int chunk = 8;
   while (h.done == kDoneNo) {
     rc = iterate<G, VT>(A, xv, (VT*)v.r, (VT*)v.z, (VT*)v.p, (VT*)v.q, v.partial, v.ctrl, &h, timing,
@@ -1810,8 +1812,8 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
     info->replacements = 0;
     info->rel_residual = h.bb > 0 ? sqrt(h.rr / h.bb) / h.rscale : 0.0;
     info->status = status_of(h.done);
-    info->spmv_ms = g_timer.ms;
-    info->spmv_timed = g_timer.timed;
+    info->spmv_ms = timing ? g_timer.ms : 0.0;
+    info->spmv_timed = timing ? g_timer.timed : 0;
   }
   if (h.done == kDoneBarrierTimeout)
     set_last_error("persistent CG: a grid-barrier or TMA-stage wait ran out (barrier timeout) after %lld iterations",
@@ -1957,9 +1959,10 @@ int fem_pcg(const fem_matrix* A, const double* b, double* x, double rtol, int64_
   cudaStream_t st = as_stream(stream);
   Vecs v;
   layout(A, 0, &v, ws);
-  if (A->format == FEM_FMT_CSR_F64) return run_pcg<1, double>(A, b, x, rtol, max_iter, v, info, st);
-  if (A->block == 2) return run_pcg<2, float>(A, b, x, rtol, max_iter, v, info, st);
-  return run_pcg<3, float>(A, b, x, rtol, max_iter, v, info, st);
+  const bool timing = g_timing != 0;
+  if (A->format == FEM_FMT_CSR_F64) return run_pcg<1, double>(A, b, x, rtol, max_iter, v, info, st, timing);
+  if (A->block == 2) return run_pcg<2, float>(A, b, x, rtol, max_iter, v, info, st, timing);
+  return run_pcg<3, float>(A, b, x, rtol, max_iter, v, info, st, timing);
 }
 
 static int64_t op_fe_len(const fem_operator64* op) {
@@ -2105,8 +2108,8 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
     info->replacements = h.replacements;
     info->rel_residual = h.bb > 0 ? sqrt(h.rr_true / h.bb) : 0.0;
     info->status = status_of(h.done);
-    info->spmv_ms = g_timer.ms;
-    info->spmv_timed = g_timer.timed;
+    info->spmv_ms = timing ? g_timer.ms : 0.0;
+    info->spmv_timed = timing ? g_timer.timed : 0;
   }
   if (h.done == kDoneBarrierTimeout)
     set_last_error("persistent CG: a grid-barrier or TMA-stage wait ran out (barrier timeout) after %lld iterations",
@@ -2286,7 +2289,9 @@ static std::mutex g_scratch_mutex;
 
 // Device address of the scratch array on the current device.  The array's
 // name is a host-side stand-in, so the address is looked up once per device
-// with that device current.
+// with that device current and kept for the life of the process: the entry
+// point must not be used on a device after cudaDeviceReset (or any other
+// re-creation of its primary context) in this process.
 static int static_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return check_cuda("fem_pcg_static: cudaGetDevice");
@@ -2318,11 +2323,17 @@ int fem_pcg_static(const fem_matrix* A, const double* b, double* x, double rtol,
                    fem_solve_info* info, void* stream) {
   int rc = validate_matrix(A);
   if (rc) return rc;
+  if (A->n > kStaticMaxUnknowns) {
+    set_last_error("fem_pcg_static: %lld unknowns exceed the static workspace limit of %lld unknowns; "
+                   "use fem_pcg with a caller workspace",
+                   (long long)A->n, (long long)kStaticMaxUnknowns);
+    return FEM_BOUNDS;
+  }
   const size_t need = fem_pcg_workspace_bytes(A);
-  if (A->n > kStaticMaxUnknowns || need > kStaticScratchBytes) {
-    set_last_error("fem_pcg_static: %lld unknowns exceed the static workspace limit of %lld "
-                   "(%zu bytes needed, %zu available); use fem_pcg with a caller workspace",
-                   (long long)A->n, (long long)kStaticMaxUnknowns, need, kStaticScratchBytes);
+  if (need > kStaticScratchBytes) {
+    set_last_error("fem_pcg_static: the solve needs %zu bytes of scratch, more than the static workspace "
+                   "limit of %zu bytes; use fem_pcg with a caller workspace",
+                   need, kStaticScratchBytes);
     return FEM_BOUNDS;
   }
   void* ws = nullptr;
@@ -2331,13 +2342,11 @@ int fem_pcg_static(const fem_matrix* A, const double* b, double* x, double rtol,
   cudaStream_t st = as_stream(stream);
   Vecs v;
   layout(A, 0, &v, ws);
-  // The SpMV event timer creates CUDA events on first use; keep it off here.
-  const int timing = g_timing;
-  g_timing = 0;
-  if (A->format == FEM_FMT_CSR_F64) rc = run_pcg<1, double>(A, b, x, rtol, max_iter, v, info, st);
-  else if (A->block == 2) rc = run_pcg<2, float>(A, b, x, rtol, max_iter, v, info, st);
-  else rc = run_pcg<3, float>(A, b, x, rtol, max_iter, v, info, st);
-  g_timing = timing;
+  // no SpMV event timing here: the timer creates CUDA events on first use
+  // (and the process-wide timing switch is left alone)
+  if (A->format == FEM_FMT_CSR_F64) rc = run_pcg<1, double>(A, b, x, rtol, max_iter, v, info, st, false);
+  else if (A->block == 2) rc = run_pcg<2, float>(A, b, x, rtol, max_iter, v, info, st, false);
+  else rc = run_pcg<3, float>(A, b, x, rtol, max_iter, v, info, st, false);
   return rc;
 }
 

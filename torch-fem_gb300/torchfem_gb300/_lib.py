@@ -204,6 +204,9 @@ _SIGNATURES = {
         C.c_int, [_P(FemMesh), vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     ),
     "fem_heat_mass": (C.c_int, [_P(FemMesh), vp, vp, C.c_int, vp, vp, vp]),
+    "fem_heat_mass_vjp": (C.c_int, [_P(FemMesh), vp, vp, vp, vp, vp]),
+    "fem_mass_matrices": (C.c_int, [_P(FemMesh), vp, vp, C.c_int, vp, vp]),
+    "fem_csr_spmm": (C.c_int, [_P(FemMatrix), C.c_int, vp, vp, vp]),
     "fem_csr_combine": (C.c_int, [i64, C.c_double, vp, C.c_double, vp, vp, vp]),
     "fem_heat_cn_workspace_bytes": (C.c_size_t, [i64]),
     "fem_heat_cn_residual": (
@@ -233,6 +236,7 @@ _SIGNATURES = {
     "fem_jacobi": (C.c_int, [vp, vp, i64, vp, vp, vp]),
     "fem_block_jacobi": (C.c_int, [_P(FemBlocks), vp, vp, vp, vp, vp]),
     "fem_set_timing": (None, [C.c_int]),
+    "fem_amg_set_half_smoother": (None, [C.c_int]),
     "fem_set_cg_path": (None, [C.c_int]),
     "fem_get_cg_path": (C.c_int, []),
     "fem_pcg_workspace_bytes": (C.c_size_t, [_P(FemMatrix)]),

@@ -17,7 +17,7 @@ from ._device import DeviceMesh
 from .elements import Element
 from .materials import Material
 from ._nonlinear import IntegrateNonlinear, NewtonNonlinear, NLContext
-from .sparse import IntegrateMaterial, NewtonLinear, SolveContext
+from .sparse import CrankNicolsonStep, IntegrateMaterial, NewtonLinear, SolveContext, TransientContext
 
 _REFERENCE_METHODS = ("spsolve", "minres", "cg", "pardiso", "amgx")
 _GPU_METHODS = {None: "fp64", "cg": "fp64", "gb300": "fp64", "gb300-mixed": "mixed"}
@@ -190,6 +190,35 @@ class FEM:
         del refs
         return ke.to(self.nodes.device, self.nodes.dtype)
 
+    def solve_modes(self, n_modes: int, tol: float = 1e-10, max_iter: int = 500) -> tuple[Tensor, Tensor]:
+        """Natural frequencies and mode shapes (base.py:1097-1129): the
+        n_modes lowest eigenpairs of K phi = omega^2 M phi on the free DOFs.
+
+        Returns (omega_sq [n_modes], differentiable w.r.t. the material
+        parameters, the density and the thickness; modes [n_modes, n_nod,
+        n_dof_per_node], detached, M-normalised), like the reference.  The
+        eigenpairs come from LOBPCG on the GPU (torchfem_gb300.modal) instead
+        of shift-invert eigsh; `tol` is the relative eigen-residual
+        ||K phi - omega^2 M phi|| / ||K phi|| at which a mode has converged.
+        """
+        from .modal import ModalSolve
+
+        dm = self.device_mesh
+        dev = dm.device
+        assert self.material is not None
+        kind, mat_data = self.material.kernel_data(self.n_elem)
+        if isinstance(kind, str):
+            raise NotImplementedError(f"{type(self.material).__name__} has a state-dependent tangent")
+        mat_data = mat_data.to(dev, torch.float64).contiguous()
+        thickness = self._thickness()
+        if thickness is not None:
+            thickness = thickness.to(dev, torch.float64).contiguous()
+        rho = torch.as_tensor(self.material.rho).to(dev, torch.float64).expand(self.n_elem).contiguous()
+        omega_sq, phi = ModalSolve.apply(self, int(n_modes), mat_data, thickness, rho, tol, max_iter)
+        modes = phi.T.reshape(n_modes, self.n_nod, self.n_dof_per_node)
+        out = self.nodes.device
+        return omega_sq.to(out, self.nodes.dtype), modes.detach().to(out, self.nodes.dtype)
+
     # -------------------------------------------------------------- solve --
     def solve(
         self,
@@ -246,7 +275,9 @@ class FEM:
         dev = dm.device
         out_dev = self.nodes.device
         d = self.n_dof_per_node
-        con_bool = self._constraints.reshape(-1).to(dev)
+        # a copy: a later in-place edit of the model's constraints must not
+        # reach the mask this solve's backward uses
+        con_bool = self._constraints.reshape(-1).to(dev).clone()
         con_mask = con_bool.to(torch.uint8).contiguous()
         assert self.material is not None
         mat_kind, mat_data = self.material.kernel_data(self.n_elem)
@@ -529,15 +560,26 @@ class Heat(FEM):
         `solve` with every DOF constrained; each later time step runs Newton
         iterations on r = M du + dt/2 (f_old + f_int + f_ext) (r = 0 on
         constrained DOFs) with (M + dt/2 K) du = -r solved by the GPU CG to
-        `stol`.  As in the reference, the internal heat flux of the first
-        step's f_old is zero.  Gradients through the time integration are not
-        implemented on this path.
+        `stol` in FP64 (`CrankNicolsonStep`).  As in the reference, the
+        internal heat flux of the first step's f_old is zero.
+
+        Gradients flow through the whole integration as in the reference's
+        autograd through its Newton steps: every step is an autograd node with
+        a hand-written adjoint (`CrankNicolsonStep.backward`), and the
+        converged-state evaluation of each step is `IntegrateMaterial`, so a
+        loss on temperatures, internal heat fluxes and fluxes reaches the
+        conductivity, density, thickness and heat sources.  Prescribed
+        temperatures are not differentiable on this path.
         """
-        if differentiable_parameters is not None:
-            params = (differentiable_parameters,) if isinstance(differentiable_parameters, Tensor) \
-                else tuple(differentiable_parameters)
-            if any(p.requires_grad for p in params):
-                raise NotImplementedError("gradients through time_integration are not implemented on the GPU path")
+        if differentiable_parameters is None:
+            params: tuple = ()
+        elif isinstance(differentiable_parameters, Tensor):
+            params = (differentiable_parameters,)
+        else:
+            params = tuple(differentiable_parameters)
+        track = any(p.requires_grad for p in params)
+        if track and self._dirichlet.requires_grad:
+            raise NotImplementedError("prescribed temperatures are not differentiable on the GPU path")
         resolve_precision(method, None)
         if device is not None and torch.device(device).type != "cuda":
             raise RuntimeError("torchfem_gb300 solves on a CUDA device only")
@@ -549,14 +591,6 @@ class Heat(FEM):
         if (t_output[1:] <= t_output[:-1]).any():
             raise ValueError("t_output must be strictly increasing.")
 
-        # equilibrium at t = 0 with the temperatures imposed everywhere
-        bc_constraints = self.constraints.clone()
-        self.constraints[:] = True
-        try:
-            temp_eq, _, flux_eq, grad_eq, state_eq = self.solve(aggregate_integration_points=False, stol=stol)
-        finally:
-            self.constraints[:] = bc_constraints
-
         increments, t_rows = time_grid(t_output, delta_t)
         dts = (increments[1:] - increments[:-1]).tolist()
         n_out = len(increments)
@@ -565,77 +599,76 @@ class Heat(FEM):
         dev = dm.device
         con_mask = self._constraints.reshape(-1).to(dev).to(torch.uint8).contiguous()
         con = con_mask.bool()
-        mesh, mat, refs = self._device_material()
-        rho = torch.as_tensor(self.material.rho).detach().to(dev, torch.float64).expand(self.n_elem).contiguous()
         nip, fs = dm.nip, dm.flux_shape
-        u = torch.zeros(n_out, self.n_dofs, dtype=torch.float64, device=dev)
-        f = torch.zeros(n_out, self.n_dofs, dtype=torch.float64, device=dev)
-        flux = torch.zeros(n_out, nip, self.n_elem, *fs, dtype=torch.float64, device=dev)
-        grad = torch.zeros_like(flux)
-        state = torch.zeros(n_out, nip, self.n_elem, self.n_state, dtype=torch.float64, device=dev)
-        u[0] = temp_eq.reshape(-1).to(dev, torch.float64)
-        flux[0] = flux_eq.to(dev, torch.float64).reshape(nip, self.n_elem, *fs)
-        grad[0] = grad_eq.to(dev, torch.float64).reshape(nip, self.n_elem, *fs)
-        state[0] = state_eq.to(dev, torch.float64).reshape(nip, self.n_elem, self.n_state)
-        dirichlet = self._dirichlet.reshape(-1).to(dev, torch.float64)
-        u[0] = torch.where(con, dirichlet, u[0])
-        f_ext = self._neumann.reshape(-1).to(dev, torch.float64).contiguous()
+        assert self.material is not None
+        mat_kind, mat_data = self.material.kernel_data(self.n_elem)
+        if isinstance(mat_kind, str):
+            raise NotImplementedError(f"{type(self.material).__name__} has a state-dependent tangent")
 
-        # constant conductivity and capacity: both assembled once
-        kval = dm.assemble_csr(dm.element_stiffness(mesh, mat, torch.float64), con_mask)
-        mval = dm.assemble_csr(dm.heat_mass(mesh, rho), con_mask)
-        mass = dm.csr_system(mval, con_mask)
-        systems: dict[float, object] = {}
-        self.iterations: list[int] = []
+        with torch.set_grad_enabled(track):
+            # equilibrium at t = 0 with the temperatures imposed everywhere (the
+            # constraints are swapped, not written in place: the solve's
+            # autograd graph keeps the mask it ran with)
+            bc_constraints = self._constraints
+            self._constraints = torch.ones_like(bc_constraints)
+            try:
+                temp_eq, _, flux_eq, grad_eq, state_eq = self.solve(
+                    aggregate_integration_points=False, stol=stol, differentiable_parameters=params)
+            finally:
+                self._constraints = bc_constraints
+            mat_data = mat_data.to(dev, torch.float64).contiguous()
+            thickness = self._thickness()
+            if thickness is not None:
+                thickness = thickness.to(dev, torch.float64).contiguous()
+            rho = torch.as_tensor(self.material.rho).to(dev, torch.float64).expand(self.n_elem).contiguous()
+            f_ext = self._neumann.reshape(-1).to(dev, torch.float64).contiguous()
+            dirichlet = self._dirichlet.reshape(-1).to(dev, torch.float64).detach()
+            u_cur = torch.where(con, dirichlet, temp_eq.reshape(-1).to(dev, torch.float64))
+            flux_cur = flux_eq.to(dev, torch.float64).reshape(nip, self.n_elem, *fs)
+            grad_cur = grad_eq.to(dev, torch.float64).reshape(nip, self.n_elem, *fs)
+            state_cur = state_eq.to(dev, torch.float64).reshape(nip, self.n_elem, self.n_state)
+            f_cur = torch.zeros(self.n_dofs, dtype=torch.float64, device=dev)
 
-        for n in range(1, n_out):
-            dt_n = dts[n - 1]
-            u_prev = u[n - 1]
-            u_guess = u_prev.clone()
-            f_old = f[n - 1]
-            flux_prev = flux[n - 1].contiguous()
-            res0 = None
-            res_norm = float("inf")
-            f_int = f_old
-            if verbose:
-                print(f"time step {n}: t = {float(increments[n]):.6g}")
-            for it in range(max_iter):
-                du = (u_guess - u_prev).contiguous()
-                fe, flux_n, h_inc = dm.element_force(mesh, mat, du, None, None, 0, flux_prev, None,
-                                                     want_flux=True, want_h=True)
-                f_int, _ = dm.gather(fe)
-                flux[n] = flux_n.view(nip, self.n_elem, *fs)
-                grad[n] = grad[n - 1] + h_inc.view(nip, self.n_elem, *fs)
-                res, sumsq = dm.cn_residual(mass, du, f_old, f_int, f_ext, 0.5 * dt_n, con_mask)
-                res_norm = math.sqrt(float(sumsq.item()))
-                if it == 0:
-                    res0 = res_norm
+            # constant conductivity and capacity: both assembled once
+            mesh, mat, refs = self._device_material()
+            kval = dm.assemble_csr(dm.element_stiffness(mesh, mat, torch.float64), con_mask)
+            mval = dm.assemble_csr(dm.heat_mass(mesh, rho.detach()), con_mask)
+            del refs
+            tc = TransientContext(dm, con_mask, mat_kind, mval, kval, max_iter, rtol, atol, stol, verbose)
+            sc = SolveContext(dm, con_mask, mat_kind, "fp64", max_iter, rtol, atol, stol, None)
+            self.iterations = tc.iterations
+
+            us, fs_, fluxes, grads = [u_cur], [f_cur], [flux_cur], [grad_cur]
+            for n in range(1, n_out):
+                dt_n = dts[n - 1]
                 if verbose:
-                    print(f"  newton {it:2d}  |res| = {res_norm:.6e}")
-                if res_norm < rtol * res0 or res_norm < atol:
-                    break
-                sysm = systems.get(dt_n)
-                if sysm is None:
-                    sysm = dm.csr_system(dm.csr_combine(1.0, mval, 0.5 * dt_n, kval), con_mask)
-                    systems[dt_n] = sysm
-                x = dm.solve(sysm, (-res).contiguous(), stol)
-                self.iterations.append(sysm.stats.iterations)
-                u_guess = u_guess + x
-            if res_norm > rtol * res0 and res_norm > atol:
-                raise RuntimeError("Newton-Raphson iteration did not converge.")
-            u[n] = u_guess
-            f[n] = f_int
-        del refs
+                    print(f"time step {n}: t = {float(increments[n]):.6g}")
+                du = CrankNicolsonStep.apply(tc, dt_n, f_cur, flux_cur, f_ext, mat_data, thickness, rho)
+                f_int, flux_new, h_inc = IntegrateMaterial.apply(sc, du, flux_cur, None, mat_data, thickness)
+                u_cur = u_cur + du
+                f_cur = f_int
+                flux_cur = flux_new
+                grad_cur = grad_cur + h_inc
+                us.append(u_cur)
+                fs_.append(f_cur)
+                fluxes.append(flux_cur)
+                grads.append(grad_cur)
 
-        out_u = u[t_rows].reshape(-1, self.n_nod, 1)
-        out_f = f[t_rows].reshape(-1, self.n_nod, 1)
-        out_flux, out_grad, out_state = flux[t_rows], grad[t_rows], state[t_rows]
-        if aggregate_integration_points:
-            out_grad = out_grad.mean(dim=1)
-            out_flux = out_flux.mean(dim=1)
-            out_state = out_state.mean(dim=1)
-        out_flux = out_flux.squeeze((-2, -1))
-        out_grad = out_grad.squeeze((-2, -1))
+            rows = t_rows.tolist()
+            out_u = torch.stack([us[r] for r in rows]).reshape(-1, self.n_nod, 1)
+            out_f = torch.stack([fs_[r] for r in rows]).reshape(-1, self.n_nod, 1)
+            out_flux = torch.stack([fluxes[r] for r in rows])
+            out_grad = torch.stack([grads[r] for r in rows])
+            out_state = state_cur.unsqueeze(0).expand(len(rows), *state_cur.shape)
+            if aggregate_integration_points:
+                out_grad = out_grad.mean(dim=1)
+                out_flux = out_flux.mean(dim=1)
+                out_state = out_state.mean(dim=1)
+            out_flux = out_flux.squeeze((-2, -1))
+            out_grad = out_grad.squeeze((-2, -1))
+            if not track:
+                out_u, out_f, out_flux, out_grad, out_state = (
+                    t.detach() for t in (out_u, out_f, out_flux, out_grad, out_state))
         dt = self.nodes.dtype
         out_dev = self.nodes.device
         return tuple(t.to(out_dev, dt) for t in (out_u, out_f, out_flux, out_grad, out_state))

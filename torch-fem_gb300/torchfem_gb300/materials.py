@@ -115,13 +115,13 @@ class IsotropicElasticity3D(Material):
 
     def __init__(self, E, nu, rho=1.0):
         self.E = torch.as_tensor(E)
-        self.nu = torch.as_tensor(nu)
+        self.nu = torch.as_tensor(nu, device=self.E.device)
         self.rho = torch.as_tensor(rho)
         self.n_state = 0
         self.is_vectorized = self.E.dim() > 0
         self.lbd = self.E * self.nu / ((1.0 + self.nu) * (1.0 - 2.0 * self.nu))
         self.G = self.E / (2.0 * (1.0 + self.nu))
-        eye = torch.eye(3)
+        eye = torch.eye(3, dtype=self.lbd.dtype, device=self.lbd.device)
         i4 = torch.einsum("ij,kl->ijkl", eye, eye)
         i4s = torch.einsum("ik,jl->ijkl", eye, eye) + torch.einsum("il,jk->ijkl", eye, eye)
         self.C = self.lbd[..., None, None, None, None] * i4 + self.G[..., None, None, None, None] * i4s

@@ -19,12 +19,14 @@ increment, with its own kernel-based backward.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import warnings
 
 import torch
 from torch import Tensor
 
 from ._device import DeviceMesh, LinearSystem
+from ._lib import check, ptr
 
 
 class SolveContext:
@@ -224,4 +226,132 @@ class IntegrateMaterial(torch.autograd.Function):
             None if gde0 is None else gde0.view_as(de0),
             None if gmat is None else gmat.view_as(mat_data),
             gthick,
+        )
+
+
+class TransientContext:
+    """What one time_integration() call shares between its Crank-Nicolson
+    steps and their backward: the assembled capacity and conductivity values,
+    the step systems M + dt/2 K (one per distinct dt, FP64 Jacobi CG) and the
+    Newton controls."""
+
+    def __init__(self, dm: DeviceMesh, con_mask: Tensor, mat_kind: int, mval: Tensor, kval: Tensor,
+                 max_iter: int, rtol: float, atol: float, stol: float, verbose: bool):
+        self.dm = dm
+        self.con_mask = con_mask
+        self.con_bool = con_mask.bool()
+        self.mat_kind = mat_kind
+        self.mval = mval
+        self.kval = kval
+        self.mass = dm.csr_system(mval, con_mask)
+        self.systems: dict[float, LinearSystem] = {}
+        self.max_iter = max_iter
+        self.rtol = rtol
+        self.atol = atol
+        self.stol = stol
+        self.verbose = verbose
+        self.iterations: list[int] = []
+        self.nval = dm.etype.N(dm.etype.ipoints().to(torch.float64)).to(dm.device, torch.float64).contiguous()
+
+    def system(self, dt: float) -> LinearSystem:
+        sysm = self.systems.get(dt)
+        if sysm is None:
+            sysm = self.dm.csr_system(self.dm.csr_combine(1.0, self.mval, 0.5 * dt, self.kval), self.con_mask)
+            self.systems[dt] = sysm
+        return sysm
+
+    def structs(self, mat_data: Tensor, thickness: Tensor | None):
+        from . import _lib
+
+        mesh = self.dm.make_mesh(thickness)
+        return mesh, _lib.FemMaterial(self.mat_kind, mat_data.data_ptr())
+
+
+class CrankNicolsonStep(torch.autograd.Function):
+    """One Crank-Nicolson time step of Heat.time_integration
+    (src/torchfem/base.py:1420-1530): Newton iterations on
+
+        r(du) = M du + dt/2 (f_old + f_int(du; flux_prev, kappa, t) + f_ext),
+        r = 0 on constrained DOFs,
+
+    each correction (M + dt/2 K) x = -r solved by the FP64 CG; returns du.
+
+    backward is the reference's NewtonRaphsonAdjoint at the converged step
+    (sparse.py:641-724) written out for this residual: the adjoint solve
+    (M + dt/2 K) lambda = grad_du on the free DOFs on the same CG, then the
+    residual's vector-Jacobian product with cotangent c = -lambda:
+    dt/2 c to f_old and f_ext, the heat-force vjp kernel with cotangent
+    dt/2 c to flux_prev, the conductivity and the thickness, and the capacity
+    vjp kernel (fem_heat_mass_vjp) c^T (dM/d theta) du to the density and the
+    thickness."""
+
+    @staticmethod
+    def forward(ctx, tc: TransientContext, dt: float, f_old, flux_prev, f_ext, mat_data, thickness, rho):
+        dm = tc.dm
+        mesh, mat = tc.structs(mat_data, thickness)
+        half = 0.5 * dt
+        du = torch.zeros(dm.n_dofs, dtype=torch.float64, device=dm.device)
+        res0 = None
+        converged = False
+        for it in range(tc.max_iter):
+            fe, _, _ = dm.element_force(mesh, mat, du, None, None, 0, flux_prev, None)
+            f_int, _ = dm.gather(fe)
+            res, sumsq = dm.cn_residual(tc.mass, du, f_old, f_int, f_ext, half, tc.con_mask)
+            res_norm = math.sqrt(float(sumsq.item()))
+            if it == 0:
+                res0 = res_norm
+            if tc.verbose:
+                print(f"  newton {it:2d}  |res| = {res_norm:.6e}")
+            if res_norm < tc.rtol * res0 or res_norm < tc.atol:
+                converged = True
+                break
+            sysm = tc.system(dt)
+            du = du + dm.solve(sysm, (-res).contiguous(), tc.stol)
+            tc.iterations.append(sysm.stats.iterations)
+        if not converged:
+            raise RuntimeError("Newton-Raphson iteration did not converge.")
+        ctx.tc = tc
+        ctx.dt = dt
+        ctx.save_for_backward(du, flux_prev, mat_data, thickness, rho)
+        return du
+
+    @staticmethod
+    def backward(ctx, grad_du):
+        tc: TransientContext = ctx.tc
+        dm = tc.dm
+        du, flux_prev, mat_data, thickness, rho = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        half = 0.5 * ctx.dt
+        g = torch.where(tc.con_bool, torch.zeros_like(grad_du), grad_du).contiguous()
+        sysm = tc.system(ctx.dt)
+        lam = dm.solve(sysm, g, tc.stol)
+        tc.iterations.append(sysm.stats.iterations)
+        c = (-lam).contiguous()
+        ch = (half * c).contiguous()
+        mesh, mat = tc.structs(mat_data, thickness)
+        want_thick = need[6] and thickness is not None
+        gsig = gmat = gthick = None
+        if need[3] or need[5] or want_thick:
+            gsig, gmat, gthick, _, _ = dm.vjp(
+                mesh, mat, du, ch, None, None, 0, flux_prev, None,
+                want_sig=need[3], want_mat=need[5], want_thick=want_thick, mat_numel=mat_data.numel(),
+            )
+        g_rho = None
+        if need[7] or want_thick:
+            p = torch.empty(dm.n_elem, dtype=torch.float64, device=dm.device)
+            check(dm.lib.fem_heat_mass_vjp(C.byref(mesh), ptr(tc.nval), ptr(c), ptr(du), ptr(p), dm.stream),
+                  "fem_heat_mass_vjp")
+            if need[7]:
+                g_rho = p * thickness if thickness is not None else p
+            if want_thick:
+                gthick = gthick + p * rho
+        return (
+            None,
+            None,
+            ch if need[2] else None,
+            None if gsig is None else gsig.view_as(flux_prev),
+            ch if need[4] else None,
+            None if gmat is None else gmat.view_as(mat_data),
+            gthick,
+            g_rho,
         )
