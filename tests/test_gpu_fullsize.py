@@ -17,6 +17,16 @@ API, and compares it with fixtures written by the reference itself
   sigma and d(sum u)/d(forces), their max-abs values and 2-norms, and
   full-field checksums <w, x>.
 
+- config 3, the SIMP cantilever (Quad1 400 x 200, 161,202 DOF) in mixed
+  precision: compliance and dL/drho on the reference's 20 seeded elements
+  against simp_400x200.npz.  The 125x stiffness contrast limits how deep
+  FP64 refinement of an FP32 matrix reaches: the tests refine to 1e-10
+  (the configuration's mixed-precision target) and check that 1e-12 is
+  refused with an error rather than returned inaccurate;
+- config 5, the O-grid plate with a hole (256 x 64, 33,280 DOF, J2 plane
+  strain, 20 increments) in mixed precision against the reference's own
+  full-size run (plastic_ogrid_256x64.npz).
+
 Tolerance: 1e-8 relative (max-abs error over max-abs value), the accuracy
 target of the forward + adjoint path; gradients of nonlinear solves 1e-7.
 """
@@ -116,3 +126,91 @@ def test_jittered_cube10_assembly_order_bit_exact(cuda):
     is_con[con_idx] = True
     free = ~(is_con[om.glob_idx[0]] | is_con[om.glob_idx[1]])
     assert int((rev[free] != ref[free]).sum()) > 1000
+
+
+def _simp(rho):
+    from torchfem_gb300 import Planar, mesh
+    from torchfem_gb300.materials import IsotropicElasticityPlaneStress
+
+    nodes, el = mesh.rect_quad(401, 201, 2.0, 1.0)
+    m = Planar(nodes, el, IsotropicElasticityPlaneStress(rho**3 * 1.0, 0.3))
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    tip = torch.argmin(((nodes - torch.tensor([2.0, 0.5])) ** 2).sum(1))
+    m.forces[tip, 1] = -1.0
+    return m
+
+
+def _simp_rho():
+    return 0.2 + 0.8 * torch.rand(80000, generator=torch.Generator().manual_seed(0), dtype=torch.float64)
+
+
+def test_config3_mixed_vs_reference(cuda, golden):
+    """Config 3 in mixed precision with the multigrid preconditioner (FP32 K
+    and CG, FP64 refinement to 1e-10): compliance and the reference's 20
+    sampled dL/drho to 1e-8.  (With block Jacobi the adjoint's FP32 CG runs
+    to the 10 n iteration cap on this contrast, so config 3 in mixed
+    precision needs the multigrid.)"""
+    precond = "amg"
+    g = golden("simp_400x200.npz")
+    rho = _simp_rho().requires_grad_(True)
+    m = _simp(rho)
+    u, f, _, _, _ = m.solve(stol=1e-10, precision="mixed", preconditioner=precond, differentiable_parameters=rho)
+    L = torch.inner(f.ravel(), u.ravel())
+    assert abs(float(L.detach()) - float(g["compliance"])) <= RTOL * abs(float(g["compliance"]))
+    (gr,) = torch.autograd.grad(L, rho)
+    idx = torch.tensor(g["sample_idx"])
+    ref = torch.tensor(g["grad_rho_sample"])
+    err = float((gr[idx].cpu() - ref).abs().max() / ref.abs().max())
+    assert err <= RTOL, err
+    assert abs(float(gr.norm()) - float(g["grad_norm"])) <= RTOL * float(g["grad_norm"])
+
+
+def test_config3_mixed_refinement_floor_is_refused(cuda):
+    """FP64 refinement of the FP32 SIMP matrix stagnates above 1e-12: the
+    solve stops with an error (the stagnation or iteration-cap message,
+    chained under the reference's cutback message) instead of returning an
+    inaccurate result."""
+    m = _simp(_simp_rho())
+    with pytest.raises(RuntimeError) as info:
+        m.solve(stol=1e-12, precision="mixed", preconditioner="jacobi")
+    msg = str(info.value) + " " + str(info.value.__cause__)
+    assert "stagnated" in msg or "did not converge" in msg or "failed" in msg, msg
+
+
+@pytest.mark.parametrize("precond", ["amg", "jacobi"])
+def test_config5_mixed_vs_reference(cuda, golden, precond):
+    """Config 5 in mixed precision: u, f, sigma, state, the reaction and its
+    thickness gradient against the reference's full-size run (1e-8, the
+    gradient 1e-7)."""
+    from torchfem_gb300 import Planar
+    from torchfem_gb300.materials import IsotropicPlasticityPlaneStrain
+
+    g = golden("plastic_ogrid_256x64.npz")
+    nodes = torch.tensor(g["nodes"])
+    el = torch.tensor(g["elements"])
+    mat = IsotropicPlasticityPlaneStrain(1000.0, 0.3, lambda q: 1.0 + 100.0 * q,
+                                         lambda q: 100.0 * torch.ones_like(q))
+    t = torch.ones(len(el), dtype=torch.float64, requires_grad=True)
+    m = Planar(nodes, el, mat, thickness=t)
+    left = torch.isclose(nodes[:, 0], torch.tensor(0.0, dtype=torch.float64))
+    right = torch.isclose(nodes[:, 0], torch.tensor(2.0, dtype=torch.float64))
+    m.constraints[left, 0] = True
+    pin = torch.argmin(((nodes - torch.tensor([0.0, 0.5])) ** 2).sum(1))
+    m.constraints[pin, 1] = True
+    m.constraints[right, 0] = True
+    m.displacements[right, 0] = 0.02
+    assert m.n_dofs == 33_280
+    u, f, s, _, st = m.solve(increments=torch.linspace(0.0, 1.0, 21), rtol=1e-12, atol=1e-12, max_iter=80,
+                             stol=1e-12, precision="mixed", preconditioner=precond, differentiable_parameters=t)
+
+    def rel(a, b):
+        return float(np.abs(a.detach().cpu().numpy() - b).max() / np.abs(b).max())
+
+    assert rel(u, g["u"]) <= RTOL
+    assert rel(f, g["f"]) <= RTOL
+    assert rel(s, g["sigma"]) <= RTOL
+    assert rel(st, g["state"]) <= RTOL
+    R = f[right.to(f.device), 0].sum()
+    assert abs(float(R.detach()) - float(g["reaction"])) <= RTOL * abs(float(g["reaction"]))
+    (gt,) = torch.autograd.grad(R, t)
+    assert rel(gt, g["grad_t"]) <= 1e-7
