@@ -944,7 +944,6 @@ struct OpArgs {
   double* partial;
   AmgCtrl* ctrl;
   double* lz;      // Lanczos coefficients (kOpLzQ)
-  unsigned int* gcount;  // arrival counters of the level-0 reduction groups (grid_sum2)
   const __half* sv16;    // level 0: FP16 smoothing copy of the sliced matrix (scaled by 1 / *s16inv)
   const float* s16inv;
 };
@@ -1063,48 +1062,6 @@ __host__ __device__ constexpr bool op_has_dot() {
 // damp the rough error, and one consistent copy in all four passes keeps the
 // V-cycle a fixed symmetric operator (pre- and post-smoothing are adjoint),
 // so CG still applies; CG's own q = A p always uses the FP32 matrix.
-constexpr int kDotGroup = 64;  // CTAs whose partial sums one arriving CTA adds first
-
-// True in every thread of the CTA that arrives last of n at `counter`.
-__device__ __forceinline__ bool arrive_last_of(unsigned int* counter, unsigned int n) {
-  __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == n - 1;
-  __syncthreads();
-  return last;
-}
-
-// Deterministic sum of v over the grid in two levels: each CTA writes its
-// sum to partial[b]; the last CTA to arrive in its group of kDotGroup
-// consecutive CTAs adds the group's partials in a fixed order into
-// partial[gridDim.x + g]; the last group to finish adds the group sums in a
-// fixed order.  The CTA that does that returns true with the total in *tot
-// (thread 0).  Every sum has a fixed order, whichever CTA computes it, so
-// the result does not depend on the arrival order.  Needs blockDim.x >=
-// kDotGroup, partial[gridDim.x + ceil(gridDim.x / kDotGroup)] and zeroed
-// counters.
-__device__ __forceinline__ bool grid_sum2(double v, double* partial, unsigned int* gcount, unsigned int* counter,
-                                          double* red, double* tot) {
-  const unsigned int n = gridDim.x, b = blockIdx.x;
-  const double s = block_sum(v, red);
-  if (threadIdx.x == 0) partial[b] = s;
-  const unsigned int g = b / kDotGroup, g0 = g * kDotGroup;
-  const unsigned int gn = min((unsigned int)kDotGroup, n - g0);
-  const unsigned int n_groups = (n + kDotGroup - 1) / kDotGroup;
-  if (!arrive_last_of(&gcount[g], gn)) return false;
-  const double gs = block_sum(threadIdx.x < gn ? __ldcg(partial + g0 + threadIdx.x) : 0.0, red);
-  if (threadIdx.x == 0) {
-    partial[n + g] = gs;
-    gcount[g] = 0;
-  }
-  if (!arrive_last_of(counter, n_groups)) return false;
-  const double t = sum_partials(partial + n, (int)n_groups, 1, 0, red);
-  if (threadIdx.x == 0) *counter = 0;
-  *tot = t;
-  return true;
-}
-
 __device__ __forceinline__ uint32_t ld_l2_b32(const void* ptr, uint64_t pol) {
   uint32_t v;
   asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(pol));
@@ -1162,7 +1119,6 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
                                                          const float* __restrict__ sval, OpArgs a) {
   constexpr int DD = D * D;
   __shared__ float ys[kSellW][D][32];
-  __shared__ double red[32];
   if (amg_idle(a.ctrl)) return;
   const float* __restrict__ v = op_operand<MODE>(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1224,11 +1180,28 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
       dot += op_epilogue<D, MODE>(a, i, yt);
     }
   }
+  // the modes that end in a dot product leave the slice's share of it in
+  // partial[slice]; k_dot_finish adds them (no CTA waits on another, and
+  // warps 1-3 are done as soon as their rows are in shared memory)
   if constexpr (op_has_dot<MODE>()) {
-    double tot = 0.0;
-    if (grid_sum2(dot, a.partial, a.gcount, &a.ctrl->counter, red, &tot) && threadIdx.x == 0)
-      op_finish<MODE>(a, tot);
+    if (w == 0) {
+      const double t = warp_sum(dot);
+      if (lane == 0) a.partial[blockIdx.x] = t;
+    }
   }
+}
+
+// The dot product of a level-0 pass that ends in one: the per-slice shares
+// left by k_sell_op added in a fixed order by one CTA, then the CG (or
+// Lanczos) scalar update.  Deterministic; idle exactly when the pass was.
+template <int MODE>
+__global__ void __launch_bounds__(1024) k_dot_finish(int64_t n, OpArgs a) {
+  __shared__ double red[32];
+  if (amg_idle(a.ctrl)) return;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(a.partial + i);
+  const double tot = block_sum(s, red);
+  if (threadIdx.x == 0) op_finish<MODE>(a, tot);
 }
 
 // The FP16 smoothing copy: max |a_ij| over the sliced FP32 values (as the
@@ -1898,7 +1871,6 @@ struct fem_amg {
   tfg::AmgCtrl* lzc = nullptr;
   double* lz = nullptr;
   double* partial = nullptr;
-  unsigned int* gcount = nullptr;  // arrival counters of the level-0 reduction groups
   int32_t* status = nullptr;
   unsigned long long* counter = nullptr;
   std::vector<void*> mem;
@@ -2222,15 +2194,12 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
   // per-CTA partial sums: the level-0 SpMV grid has one CTA per slice
   const int64_t n_partial = std::max<int64_t>(kPartialLen, (n0 + 31) / 32 + 1);
   h->partial = h->alloc<double>(2 * n_partial, st);
-  const int64_t n_groups = n_partial / kDotGroup + 2;
-  h->gcount = h->alloc<unsigned int>(n_groups, st);
   h->s16inv = h->alloc<float>(1, st);
   h->absmax = h->alloc<unsigned int>(1, st);
   double* origin = h->alloc<double>(3, st);
-  if (!h->active || !h->status || !h->counter || !h->ctrl || !h->lzc || !h->lz || !h->partial || !h->gcount ||
+  if (!h->active || !h->status || !h->counter || !h->ctrl || !h->lzc || !h->lz || !h->partial ||
       !h->s16inv || !h->absmax || !origin)
     return check_cuda("AMG buffers");
-  cudaMemsetAsync(h->gcount, 0, sizeof(unsigned int) * n_groups, st);
   cudaMemsetAsync(h->status, 0, sizeof(int32_t), st);
   cudaMemsetAsync(h->ctrl, 0, sizeof(AmgCtrl), st);
   cudaMemsetAsync(h->lzc, 0, sizeof(AmgCtrl), st);
@@ -2327,7 +2296,6 @@ OpArgs level_args(fem_amg* h, int l, AmgCtrl* ctrl) {
   a.partial = h->partial;
   a.ctrl = ctrl;
   a.lz = h->lz;
-  a.gcount = h->gcount;
   a.sv16 = h->sv16;
   a.s16inv = h->s16inv;
   return a;
@@ -2346,6 +2314,10 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
     else
       k_sell_op<B0, MODE, false><<<(unsigned)ns, kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val,
                                                                         a);
+    if constexpr (op_has_dot<MODE>()) {
+      k_dot_finish<MODE><<<1, 1024, 0, st>>>(ns, a);
+      note_launch();
+    }
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used++ + 1], st);
   } else {
     k_csr_op<K, MODE><<<capped(L.n, 16), kRowT, 0, st>>>(L.n, L.a_ptr, L.a_col, L.a_val, a);
@@ -2370,7 +2342,6 @@ int lanczos_level(fem_amg* h, int l, cudaStream_t st, double* rho) {
   a.partial = h->partial;
   a.ctrl = h->lzc;
   a.lz = h->lz;
-  a.gcount = h->gcount;
   for (int j = 0; j < kLanczos; ++j) {
     bool sliced = false;
     if constexpr (B <= 3) {  // level 0 (B = dim) holds the sliced matrix
@@ -2378,6 +2349,8 @@ int lanczos_level(fem_amg* h, int l, cudaStream_t st, double* rho) {
         const int64_t ns = (n + 31) / 32;
         k_sell_op<B, kOpLzQ, false><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
                                                                            a);
+        note_launch();
+        k_dot_finish<kOpLzQ><<<1, 1024, 0, st>>>(ns, a);
         sliced = true;
       }
     }
@@ -2551,7 +2524,6 @@ void launch_iteration(fem_amg* h, cudaStream_t st) {
   a.xb = h->z;
   a.partial = h->partial;
   a.ctrl = h->ctrl;
-  a.gcount = h->gcount;
   launch_op<B0, K, kOpQc>(h, 0, a, st);
   k_cg_update<B0><<<capped(grid_for(h->L[0].n, kT), 8), kT, 0, st>>>(h->L[0].n, h->xlo, h->rcg, h->p, h->q, h->dinv0,
                                                                       h->L[0].theta_inv, h->L[0].d, h->L[0].x,
