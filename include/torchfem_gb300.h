@@ -524,6 +524,17 @@ int fem_amg_setup(fem_amg* amg, const fem_matrix* A32, void* stream);
  * counterpart in the reference (its AMG runs in FP64). */
 void fem_amg_set_half_smoother(int enable);
 
+/* How a V-cycle runs its coarse levels (process-wide; default 1).  1: the
+ * restriction from level 0, every coarser level's Chebyshev passes, the
+ * coarsest solve and the prolongations back to level 0 run as one
+ * cooperative launch whose phases are separated by grid barriers with
+ * bounded waits (a wait that runs out ends the solve with FEM_CUDA_ERROR and
+ * a "barrier timeout" message).  0, or a device that refuses the
+ * cooperative launch: one launch per level operation.  Both keep fixed
+ * summation orders, so each is deterministic; they differ only in the order
+ * of partial row sums.  No counterpart in the reference. */
+void fem_amg_set_fused_cycle(int enable);
+
 /* CG preconditioned by one V-cycle (Chebyshev smoothing) on the matrix of
  * the last fem_amg_setup, from x = 0.  With op != NULL: FP64 residual
  * replacement as in fem_pcg_mixed (threshold delta), stopping at

@@ -277,6 +277,45 @@ def test_amg_half_smoother_matches_fp32_smoother(cuda, half_smoother, kind):
     assert its[1] <= 1.15 * its[0] + 1, its
 
 
+@pytest.mark.parametrize("kind", ["elastic", "planar", "heat"])
+def test_amg_fused_coarse_cycle_matches_per_level_kernels(cuda, half_smoother, kind):
+    """The coarse levels of the V-cycle as one cooperative launch (grid
+    barriers between phases) against one launch per level operation: the
+    same preconditioner up to the order of partial row sums, so the solutions
+    agree to 1e-8, CG iteration counts within one, and repeated fused solves
+    are bitwise identical."""
+    lib = half_smoother
+    if kind == "elastic":
+        m, _, _ = cube_problem(16)
+    elif kind == "planar":
+        nodes, el = mesh.rect_quad(41, 21, 2.0, 1.0)
+        m = Planar(nodes.to(cuda), el.to(cuda), IsotropicElasticityPlaneStress(1000.0, 0.3))
+        m.constraints[(nodes[:, 0] == 0.0).to(cuda), :] = True
+        m.forces[(nodes[:, 0] == 2.0).to(cuda), 1] = -1.0
+    else:
+        from torchfem_gb300 import SolidHeat
+        from torchfem_gb300.materials import IsotropicConductivity3D
+
+        nodes, el = jittered_cube(24)
+        m = SolidHeat(nodes.to(cuda), el.to(cuda), IsotropicConductivity3D(1.0))
+        m.constraints[(nodes[:, 0] == 0.0).to(cuda)] = True
+        m.heat_flux[:] = 1.0 / len(nodes)
+    out, its = {}, {}
+    try:
+        for fused in (0, 1):
+            lib.fem_amg_set_fused_cycle(fused)
+            out[fused] = m.solve(stol=1e-12, precision="mixed", preconditioner="amg")[0].clone()
+            assert m.last_solve.system.amg is not None
+            assert len(m.last_solve.system.amg.levels()) >= 3
+            its[fused] = list(m.last_solve.iterations)
+        again = m.solve(stol=1e-12, precision="mixed", preconditioner="amg")[0]
+    finally:
+        lib.fem_amg_set_fused_cycle(1)
+    assert torch.equal(again, out[1])
+    assert rel(out[1], out[0]) <= RTOL
+    assert all(abs(a - b) <= 1 for a, b in zip(its[0], its[1])), its
+
+
 def test_config2_full_size_amg_iterations(cuda, half_smoother):
     """Config 2 at full size (70^3 jittered Hexa1, 1,073,733 DOF): the
     V-cycle CG iteration counts of solve + adjoint stay flat (tens, against

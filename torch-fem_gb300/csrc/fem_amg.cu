@@ -43,6 +43,7 @@ namespace tfg {
 int etype_info(int etype, int* ne, int* d, int* nip);
 extern int g_timing;  // fem_set_timing
 int g_amg_half = 1;   // FP16 smoothing copy of the level-0 matrix (fem_amg_set_half_smoother)
+int g_amg_fused = 1;  // coarse levels as one cooperative launch per V-cycle (fem_amg_set_fused_cycle)
 size_t scan_workspace_bytes(int64_t n);
 int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
 
@@ -97,7 +98,7 @@ __device__ __forceinline__ uint64_t join_key(int64_t j) {
 }
 
 // ------------------------------------------------------------ control ----
-enum { kRun = 0, kConverged = 1, kMaxIter = 2, kNonFinite = 3, kBreakdown = 4 };
+enum { kRun = 0, kConverged = 1, kMaxIter = 2, kNonFinite = 3, kBreakdown = 4, kBarrierTimeout = 5 };
 
 struct AmgCtrl {
   double rz;       // r.z of the current direction
@@ -1491,6 +1492,303 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(int64_t n_c, const int64_
   }
 }
 
+// ------------------------------------------------------- fused coarse cycle --
+// Everything of a V-cycle below level 0 -- restriction from level 0, the
+// Chebyshev passes of every coarser level, the coarsest solve and the
+// prolongations back to level 0 -- as one cooperative launch: phases
+// separated by grid barriers, instead of about fourteen short launches whose
+// work (a few thousand rows, or 96) is mostly launch and tail latency.
+//
+// Work decomposition: a warp per block row of a coarse operator (lanes hold
+// (block, row) items, 32 / K blocks per pass, partial rows summed across
+// lanes by shuffles in a fixed order), a warp per coarse row of a
+// restriction, a thread per (fine row, component) of a prolongation, and CTA
+// 0 for the coarsest solve.  Every sum keeps a fixed order, so results are
+// identical run to run; the arithmetic is that of the per-level kernels
+// above up to the order of partial row sums.
+constexpr int kCycT = 512;    // threads per CTA
+constexpr int kCycPerSm = 2;  // CTAs per SM at most (occupancy may allow fewer)
+constexpr long long kCycSpin = 4000000000LL;  // clock cycles a barrier wait may last (about 2 s)
+
+struct CycLevel {
+  int64_t n;  // block rows
+  const int64_t* a_ptr;
+  const int32_t* a_col;
+  const float* a_val;
+  const float* dinv;
+  float *f, *x, *xb, *r, *d, *db;
+  float theta_inv, c1, c2;
+  // transfer to the next level
+  const int64_t* p_ptr;
+  const int32_t* p_col;
+  const __half* p_h;
+  const int64_t* pt_ptr;
+  const int32_t* pt_row;
+  const __half* pt_val;
+};
+
+// Arrival counter and error flag of the fused cycle's grid barriers (one
+// per handle, zeroed at the start of every solve).
+struct CycBarrier {
+  unsigned long long seq;
+  int error;
+};
+
+struct CycArgs {
+  int n_levels;
+  CycLevel L[kMaxLevels];
+  const float* coarse_inv;
+  AmgCtrl* ctrl;
+  CycBarrier* bar;
+};
+
+// Grid barrier with a bounded wait: one monotonic 64-bit arrival counter per
+// solve, release add by thread 0 of each CTA after a CTA barrier (cumulative:
+// it publishes the CTA's writes), relaxed polling with a short sleep, one
+// acquire fence.  A wait that runs out sets the error flag and the CG's
+// done code; returns false on every thread once any CTA's wait ran out.
+__device__ __forceinline__ bool cyc_barrier(CycBarrier* b, AmgCtrl* c) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long old;
+    asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(old) : "l"(&b->seq) : "memory");
+    const unsigned long long target = (old / gridDim.x + 1) * gridDim.x;
+    const long long t0 = clock64();
+    int good = 1;
+    while (true) {
+      unsigned long long now;
+      asm volatile("ld.relaxed.gpu.u64 %0, [%1];" : "=l"(now) : "l"(&b->seq) : "memory");
+      if (now >= target) break;
+      if (*(volatile int*)&b->error) {
+        good = 0;
+        break;
+      }
+      if (clock64() - t0 > kCycSpin) {
+        atomicExch(&b->error, 1);
+        atomicExch(&c->done, kBarrierTimeout);
+        good = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// One Chebyshev pass of a coarse level on block row i by one warp (the
+// modes S1..S4 of op_epilogue).
+template <int K, int MODE>
+__device__ __forceinline__ void cyc_row(const CycLevel& L, int64_t i, int lane, uint64_t pol) {
+  constexpr int PB = 32 / K;  // blocks per pass
+  constexpr int U = 2;        // passes with loads in flight together
+  const float* __restrict__ v = MODE == kOpS1 || MODE == kOpS4 ? L.d : MODE == kOpS2 ? L.db : L.x;
+  const int blk = lane / K, r = lane - (lane / K) * K;
+  float y = 0.f;
+  if (blk < PB) {
+    const int64_t e1 = L.a_ptr[i + 1];
+    for (int64_t e = L.a_ptr[i] + blk; e < e1; e += U * PB) {
+      int64_t c[U];
+#pragma unroll
+      for (int w = 0; w < U; ++w) c[w] = e + w * PB < e1 ? (int64_t)ld_l2(L.a_col + e + w * PB, pol) : -1;
+      float m[U][K], xv[U][K];
+#pragma unroll
+      for (int w = 0; w < U; ++w)
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+          m[w][q] = c[w] >= 0 ? ld_l2(L.a_val + (e + w * PB) * K * K + r * K + q, pol) : 0.f;
+          xv[w][q] = c[w] >= 0 ? v[c[w] * K + q] : 0.f;
+        }
+#pragma unroll
+      for (int w = 0; w < U; ++w)
+#pragma unroll
+        for (int q = 0; q < K; ++q) y = fmaf(m[w][q], xv[w][q], y);
+    }
+  }
+  // lane r (< K) adds the lanes r + b K, b = 1 .. PB-1, in order
+  float t = y;
+#pragma unroll
+  for (int b = 1; b < PB; ++b) t += __shfl_sync(0xffffffffu, y, (r + b * K) & 31);
+  const int64_t o = i * K + r;
+  float rn = 0.f;
+  if (lane < K) {
+    if constexpr (MODE == kOpS1 || MODE == kOpS3) rn = L.f[o] - t;
+    else if constexpr (MODE == kOpS4) rn = L.r[o] - t;
+  }
+  float tv = 0.f;
+  if constexpr (MODE != kOpS2) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      const float rq = __shfl_sync(0xffffffffu, rn, q);
+      if (lane < K) tv = fmaf(L.dinv[o * K + q], rq, tv);
+    }
+  }
+  if (lane < K) {
+    if constexpr (MODE == kOpS1) {
+      const float dn = L.c1 * L.d[o] + L.c2 * tv;
+      L.r[o] = rn;
+      L.db[o] = dn;
+      L.x[o] += dn;
+    } else if constexpr (MODE == kOpS2) {
+      L.r[o] -= t;
+    } else if constexpr (MODE == kOpS3) {
+      const float dn = L.theta_inv * tv;
+      L.r[o] = rn;
+      L.d[o] = dn;
+      L.xb[o] = L.x[o] + dn;
+    } else {
+      L.xb[o] = L.xb[o] + (L.c1 * L.d[o] + L.c2 * tv);
+    }
+  }
+}
+
+// Restriction f_c = P^T r of coarse row I by one warp (P^T in transposed
+// order, FP16), xor-tree sums, then the first Chebyshev step of the coarse
+// level: d = D^-1 f / theta, x = d.
+template <int BF, int K>
+__device__ __forceinline__ void cyc_restrict(const CycLevel& F, const CycLevel& C, int64_t I, int lane) {
+  float acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.f;
+  for (int64_t e = F.pt_ptr[I] + lane; e < F.pt_ptr[I + 1]; e += 32) {
+    const int64_t i = F.pt_row[e];
+    float pv[BF * K];
+    load_half<BF * K>(F.pt_val + e * BF * K, pv);
+#pragma unroll
+    for (int q = 0; q < BF; ++q) {
+      const float rv = F.r[i * BF + q];
+#pragma unroll
+      for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+  if (lane < K) {
+    float t = 0.f, fk = 0.f;
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      t = fmaf(C.dinv[(I * K + lane) * K + q], acc[q], t);
+      if (q == lane) fk = acc[q];
+    }
+    const float dn = C.theta_inv * t;
+    C.f[I * K + lane] = fk;
+    C.d[I * K + lane] = dn;
+    C.x[I * K + lane] = dn;
+  }
+}
+
+// Restriction onto the coarsest level and its dense solve, by one CTA.
+template <int BF, int K>
+__device__ __forceinline__ void cyc_coarsest(const CycLevel& F, const CycLevel& C, const float* __restrict__ inv,
+                                             float* fs) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t I = w; I < C.n; I += kCycT / 32) {
+    float acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.f;
+    for (int64_t e = F.pt_ptr[I] + lane; e < F.pt_ptr[I + 1]; e += 32) {
+      const int64_t i = F.pt_row[e];
+      float pv[BF * K];
+      load_half<BF * K>(F.pt_val + e * BF * K, pv);
+#pragma unroll
+      for (int q = 0; q < BF; ++q) {
+        const float rv = F.r[i * BF + q];
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < K; ++k) fs[I * K + k] = acc[k];
+  }
+  __syncthreads();
+  const int m = (int)(C.n * K);
+  for (int t = threadIdx.x; t < m; t += kCycT) {
+    float s = 0.f;
+    for (int j = 0; j < m; ++j) s = fmaf(inv[(int64_t)t * m + j], fs[j], s);
+    C.xb[t] = s;
+  }
+}
+
+// Prolongation x += P x_c over the grid, a thread per (fine row, component).
+template <int BF, int K>
+__device__ __forceinline__ void cyc_prolong(const CycLevel& F, const float* __restrict__ xc, float* __restrict__ x) {
+  const int64_t n = F.n * BF;
+  for (int64_t t = (int64_t)blockIdx.x * kCycT + threadIdx.x; t < n; t += (int64_t)gridDim.x * kCycT) {
+    const int64_t i = t / BF;
+    const int r = (int)(t - i * BF);
+    float s = 0.f;
+    for (int64_t e = F.p_ptr[i]; e < F.p_ptr[i + 1]; ++e) {
+      float pv[K];
+      load_half<K>(F.p_h + e * BF * K + r * K, pv);
+      const float* cv = xc + (int64_t)F.p_col[e] * K;
+#pragma unroll
+      for (int k = 0; k < K; ++k) s = fmaf(pv[k], cv[k], s);
+    }
+    x[t] += s;
+  }
+}
+
+template <int K, int MODE>
+__device__ __forceinline__ void cyc_pass(const CycLevel& L, int lane, int64_t warp, int64_t n_warps, uint64_t pol) {
+  for (int64_t i = warp; i < L.n; i += n_warps) cyc_row<K, MODE>(L, i, lane, pol);
+}
+
+template <int B0, int K>
+__global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
+  __shared__ float fs[kCoarseMaxDof];
+  AmgCtrl* c = a.ctrl;
+  CycBarrier* bar = a.bar;
+  if (amg_idle(c)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * kCycT + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * kCycT) >> 5;
+  const uint64_t pol = l2_policy(true);
+  const int last = a.n_levels - 1;
+  // down: restrict (with the first Chebyshev step), then the level's second
+  // pass and residual
+  for (int l = 0; l < last; ++l) {
+    const CycLevel& F = a.L[l];
+    const CycLevel& C = a.L[l + 1];
+    if (l + 1 == last) {
+      if (blockIdx.x == 0) {
+        if (l == 0) cyc_coarsest<B0, K>(F, C, a.coarse_inv, fs);
+        else cyc_coarsest<K, K>(F, C, a.coarse_inv, fs);
+      }
+      break;
+    }
+    for (int64_t I = warp; I < C.n; I += n_warps) {
+      if (l == 0) cyc_restrict<B0, K>(F, C, I, lane);
+      else cyc_restrict<K, K>(F, C, I, lane);
+    }
+    if (!cyc_barrier(bar, c)) return;
+    cyc_pass<K, kOpS1>(C, lane, warp, n_warps, pol);
+    if (!cyc_barrier(bar, c)) return;
+    cyc_pass<K, kOpS2>(C, lane, warp, n_warps, pol);
+    if (!cyc_barrier(bar, c)) return;
+  }
+  // up: prolongate, then the level's post-smoothing; level 0 continues in
+  // the next launch
+  for (int l = last - 1; l >= 0; --l) {
+    if (!cyc_barrier(bar, c)) return;
+    const CycLevel& F = a.L[l];
+    if (l == 0) {
+      cyc_prolong<B0, K>(F, a.L[1].xb, F.x);
+      break;
+    }
+    cyc_prolong<K, K>(F, a.L[l + 1].xb, F.x);
+    if (!cyc_barrier(bar, c)) return;
+    cyc_pass<K, kOpS3>(F, lane, warp, n_warps, pol);
+    if (!cyc_barrier(bar, c)) return;
+    cyc_pass<K, kOpS4>(F, lane, warp, n_warps, pol);
+  }
+}
+
 // ---------------------------------------------------------------- CG ------
 // p = z + beta p.
 __global__ void __launch_bounds__(256) k_pup(int64_t n, const float* __restrict__ z, float* __restrict__ p,
@@ -1893,6 +2191,9 @@ struct fem_amg {
   int64_t sv16_len = 0;
   float* s16inv = nullptr;
   unsigned int* absmax = nullptr;
+  // fused coarse cycle: CTAs (0 not yet sized, -1 unavailable) and barrier state
+  int cyc_blocks = 0;
+  tfg::CycBarrier* cyc_bar = nullptr;
 
   template <typename T>
   T* alloc(int64_t count, cudaStream_t st) {
@@ -2196,9 +2497,10 @@ int create_impl(fem_amg* h, const fem_blocks* B, const double* coords, const uin
   h->partial = h->alloc<double>(2 * n_partial, st);
   h->s16inv = h->alloc<float>(1, st);
   h->absmax = h->alloc<unsigned int>(1, st);
+  h->cyc_bar = h->alloc<CycBarrier>(1, st);
   double* origin = h->alloc<double>(3, st);
   if (!h->active || !h->status || !h->counter || !h->ctrl || !h->lzc || !h->lz || !h->partial ||
-      !h->s16inv || !h->absmax || !origin)
+      !h->s16inv || !h->absmax || !h->cyc_bar || !origin)
     return check_cuda("AMG buffers");
   cudaMemsetAsync(h->status, 0, sizeof(int32_t), st);
   cudaMemsetAsync(h->ctrl, 0, sizeof(AmgCtrl), st);
@@ -2476,15 +2778,20 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
 }
 
 // ------------------------------------------------------------------ solve --
+// The coarse part of a V-cycle, one launch per level operation: restriction
+// from level 0, every coarser level's smoothing passes, the coarsest solve
+// and the prolongations back to level 0.
 template <int B0, int K>
-void launch_vcycle(fem_amg* h, cudaStream_t st) {
+void launch_coarse_levels(fem_amg* h, cudaStream_t st) {
   const int last = h->n_levels - 1;
   for (int l = 0; l < last; ++l) {
     AmgLevel& L = h->L[l];
     AmgLevel& C = h->L[l + 1];
-    const OpArgs a = level_args(h, l, h->ctrl);
-    launch_op<B0, K, kOpS1>(h, l, a, st);
-    launch_op<B0, K, kOpS2>(h, l, a, st);
+    if (l > 0) {
+      const OpArgs a = level_args(h, l, h->ctrl);
+      launch_op<B0, K, kOpS1>(h, l, a, st);
+      launch_op<B0, K, kOpS2>(h, l, a, st);
+    }
     if (l + 1 == last) {
       if (l == 0)
         k_coarse_solve<B0, K><<<1, 1024, 0, st>>>(C.n, L.pt_ptr, L.pt_row, L.pt_val, L.r, h->coarse_inv, C.xb,
@@ -2508,11 +2815,80 @@ void launch_vcycle(fem_amg* h, cudaStream_t st) {
     else
       k_prolong<K, K><<<grid_for(L.n * K, 256), 256, 0, st>>>(L.n, L.p_ptr, L.p_col, L.p_h, C.xb, L.x, h->ctrl);
     note_launch();
-    const OpArgs a = level_args(h, l, h->ctrl);
-    launch_op<B0, K, kOpS3>(h, l, a, st);
-    if (l == 0) launch_op<B0, K, kOpS4Dot>(h, l, a, st);
-    else launch_op<B0, K, kOpS4>(h, l, a, st);
+    if (l > 0) {
+      const OpArgs a = level_args(h, l, h->ctrl);
+      launch_op<B0, K, kOpS3>(h, l, a, st);
+      launch_op<B0, K, kOpS4>(h, l, a, st);
+    }
   }
+}
+
+// The same coarse part as one cooperative launch of k_coarse_cycle.  Returns
+// false when the launch is refused (the caller then runs the per-level
+// kernels), after which the handle stops trying.
+template <int B0, int K>
+bool launch_coarse_fused(fem_amg* h, cudaStream_t st) {
+  if (h->cyc_blocks < 0) return false;
+  if (h->cyc_blocks == 0) {
+    int dev = 0, coop = 0, occ = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_coarse_cycle<B0, K>, kCycT, 0) != cudaSuccess ||
+        occ < 1) {
+      cudaGetLastError();
+      h->cyc_blocks = -1;
+      return false;
+    }
+    h->cyc_blocks = std::min(occ, kCycPerSm) * sm_count();
+  }
+  CycArgs ca{};
+  ca.n_levels = h->n_levels;
+  for (int l = 0; l < h->n_levels; ++l) {
+    const AmgLevel& L = h->L[l];
+    CycLevel& c = ca.L[l];
+    c.n = L.n;
+    c.a_ptr = L.a_ptr;
+    c.a_col = L.a_col;
+    c.a_val = L.a_val;
+    c.dinv = l == 0 ? h->dinv0 : L.dinv;
+    c.f = L.f;
+    c.x = L.x;
+    c.xb = L.xb;
+    c.r = L.r;
+    c.d = L.d;
+    c.db = L.db;
+    c.theta_inv = L.theta_inv;
+    c.c1 = L.c1;
+    c.c2 = L.c2;
+    c.p_ptr = L.p_ptr;
+    c.p_col = L.p_col;
+    c.p_h = L.p_h;
+    c.pt_ptr = L.pt_ptr;
+    c.pt_row = L.pt_row;
+    c.pt_val = L.pt_val;
+  }
+  ca.coarse_inv = h->coarse_inv;
+  ca.ctrl = h->ctrl;
+  ca.bar = h->cyc_bar;
+  void* args[] = {&ca};
+  if (cudaLaunchCooperativeKernel((const void*)k_coarse_cycle<B0, K>, dim3(h->cyc_blocks), dim3(kCycT), args, 0,
+                                  st) != cudaSuccess) {
+    cudaGetLastError();
+    h->cyc_blocks = -1;
+    return false;
+  }
+  note_launch();
+  return true;
+}
+
+template <int B0, int K>
+void launch_vcycle(fem_amg* h, cudaStream_t st) {
+  const OpArgs a = level_args(h, 0, h->ctrl);
+  launch_op<B0, K, kOpS1>(h, 0, a, st);
+  launch_op<B0, K, kOpS2>(h, 0, a, st);
+  if (h->n_levels > 1 && !(g_amg_fused && launch_coarse_fused<B0, K>(h, st))) launch_coarse_levels<B0, K>(h, st);
+  launch_op<B0, K, kOpS3>(h, 0, a, st);
+  launch_op<B0, K, kOpS4Dot>(h, 0, a, st);
 }
 
 template <int B0, int K>
@@ -2543,6 +2919,7 @@ int status_code(int done) {
     case kConverged: return FEM_OK;
     case kMaxIter: return FEM_NOT_CONVERGED;
     case kNonFinite: return FEM_NONFINITE;
+    case kBarrierTimeout: return FEM_CUDA_ERROR;
     default: return FEM_BREAKDOWN;
   }
 }
@@ -2569,6 +2946,7 @@ int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, d
   cudaMemsetAsync(h->xlo, 0, sizeof(float) * n, st);
   cudaMemsetAsync(h->p, 0, sizeof(float) * n, st);
   cudaMemsetAsync(h->q, 0, sizeof(float) * n, st);  // q carries A p: finite before the first beta = 0 update
+  cudaMemsetAsync(h->cyc_bar, 0, sizeof(CycBarrier), st);  // the fused cycle's barriers count from 0 per solve
   const unsigned gv = capped(grid_for(nn, kT), 8);
   k_cg_bnorm<<<capped(grid_for(n, kT), 8), kT, 0, st>>>(n, b, rtol * rtol, h->partial, h->ctrl);
   note_launch();
@@ -2670,7 +3048,9 @@ int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, d
     info->spmv_ms = h->timed_ms;
     info->spmv_timed = h->timed_n;
   }
-  if (c.done != kConverged)
+  if (c.done == kBarrierTimeout)
+    set_last_error("multigrid CG: a grid-barrier wait of the fused coarse cycle ran out (barrier timeout)");
+  else if (c.done != kConverged)
     set_last_error("multigrid CG did not converge: %lld iterations, relative residual %.3e, code %d", c.iters, rel,
                    c.done);
   return status_code(c.done);
@@ -2764,6 +3144,8 @@ int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const
 }
 
 void fem_amg_set_half_smoother(int enable) { g_amg_half = enable ? 1 : 0; }
+
+void fem_amg_set_fused_cycle(int enable) { g_amg_fused = enable ? 1 : 0; }
 
 int fem_amg_levels(const fem_amg* h) { return h ? h->n_levels : 0; }
 
