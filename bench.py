@@ -578,6 +578,8 @@ def main():
     ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
                     help="preconditioner of the mixed-precision headline")
     ap.add_argument("--workload", choices=["elastic", "heat", "thermal"], default="elastic")
+    ap.add_argument("--amg-delta", type=float, default=None,
+                    help="FP64 replacement threshold of the multigrid CG (default: the library's)")
     ap.add_argument("--smoother", choices=["fp16", "fp32"], default="fp16",
                     help="level-0 smoothing passes of the multigrid V-cycle: FP16 copy or the FP32 matrix")
     ap.add_argument("--thermal-n", type=int, default=1024, help="N of the thermal slab (N x N/2 x 1 elements)")
@@ -590,8 +592,11 @@ def main():
         return
     if torch.cuda.is_available():
         from torchfem_gb300 import _lib
+        from torchfem_gb300.sparse import SolveContext
 
         _lib.load().fem_amg_set_half_smoother(1 if args.smoother == "fp16" else 0)
+        if args.amg_delta is not None:
+            SolveContext.AMG_DELTA = args.amg_delta
     if args.workload == "heat":
         run_heat(args)
         return

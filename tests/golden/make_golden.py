@@ -801,6 +801,37 @@ def make_hyper_full(tf, name="hyper_tet2_30x10x10.npz", counts=(10, 20, 40)):
     np.savez_compressed(OUT / name, **out)
 
 
+def make_hyper_mid(tf, name="hyper_tet2_15x5x5.npz", counts=(10, 20)):
+    """Config 4's problem at half the resolution (15 x 5 x 5 box, 6 Tetra2
+    per hex, 11,163 DOF), where the reference's own direct solve
+    (method="spsolve") is affordable: the load is applied in 10 increments
+    as the configuration states, and when the reference raises there its
+    message is stored and 20 increments are run.  Stored: u, f, the tip
+    reaction and its gradient w.r.t. the per-element E of the count that
+    completes, with the wall times."""
+    out = {"counts_tried": np.array(counts)}
+    for n_inc in counts:
+        model, E, right, nodes, elements = hyper_problem(15, 5, 5)
+        inc = torch.linspace(0.0, 1.0, n_inc + 1)
+        t0 = time.perf_counter()
+        try:
+            u, f, s, F, _ = model.solve(increments=inc, nlgeom=True, method="spsolve", rtol=1e-10, atol=1e-10,
+                                        max_iter=20, differentiable_parameters=E)
+        except RuntimeError as err:
+            out[f"inc{n_inc}_error"] = str(err)
+            out[f"inc{n_inc}_seconds"] = time.perf_counter() - t0
+            print(f"{n_inc} increments: the reference raised: {err}", flush=True)
+            continue
+        t1 = time.perf_counter()
+        R = f[right, 0].sum()
+        (gE,) = torch.autograd.grad(R, E)
+        out.update(increments=n_inc, nodes=nodes.numpy(), elements=elements.numpy(), E=E.detach().numpy(),
+                   u=u.detach().numpy(), f=f.detach().numpy(), sigma=s.detach().numpy(), reaction=R.detach().numpy(),
+                   grad_E=gE.numpy(), t_fwd=t1 - t0, t_adj=time.perf_counter() - t1, torch_version=torch.__version__)
+        print(f"{n_inc} increments: ok, reaction {float(R):.12g}", flush=True)
+        break
+    np.savez_compressed(OUT / name, **out)
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
@@ -810,10 +841,10 @@ MAKERS = {
     "plastic_full": lambda tf: make_plastic(tf, 256, 64, "plastic_ogrid_256x64.npz"),
     "hexa2": make_hexa2, "heat": make_heat, "heat_transient_grad": make_heat_transient_grad,
     "modes": make_modes,
-    "c2": make_c2, "c2_crosscheck": make_c2_crosscheck, "hyper_full": make_hyper_full,
+    "c2": make_c2, "c2_crosscheck": make_c2_crosscheck, "hyper_full": make_hyper_full, "hyper_mid": make_hyper_mid,
 }
 # targets that take minutes to an hour of CPU; run only when named
-SLOW = {"c2", "c2_crosscheck", "hyper_full", "plastic_full", "simp_full"}
+SLOW = {"c2", "c2_crosscheck", "hyper_full", "hyper_mid", "plastic_full", "simp_full"}
 
 
 def main():

@@ -214,3 +214,54 @@ def test_config5_mixed_vs_reference(cuda, golden, precond):
     assert abs(float(R.detach()) - float(g["reaction"])) <= RTOL * abs(float(g["reaction"]))
     (gt,) = torch.autograd.grad(R, t)
     assert rel(gt, g["grad_t"]) <= 1e-7
+
+
+def _hyper(g, E):
+    from torchfem_gb300 import Solid
+    from torchfem_gb300.materials import Hyperelastic3D, neo_hookean_psi
+
+    nodes = torch.tensor(g["nodes"])
+    el = torch.tensor(g["elements"])
+    nu = 0.45
+    mu = E / (2.0 * (1.0 + nu))
+    lbd = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    m = Solid(nodes, el, Hyperelastic3D(neo_hookean_psi, torch.stack([mu, lbd], dim=-1)))
+    right = nodes[:, 0] == 3.0
+    m.constraints[nodes[:, 0] == 0.0, :] = True
+    m.constraints[right, 0] = True
+    m.displacements[right, 0] = 0.5
+    return m, right
+
+
+@pytest.mark.parametrize("precision,precond", [("fp64", None), ("mixed", "amg")])
+def test_config4_problem_increments_like_the_reference(cuda, golden, precision, precond):
+    """Config 4's problem (Neo-Hookean Tetra2 box pulled to +0.5, nlgeom) at
+    half the resolution, where the reference's direct solve is affordable
+    (hyper_tet2_15x5x5.npz, 11,163 DOF): with the 10 load increments the
+    configuration states, the reference's own solve raises (its warm start,
+    the previous substep's increment, overshoots after a cutback); the GPU
+    path raises with the same message.  With 20 increments both complete:
+    u, f, sigma and the tip reaction to 1e-8, d(reaction)/dE_e to 1e-7."""
+    g = golden("hyper_tet2_15x5x5.npz")
+    E0 = torch.tensor(g["E"])
+    m, right = _hyper(g, E0)
+    with pytest.raises(RuntimeError, match="increment 9 after 10 cutbacks"):
+        m.solve(increments=torch.linspace(0.0, 1.0, 11), nlgeom=True, rtol=1e-10, atol=1e-10, max_iter=20,
+                stol=1e-12, precision=precision, preconditioner=precond)
+    assert str(g["inc10_error"]).endswith("increment 9 after 10 cutbacks.")
+    E = E0.clone().requires_grad_(True)
+    m, right = _hyper(g, E)
+    u, f, s, _, _ = m.solve(increments=torch.linspace(0.0, 1.0, int(g["increments"]) + 1), nlgeom=True, rtol=1e-10,
+                            atol=1e-10, max_iter=20, stol=1e-12, precision=precision, preconditioner=precond,
+                            differentiable_parameters=E)
+
+    def rel(a, b):
+        return float(np.abs(a.detach().cpu().numpy() - b).max() / np.abs(b).max())
+
+    assert rel(u, g["u"]) <= RTOL
+    assert rel(f, g["f"]) <= RTOL
+    assert rel(s, g["sigma"]) <= RTOL
+    R = f[right.to(f.device), 0].sum()
+    assert abs(float(R.detach()) - float(g["reaction"])) <= RTOL * abs(float(g["reaction"]))
+    (gE,) = torch.autograd.grad(R, E)
+    assert rel(gE, g["grad_E"]) <= 1e-7

@@ -1509,6 +1509,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(int64_t n_c, const int64_
 constexpr int kCycT = 512;    // threads per CTA
 constexpr int kCycPerSm = 2;  // CTAs per SM at most (occupancy may allow fewer)
 constexpr long long kCycSpin = 4000000000LL;  // clock cycles a barrier wait may last (about 2 s)
+constexpr int64_t kTailDof = 2048;  // coarse levels of at most this many unknowns run on one CTA
 
 struct CycLevel {
   int64_t n;  // block rows
@@ -1536,6 +1537,7 @@ struct CycBarrier {
 
 struct CycArgs {
   int n_levels;
+  int tail_start;  // first coarse level run by CTA 0 alone (n_levels - 1: none before the coarsest)
   CycLevel L[kMaxLevels];
   const float* coarse_inv;
   AmgCtrl* ctrl;
@@ -1715,28 +1717,91 @@ __device__ __forceinline__ void cyc_coarsest(const CycLevel& F, const CycLevel& 
   }
 }
 
-// Prolongation x += P x_c over the grid, a thread per (fine row, component).
+// Prolongation x += P x_c, a thread per (fine row, component), threads
+// t0, t0 + stride, ...; each thread keeps kProlongU items' loads in flight
+// (every item still sums its blocks in ascending order).
+constexpr int kProlongU = 4;
 template <int BF, int K>
-__device__ __forceinline__ void cyc_prolong(const CycLevel& F, const float* __restrict__ xc, float* __restrict__ x) {
+__device__ __forceinline__ void cyc_prolong(const CycLevel& F, const float* __restrict__ xc, float* __restrict__ x,
+                                            int64_t t0, int64_t stride) {
   const int64_t n = F.n * BF;
-  for (int64_t t = (int64_t)blockIdx.x * kCycT + threadIdx.x; t < n; t += (int64_t)gridDim.x * kCycT) {
-    const int64_t i = t / BF;
-    const int r = (int)(t - i * BF);
-    float s = 0.f;
-    for (int64_t e = F.p_ptr[i]; e < F.p_ptr[i + 1]; ++e) {
-      float pv[K];
-      load_half<K>(F.p_h + e * BF * K + r * K, pv);
-      const float* cv = xc + (int64_t)F.p_col[e] * K;
+  for (int64_t t = t0; t < n; t += kProlongU * stride) {
+    int64_t e[kProlongU], e1[kProlongU];
+    float s[kProlongU];
 #pragma unroll
-      for (int k = 0; k < K; ++k) s = fmaf(pv[k], cv[k], s);
+    for (int u = 0; u < kProlongU; ++u) {
+      const int64_t tu = t + u * stride;
+      s[u] = 0.f;
+      e[u] = e1[u] = 0;
+      if (tu < n) {
+        const int64_t i = tu / BF;
+        e[u] = F.p_ptr[i];
+        e1[u] = F.p_ptr[i + 1];
+      }
     }
-    x[t] += s;
+    bool more = true;
+    while (more) {
+      more = false;
+#pragma unroll
+      for (int u = 0; u < kProlongU; ++u) {
+        if (e[u] < e1[u]) {
+          const int64_t tu = t + u * stride;
+          const int r = (int)(tu - (tu / BF) * BF);
+          float pv[K];
+          load_half<K>(F.p_h + e[u] * BF * K + r * K, pv);
+          const float* cv = xc + (int64_t)F.p_col[e[u]] * K;
+#pragma unroll
+          for (int k = 0; k < K; ++k) s[u] = fmaf(pv[k], cv[k], s[u]);
+          ++e[u];
+          more = true;
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kProlongU; ++u) {
+      const int64_t tu = t + u * stride;
+      if (tu < n) x[tu] += s[u];
+    }
   }
 }
 
 template <int K, int MODE>
 __device__ __forceinline__ void cyc_pass(const CycLevel& L, int lane, int64_t warp, int64_t n_warps, uint64_t pol) {
   for (int64_t i = warp; i < L.n; i += n_warps) cyc_row<K, MODE>(L, i, lane, pol);
+}
+
+// The small coarse levels (tail_start .. the coarsest) by CTA 0 alone, CTA
+// barriers between the phases: pre-smoothing, restriction, the coarsest
+// solve, prolongation and post-smoothing of every tail level.  The grid has
+// already restricted into tail_start.
+template <int K>
+__device__ __forceinline__ void cyc_tail(const CycArgs& a, int ts, float* fs, uint64_t pol) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  constexpr int nw = kCycT / 32;
+  const int last = a.n_levels - 1;
+  for (int l = ts; l < last; ++l) {
+    const CycLevel& F = a.L[l];
+    const CycLevel& C = a.L[l + 1];
+    cyc_pass<K, kOpS1>(F, lane, w, nw, pol);
+    __syncthreads();
+    cyc_pass<K, kOpS2>(F, lane, w, nw, pol);
+    __syncthreads();
+    if (l + 1 == last) {
+      cyc_coarsest<K, K>(F, C, a.coarse_inv, fs);
+    } else {
+      for (int64_t I = w; I < C.n; I += nw) cyc_restrict<K, K>(F, C, I, lane);
+    }
+    __syncthreads();
+  }
+  for (int l = last - 1; l >= ts; --l) {
+    const CycLevel& F = a.L[l];
+    cyc_prolong<K, K>(F, a.L[l + 1].xb, F.x, threadIdx.x, kCycT);
+    __syncthreads();
+    cyc_pass<K, kOpS3>(F, lane, w, nw, pol);
+    __syncthreads();
+    cyc_pass<K, kOpS4>(F, lane, w, nw, pol);
+    __syncthreads();
+  }
 }
 
 template <int B0, int K>
@@ -1748,10 +1813,14 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * kCycT + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * kCycT) >> 5;
+  const int64_t tid = (int64_t)blockIdx.x * kCycT + threadIdx.x;
+  const int64_t n_threads = (int64_t)gridDim.x * kCycT;
   const uint64_t pol = l2_policy(true);
   const int last = a.n_levels - 1;
+  const int ts = a.tail_start;  // first level done by CTA 0 alone (last: none but the coarsest)
   // down: restrict (with the first Chebyshev step), then the level's second
   // pass and residual
+  int up_from = last - 1;
   for (int l = 0; l < last; ++l) {
     const CycLevel& F = a.L[l];
     const CycLevel& C = a.L[l + 1];
@@ -1767,6 +1836,11 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
       else cyc_restrict<K, K>(F, C, I, lane);
     }
     if (!cyc_barrier(bar, c)) return;
+    if (l + 1 == ts) {
+      if (blockIdx.x == 0) cyc_tail<K>(a, ts, fs, pol);
+      up_from = ts - 1;
+      break;
+    }
     cyc_pass<K, kOpS1>(C, lane, warp, n_warps, pol);
     if (!cyc_barrier(bar, c)) return;
     cyc_pass<K, kOpS2>(C, lane, warp, n_warps, pol);
@@ -1774,14 +1848,14 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
   }
   // up: prolongate, then the level's post-smoothing; level 0 continues in
   // the next launch
-  for (int l = last - 1; l >= 0; --l) {
+  for (int l = up_from; l >= 0; --l) {
     if (!cyc_barrier(bar, c)) return;
     const CycLevel& F = a.L[l];
     if (l == 0) {
-      cyc_prolong<B0, K>(F, a.L[1].xb, F.x);
+      cyc_prolong<B0, K>(F, a.L[1].xb, F.x, tid, n_threads);
       break;
     }
-    cyc_prolong<K, K>(F, a.L[l + 1].xb, F.x);
+    cyc_prolong<K, K>(F, a.L[l + 1].xb, F.x, tid, n_threads);
     if (!cyc_barrier(bar, c)) return;
     cyc_pass<K, kOpS3>(F, lane, warp, n_warps, pol);
     if (!cyc_barrier(bar, c)) return;
@@ -2870,6 +2944,14 @@ bool launch_coarse_fused(fem_amg* h, cudaStream_t st) {
   ca.coarse_inv = h->coarse_inv;
   ca.ctrl = h->ctrl;
   ca.bar = h->cyc_bar;
+  // the small levels below level 1 go to one CTA (level 1 and up are never
+  // the tail: their restriction from the level above is a grid phase)
+  ca.tail_start = h->n_levels - 1;
+  for (int l = 2; l < h->n_levels - 1; ++l)
+    if (h->L[l].n * K <= kTailDof) {
+      ca.tail_start = l;
+      break;
+    }
   void* args[] = {&ca};
   if (cudaLaunchCooperativeKernel((const void*)k_coarse_cycle<B0, K>, dim3(h->cyc_blocks), dim3(kCycT), args, 0,
                                   st) != cudaSuccess) {

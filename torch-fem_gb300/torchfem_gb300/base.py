@@ -326,6 +326,10 @@ class FEM:
 
         lam = float(increments[0])
         step_frac = 1.0
+        # until the first substep converges, a linear material's Newton start
+        # (zero increment, zero stress) gives zero internal forces when no
+        # displacement is prescribed: its first residual needs no element pass
+        fresh = not nonlinear and (de0_full is None) and not bool(DU_dir.any())
         with torch.set_grad_enabled(track):
             for n in range(1, N):
                 target = float(increments[n])
@@ -350,6 +354,7 @@ class FEM:
                                 sigma_prev.contiguous(), st_prev.contiguous(), de0, mat_data, thickness,
                             )
                         else:
+                            sc.zero_start = fresh
                             du = NewtonLinear.apply(
                                 sc, du.detach(), F_ext.contiguous(), DU.contiguous(),
                                 sigma_prev.contiguous(), de0, mat_data, thickness,
@@ -385,6 +390,7 @@ class FEM:
                     u_cur = u_cur + du_eval
                     flux_cur = flux_new
                     du = du_eval
+                    fresh = False
                     lam += step
                     step_size = min(growth_factor * step_size, abs(span))
                 step_frac = min(step_size / abs(span), 1.0) if span != 0.0 else 1.0

@@ -32,6 +32,8 @@ from ._lib import check, ptr
 class SolveContext:
     """What one solve() call shares between its Newton steps and backward."""
 
+    AMG_DELTA = 1e-4  # default FP64 replacement threshold of the multigrid CG
+
     def __init__(self, dm: DeviceMesh, con_mask: Tensor, mat_kind: int, precision: str,
                  max_iter: int, rtol: float, atol: float, stol: float, cg_max_iter: int | None,
                  delta: float = 0.1):
@@ -57,7 +59,13 @@ class SolveContext:
         self.precond_explicit = False  # the caller asked for this preconditioner by name
         # FP64 replacement threshold of the multigrid CG: each V-cycle cuts the
         # residual severalfold, so replacements are spaced by a deeper drop
-        self.amg_delta = 1e-4
+        self.amg_delta = SolveContext.AMG_DELTA
+        # set by the caller when the Newton start is known to give zero internal
+        # forces (zero increment, zero previous stress, zero prescribed values)
+        self.zero_start = False
+        # (f_e, flux, H) of the residual evaluation at which Newton converged,
+        # taken by the converged-state evaluation of the same increment
+        self.converged_eval = None
 
     def structs(self, mat_data: Tensor, thickness: Tensor | None):
         from . import _lib
@@ -119,14 +127,21 @@ class SolveContext:
         return x
 
 
-def _residual(sc: SolveContext, du, F_ext, DU, sigma_prev, de0, mat_data, thickness):
-    """res = F_int(du_bc) - F_ext with res[con] = 0, and ||res|| (device)."""
+def _residual(sc: SolveContext, du, F_ext, DU, sigma_prev, de0, mat_data, thickness, zero=False):
+    """res = F_int(du_bc) - F_ext with res[con] = 0, and ||res||^2 (device);
+    also the element forces, fluxes and increment gradients of du_bc, which
+    the converged-state evaluation reuses.  zero=True: F_int is known to be
+    zero (zero increment, prescribed values and previous stress, no initial
+    strain), so no element pass runs."""
+    if zero:
+        res = torch.where(sc.con_bool, torch.zeros_like(F_ext), -F_ext).contiguous()
+        return res, (res * res).sum().reshape(1), None
     mesh, mat = sc.structs(mat_data, thickness)
-    fe, _, _ = sc.dm.element_force(
-        mesh, mat, du, sc.con_mask, DU, 1, sigma_prev, de0
+    fe, flux, hg = sc.dm.element_force(
+        mesh, mat, du, sc.con_mask, DU, 1, sigma_prev, de0, want_flux=True, want_h=True
     )
     res, sumsq = sc.dm.gather(fe, sub=F_ext, con_mask=sc.con_mask, con_mode=1, want_norm=True)
-    return res, sumsq
+    return res, sumsq, (fe, flux, hg)
 
 
 class NewtonLinear(torch.autograd.Function):
@@ -137,8 +152,10 @@ class NewtonLinear(torch.autograd.Function):
         du = du.detach().clone()
         res0 = None
         converged = False
+        sc.converged_eval = None
         for i in range(sc.max_iter):
-            res, sumsq = _residual(sc, du, F_ext, DU, sigma_prev, de0, mat_data, thickness)
+            res, sumsq, ev = _residual(sc, du, F_ext, DU, sigma_prev, de0, mat_data, thickness,
+                                       zero=(i == 0 and sc.zero_start and de0 is None))
             res_norm = float(sumsq.sqrt().item())
             if i == 0:
                 res0 = res_norm
@@ -149,6 +166,7 @@ class NewtonLinear(torch.autograd.Function):
             if res_norm < sc.rtol * res0 or res_norm < sc.atol:
                 converged = True
                 sc.newton_iterations.append(i)
+                sc.converged_eval = ev
                 break
             if res_norm != res_norm or res_norm in (float("inf"), float("-inf")):
                 break
@@ -196,9 +214,15 @@ class IntegrateMaterial(torch.autograd.Function):
     def forward(ctx, sc: SolveContext, du_eval, sigma_prev, de0, mat_data, thickness):
         mesh, mat = sc.structs(mat_data, thickness)
         dm = sc.dm
-        fe, flux, hg = dm.element_force(
-            mesh, mat, du_eval, None, None, 0, sigma_prev, de0, want_flux=True, want_h=True
-        )
+        cached, sc.converged_eval = sc.converged_eval, None
+        if cached is not None:
+            # the Newton iteration's last residual was evaluated at this same
+            # displacement (du with the prescribed values on constrained DOFs)
+            fe, flux, hg = cached
+        else:
+            fe, flux, hg = dm.element_force(
+                mesh, mat, du_eval, None, None, 0, sigma_prev, de0, want_flux=True, want_h=True
+            )
         f_int, _ = dm.gather(fe)
         shape = (dm.nip, dm.n_elem, *dm.flux_shape)
         ctx.sc = sc
