@@ -1503,13 +1503,13 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(int64_t n_c, const int64_
 // (block, row) items, 32 / K blocks per pass, partial rows summed across
 // lanes by shuffles in a fixed order), a warp per coarse row of a
 // restriction, a thread per (fine row, component) of a prolongation, and CTA
-// 0 for the coarsest solve.  Every sum keeps a fixed order, so results are
+// 0 for the coarsest solve; a level with no more rows than the grid has CTAs
+// takes a CTA per row instead of a warp.  Every sum keeps a fixed order, so results are
 // identical run to run; the arithmetic is that of the per-level kernels
 // above up to the order of partial row sums.
 constexpr int kCycT = 512;    // threads per CTA
 constexpr int kCycPerSm = 2;  // CTAs per SM at most (occupancy may allow fewer)
 constexpr long long kCycSpin = 4000000000LL;  // clock cycles a barrier wait may last (about 2 s)
-constexpr int64_t kTailDof = 2048;  // coarse levels of at most this many unknowns run on one CTA
 
 struct CycLevel {
   int64_t n;  // block rows
@@ -1537,7 +1537,6 @@ struct CycBarrier {
 
 struct CycArgs {
   int n_levels;
-  int tail_start;  // first coarse level run by CTA 0 alone (n_levels - 1: none before the coarsest)
   CycLevel L[kMaxLevels];
   const float* coarse_inv;
   AmgCtrl* ctrl;
@@ -1770,43 +1769,124 @@ __device__ __forceinline__ void cyc_pass(const CycLevel& L, int lane, int64_t wa
   for (int64_t i = warp; i < L.n; i += n_warps) cyc_row<K, MODE>(L, i, lane, pol);
 }
 
-// The small coarse levels (tail_start .. the coarsest) by CTA 0 alone, CTA
-// barriers between the phases: pre-smoothing, restriction, the coarsest
-// solve, prolongation and post-smoothing of every tail level.  The grid has
-// already restricted into tail_start.
-template <int K>
-__device__ __forceinline__ void cyc_tail(const CycArgs& a, int ts, float* fs, uint64_t pol) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  constexpr int nw = kCycT / 32;
-  const int last = a.n_levels - 1;
-  for (int l = ts; l < last; ++l) {
-    const CycLevel& F = a.L[l];
-    const CycLevel& C = a.L[l + 1];
-    cyc_pass<K, kOpS1>(F, lane, w, nw, pol);
-    __syncthreads();
-    cyc_pass<K, kOpS2>(F, lane, w, nw, pol);
-    __syncthreads();
-    if (l + 1 == last) {
-      cyc_coarsest<K, K>(F, C, a.coarse_inv, fs);
-    } else {
-      for (int64_t I = w; I < C.n; I += nw) cyc_restrict<K, K>(F, C, I, lane);
+// The same pass on block row i by a whole CTA, for levels with fewer rows
+// than the grid has CTAs (their rows are long: the operator fills in as the
+// levels coarsen).  Thread t < PB K holds (block t / K, row t % K) items;
+// the PB partial rows are summed in shared memory in a fixed order.
+template <int K, int MODE>
+__device__ __forceinline__ void cyc_row_cta(const CycLevel& L, int64_t i, uint64_t pol, float* part) {
+  constexpr int PB = kCycT / K;
+  const int t = threadIdx.x;
+  const float* __restrict__ v = MODE == kOpS1 || MODE == kOpS4 ? L.d : MODE == kOpS2 ? L.db : L.x;
+  const int blk = t / K, r = t - (t / K) * K;
+  float y = 0.f;
+  if (blk < PB) {
+    const int64_t e1 = L.a_ptr[i + 1];
+    for (int64_t e = L.a_ptr[i] + blk; e < e1; e += PB) {
+      const int64_t c = ld_l2(L.a_col + e, pol);
+#pragma unroll
+      for (int q = 0; q < K; ++q) y = fmaf(ld_l2(L.a_val + e * K * K + r * K + q, pol), v[c * K + q], y);
     }
-    __syncthreads();
   }
-  for (int l = last - 1; l >= ts; --l) {
-    const CycLevel& F = a.L[l];
-    cyc_prolong<K, K>(F, a.L[l + 1].xb, F.x, threadIdx.x, kCycT);
-    __syncthreads();
-    cyc_pass<K, kOpS3>(F, lane, w, nw, pol);
-    __syncthreads();
-    cyc_pass<K, kOpS4>(F, lane, w, nw, pol);
-    __syncthreads();
+  part[t] = y;
+  __syncthreads();
+  __shared__ float rs[8];
+  const int64_t o = i * K + t;
+  float yr = 0.f, rn = 0.f;
+  if (t < K) {
+    for (int b = 0; b < PB; ++b) yr += part[t + b * K];
+    if constexpr (MODE == kOpS1 || MODE == kOpS3) rn = L.f[o] - yr;
+    else if constexpr (MODE == kOpS4) rn = L.r[o] - yr;
+    rs[t] = rn;
+  }
+  __syncthreads();
+  if (t < K) {
+    float tv = 0.f;
+    if constexpr (MODE != kOpS2) {
+#pragma unroll
+      for (int q = 0; q < K; ++q) tv = fmaf(L.dinv[o * K + q], rs[q], tv);
+    }
+    if constexpr (MODE == kOpS1) {
+      const float dn = L.c1 * L.d[o] + L.c2 * tv;
+      L.r[o] = rn;
+      L.db[o] = dn;
+      L.x[o] += dn;
+    } else if constexpr (MODE == kOpS2) {
+      L.r[o] -= yr;
+    } else if constexpr (MODE == kOpS3) {
+      const float dn = L.theta_inv * tv;
+      L.r[o] = rn;
+      L.d[o] = dn;
+      L.xb[o] = L.x[o] + dn;
+    } else {
+      L.xb[o] = L.xb[o] + (L.c1 * L.d[o] + L.c2 * tv);
+    }
+  }
+  __syncthreads();
+}
+
+// Restriction onto coarse row I by a whole CTA (coarse levels with no more
+// rows than the grid has CTAs): threads over the row's P^T entries, warp
+// xor-trees, then the warps' sums in order; then the first Chebyshev step.
+template <int BF, int K>
+__device__ __forceinline__ void cyc_restrict_cta(const CycLevel& F, const CycLevel& C, int64_t I, float* part) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  constexpr int NWp = kCycT / 32;
+  float acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.f;
+  for (int64_t e = F.pt_ptr[I] + t; e < F.pt_ptr[I + 1]; e += kCycT) {
+    const int64_t i = F.pt_row[e];
+    float pv[BF * K];
+    load_half<BF * K>(F.pt_val + e * BF * K, pv);
+#pragma unroll
+    for (int q = 0; q < BF; ++q) {
+      const float rv = F.r[i * BF + q];
+#pragma unroll
+      for (int k = 0; k < K; ++k) acc[k] = fmaf(pv[q * K + k], rv, acc[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) part[w * K + k] = acc[k];
+  __syncthreads();
+  __shared__ float fsum[8];
+  if (t < K) {
+    float f = 0.f;
+    for (int u = 0; u < NWp; ++u) f += part[u * K + t];
+    fsum[t] = f;
+  }
+  __syncthreads();
+  if (t < K) {
+    float tv = 0.f;
+#pragma unroll
+    for (int q = 0; q < K; ++q) tv = fmaf(C.dinv[(I * K + t) * K + q], fsum[q], tv);
+    const float dn = C.theta_inv * tv;
+    C.f[I * K + t] = fsum[t];
+    C.d[I * K + t] = dn;
+    C.x[I * K + t] = dn;
+  }
+  __syncthreads();
+}
+
+// One pass over a coarse level: a warp per row, or a CTA per row when the
+// level has no more rows than the grid has CTAs.
+template <int K, int MODE>
+__device__ __forceinline__ void cyc_level_pass(const CycLevel& L, int lane, int64_t warp, int64_t n_warps,
+                                               uint64_t pol, float* part) {
+  if (L.n <= (int64_t)gridDim.x) {
+    for (int64_t i = blockIdx.x; i < L.n; i += gridDim.x) cyc_row_cta<K, MODE>(L, i, pol, part);
+  } else {
+    cyc_pass<K, MODE>(L, lane, warp, n_warps, pol);
   }
 }
 
 template <int B0, int K>
 __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
   __shared__ float fs[kCoarseMaxDof];
+  __shared__ float part[kCycT];
   AmgCtrl* c = a.ctrl;
   CycBarrier* bar = a.bar;
   if (amg_idle(c)) return;
@@ -1817,10 +1897,8 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
   const int64_t n_threads = (int64_t)gridDim.x * kCycT;
   const uint64_t pol = l2_policy(true);
   const int last = a.n_levels - 1;
-  const int ts = a.tail_start;  // first level done by CTA 0 alone (last: none but the coarsest)
   // down: restrict (with the first Chebyshev step), then the level's second
   // pass and residual
-  int up_from = last - 1;
   for (int l = 0; l < last; ++l) {
     const CycLevel& F = a.L[l];
     const CycLevel& C = a.L[l + 1];
@@ -1831,24 +1909,26 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
       }
       break;
     }
-    for (int64_t I = warp; I < C.n; I += n_warps) {
-      if (l == 0) cyc_restrict<B0, K>(F, C, I, lane);
-      else cyc_restrict<K, K>(F, C, I, lane);
+    if (C.n <= (int64_t)gridDim.x) {
+      for (int64_t I = blockIdx.x; I < C.n; I += gridDim.x) {
+        if (l == 0) cyc_restrict_cta<B0, K>(F, C, I, part);
+        else cyc_restrict_cta<K, K>(F, C, I, part);
+      }
+    } else {
+      for (int64_t I = warp; I < C.n; I += n_warps) {
+        if (l == 0) cyc_restrict<B0, K>(F, C, I, lane);
+        else cyc_restrict<K, K>(F, C, I, lane);
+      }
     }
     if (!cyc_barrier(bar, c)) return;
-    if (l + 1 == ts) {
-      if (blockIdx.x == 0) cyc_tail<K>(a, ts, fs, pol);
-      up_from = ts - 1;
-      break;
-    }
-    cyc_pass<K, kOpS1>(C, lane, warp, n_warps, pol);
+    cyc_level_pass<K, kOpS1>(C, lane, warp, n_warps, pol, part);
     if (!cyc_barrier(bar, c)) return;
-    cyc_pass<K, kOpS2>(C, lane, warp, n_warps, pol);
+    cyc_level_pass<K, kOpS2>(C, lane, warp, n_warps, pol, part);
     if (!cyc_barrier(bar, c)) return;
   }
   // up: prolongate, then the level's post-smoothing; level 0 continues in
   // the next launch
-  for (int l = up_from; l >= 0; --l) {
+  for (int l = last - 1; l >= 0; --l) {
     if (!cyc_barrier(bar, c)) return;
     const CycLevel& F = a.L[l];
     if (l == 0) {
@@ -1857,9 +1937,9 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
     }
     cyc_prolong<K, K>(F, a.L[l + 1].xb, F.x, tid, n_threads);
     if (!cyc_barrier(bar, c)) return;
-    cyc_pass<K, kOpS3>(F, lane, warp, n_warps, pol);
+    cyc_level_pass<K, kOpS3>(F, lane, warp, n_warps, pol, part);
     if (!cyc_barrier(bar, c)) return;
-    cyc_pass<K, kOpS4>(F, lane, warp, n_warps, pol);
+    cyc_level_pass<K, kOpS4>(F, lane, warp, n_warps, pol, part);
   }
 }
 
@@ -2944,14 +3024,7 @@ bool launch_coarse_fused(fem_amg* h, cudaStream_t st) {
   ca.coarse_inv = h->coarse_inv;
   ca.ctrl = h->ctrl;
   ca.bar = h->cyc_bar;
-  // the small levels below level 1 go to one CTA (level 1 and up are never
-  // the tail: their restriction from the level above is a grid phase)
-  ca.tail_start = h->n_levels - 1;
-  for (int l = 2; l < h->n_levels - 1; ++l)
-    if (h->L[l].n * K <= kTailDof) {
-      ca.tail_start = l;
-      break;
-    }
+
   void* args[] = {&ca};
   if (cudaLaunchCooperativeKernel((const void*)k_coarse_cycle<B0, K>, dim3(h->cyc_blocks), dim3(kCycT), args, 0,
                                   st) != cudaSuccess) {

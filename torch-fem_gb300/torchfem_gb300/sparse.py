@@ -186,13 +186,19 @@ class NewtonLinear(torch.autograd.Function):
         g = torch.where(sc.con_bool, torch.zeros_like(grad_du), grad_du).contiguous()
         sc.get_system(mat_data, thickness)
         lam = sc.solve(g)
-        mesh, mat = sc.structs(mat_data, thickness)
-        neg = (-lam).contiguous()
-        gsig, gmat, gthick, gde0, gv = sc.dm.vjp(
-            mesh, mat, du, neg, sc.con_mask, DU, 1, sigma_prev, de0,
-            want_sig=need[4], want_mat=need[6], want_thick=need[7] and thickness is not None,
-            want_de0=need[5] and de0 is not None, want_v=need[3], mat_numel=mat_data.numel(),
-        )
+        gsig = gmat = gthick = gde0 = gv = None
+        want_thick = need[7] and thickness is not None
+        want_de0 = need[5] and de0 is not None
+        if need[3] or need[4] or need[6] or want_thick or want_de0:
+            # the residual's parameter pull-back (a gradient w.r.t. the loads
+            # alone is lambda itself and needs no element pass)
+            mesh, mat = sc.structs(mat_data, thickness)
+            neg = (-lam).contiguous()
+            gsig, gmat, gthick, gde0, gv = sc.dm.vjp(
+                mesh, mat, du, neg, sc.con_mask, DU, 1, sigma_prev, de0,
+                want_sig=need[4], want_mat=need[6], want_thick=want_thick,
+                want_de0=want_de0, want_v=need[3], mat_numel=mat_data.numel(),
+            )
         g_F = lam if need[2] else None
         g_DU = torch.where(sc.con_bool, gv, torch.zeros_like(gv)) if need[3] else None
         return (
