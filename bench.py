@@ -522,6 +522,136 @@ def run_heat(args):
     print(json.dumps(line))
 
 
+CONFIG_METRIC = "config {k}: solve+grad s per 1M DOF, mixed precision (FP32 multigrid CG + FP64 refinement) vs plain FP64"
+
+
+def config_workload(k: int, device):
+    """The BASELINE configurations 3, 4 and 5 as (model, parameter, step):
+    step(precision, precond) runs the configuration's solve and the gradient
+    of its loss and returns (primary field, gradient).
+      3: SIMP cantilever, Quad1 400 x 200, compliance f.u, dL/drho;
+      4: Neo-Hookean Tetra2 box 30 x 10 x 10 pulled to +0.5 with nlgeom in 40
+         increments (10 and 20 fail in the reference's algorithm as in this
+         one), tip reaction, d/dE_e;
+      5: J2 plane-strain O-grid plate 256 x 64 with a hole, 20 increments,
+         reaction, d/d(thickness)."""
+    from torchfem_gb300 import Planar, Solid, mesh
+    from torchfem_gb300.materials import (Hyperelastic3D, IsotropicElasticityPlaneStress,
+                                          IsotropicPlasticityPlaneStrain, neo_hookean_psi)
+
+    if k == 3:
+        nodes, el = mesh.rect_quad(401, 201, 2.0, 1.0)
+        rho0 = 0.2 + 0.8 * torch.rand(len(el), generator=torch.Generator().manual_seed(0), dtype=torch.float64)
+        tip = torch.argmin(((nodes - torch.tensor([2.0, 0.5])) ** 2).sum(1))
+
+        def step(precision, precond):
+            rho = rho0.to(device).requires_grad_(True)
+            m = Planar(nodes.to(device), el.to(device), IsotropicElasticityPlaneStress(rho**3 * 1.0, 0.3))
+            m.constraints[(nodes[:, 0] == 0.0).to(device), :] = True
+            m.forces[tip, 1] = -1.0
+            u, f, _, _, _ = m.solve(stol=1e-10, precision=precision, preconditioner=precond,
+                                    differentiable_parameters=rho)
+            (g,) = torch.autograd.grad(torch.inner(f.ravel(), u.ravel()), rho)
+            return m, u, g
+        return step, "quad1_simp_cantilever_400x200_compliance+dL/drho", {"stol": 1e-10}
+    if k == 4:
+        nodes, el = mesh.linear_to_quadratic(*mesh.box_tetra6(31, 11, 11, 3.0, 1.0, 1.0))
+        E0 = 1000.0 * (1.0 + 0.1 * torch.randn(len(el), generator=torch.Generator().manual_seed(0),
+                                               dtype=torch.float64))
+        right = nodes[:, 0] == 3.0
+
+        def step(precision, precond):
+            E = E0.to(device).requires_grad_(True)
+            nu = 0.45
+            mu, lbd = E / (2.0 * (1.0 + nu)), E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+            m = Solid(nodes.to(device), el.to(device), Hyperelastic3D(neo_hookean_psi, torch.stack([mu, lbd], -1)))
+            m.constraints[(nodes[:, 0] == 0.0).to(device), :] = True
+            m.constraints[right.to(device), 0] = True
+            m.displacements[right.to(device), 0] = 0.5
+            u, f, _, _, _ = m.solve(increments=torch.linspace(0.0, 1.0, 41), nlgeom=True, rtol=1e-10, atol=1e-10,
+                                    max_iter=20, stol=1e-12, precision=precision, preconditioner=precond,
+                                    differentiable_parameters=E)
+            (g,) = torch.autograd.grad(f[right.to(device), 0].sum(), E)
+            return m, u, g
+        return step, "tetra2_neo_hookean_box_30x10x10_40_increments_reaction+dR/dE", \
+            {"stol": 1e-12, "increments": 40, "newton_rtol": 1e-10}
+    nodes, el = mesh.plate_hole_ogrid(256, 64)
+    left = torch.isclose(nodes[:, 0], torch.tensor(0.0, dtype=torch.float64))
+    right = torch.isclose(nodes[:, 0], torch.tensor(2.0, dtype=torch.float64))
+    pin = torch.argmin(((nodes - torch.tensor([0.0, 0.5])) ** 2).sum(1))
+
+    def step(precision, precond):
+        mat = IsotropicPlasticityPlaneStrain(1000.0, 0.3, lambda q: 1.0 + 100.0 * q,
+                                             lambda q: 100.0 * torch.ones_like(q))
+        t = torch.ones(len(el), dtype=torch.float64, device=device, requires_grad=True)
+        m = Planar(nodes.to(device), el.to(device), mat, thickness=t)
+        m.constraints[left.to(device), 0] = True
+        m.constraints[pin, 1] = True
+        m.constraints[right.to(device), 0] = True
+        m.displacements[right.to(device), 0] = 0.02
+        u, f, _, _, _ = m.solve(increments=torch.linspace(0.0, 1.0, 21), rtol=1e-12, atol=1e-12, max_iter=80,
+                                stol=1e-12, precision=precision, preconditioner=precond, differentiable_parameters=t)
+        (g,) = torch.autograd.grad(f[right.to(device), 0].sum(), t)
+        return m, u, g
+    return step, "quad1_ogrid_plate_hole_256x64_j2_plane_strain_20_increments_reaction+dR/dt", \
+        {"stol": 1e-12, "increments": 20, "newton_rtol": 1e-12}
+
+
+def run_config(args):
+    """One of the configurations 3, 4, 5 (--workload config3|config4|config5):
+    --warmup untimed and --steps timed steps of the mixed path (multigrid),
+    then one timed step of the FP64 path; CUDA events on the launching
+    stream.  The roofline is the level-0 SpMV of the multigrid CG (its
+    CUDA-event mean over the timed steps' last linear solve)."""
+    from torchfem_gb300 import _lib
+
+    k = int(args.workload[-1])
+    dev = torch.device("cuda", 0)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    stepf, name, settings = config_workload(k, dev)
+    holder = {}
+
+    def run(prec, pc):
+        m, u, g = stepf(prec, pc)
+        holder["m"] = m
+        return (u, g), m
+
+    for _ in range(max(args.warmup, 0)):
+        run("mixed", "amg")
+    torch.cuda.synchronize()
+    ms, iters, u_ms, u_n, launches, clocks, (u_m, g_m) = timed_steps(lib, lambda: run("mixed", "amg"), args.steps,
+                                                                     stream)
+    m = holder["m"]
+    dm = m.device_mesh
+    n_dofs = m.n_dofs
+    p_ms, p_iters, _, _, _, _, (u_p, g_p) = timed_steps(lib, lambda: run("fp64", None), 1, stream)
+    peak, peak_kind = measured_peak_hbm()
+    unit_s = (u_ms / u_n) / 1e3 if u_n else None
+    sb = level0_launch_bytes(dm, args.smoother)
+    achieved = sb / unit_s / 1e9 if unit_s else None
+    line = {
+        "metric": CONFIG_METRIC.format(k=k), "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded, the configuration's)",
+        "config": {"workload": f"config{k}: {name}", "dofs": n_dofs, "nnz": dm.nnz, "n_elem": m.n_elem,
+                   "preconditioner": "smoothed-aggregation multigrid", **settings},
+        "cg_iterations_last_step": ({"solves": len(iters[-1]), "total": sum(iters[-1]),
+                                     "max": max(iters[-1])} if iters and iters[-1] else None),
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_sell_op<d,*> (level-0 SpMV of the multigrid CG)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None, "algorithmic_bytes": sb,
+                     "avg_unit_us": unit_s * 1e6 if unit_s else None, "peak_source": peak_kind},
+        "plain_fp64": {"value": p_ms / 1e3 / (n_dofs / 1e6), "ms_per_step": p_ms},
+        "mixed_speedup_vs_plain": p_ms / ms,
+        "rel_err_mixed_vs_fp64": {"u": float((u_m - u_p).detach().abs().max() / u_p.detach().abs().max()),
+                                  "grad": float((g_m - g_p).abs().max() / g_p.abs().max())},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def run_profile_step(args):
     """For a launch list: the cube's set-up, --warmup mixed steps, then
     exactly one more (the one a summary describes)."""
@@ -577,7 +707,8 @@ def main():
     ap.add_argument("--cg-path", choices=["persistent", "persistent-regs", "kernels"], default="persistent")
     ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
                     help="preconditioner of the mixed-precision headline")
-    ap.add_argument("--workload", choices=["elastic", "heat", "thermal"], default="elastic")
+    ap.add_argument("--workload", choices=["elastic", "heat", "thermal", "config3", "config4", "config5"],
+                    default="elastic")
     ap.add_argument("--amg-delta", type=float, default=None,
                     help="FP64 replacement threshold of the multigrid CG (default: the library's)")
     ap.add_argument("--smoother", choices=["fp16", "fp32"], default="fp16",
@@ -597,6 +728,9 @@ def main():
         _lib.load().fem_amg_set_half_smoother(1 if args.smoother == "fp16" else 0)
         if args.amg_delta is not None:
             SolveContext.AMG_DELTA = args.amg_delta
+    if args.workload.startswith("config"):
+        run_config(args)
+        return
     if args.workload == "heat":
         run_heat(args)
         return

@@ -1507,8 +1507,14 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(int64_t n_c, const int64_
 // takes a CTA per row instead of a warp.  Every sum keeps a fixed order, so results are
 // identical run to run; the arithmetic is that of the per-level kernels
 // above up to the order of partial row sums.
-constexpr int kCycT = 512;    // threads per CTA
-constexpr int kCycPerSm = 2;  // CTAs per SM at most (occupancy may allow fewer)
+#ifndef TFG_CYC_THREADS
+#define TFG_CYC_THREADS 512
+#endif
+#ifndef TFG_CYC_PER_SM
+#define TFG_CYC_PER_SM 2
+#endif
+constexpr int kCycT = TFG_CYC_THREADS;    // threads per CTA
+constexpr int kCycPerSm = TFG_CYC_PER_SM;  // CTAs per SM at most (occupancy may allow fewer)
 constexpr long long kCycSpin = 4000000000LL;  // clock cycles a barrier wait may last (about 2 s)
 
 struct CycLevel {
