@@ -352,7 +352,7 @@ def run_thermal(args):
     dm = model.device_mesh
     n_dofs = model.n_dofs
     roof, roof_plain = scalar_rooflines(lib, dm, n_dofs, (u_ms / u_n) / 1e3 if u_n else None,
-                                        (p_ums / p_un) / 1e3 if p_un else None)
+                                        (p_ums / p_un) / 1e3 if p_un else None, args.smoother)
     line = {
         "metric": THERMAL_METRIC, "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
@@ -360,6 +360,7 @@ def run_thermal(args):
         "config": {"workload": f"thermal_slab_simp N={args.thermal_n} (benchmarks/thermal.py)",
                    "dofs": n_dofs, "nnz": dm.nnz, "n_elem": model.n_elem, "stol": args.stol,
                    "preconditioner": "smoothed-aggregation multigrid (constant near-null vector)",
+                   "fp64_residual": "element pass" if args.residual == "elements" else "FP64 copy of the sliced matrix",
                    "l2": "inputs larger than L2 (FP64 gradient cache %.0f MB)"
                          % ((dm.bt.numel() + dm.detj.numel()) * 8 / 1e6)},
         "cg_iterations": iters, "gpu_launches": launches,
@@ -412,20 +413,42 @@ def heat_step(m, kappa0, q, stol, precision="mixed"):
     return T, g
 
 
-def heat_cpu_baseline(n_sample: int):
-    """The heat oracle's solve + adjoint (numpy assembly, scipy Jacobi-CG to
-    1e-10) on a smaller cube of the same kind, scaled linearly to 1M DOF."""
+def _heat_port_step(n: int):
+    """One solve + adjoint of the heat oracle on the heat cube of size n:
+    (seconds, of which CG seconds, DOF, CG iterations of both solves)."""
     from oracle import heat_oracle as H
 
-    nodes, el, kappa, x0 = (t.numpy() for t in heat_inputs(n_sample))
+    nodes, el, kappa, x0 = (t.numpy() for t in heat_inputs(n))
+    H.HeatModel.cg_iterations.clear()
+    H.HeatModel.cg_seconds.clear()
     t0 = time.perf_counter()
     om = H.HeatModel(nodes, el, kappa[:, None, None] * np.eye(3))
     om.solve(np.full(len(nodes), 1.0 / len(nodes)), x0, method="cg", rtol=1e-10)
     om.adjoint(np.ones(len(nodes)), method="cg", rtol=1e-10)
     t = time.perf_counter() - t0
-    return {"value": t / (len(nodes) / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-            "sample": f"heat oracle (numpy assembly + scipy Jacobi-CG, rtol 1e-10, solve + adjoint) on the {n_sample}^3 "
-                      f"jittered Hexa1 cube ({len(nodes)} DOF), scaled linearly to 1M DOF"}
+    return t, sum(H.HeatModel.cg_seconds), len(nodes), sum(H.HeatModel.cg_iterations)
+
+
+def heat_cpu_baseline(n_sample: int, n_target: int):
+    """The heat oracle's solve + adjoint (numpy assembly, scipy Jacobi-CG to
+    1e-10) on two cubes of the same kind, (2 n_sample / 3)^3 and n_sample^3,
+    extrapolated to the n_target^3 workload as cpu_baseline does: set-up by
+    DOF, the CG by DOF x iterations with the measured iteration growth."""
+    n_small = max(4, (2 * n_sample) // 3)
+    t_s, cg_s, dofs_s, it_s = _heat_port_step(n_small)
+    t_l, cg_l, dofs_l, it_l = _heat_port_step(n_sample)
+    alpha = math.log(it_l / it_s) / math.log(n_sample / n_small) if it_s > 0 and it_l > 0 else 1.0
+    dofs_t = (n_target + 1) ** 3
+    it_t = it_l * (n_target / n_sample) ** alpha
+    t_t = (t_l - cg_l) * (dofs_t / dofs_l) + cg_l * (dofs_t / dofs_l) * (it_t / it_l)
+    return {"value": t_t / (dofs_t / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"heat oracle (numpy assembly + scipy Jacobi-CG, rtol 1e-10, solve + adjoint) on the "
+                      f"{n_small}^3 and {n_sample}^3 jittered Hexa1 cubes ({dofs_s} and {dofs_l} DOF: {t_s:.2f} s "
+                      f"and {t_l:.2f} s, of which CG {cg_s:.2f} s and {cg_l:.2f} s over {it_s} and {it_l} "
+                      f"iterations), extrapolated to {n_target}^3 ({dofs_t} DOF): set-up by DOF, CG by DOF x "
+                      f"iterations with iterations ~ n^{alpha:.2f} ({it_t:.0f} predicted)",
+            "samples": {"n": [n_small, n_sample], "seconds": [t_s, t_l], "cg_seconds": [cg_s, cg_l],
+                        "cg_iterations": [it_s, it_l], "iteration_exponent": alpha, "predicted_seconds": t_t}}
 
 
 def timed_steps(lib, fn, steps, stream):
@@ -453,10 +476,12 @@ def timed_steps(lib, fn, steps, stream):
     return ev0.elapsed_time(ev1) / steps, iters, spmv_ms, spmv_n, launches, clocks.summary(), out
 
 
-def scalar_rooflines(lib, dm, n_dofs, mixed_unit, plain_unit):
-    """Roofline objects of the two heat paths: the level-0 FP32 SpMV of the
-    multigrid CG (4-byte value and int32 column per stored entry, x read
-    once, y written once) and one FP64 Jacobi-CG iteration of the persistent
+def scalar_rooflines(lib, dm, n_dofs, mixed_unit, plain_unit, smoother="fp16"):
+    """Roofline objects of the two heat paths: the level-0 SpMVs of the
+    multigrid CG (level0_launch_bytes: four smoothing passes on the FP16 copy,
+    2-byte value and int32 column per stored entry, and q = A p on the FP32
+    matrix, 4-byte value; x read once, y written once) and one FP64
+    Jacobi-CG iteration of the persistent
     kernel (8-byte value and int32 column per entry, int64 row pointers,
     twelve FP64 vector streams and the inverse diagonal)."""
     peak, peak_kind = measured_peak_hbm()
@@ -467,7 +492,9 @@ def scalar_rooflines(lib, dm, n_dofs, mixed_unit, plain_unit):
                 "frac": (achieved / peak) if achieved else None, "traffic": None, "algorithmic_bytes": sb,
                 "avg_unit_us": unit_s * 1e6 if unit_s else None, "peak_source": peak_kind}
 
-    mixed = obj("k_sell_op<1,*> (level-0 FP32 SpMV of the multigrid CG)", dm.n_blocks * 8 + 8 * n_dofs, mixed_unit)
+    mixed = obj("k_sell_op1<*> (level-0 scalar SpMVs of the multigrid CG: four smoothing passes on the %s, "
+                "q = A p on the FP32 matrix)" % ("FP16 copy" if smoother == "fp16" else "FP32 matrix"),
+                level0_launch_bytes(dm, smoother), mixed_unit)
     if lib.fem_get_cg_path() in (1, 2):
         plain = obj("persistent FP64 Jacobi-CG kernel (one iteration)",
                     dm.nnz * 12 + (n_dofs + 1) * 8 + 13 * 8 * n_dofs, plain_unit)
@@ -499,7 +526,7 @@ def run_heat(args):
     dm = m.device_mesh
     n_dofs = m.n_dofs
     roof, roof_plain = scalar_rooflines(lib, dm, n_dofs, (u_ms / u_n) / 1e3 if u_n else None,
-                                        (p_ums / p_un) / 1e3 if p_un else None)
+                                        (p_ums / p_un) / 1e3 if p_un else None, args.smoother)
     line = {
         "metric": HEAT_METRIC + " (FP32 multigrid CG + FP64 refinement + adjoint)",
         "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
@@ -508,6 +535,7 @@ def run_heat(args):
         "config": {"workload": f"solidheat_hexa1_cube_{args.heat_n}^3_jittered_steady_solve+adjoint",
                    "dofs": n_dofs, "nnz": dm.nnz, "n_elem": m.n_elem, "stol": args.stol,
                    "preconditioner": "smoothed-aggregation multigrid (constant near-null vector)",
+                   "fp64_residual": "element pass" if args.residual == "elements" else "FP64 copy of the sliced matrix",
                    "l2": "inputs larger than L2 (FP64 K = %.0f MB)" % (dm.nnz * 12 / 1e6)},
         "cg_iterations": iters, "gpu_launches": launches,
         "roofline": roof,
@@ -517,7 +545,7 @@ def run_heat(args):
         "rel_err_mixed_vs_fp64": {"T": float((T_m - T_p).detach().abs().max() / T_p.detach().abs().max()),
                                   "grad": float((g_m - g_p).abs().max() / g_p.abs().max())},
         "clocks": clocks,
-        "cpu_baseline": heat_cpu_baseline(args.heat_cpu_n),
+        "cpu_baseline": heat_cpu_baseline(args.heat_cpu_n, args.heat_n),
     }
     print(json.dumps(line))
 
@@ -713,6 +741,9 @@ def main():
                     help="FP64 replacement threshold of the multigrid CG (default: the library's)")
     ap.add_argument("--smoother", choices=["fp16", "fp32"], default="fp16",
                     help="level-0 smoothing passes of the multigrid V-cycle: FP16 copy or the FP32 matrix")
+    ap.add_argument("--residual", choices=["auto", "copy", "elements"], default="auto",
+                    help="FP64 residual of the mixed solvers: FP64 copy of the sliced matrix, the element pass, "
+                         "or the library's choice (the copy for heat, the element pass for vector fields)")
     ap.add_argument("--thermal-n", type=int, default=1024, help="N of the thermal slab (N x N/2 x 1 elements)")
     ap.add_argument("--heat-n", type=int, default=100, help="elements per cube edge of the heat workload")
     ap.add_argument("--heat-cpu-n", type=int, default=30, help="cube size of the heat CPU baseline sample")
@@ -725,7 +756,10 @@ def main():
         from torchfem_gb300 import _lib
         from torchfem_gb300.sparse import SolveContext
 
+        from torchfem_gb300._device import LinearSystem
+
         _lib.load().fem_amg_set_half_smoother(1 if args.smoother == "fp16" else 0)
+        LinearSystem.RESIDUAL_COPY = {"auto": None, "copy": True, "elements": False}[args.residual]
         if args.amg_delta is not None:
             SolveContext.AMG_DELTA = args.amg_delta
     if args.workload.startswith("config"):
@@ -903,6 +937,8 @@ def main():
             "config": {"workload": f"hexa1_cube_{args.n}^3_jittered_linear_elastic_solve+adjoint",
                        "preconditioner": "smoothed-aggregation multigrid" if pc == "amg" else "block Jacobi",
                        "level0_smoothing": args.smoother if pc == "amg" else None,
+                       "fp64_residual": "FP64 copy of the sliced matrix" if args.residual == "copy"
+                       else "element pass",
                        "dofs": n_dofs, "nnz": dm.nnz, "n_elem": n_elem, "stol": args.stol,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (FP32 K = %.0f MB)" % (dm.n_blocks * 40 / 1e6)},

@@ -366,6 +366,15 @@ int fem_assemble_sell(const fem_blocks* blocks, int ke_dtype, const void* ke,
                       const uint8_t* con_mask, const int64_t* sell_base, int64_t n_slots,
                       float* sval, void* stream);
 
+/* Both copies of the sliced matrix in one pass over FP64 element matrices:
+ * sval the FP32 values (each slot's FP64 sum rounded once) and sval64 the
+ * FP64 values [n_slots * dim^2] in the same layout.  sval64 serves the
+ * mixed solvers' FP64 residual replacements (fem_operator64.sell_val64).
+ * No counterpart in the reference, whose solves use one FP64 matrix. */
+int fem_assemble_sell_pair(const fem_blocks* blocks, const double* ke, const uint8_t* con_mask,
+                           const int64_t* sell_base, int64_t n_slots, float* sval, double* sval64,
+                           void* stream);
+
 /* Jacobi: inv_diag[r] = 1 / val[diag_map[r]] (sparse.py:406-407). */
 int fem_jacobi(const double* val, const int64_t* diag_map, int64_t n, double* inv_diag,
                int32_t* status, void* stream);
@@ -463,16 +472,30 @@ int fem_pcg_static(const fem_matrix* A, const double* b, double* x, double rtol,
 
 /* FP64 matrix-free operator y = A x of the condensed system: the element
  * kernels apply K to x with constrained entries zeroed, and y = x at
- * constrained DOFs (the matrix assemble_matrix builds, base.py:410-419). */
+ * constrained DOFs (the matrix assemble_matrix builds, base.py:410-419).
+ * sell_val64 (nullable) holds the FP64 values of the same condensed matrix
+ * in the sliced layout of the FP32 matrix passed beside the operator
+ * (fem_assemble_sell_pair); when set, fem_pcg_mixed and fem_amg_pcg compute
+ * their FP64 residuals as one FP64 sliced SpMV over it instead of the
+ * element pass.  fem_apply64 always runs the element pass. */
 typedef struct fem_operator64 {
   const fem_mesh* mesh;
   const fem_material* mat;
-  const uint8_t* con_mask; /* [n_nod*dim] */
+  const uint8_t* con_mask;   /* [n_nod*dim] */
+  const double* sell_val64;  /* [n_slots*dim*dim] or NULL */
 } fem_operator64;
 
 size_t fem_apply64_workspace_bytes(const fem_operator64* op);
 int fem_apply64(const fem_operator64* op, const double* x, double* y, void* ws, size_t ws_bytes,
                 void* stream);
+
+/* y = A x in FP64 over the FP64 copy of a sliced matrix
+ * (fem_assemble_sell_pair), with the layout of the FP32 sliced
+ * matrix A32 (row_ptr = sell_base, col, block): the FP64 residual of the
+ * mixed solvers.  Equals fem_apply64 on the same condensed system up to
+ * summation order. */
+int fem_sell_apply64(const fem_matrix* A32, const double* sval64, const double* x, double* y,
+                     void* stream);
 
 size_t fem_pcg_mixed_workspace_bytes(const fem_matrix* A32, const fem_operator64* op);
 

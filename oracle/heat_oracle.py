@@ -24,6 +24,7 @@ Restated reference code (paths relative to the torch-fem repository):
 from __future__ import annotations
 
 import math
+import time
 
 import numpy as np
 import scipy.sparse as sp
@@ -97,14 +98,25 @@ class HeatModel:
         f, flux, g = self.integrate(T, flux_prev)
         return assemble_rhs(f, self.idx, self.n_nod), flux, g
 
+    cg_iterations: list = []  # iterations of every Jacobi-CG solve (appended per solve)
+    cg_seconds: list = []  # wall time of every Jacobi-CG solve
+
     @staticmethod
     def linear_solve(K, b, method="spsolve", rtol=1e-12):
         """spsolve, or Jacobi-preconditioned CG to ||r|| <= rtol ||b||."""
         if method == "spsolve":
             return spla.spsolve(K.tocsc(), b)
         dinv = 1.0 / K.diagonal()
+        count = [0]
+
+        def tick(_):
+            count[0] += 1
+
+        t0 = time.perf_counter()
         x, info = spla.cg(K.tocsr(), b, rtol=rtol, atol=0.0, maxiter=10 * K.shape[0],
-                          M=spla.LinearOperator(K.shape, matvec=lambda v: dinv * v))
+                          M=spla.LinearOperator(K.shape, matvec=lambda v: dinv * v), callback=tick)
+        HeatModel.cg_seconds.append(time.perf_counter() - t0)
+        HeatModel.cg_iterations.append(count[0])
         if info != 0:
             raise RuntimeError(f"CG did not converge ({info})")
         return x

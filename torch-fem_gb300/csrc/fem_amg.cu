@@ -44,6 +44,7 @@ int etype_info(int etype, int* ne, int* d, int* nip);
 extern int g_timing;  // fem_set_timing
 int g_amg_half = 1;   // FP16 smoothing copy of the level-0 matrix (fem_amg_set_half_smoother)
 int g_amg_fused = 1;  // coarse levels as one cooperative launch per V-cycle (fem_amg_set_fused_cycle)
+int sell_apply64(const fem_matrix* A32, const double* sval64, const double* x, double* y, cudaStream_t st);
 size_t scan_workspace_bytes(int64_t n);
 int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
 
@@ -1134,24 +1135,9 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   float y[D];
 #pragma unroll
   for (int c = 0; c < D; ++c) y[c] = 0.f;
-  int k0 = w;
-  if constexpr (D == 1) {
-    // one value per slot: eight slots' loads in flight per thread before the
-    // gathers (same summation order as the loop below)
-    for (; k0 + 7 * kSellW < len; k0 += 8 * kSellW) {
-      int64_t cc[8];
-      float mv[8][1];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        cc[u] = ld_l2(cp + (int64_t)(k0 + u * kSellW) * 32, pol);
-        load_slot<1, H>(vp, hp, k0 + u * kSellW, lane, pol, mv[u]);
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) y[0] = fmaf(mv[u][0], v[cc[u]], y[0]);
-    }
-  }
+  static_assert(D > 1, "scalar rows use k_sell_op1");
 #pragma unroll 2
-  for (int k = k0; k < len; k += kSellW) {
+  for (int k = w; k < len; k += kSellW) {
     const int64_t cc = ld_l2(cp + (int64_t)k * 32, pol);
     float m[DD];
     load_slot<DD, H>(vp, hp, k, lane, pol, m);
@@ -1190,6 +1176,119 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
       if (lane == 0) a.partial[blockIdx.x] = t;
     }
   }
+}
+
+// Level 0 of a scalar field (heat): a slot holds one 4-byte value, so a
+// 32-row slice is only a few KB and the shared-slot CTA of k_sell_op spends
+// more on its CTA and its shared-memory sum than on streaming.  Here each warp
+// owns one slice (kSell1W slices per CTA), each thread its row, and a thread
+// walks all of the row's slots in batches of kSell1U: the next batch's
+// column and value loads are issued before the current batch's gathers, so
+// the matrix stream never waits on the vector gathers.  No shared memory, no
+// barrier; the slots are summed in order.  Per-slice dot shares as in
+// k_sell_op, so k_dot_finish is the same.
+constexpr int kSell1W = 4;
+#ifndef TFG_SELL1_U
+#define TFG_SELL1_U 8
+#endif
+constexpr int kSell1U = TFG_SELL1_U;
+
+// Columns and values of slots k .. k + kSell1U - 1 of this thread's row (the
+// slots at or past len are not read and contribute 0 at column 0).
+template <bool H>
+__device__ __forceinline__ void sell1_batch(const int32_t* __restrict__ cp, const float* __restrict__ vp,
+                                            const __half* __restrict__ hp, int k, int len, int lane,
+                                            uint64_t pol, int32_t (&c)[kSell1U], float (&m)[kSell1U]) {
+#pragma unroll
+  for (int u = 0; u < kSell1U; ++u) {
+    c[u] = 0;
+    m[u] = 0.f;
+    if (k + u < len) {
+      float t[1];
+      c[u] = ld_l2(cp + (int64_t)(k + u) * 32, pol);
+      load_slot<1, H>(vp, hp, k + u, lane, pol, t);
+      m[u] = t[0];
+    }
+  }
+}
+
+template <int MODE, bool H>
+__global__ void __launch_bounds__(kSell1W * 32) k_sell_op1(int64_t n_rows, int64_t n_slices,
+                                                           const int64_t* __restrict__ sell_base,
+                                                           const int32_t* __restrict__ col,
+                                                           const float* __restrict__ sval, OpArgs a) {
+  if (amg_idle(a.ctrl)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t s = (int64_t)blockIdx.x * kSell1W + (threadIdx.x >> 5);
+  if (s >= n_slices) return;
+  const float* __restrict__ v = op_operand<MODE>(a);
+  const uint64_t pol = l2_policy(false);
+  const int64_t b0 = sell_base[s];
+  const int len = (int)((sell_base[s + 1] - b0) >> 5);
+  const int32_t* cp = col + b0 + lane;
+  const float* vp = sval + b0 + lane;
+  const __half* hp = H ? a.sv16 + b0 : nullptr;
+  float y = 0.f;
+#if defined(TFG_SELL1_PIPE) && TFG_SELL1_PIPE == 0
+  int k = 0;
+  for (; k + 8 <= len; k += 8) {
+    int32_t cc[8];
+    float mv[8][1];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      cc[u] = ld_l2(cp + (int64_t)(k + u) * 32, pol);
+      load_slot<1, H>(vp, hp, k + u, lane, pol, mv[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) y = fmaf(mv[u][0], v[cc[u]], y);
+  }
+  for (; k < len; ++k) {
+    const int32_t cc = ld_l2(cp + (int64_t)k * 32, pol);
+    float m[1];
+    load_slot<1, H>(vp, hp, k, lane, pol, m);
+    y = fmaf(m[0], v[cc], y);
+  }
+#else
+  int32_t cc[kSell1U];
+  float mv[kSell1U];
+  sell1_batch<H>(cp, vp, hp, 0, len, lane, pol, cc, mv);
+  for (int k = 0; k < len; k += kSell1U) {
+    int32_t cn[kSell1U];
+    float mn[kSell1U];
+    sell1_batch<H>(cp, vp, hp, k + kSell1U, len, lane, pol, cn, mn);
+#pragma unroll
+    for (int u = 0; u < kSell1U; ++u)
+      if (k + u < len) y = fmaf(mv[u], v[cc[u]], y);
+#pragma unroll
+    for (int u = 0; u < kSell1U; ++u) {
+      cc[u] = cn[u];
+      mv[u] = mn[u];
+    }
+  }
+#endif
+  double dot = 0.0;
+  const int64_t i = s * 32 + lane;
+  if (i < n_rows) {
+    const float yt[1] = {H ? y * *a.s16inv : y};  // a power of two: exact
+    dot = op_epilogue<1, MODE>(a, i, yt);
+  }
+  if constexpr (op_has_dot<MODE>()) {
+    const double t = warp_sum(dot);
+    if (lane == 0) a.partial[s] = t;
+  }
+}
+
+// One level-0 pass: the shared-slot kernel for 2×2 / 3×3 blocks, the
+// warp-per-slice kernel for scalar rows.
+template <int D, int MODE, bool H>
+void launch_sell(int64_t n, const int64_t* sell_base, const int32_t* sell_col, const float* sell_val,
+                 const OpArgs& a, cudaStream_t st) {
+  const int64_t ns = (n + 31) / 32;
+  if constexpr (D == 1)
+    k_sell_op1<MODE, H><<<(unsigned)((ns + kSell1W - 1) / kSell1W), kSell1W * 32, 0, st>>>(n, ns, sell_base, sell_col,
+                                                                                          sell_val, a);
+  else
+    k_sell_op<D, MODE, H><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, sell_base, sell_col, sell_val, a);
 }
 
 // The dot product of a level-0 pass that ends in one: the per-slice shares
@@ -2772,10 +2871,9 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
     const bool timed = h->ev_ready && h->ev_used < fem_amg::kTimed;
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used], st);
     if (op_smoothing<MODE>() && h->sv16 && g_amg_half)
-      k_sell_op<B0, MODE, true><<<(unsigned)ns, kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val, a);
+      launch_sell<B0, MODE, true>(L.n, h->sell_base, h->sell_col, h->sell_val, a, st);
     else
-      k_sell_op<B0, MODE, false><<<(unsigned)ns, kSellW * 32, 0, st>>>(L.n, h->sell_base, h->sell_col, h->sell_val,
-                                                                        a);
+      launch_sell<B0, MODE, false>(L.n, h->sell_base, h->sell_col, h->sell_val, a, st);
     if constexpr (op_has_dot<MODE>()) {
       k_dot_finish<MODE><<<1, 1024, 0, st>>>(ns, a);
       note_launch();
@@ -2809,8 +2907,7 @@ int lanczos_level(fem_amg* h, int l, cudaStream_t st, double* rho) {
     if constexpr (B <= 3) {  // level 0 (B = dim) holds the sliced matrix
       if (l == 0) {
         const int64_t ns = (n + 31) / 32;
-        k_sell_op<B, kOpLzQ, false><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, h->sell_base, h->sell_col, h->sell_val,
-                                                                           a);
+        launch_sell<B, kOpLzQ, false>(n, h->sell_base, h->sell_col, h->sell_val, a, st);
         note_launch();
         k_dot_finish<kOpLzQ><<<1, 1024, 0, st>>>(ns, a);
         sliced = true;
@@ -3093,8 +3190,8 @@ int64_t op_fe_len(const fem_operator64* op) {
 }
 
 template <int B0, int K>
-int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, double rtol, double delta,
-             int64_t max_iter, void* ws, fem_solve_info* info, cudaStream_t st) {
+int pcg_impl(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const double* b, double* x, double rtol,
+             double delta, int64_t max_iter, void* ws, fem_solve_info* info, cudaStream_t st) {
   const int64_t nn = h->L[0].n, n = nn * B0;
   AmgCtrl c;
   memset(&c, 0, sizeof(c));
@@ -3140,10 +3237,13 @@ int pcg_impl(fem_amg* h, const fem_operator64* op, const double* b, double* x, d
     if (c.replace) {
       k_cg_fold<<<grid_for(n, kT), kT, 0, st>>>(n, x, h->xlo, h->ctrl);
       note_launch();
-      rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, fe, nullptr, nullptr,
-                             nullptr, st);
-      if (rc) return rc;
-      rc = fem_gather_nodal(op->mesh, fe, nullptr, op->con_mask, 2, x, y64, nullptr, nullptr, 0, st);
+      if (op->sell_val64) {  // one FP64 sliced SpMV over the FP64 copy of the matrix
+        rc = sell_apply64(A, op->sell_val64, x, y64, st);
+      } else {  // the FP64 element pass
+        rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, fe, nullptr,
+                               nullptr, nullptr, st);
+        if (!rc) rc = fem_gather_nodal(op->mesh, fe, nullptr, op->con_mask, 2, x, y64, nullptr, nullptr, 0, st);
+      }
       if (rc) return rc;
       k_cg_replace<B0><<<gv, kT, 0, st>>>(nn, b, y64, h->rcg, h->dinv0, h->L[0].theta_inv, h->L[0].d, h->L[0].x,
                                           h->partial, h->ctrl);
@@ -3299,9 +3399,9 @@ int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const
     return FEM_INVALID;
   }
   cudaStream_t st = as_stream(stream);
-  if (h->dim == 3) return pcg_impl<3, 6>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
-  if (h->dim == 2) return pcg_impl<2, 3>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
-  return pcg_impl<1, 1>(h, op, b, x, rtol, delta, max_iter, ws, info, st);
+  if (h->dim == 3) return pcg_impl<3, 6>(h, A, op, b, x, rtol, delta, max_iter, ws, info, st);
+  if (h->dim == 2) return pcg_impl<2, 3>(h, A, op, b, x, rtol, delta, max_iter, ws, info, st);
+  return pcg_impl<1, 1>(h, A, op, b, x, rtol, delta, max_iter, ws, info, st);
 }
 
 void fem_amg_set_half_smoother(int enable) { g_amg_half = enable ? 1 : 0; }

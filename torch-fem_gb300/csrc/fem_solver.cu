@@ -40,7 +40,7 @@ __global__ void k_assemble(int n_e, int D, int64_t n_blocks, const int64_t* __re
                            const int64_t* __restrict__ inc_ptr, const KT* __restrict__ ke,
                            const int64_t* __restrict__ row_ptr, const uint8_t* __restrict__ con,
                            double* __restrict__ val, const int64_t* __restrict__ sell_base,
-                           float* __restrict__ sval) {
+                           float* __restrict__ sval, double* __restrict__ sval64 = nullptr) {
   const int64_t blk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (blk >= n_blocks) return;
   const int64_t a = blk_row[blk];
@@ -71,12 +71,100 @@ __global__ void k_assemble(int n_e, int D, int64_t n_blocks, const int64_t* __re
       if (rc || con[cdof]) v = 0.0;
       if (r == cdof && rc) v = 1.0;
       if (kSELL) {
-        sval[sell_index(sell_base, a, k, i * D + j, D * D)] = (float)v;
+        const int64_t at = sell_index(sell_base, a, k, i * D + j, D * D);
+        sval[at] = (float)v;
+        if (sval64) sval64[at] = v;
       } else {
         if (orphan) {
           if (i == j) val[row_ptr[r]] = v;
         } else {
           val[row_ptr[r] + k * D + j] = v;
+        }
+      }
+    }
+  }
+}
+
+// FP64 y = A x over the FP64 copy of the sliced matrix (fem_assemble_sell_pair):
+// the mixed solvers' residual replacement.  The copy is the condensed matrix
+// itself (identity rows and columns at constrained DOFs), so y equals the
+// element pass with constrained entries zeroed and y = x there.  Blocks of
+// 2x2 / 3x3: one slice per CTA, kApplyW warps sharing its slots, partial rows
+// summed in shared memory in a fixed order; scalar rows: a warp per slice,
+// a thread per row, four slots' loads in flight.  Bound by the FP64 pipe
+// (one FMA per stored value) more than by the 8-byte values.
+constexpr int kApplyW = 4;
+
+template <int D>
+__global__ void __launch_bounds__(kApplyW * 32) k_sell_apply64(int64_t n_rows, int64_t n_slices,
+                                                               const int64_t* __restrict__ sell_base,
+                                                               const int32_t* __restrict__ col,
+                                                               const double* __restrict__ sval,
+                                                               const double* __restrict__ x,
+                                                               double* __restrict__ y) {
+  constexpr int DD = D * D;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t pol = l2_policy(false);
+  if constexpr (D == 1) {
+    const int64_t s = (int64_t)blockIdx.x * kApplyW + w;
+    if (s >= n_slices) return;
+    const int64_t b0 = sell_base[s];
+    const int len = (int)((sell_base[s + 1] - b0) >> 5);
+    const int32_t* cp = col + b0 + lane;
+    const double* vp = sval + b0 + lane;
+    double acc = 0.0;
+    int k = 0;
+    for (; k + 4 <= len; k += 4) {
+      int32_t cc[4];
+      double mv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        cc[u] = ld_l2(cp + (int64_t)(k + u) * 32, pol);
+        mv[u] = ld_l2(vp + (int64_t)(k + u) * 32, pol);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc = fma(mv[u], x[cc[u]], acc);
+    }
+    for (; k < len; ++k) acc = fma(ld_l2(vp + (int64_t)k * 32, pol), x[ld_l2(cp + (int64_t)k * 32, pol)], acc);
+    const int64_t i = s * 32 + lane;
+    if (i < n_rows) y[i] = acc;
+  } else {
+    __shared__ double ys[kApplyW][D][32];
+    const int64_t s = blockIdx.x;
+    const int64_t b0 = sell_base[s];
+    const int len = (int)((sell_base[s + 1] - b0) >> 5);
+    const int32_t* cp = col + b0 + lane;
+    const double* vp = sval + b0 * DD + lane;
+    double acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = 0.0;
+#pragma unroll 2
+    for (int k = w; k < len; k += kApplyW) {
+      const int64_t cc = ld_l2(cp + (int64_t)k * 32, pol);
+      const double* vk = vp + (int64_t)k * DD * 32;
+      double m[DD];
+#pragma unroll
+      for (int e = 0; e < DD; ++e) m[e] = ld_l2(vk + e * 32, pol);
+      double xv[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) xv[j] = x[cc * D + j];
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int j = 0; j < D; ++j) acc[r] = fma(m[r * D + j], xv[j], acc[r]);
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) ys[w][c][lane] = acc[c];
+    __syncthreads();
+    if (w == 0) {
+      const int64_t i = s * 32 + lane;
+      if (i < n_rows) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          double t = ys[0][c][lane];
+#pragma unroll
+          for (int u = 1; u < kApplyW; ++u) t += ys[u][c][lane];
+          y[i * D + c] = t;
         }
       }
     }
@@ -1824,6 +1912,31 @@ static int run_pcg(const fem_matrix* A, const double* b, double* x, double rtol,
   return status_of(h.done);
 }
 
+// y = A x in FP64 over the FP64 copy of the sliced matrix A32 describes
+// (A32->n_rows block rows of A32->block DOFs).
+int sell_apply64(const fem_matrix* A32, const double* sval64, const double* x, double* y, cudaStream_t st) {
+  const int64_t nr = A32->n_rows;
+  const int64_t ns = (nr + 31) / 32;
+  if (ns == 0) return FEM_OK;
+  switch (A32->block) {
+    case 1:
+      k_sell_apply64<1><<<(unsigned)((ns + kApplyW - 1) / kApplyW), kApplyW * 32, 0, st>>>(
+          nr, ns, A32->row_ptr, A32->col, sval64, x, y);
+      break;
+    case 2:
+      k_sell_apply64<2><<<(unsigned)ns, kApplyW * 32, 0, st>>>(nr, ns, A32->row_ptr, A32->col, sval64, x, y);
+      break;
+    case 3:
+      k_sell_apply64<3><<<(unsigned)ns, kApplyW * 32, 0, st>>>(nr, ns, A32->row_ptr, A32->col, sval64, x, y);
+      break;
+    default:
+      set_last_error("FP64 sliced apply: block size %d", A32->block);
+      return FEM_INVALID;
+  }
+  ::tfg::note_launch();
+  return check_cuda("FP64 sliced apply");
+}
+
 }  // namespace tfg
 
 using namespace tfg;
@@ -1924,6 +2037,37 @@ int fem_assemble_sell(const fem_blocks* B, int ke_dtype, const void* ke, const u
         B->inc_ptr, (const float*)ke, nullptr, con_mask, nullptr, sell_base, sval);
   ::tfg::note_launch();
   return check_cuda("fem_assemble_sell");
+}
+
+int fem_assemble_sell_pair(const fem_blocks* B, const double* ke, const uint8_t* con_mask,
+                           const int64_t* sell_base, int64_t n_slots, float* sval, double* sval64,
+                           void* stream) {
+  cudaStream_t st = as_stream(stream);
+  if (B->dim < 1 || B->dim > 3) {
+    set_last_error("fem_assemble_sell_pair: dim must be 1..3");
+    return FEM_INVALID;
+  }
+  if (!sval || !sval64) {
+    set_last_error("fem_assemble_sell_pair: sval and sval64 are required");
+    return FEM_INVALID;
+  }
+  const size_t nv = (size_t)n_slots * B->dim * B->dim;
+  cudaMemsetAsync(sval, 0, sizeof(float) * nv, st);
+  cudaMemsetAsync(sval64, 0, sizeof(double) * nv, st);
+  if (B->n_blocks == 0) return check_cuda("fem_assemble_sell_pair");
+  k_assemble<double, double, true><<<grid_for(B->n_blocks, 128), 128, 0, st>>>(
+      B->n_e, B->dim, B->n_blocks, B->nbr_ptr, B->nbr, B->blk_ptr, B->contrib, B->blk_row, B->inc_ptr, ke,
+      nullptr, con_mask, nullptr, sell_base, sval, sval64);
+  ::tfg::note_launch();
+  return check_cuda("fem_assemble_sell_pair");
+}
+
+int fem_sell_apply64(const fem_matrix* A32, const double* sval64, const double* x, double* y, void* stream) {
+  if (!A32 || A32->format != FEM_FMT_SELL_F32 || !sval64) {
+    set_last_error("fem_sell_apply64: needs the FP32 sliced matrix's layout and its FP64 copy");
+    return FEM_INVALID;
+  }
+  return sell_apply64(A32, sval64, x, y, as_stream(stream));
 }
 
 int fem_jacobi(const double* val, const int64_t* diag_map, int64_t n, double* inv_diag,
@@ -2054,11 +2198,15 @@ int fem_pcg_mixed(const fem_matrix* A, const fem_operator64* op, const double* b
       // FP64 reliable update: x += x_lo; r = b - A x (matrix-free FP64).
       k_fold<<<grid_for(A->n, kThreads), kThreads, 0, st>>>(A->n, x, xl, v.ctrl);
       ::tfg::note_launch();
-      rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, v.fe,
-                             nullptr, nullptr, nullptr, stream);
-      if (rc) return rc;
-      rc = fem_gather_nodal(op->mesh, v.fe, nullptr, op->con_mask, 2, x, v.y64, nullptr, nullptr, 0,
-                            stream);
+      if (op->sell_val64) {
+        rc = sell_apply64(A, op->sell_val64, x, v.y64, st);
+      } else {
+        rc = fem_element_force(op->mesh, op->mat, x, op->con_mask, nullptr, 2, nullptr, nullptr, v.fe,
+                               nullptr, nullptr, nullptr, stream);
+        if (!rc)
+          rc = fem_gather_nodal(op->mesh, v.fe, nullptr, op->con_mask, 2, x, v.y64, nullptr, nullptr, 0,
+                                stream);
+      }
       if (rc) return rc;
       if (G == 2)
         k_replace<2><<<grid_for(ng, kThreads), kThreads, 0, st>>>(ng, b, v.y64, r, z, A->precond,

@@ -42,9 +42,27 @@ class LinearSystem:
     precision "fp64": scalar CSR in the reference pattern, FP64 values,
     Jacobi preconditioner (the CuPy branch of sparse.py:406-421).
     precision "mixed": FP32 block-CSR over the node graph, FP32 block-Jacobi
-    or smoothed-aggregation multigrid (`amg`), with FP64 matrix-free
-    residual replacement.
+    or smoothed-aggregation multigrid (`amg`), with FP64 residual
+    replacement: one FP64 SpMV over an FP64 copy of the same sliced matrix,
+    or the matrix-free FP64 element pass (`RESIDUAL_COPY`).
     """
+
+    # The mixed solvers' FP64 residual.  True keeps an FP64 copy of the sliced
+    # matrix (8 bytes per stored value more), built from FP64 element
+    # matrices, and applies it with one FP64 SpMV: about a sixth of the FP64
+    # work of the element pass per replacement.  False recomputes K x from
+    # the element geometry on every replacement.  None (the default) takes
+    # the copy where the element matrices are integrated in FP64 anyway (heat
+    # conduction, one DOF per node), and the element pass for vector fields,
+    # whose FP32 element matrices are integrated in FP32: integrating them in
+    # FP64 costs more FP64 work than the replacements of a solve save.
+    RESIDUAL_COPY: bool | None = None
+
+    @staticmethod
+    def residual_copy(dm: "DeviceMesh") -> bool:
+        if LinearSystem.RESIDUAL_COPY is None:
+            return dm.heat
+        return bool(LinearSystem.RESIDUAL_COPY)
 
     _tokens = 0
 
@@ -53,6 +71,7 @@ class LinearSystem:
         self.precision = precision
         self.val: Tensor | None = None
         self.bval: Tensor | None = None
+        self.bval64: Tensor | None = None
         self.precond: Tensor | None = None
         self.matrix = _lib.FemMatrix()
         self.ws: Tensor | None = None
@@ -403,6 +422,22 @@ class DeviceMesh:
         )
         return sval
 
+    def assemble_sell_pair(self, ke: Tensor, con_mask: Tensor) -> tuple[Tensor, Tensor]:
+        """FP32 and FP64 copies of the sliced matrix from FP64 element
+        matrices, in one pass."""
+        base, _, n_slots = self.sell()
+        nv = max(n_slots, 1) * self.d * self.d
+        sval = self._empty(nv, torch.float32)
+        sval64 = self._empty(nv, torch.float64)
+        check(
+            self.lib.fem_assemble_sell_pair(
+                C.byref(self.blocks), ptr(ke), ptr(con_mask), ptr(base), n_slots, ptr(sval), ptr(sval64),
+                self.stream,
+            ),
+            "fem_assemble_sell_pair",
+        )
+        return sval, sval64
+
     def amg_hierarchy(self, con_mask: Tensor) -> AmgHierarchy:
         """The multigrid hierarchy of this mesh for the constraint mask (built
         once per mask: it depends on the mesh and the constraints only)."""
@@ -426,8 +461,12 @@ class DeviceMesh:
             del ke
             ws_bytes = self._set_csr(sysm, val)
         elif precision == "mixed":
-            ke = self.element_stiffness(mesh, mat, torch.float32)
-            sysm.bval = self.assemble_sell(ke, con_mask)
+            if LinearSystem.residual_copy(self):
+                ke = self.element_stiffness(mesh, mat, torch.float64)
+                sysm.bval, sysm.bval64 = self.assemble_sell_pair(ke, con_mask)
+            else:
+                ke = self.element_stiffness(mesh, mat, torch.float32)
+                sysm.bval = self.assemble_sell(ke, con_mask)
             del ke
             base, col, _ = self.sell()
             sysm.precond = self._empty(self.n_nod * self.d * self.d, torch.float32)
@@ -442,7 +481,7 @@ class DeviceMesh:
             )
             sysm.op_mesh = mesh
             sysm.op_mat = mat
-            sysm.op = _lib.FemOperator64(C.pointer(mesh), C.pointer(mat), ptr(con_mask))
+            sysm.op = _lib.FemOperator64(C.pointer(mesh), C.pointer(mat), ptr(con_mask), ptr(sysm.bval64))
             ws_bytes = L.fem_pcg_mixed_workspace_bytes(C.byref(sysm.matrix), C.byref(sysm.op))
             if precond == "amg":
                 sysm.amg = self.amg_hierarchy(con_mask)

@@ -116,6 +116,7 @@ class FemOperator64(C.Structure):
         ("mesh", C.POINTER(FemMesh)),
         ("mat", C.POINTER(FemMaterial)),
         ("con_mask", vp),
+        ("sell_val64", vp),
     ]
 
 
@@ -233,6 +234,8 @@ _SIGNATURES = {
     "fem_sell_layout": (C.c_int, [_P(FemBlocks), vp, _P(i64), vp, C.c_size_t, vp]),
     "fem_sell_columns": (C.c_int, [_P(FemBlocks), vp, vp, vp]),
     "fem_assemble_sell": (C.c_int, [_P(FemBlocks), C.c_int, vp, vp, vp, i64, vp, vp]),
+    "fem_assemble_sell_pair": (C.c_int, [_P(FemBlocks), vp, vp, vp, i64, vp, vp, vp]),
+    "fem_sell_apply64": (C.c_int, [_P(FemMatrix), vp, vp, vp, vp]),
     "fem_jacobi": (C.c_int, [vp, vp, i64, vp, vp, vp]),
     "fem_block_jacobi": (C.c_int, [_P(FemBlocks), vp, vp, vp, vp, vp]),
     "fem_set_timing": (None, [C.c_int]),
