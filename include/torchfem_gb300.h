@@ -179,6 +179,15 @@ int fem_geometry(const fem_mesh* mesh, const double* dndxi, double* bt, double* 
 int fem_element_stiffness(const fem_mesh* mesh, const fem_material* mat, int out_dtype,
                           void* ke, int32_t* status, void* stream);
 
+/* The same FP64 element matrices for an isotropic material (FEM_MAT_ISO),
+ * regrouped as K_ab = lambda M + G M^T + G tr(M) I with the moments
+ * M = sum_ip w detJ t g_a g_b^T, one thread per node pair a <= b: the FP64
+ * element matrices of the mixed solvers' FP64 matrix copy
+ * (fem_assemble_sell_pair).  Equal to fem_element_stiffness(FEM_F64) up to
+ * summation order; no counterpart in the reference. */
+int fem_element_stiffness_iso64(const fem_mesh* mesh, const fem_material* mat, double* ke,
+                                int32_t* status, void* stream);
+
 /* Element internal forces f_e = sum_ip w detJ t B^T sigma with the linear
  * stress update sigma = sigma_prev + C:(sym grad v - de0) (base.py:1050-1083,
  * elasticity.py:119-127).  con_mode: 0 use v as is, 1 replace v at

@@ -142,11 +142,39 @@ def test_fp64_copy_solution_against_oracle(cuda, residual_copy):
 
 def test_default_residual_choice(cuda, residual_copy):
     """By default the FP64 copy serves heat conduction (element matrices
-    integrated in FP64 anyway) and the element pass serves vector fields."""
+    integrated in FP64 anyway) and isotropic elasticity (the moment form);
+    per-point tangents keep the element pass."""
     LinearSystem.RESIDUAL_COPY = None
     h = _heat_cube()
     h.solve(stol=1e-12, precision="mixed")
     assert h.last_solve.system.bval64 is not None
     m = _planar()
     m.solve(stol=1e-12, precision="mixed", preconditioner="amg")
-    assert m.last_solve.system.bval64 is None
+    assert m.last_solve.system.bval64 is not None
+    dm = m.device_mesh
+    tangent = _lib.FemMaterial(_lib.FEM_MAT_TANGENT_IP, 0)
+    assert not LinearSystem.residual_copy(dm, tangent)
+
+
+def _iso_models():
+    nodes, el = mesh.cube_tetra(4, 3, 3)
+    nodes2, el2 = mesh.linear_to_quadratic(nodes, el)
+    tet2 = Solid(nodes2, el2, IsotropicElasticity3D(210.0, 0.25))
+    return {"hexa1": _elastic_cube(), "quad1": _planar(), "tetra2": tet2}
+
+
+def test_iso64_element_matrices_equal_fp64_stiffness(cuda):
+    """fem_element_stiffness_iso64 (moment form, a thread per node pair)
+    equals fem_element_stiffness in FP64 up to summation order, with a
+    per-element thickness on the planar mesh."""
+    for name, m in _iso_models().items():
+        if name == "quad1":
+            m.thickness = 0.5 + torch.rand(len(m.elements), generator=torch.Generator().manual_seed(5),
+                                           dtype=torch.float64)
+        dm = m.device_mesh
+        mesh_, mat, _refs = m._device_material()
+        k64 = dm.element_stiffness(mesh_, mat, torch.float64)
+        kiso = dm.element_stiffness_iso64(mesh_, mat)
+        torch.cuda.synchronize()
+        assert rel(kiso, k64) <= 1e-13, name
+        assert torch.equal(kiso, kiso.transpose(1, 2)), name

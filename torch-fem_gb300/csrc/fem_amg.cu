@@ -1188,10 +1188,7 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
 // barrier; the slots are summed in order.  Per-slice dot shares as in
 // k_sell_op, so k_dot_finish is the same.
 constexpr int kSell1W = 4;
-#ifndef TFG_SELL1_U
-#define TFG_SELL1_U 8
-#endif
-constexpr int kSell1U = TFG_SELL1_U;
+constexpr int kSell1U = 4;
 
 // Columns and values of slots k .. k + kSell1U - 1 of this thread's row (the
 // slots at or past len are not read and contribute 0 at column 0).
@@ -1229,26 +1226,6 @@ __global__ void __launch_bounds__(kSell1W * 32) k_sell_op1(int64_t n_rows, int64
   const float* vp = sval + b0 + lane;
   const __half* hp = H ? a.sv16 + b0 : nullptr;
   float y = 0.f;
-#if defined(TFG_SELL1_PIPE) && TFG_SELL1_PIPE == 0
-  int k = 0;
-  for (; k + 8 <= len; k += 8) {
-    int32_t cc[8];
-    float mv[8][1];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      cc[u] = ld_l2(cp + (int64_t)(k + u) * 32, pol);
-      load_slot<1, H>(vp, hp, k + u, lane, pol, mv[u]);
-    }
-#pragma unroll
-    for (int u = 0; u < 8; ++u) y = fmaf(mv[u][0], v[cc[u]], y);
-  }
-  for (; k < len; ++k) {
-    const int32_t cc = ld_l2(cp + (int64_t)k * 32, pol);
-    float m[1];
-    load_slot<1, H>(vp, hp, k, lane, pol, m);
-    y = fmaf(m[0], v[cc], y);
-  }
-#else
   int32_t cc[kSell1U];
   float mv[kSell1U];
   sell1_batch<H>(cp, vp, hp, 0, len, lane, pol, cc, mv);
@@ -1265,7 +1242,6 @@ __global__ void __launch_bounds__(kSell1W * 32) k_sell_op1(int64_t n_rows, int64
       mv[u] = mn[u];
     }
   }
-#endif
   double dot = 0.0;
   const int64_t i = s * 32 + lane;
   if (i < n_rows) {

@@ -212,6 +212,89 @@ k_stiffness(const double* __restrict__ bt, const double* __restrict__ detj,
     for (int q = 0; q < ND; ++q) out[i * ND + q] = acc[i][q];
 }
 
+// FP64 element matrices of an isotropic material by moments, for the FP64
+// copy of the mixed solvers' sliced matrix.  For C = lambda I(x)I + 2 G Isym
+// the (a, b) block of Ke is
+//   K_ab[i][k] = lambda M[i][k] + G M[k][i] + G tr(M) delta_ik,
+//   M = sum_ip w detJ t g_a g_b^T,
+// the same sum as k_stiffness's, regrouped.  A CTA takes iso_epb(NE)
+// elements: it stages their gradients g and the scaled gradients
+// w detJ t g of every integration point in shared memory once, then a thread
+// per (element, node pair a <= b) accumulates the 3x3 (2x2) moment and writes
+// K_ab and K_ba = K_ab^T.  NE (NE + 1) / 2 pairs of D^2 FMAs per point
+// instead of NE^2 rows of products: this GPU's FP64 pipe is narrow.
+__host__ __device__ constexpr int iso_pairs(int ne) { return ne * (ne + 1) / 2; }
+__host__ __device__ constexpr int iso_epb(int ne) { return iso_pairs(ne) >= 128 ? 1 : 128 / iso_pairs(ne); }
+
+template <int NE, int D, int NIP>
+__global__ void __launch_bounds__(iso_epb(NE) * iso_pairs(NE))
+k_stiffness_iso64(const double* __restrict__ bt, const double* __restrict__ detj,
+                  const double* __restrict__ weights, const double* __restrict__ thickness,
+                  const double* __restrict__ mat, int64_t n_elem, double* __restrict__ ke) {
+  constexpr int ND = NE * D;
+  constexpr int NP = iso_pairs(NE);
+  constexpr int EPB = iso_epb(NE);
+  __shared__ double g_s[EPB][NIP][ND];   // g
+  __shared__ double sg_s[EPB][NIP][ND];  // w detJ t g
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  for (int q = threadIdx.x; q < EPB * NIP * ND; q += blockDim.x) {
+    const int le = q / (NIP * ND);
+    const int ip = (q / ND) % NIP;
+    const int c = q % ND;
+    const int64_t e = e0 + le;
+    double g = 0.0, sc = 0.0;
+    if (e < n_elem) {
+      g = bt[((int64_t)ip * n_elem + e) * ND + c];
+      sc = weights[ip] * detj[(int64_t)ip * n_elem + e] * (thickness ? thickness[e] : 1.0);
+    }
+    g_s[le][ip][c] = g;
+    sg_s[le][ip][c] = sc * g;
+  }
+  __syncthreads();
+  const int le = threadIdx.x / NP;
+  const int64_t e = e0 + le;
+  if (le >= EPB || e >= n_elem) return;
+  int p = threadIdx.x - le * NP;
+  int a = 0;
+  while (p >= NE - a) {  // pairs of row a: (a, a) .. (a, NE - 1)
+    p -= NE - a;
+    ++a;
+  }
+  const int b = a + p;
+  double M[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int k = 0; k < D; ++k) M[i][k] = 0.0;
+#pragma unroll
+  for (int ip = 0; ip < NIP; ++ip) {
+    double ga[D], gb[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      ga[i] = sg_s[le][ip][a * D + i];
+      gb[i] = g_s[le][ip][b * D + i];
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int k = 0; k < D; ++k) M[i][k] = fma(ga[i], gb[k], M[i][k]);
+  }
+  const double lam = mat[e * 2], G = mat[e * 2 + 1];
+  double tr = 0.0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) tr += M[i][i];
+  double* kab = ke + (e * ND + (int64_t)a * D) * ND + b * D;
+  double* kba = ke + (e * ND + (int64_t)b * D) * ND + a * D;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const double v = lam * M[i][k] + G * M[k][i] + (i == k ? G * tr : 0.0);
+      kab[i * ND + k] = v;
+      kba[k * ND + i] = v;
+    }
+}
+
 // ------------------------------------------------------------------ forces --
 template <int NE, int D>
 __device__ __forceinline__ void load_field(const double* __restrict__ v, const int32_t* __restrict__ conn,
@@ -579,6 +662,25 @@ int fem_geometry(const fem_mesh* m, const double* dndxi, double* bt, double* det
   TFG_DISPATCH_ETYPE(m->etype)
 #undef TFG_BODY
   return check_cuda("fem_geometry");
+}
+
+int fem_element_stiffness_iso64(const fem_mesh* m, const fem_material* mat, double* ke, int32_t* status,
+                                void* stream) {
+  (void)status;
+  cudaStream_t st = as_stream(stream);
+  if (!m || !mat || mat->kind != FEM_MAT_ISO) {
+    set_last_error("fem_element_stiffness_iso64: needs an isotropic material");
+    return FEM_INVALID;
+  }
+  if (m->n_elem == 0) return FEM_OK;
+#define TFG_BODY                                                                                  \
+  k_stiffness_iso64<NE, D, NIP><<<(unsigned)((m->n_elem + iso_epb(NE) - 1) / iso_epb(NE)),          \
+                                  iso_epb(NE) * iso_pairs(NE), 0, st>>>(                           \
+      m->bt, m->detj, m->weights, m->thickness, mat->data, m->n_elem, ke);
+      ::tfg::note_launch();
+  TFG_DISPATCH_ETYPE(m->etype)
+#undef TFG_BODY
+  return check_cuda("fem_element_stiffness_iso64");
 }
 
 int fem_element_stiffness(const fem_mesh* m, const fem_material* mat, int out_dtype, void* ke,

@@ -52,16 +52,17 @@ class LinearSystem:
     # matrices, and applies it with one FP64 SpMV: about a sixth of the FP64
     # work of the element pass per replacement.  False recomputes K x from
     # the element geometry on every replacement.  None (the default) takes
-    # the copy where the element matrices are integrated in FP64 anyway (heat
-    # conduction, one DOF per node), and the element pass for vector fields,
-    # whose FP32 element matrices are integrated in FP32: integrating them in
-    # FP64 costs more FP64 work than the replacements of a solve save.
+    # the copy where FP64 element matrices are cheap: heat conduction (one
+    # DOF per node, integrated in FP64 anyway) and isotropic elasticity (the
+    # moment form, fem_element_stiffness_iso64).  Other materials keep FP32
+    # element matrices and the element pass: integrating their full FP64
+    # element matrices costs more FP64 work than a solve's replacements save.
     RESIDUAL_COPY: bool | None = None
 
     @staticmethod
-    def residual_copy(dm: "DeviceMesh") -> bool:
+    def residual_copy(dm: "DeviceMesh", mat) -> bool:
         if LinearSystem.RESIDUAL_COPY is None:
-            return dm.heat
+            return dm.heat or mat.kind == _lib.FEM_MAT_ISO
         return bool(LinearSystem.RESIDUAL_COPY)
 
     _tokens = 0
@@ -325,6 +326,16 @@ class DeviceMesh:
         )
         return ke.view(self.n_elem, nd, nd)
 
+    def element_stiffness_iso64(self, mesh, mat) -> Tensor:
+        """FP64 element matrices of an isotropic material in the moment form
+        (fem_element_stiffness_iso64)."""
+        nd = self.n_e * self.d
+        ke = self._empty(self.n_elem * nd * nd, torch.float64)
+        check(self.lib.fem_element_stiffness_iso64(C.byref(mesh), C.byref(mat), ptr(ke), ptr(self.status),
+                                                   self.stream),
+              "fem_element_stiffness_iso64")
+        return ke.view(self.n_elem, nd, nd)
+
     def element_force(self, mesh, mat, v, con_mask=None, con_values=None, con_mode=0,
                       sigma_prev=None, de0=None, want_flux=False, want_h=False):
         fe = self._empty(self.n_elem * self.n_e * self.d, torch.float64)
@@ -461,8 +472,11 @@ class DeviceMesh:
             del ke
             ws_bytes = self._set_csr(sysm, val)
         elif precision == "mixed":
-            if LinearSystem.residual_copy(self):
-                ke = self.element_stiffness(mesh, mat, torch.float64)
+            if LinearSystem.residual_copy(self, mat):
+                if not self.heat and mat.kind == _lib.FEM_MAT_ISO:
+                    ke = self.element_stiffness_iso64(mesh, mat)
+                else:
+                    ke = self.element_stiffness(mesh, mat, torch.float64)
                 sysm.bval, sysm.bval64 = self.assemble_sell_pair(ke, con_mask)
             else:
                 ke = self.element_stiffness(mesh, mat, torch.float32)

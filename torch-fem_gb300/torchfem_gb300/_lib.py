@@ -183,6 +183,7 @@ _SIGNATURES = {
     ),
     "fem_geometry": (C.c_int, [_P(FemMesh), vp, vp, vp, vp, vp]),
     "fem_element_stiffness": (C.c_int, [_P(FemMesh), _P(FemMaterial), C.c_int, vp, vp, vp]),
+    "fem_element_stiffness_iso64": (C.c_int, [_P(FemMesh), _P(FemMaterial), vp, vp, vp]),
     "fem_element_force": (
         C.c_int,
         [_P(FemMesh), _P(FemMaterial), vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp],
