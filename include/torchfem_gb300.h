@@ -644,6 +644,29 @@ int fem_mass_matrices(const fem_mesh* mesh, const double* rho, const double* nva
  * DOFs (sparse.py:798-827). */
 int fem_csr_spmm(const fem_matrix* A, int nvec, const double* X, double* Y, void* stream);
 
+/* ------------------------------------------------------------- assembly --
+ * Parts coupled by kinematic constraints (Assembly.solve,
+ * assembly.py:378-650): the coupling map T [n_dofs x n_retained] eliminates
+ * the secondary DOFs, u = T q, and the solved system is
+ * K_r = T^T blockdiag(K_parts) T with the Dirichlet condensation of
+ * Assembly._stiffness (assembly.py:293-330).  The host builds the pattern of
+ * K_r and, per entry, the contributing part-matrix entries once per solve.
+ *
+ * Values of K_r: out[e] = sum_{c in [ptr[e], ptr[e+1])} coef[c] * kval[src[c]]
+ * (kval: the parts' FP64 CSR values, concatenated; coef: the product of the
+ * two T coefficients), summed in list order; then fix[e] = 1 zeroes the entry
+ * (a constrained row or column) and fix[e] = 2 sets it to 1 (a constrained
+ * diagonal).  fix may be NULL.  Replaces torch.sparse.mm(T^T, K T) and the
+ * condensation of Assembly._stiffness. */
+int fem_coupled_values(int64_t n_out, const int64_t* ptr, const int64_t* src, const double* coef,
+                       const double* kval, const uint8_t* fix, double* out, void* stream);
+
+/* y = A x for a rectangular FP64 CSR matrix [n_rows x any] with int64 row
+ * pointers and int32 columns: u = T q and T^T (F_int - F_ext) of an assembly
+ * (the _mv products of assembly.py:24-26). */
+int fem_csr_apply(int64_t n_rows, const int64_t* row_ptr, const int32_t* col, const double* val,
+                  const double* x, double* y, void* stream);
+
 /* ---------------------------------------------------------------- shell --
  * Tria1 flat-facet shell, homogeneous linear-elastic section (the reference's
  * Shell with a plane-stress material, src/torchfem/shell.py:48-603).  Nodes

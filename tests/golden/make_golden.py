@@ -832,6 +832,121 @@ def make_hyper_mid(tf, name="hyper_tet2_15x5x5.npz", counts=(10, 20)):
         break
     np.savez_compressed(OUT / name, **out)
 
+def make_assembly(tf):
+    """Assemblies of coupled parts (assembly.py), solved by the reference with
+    spsolve: two tied Hexa1 blocks (with intermediate increments), a cube
+    driven by a 3D reference point's moment, a tied Tria1 shell plate with the
+    thickness gradient of the tip work, a Hexa2 solid beam continued by a
+    shell, a conducting cube held by a thermal reference point, and a Quad1
+    plate turned by a 2D reference point."""
+    from torchfem import Assembly, Planar, ReferencePoint, ReferencePointHeat, Shell, Solid, SolidHeat
+    from torchfem.elements import linear_to_quadratic
+    from torchfem.materials import (IsotropicConductivity3D, IsotropicElasticity3D,
+                                    IsotropicElasticityPlaneStress)
+    from torchfem.mesh import cube_hexa, rect_quad, rect_tri
+
+    E, NU = 1000.0, 0.3
+    SOLID = IsotropicElasticity3D(E, NU)
+    PLANE = IsotropicElasticityPlaneStress(E, NU)
+    L, B, T, P = 10.0, 1.0, 0.4, 0.05
+    out = {}
+
+    def block(z0, z1):
+        nodes = torch.tensor([[x, y, z] for z in (z0, z1) for y in (0.0, 1.0) for x in (0.0, 1.0)])
+        return nodes, torch.tensor([[0, 1, 3, 2, 4, 5, 7, 6]])
+
+    def plate(x0, Lx, Nx):
+        nodes, elements = rect_tri(Nx, 3, Lx, B)
+        nodes = nodes + torch.tensor([x0, 0.0])
+        return torch.cat([nodes, torch.zeros(len(nodes), 1)], dim=1), elements
+
+    # two tied blocks, five increments
+    n_a, e_a = block(0.0, 1.0)
+    n_b, e_b = block(1.0, 2.0)
+    a, b = Solid(n_a, e_a, SOLID), Solid(n_b, e_b, SOLID)
+    a.constraints[n_a[:, 2] == 0.0] = True
+    b.forces[n_b[:, 2] == 2.0, 2] = 25.0
+    b.forces[n_b[:, 2] == 2.0, 0] = 5.0
+    asm = Assembly([a, b])
+    asm.coupling(b, n_b[:, 2] == 1.0, a, n_a[:, 2] == 1.0)
+    u, f, s, _, _ = asm.solve(increments=torch.linspace(0.0, 1.0, 5), return_intermediate=True, method="spsolve")
+    for j in range(2):
+        out[f"blocks_u{j}"], out[f"blocks_f{j}"], out[f"blocks_s{j}"] = u[j].numpy(), f[j].numpy(), s[j].numpy()
+
+    # a cube turned by a reference point
+    nodes, elements = cube_hexa(3, 3, 3)
+    solid = Solid(nodes, elements, SOLID)
+    solid.constraints[nodes[:, 2] == 0.0] = True
+    point = ReferencePoint([0.5, 0.5, 2.0])
+    point.forces[0, 3] = 50.0
+    point.forces[0, 1] = 7.0
+    asm = Assembly([solid, point])
+    asm.coupling(solid, nodes[:, 2] == nodes[:, 2].max(), point)
+    u, f, s, _, _ = asm.solve(method="spsolve")
+    out.update(rp_u0=u[0].numpy(), rp_u1=u[1].numpy(), rp_f0=f[0].numpy(), rp_f1=f[1].numpy(), rp_s0=s[0].numpy())
+
+    # a tied shell plate and the thickness gradient of its tip work
+    n_sa, e_sa = plate(0.0, L / 2, 5)
+    n_sb, e_sb = plate(L / 2, L / 2, 5)
+
+    def work(thickness):
+        sa = Shell(n_sa, e_sa, PLANE, thickness=thickness)
+        sb = Shell(n_sb, e_sb, PLANE, thickness=T)
+        sa.constraints[n_sa[:, 0] == 0.0] = True
+        sb.forces[n_sb[:, 0] == L, 2] = P / (n_sb[:, 0] == L).sum()
+        asm = Assembly([sa, sb])
+        asm.coupling(sb, n_sb[:, 0] == L / 2, sa, n_sa[:, 0] == L / 2)
+        u, f, _, _, _ = asm.solve(differentiable_parameters=thickness, method="spsolve")
+        return torch.inner(sb.forces.ravel(), u[1].ravel()), u, f
+
+    th = torch.full((len(e_sa),), T, requires_grad=True)
+    w, u, f = work(th)
+    (g,) = torch.autograd.grad(w, th)
+    out.update(shell_na=n_sa.numpy(), shell_ea=e_sa.numpy(), shell_nb=n_sb.numpy(), shell_eb=e_sb.numpy(),
+               shell_u0=u[0].detach().numpy(), shell_u1=u[1].detach().numpy(), shell_f1=f[1].detach().numpy(),
+               shell_work=w.detach().numpy(), shell_grad=g.numpy())
+
+    # a Hexa2 solid beam continued by a shell
+    n_s, e_s = linear_to_quadratic(*cube_hexa(11, 3, 3, L / 2, B, T))
+    n_s = n_s - torch.tensor([0.0, 0.0, T / 2])
+    solid = Solid(n_s, e_s, SOLID)
+    solid.constraints[n_s[:, 0] == 0.0] = True
+    n_h, e_h = plate(L / 2, L / 2, 11)
+    shell = Shell(n_h, e_h, PLANE, thickness=T)
+    shell.forces[n_h[:, 0] == L, 2] = P / (n_h[:, 0] == L).sum()
+    asm = Assembly([solid, shell])
+    asm.coupling(solid, n_s[:, 0] == L / 2, shell, n_h[:, 0] == L / 2)
+    u, f, _, _, _ = asm.solve(method="spsolve")
+    out.update(ss_ns=n_s.numpy(), ss_es=e_s.numpy(), ss_nh=n_h.numpy(), ss_eh=e_h.numpy(),
+               ss_u0=u[0].numpy(), ss_u1=u[1].numpy())
+
+    # a conducting cube held isothermal on top by a thermal point
+    nodes, elements = cube_hexa(4, 4, 4)
+    heat = SolidHeat(nodes, elements, IsotropicConductivity3D(1.0))
+    heat.constraints[nodes[:, 2] == 0.0] = True
+    heat.heat_flux[nodes[:, 0] == 0.0, 0] = 0.1
+    hp = ReferencePointHeat([0.5, 0.5, 1.5])
+    hp.heat_flux[0, 0] = 4.0
+    asm = Assembly([heat, hp])
+    asm.coupling(heat, nodes[:, 2] == 1.0, hp)
+    T_, q, flux, _, _ = asm.solve(method="spsolve")
+    out.update(heat_T0=T_[0].numpy(), heat_T1=T_[1].numpy(), heat_q0=q[0].numpy(), heat_q1=q[1].numpy(),
+               heat_flux0=flux[0].numpy())
+
+    # a Quad1 plate turned by a 2D reference point
+    nodes, elements = rect_quad(5, 5)
+    pl = Planar(nodes, elements, PLANE)
+    pl.constraints[nodes[:, 1] == 0.0] = True
+    p2 = ReferencePoint([0.5, 1.5])
+    p2.forces[0, 2] = 20.0
+    p2.forces[0, 0] = 3.0
+    asm = Assembly([pl, p2])
+    asm.coupling(pl, nodes[:, 1] == 1.0, p2)
+    u, f, s, _, _ = asm.solve(method="spsolve")
+    out.update(planar_u0=u[0].numpy(), planar_u1=u[1].numpy(), planar_f1=f[1].numpy(), planar_s0=s[0].numpy())
+    np.savez_compressed(OUT / "assembly_cases.npz", **out)
+
+
 MAKERS = {
     "material_points": make_material_points,
     "c1": make_c1, "hexa_jitter3": make_hexa_jitter3, "patterns": make_patterns,
@@ -840,7 +955,7 @@ MAKERS = {
     "hyper": make_hyper, "plastic": make_plastic, "shell": make_shell,
     "plastic_full": lambda tf: make_plastic(tf, 256, 64, "plastic_ogrid_256x64.npz"),
     "hexa2": make_hexa2, "heat": make_heat, "heat_transient_grad": make_heat_transient_grad,
-    "modes": make_modes,
+    "modes": make_modes, "assembly": make_assembly,
     "c2": make_c2, "c2_crosscheck": make_c2_crosscheck, "hyper_full": make_hyper_full, "hyper_mid": make_hyper_mid,
 }
 # targets that take minutes to an hour of CPU; run only when named

@@ -18,7 +18,7 @@ CSRC = PKG_DIR.parent / "csrc"
 INCLUDE = PKG_DIR.parent.parent / "include"
 LIB_PATH = PKG_DIR / "libtorchfem_gb300.so"
 SOURCES = ("fem_pattern.cu", "fem_element.cu", "fem_solver.cu", "fem_nonlinear.cu", "fem_shell.cu",
-           "fem_amg.cu", "fem_heat.cu", "fem_modal.cu")
+           "fem_amg.cu", "fem_heat.cu", "fem_modal.cu", "fem_coupling.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -209,6 +209,8 @@ _SIGNATURES = {
     "fem_heat_mass_vjp": (C.c_int, [_P(FemMesh), vp, vp, vp, vp, vp]),
     "fem_mass_matrices": (C.c_int, [_P(FemMesh), vp, vp, C.c_int, vp, vp]),
     "fem_csr_spmm": (C.c_int, [_P(FemMatrix), C.c_int, vp, vp, vp]),
+    "fem_coupled_values": (C.c_int, [i64, vp, vp, vp, vp, vp, vp, vp]),
+    "fem_csr_apply": (C.c_int, [i64, vp, vp, vp, vp, vp, vp]),
     "fem_csr_combine": (C.c_int, [i64, C.c_double, vp, C.c_double, vp, vp, vp]),
     "fem_heat_cn_workspace_bytes": (C.c_size_t, [i64]),
     "fem_heat_cn_residual": (
