@@ -567,6 +567,15 @@ void fem_amg_set_half_smoother(int enable);
  * of partial row sums.  No counterpart in the reference. */
 void fem_amg_set_fused_cycle(int enable);
 
+/* How the level-0 block SpMVs read the sliced matrix (process-wide; default
+ * 1).  1: thread 0 of each slice's CTA streams the slice's slot-rows into a
+ * two-stage shared-memory ring with bulk copies (cp.async.bulk completing on
+ * mbarriers, waits bounded: a wait that runs out ends the solve with
+ * FEM_CUDA_ERROR and a "barrier timeout" message); 0: every thread loads its
+ * slot-rows directly.  Same sums in the same order either way.  Scalar rows
+ * always use the warp-per-slice kernel.  No counterpart in the reference. */
+void fem_amg_set_level0_tma(int enable);
+
 /* CG preconditioned by one V-cycle (Chebyshev smoothing) on the matrix of
  * the last fem_amg_setup, from x = 0.  With op != NULL: FP64 residual
  * replacement as in fem_pcg_mixed (threshold delta), stopping at

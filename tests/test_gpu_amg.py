@@ -316,6 +316,29 @@ def test_amg_fused_coarse_cycle_matches_per_level_kernels(cuda, half_smoother, k
     assert all(abs(a - b) <= 1 for a, b in zip(its[0], its[1])), its
 
 
+@pytest.mark.parametrize("kind", ["elastic", "planar"])
+def test_amg_level0_bulk_copies_match_direct_loads(cuda, half_smoother, kind):
+    """Level-0 block SpMVs with each slice streamed into shared memory by bulk
+    copies (fem_amg_set_level0_tma) against direct loads: the same sums in
+    the same order, so the solutions are bitwise identical."""
+    lib = half_smoother
+    if kind == "elastic":
+        m, _, _ = cube_problem(16)
+    else:
+        nodes, el = mesh.rect_quad(41, 21, 2.0, 1.0)
+        m = Planar(nodes.to(cuda), el.to(cuda), IsotropicElasticityPlaneStress(1000.0, 0.3))
+        m.constraints[(nodes[:, 0] == 0.0).to(cuda), :] = True
+        m.forces[(nodes[:, 0] == 2.0).to(cuda), 1] = -1.0
+    out = {}
+    try:
+        for tma in (0, 1):
+            lib.fem_amg_set_level0_tma(tma)
+            out[tma] = m.solve(stol=1e-12, precision="mixed", preconditioner="amg")[0].clone()
+    finally:
+        lib.fem_amg_set_level0_tma(1)
+    assert torch.equal(out[1], out[0])
+
+
 def test_config2_full_size_amg_iterations(cuda, half_smoother):
     """Config 2 at full size (70^3 jittered Hexa1, 1,073,733 DOF): the
     V-cycle CG iteration counts of solve + adjoint stay flat (tens, against

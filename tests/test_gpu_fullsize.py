@@ -169,11 +169,11 @@ def test_config3_mixed_refinement_floor_is_refused(cuda):
     """FP64 refinement of the FP32 SIMP matrix stagnates above 1e-12: the
     solve stops with an error (the stagnation or iteration-cap message,
     chained under the reference's cutback message) instead of returning an
-    inaccurate result.  The FP32 CG is capped at 20,000 iterations: with the
+    inaccurate result.  The FP32 CG is capped at 5,000 iterations: with the
     default cap of 10 n it runs 1.6M iterations (400 s) before it stops."""
     m = _simp(_simp_rho())
     with pytest.raises(RuntimeError) as info:
-        m.solve(stol=1e-12, precision="mixed", preconditioner="jacobi", cg_max_iter=20000)
+        m.solve(stol=1e-12, precision="mixed", preconditioner="jacobi", cg_max_iter=5000)
     msg = str(info.value) + " " + str(info.value.__cause__)
     assert "stagnated" in msg or "did not converge" in msg or "failed" in msg, msg
 

@@ -44,6 +44,7 @@ int etype_info(int etype, int* ne, int* d, int* nip);
 extern int g_timing;  // fem_set_timing
 int g_amg_half = 1;   // FP16 smoothing copy of the level-0 matrix (fem_amg_set_half_smoother)
 int g_amg_fused = 1;  // coarse levels as one cooperative launch per V-cycle (fem_amg_set_fused_cycle)
+int g_amg_tma = 1;    // level-0 slices streamed by bulk copies (fem_amg_set_level0_tma)
 int sell_apply64(const fem_matrix* A32, const double* sval64, const double* x, double* y, cudaStream_t st);
 size_t scan_workspace_bytes(int64_t n);
 int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
@@ -1178,6 +1179,180 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
   }
 }
 
+// Level 0 with the slice streamed by bulk copies (cp.async.bulk): one CTA per
+// slice as in k_sell_op, but thread 0 copies the slice's slot-rows (values
+// and columns) into a two-stage shared-memory ring, kTma0Rows slot-rows a
+// stage, completing on an mbarrier per stage; the warps read their slot-rows
+// from shared memory and gather x from L2.  A few bulk copies per CTA keep
+// more bytes in flight than one slot's loads per thread.  Every stage wait is
+// bounded (kTma0Spin cycles): on a timeout the CTA flags kBarrierTimeout,
+// waits (bounded) for the copies it issued and returns.
+#ifndef TFG_TMA0_ROWS
+#define TFG_TMA0_ROWS 8
+#endif
+constexpr int kTma0Rows = TFG_TMA0_ROWS;  // slot-rows per ring stage
+constexpr long long kTma0Spin = 2000000000LL;
+
+template <int D, bool H>
+__host__ __device__ constexpr int tma0_vbytes() { return H ? D * D * 64 : D * D * 128; }  // per slot-row
+template <int D, bool H>
+__host__ __device__ constexpr int tma0_stage() { return kTma0Rows * (tma0_vbytes<D, H>() + 128); }
+
+__device__ __forceinline__ uint32_t amg_smem_u32(const void* ptr) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
+}
+
+__device__ __forceinline__ bool amg_mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kTma0Spin) return false;
+  }
+}
+
+// Stage c of the slice: its slot-rows' values then columns (16-byte aligned:
+// slices start at multiples of 32 slots).
+template <int D, bool H>
+__device__ __forceinline__ void tma0_issue(uint32_t bar, uint32_t dst, const void* vals, const int32_t* cols,
+                                           int nr, uint64_t pol) {
+  const uint32_t vb = (uint32_t)(nr * tma0_vbytes<D, H>()), cb = (uint32_t)(nr * 128);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(vb + cb) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(dst),
+      "l"(vals), "r"(vb), "r"(bar), "l"(pol)
+      : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          dst + (uint32_t)(kTma0Rows * tma0_vbytes<D, H>())),
+      "l"(cols), "r"(cb), "r"(bar), "l"(pol)
+      : "memory");
+}
+
+template <int D, int MODE, bool H>
+__global__ void __launch_bounds__(kSellW * 32) k_sell_op_tma(int64_t n_rows, const int64_t* __restrict__ sell_base,
+                                                             const int32_t* __restrict__ col,
+                                                             const float* __restrict__ sval, OpArgs a) {
+  constexpr int DD = D * D;
+  constexpr int VB = tma0_vbytes<D, H>();
+  constexpr int SB = tma0_stage<D, H>();
+  extern __shared__ __align__(128) unsigned char ring[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ float ys[kSellW][D][32];
+  if (amg_idle(a.ctrl)) return;
+  const float* __restrict__ v = op_operand<MODE>(a);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t pol = l2_policy(false);
+  const int64_t s = blockIdx.x;
+  const int64_t b0 = sell_base[s];
+  const int len = (int)((sell_base[s + 1] - b0) >> 5);
+  const int nch = (len + kTma0Rows - 1) / kTma0Rows;
+  const uint32_t bar0 = amg_smem_u32(&bars[0]), buf0 = amg_smem_u32(ring);
+  const char* vsrc = H ? reinterpret_cast<const char*>(a.sv16 + b0 * DD) : reinterpret_cast<const char*>(sval + b0 * DD);
+  auto issue = [&](int c) {
+    const int r0 = c * kTma0Rows;
+    tma0_issue<D, H>(bar0 + 8u * (uint32_t)(c & 1), buf0 + (uint32_t)((c & 1) * SB), vsrc + (int64_t)r0 * VB,
+                     col + b0 + (int64_t)r0 * 32, min(kTma0Rows, len - r0), pol);
+  };
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int c = 0; c < 2 && c < nch; ++c) issue(c);
+  }
+  __syncthreads();
+  float y[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) y[c] = 0.f;
+  int done = 0;  // stages consumed
+  bool ok = true;
+  for (int c = 0; c < nch; ++c) {
+    const bool got = amg_mbar_wait(bar0 + 8u * (uint32_t)(c & 1), (uint32_t)((c >> 1) & 1));
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    const unsigned char* st = ring + (c & 1) * SB;
+    const int32_t* cs = reinterpret_cast<const int32_t*>(st + kTma0Rows * VB);
+    const int nr = min(kTma0Rows, len - c * kTma0Rows);
+    for (int k = w; k < nr; k += kSellW) {
+      const int64_t cc = cs[k * 32 + lane];
+      float m[DD];
+      if constexpr (H) {
+        const uint32_t* wv = reinterpret_cast<const uint32_t*>(st + k * VB);
+#pragma unroll
+        for (int p = 0; p < DD / 2; ++p) {
+          const uint32_t wd = wv[p * 32 + lane];
+          const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&wd));
+          m[2 * p] = f.x;
+          m[2 * p + 1] = f.y;
+        }
+        if constexpr (DD % 2 == 1) {
+          const __half* hv = reinterpret_cast<const __half*>(st + k * VB) + (DD / 2) * 64;
+          m[DD - 1] = __half2float(hv[lane]);
+        }
+      } else {
+        const float* fv = reinterpret_cast<const float*>(st + k * VB);
+#pragma unroll
+        for (int e = 0; e < DD; ++e) m[e] = fv[e * 32 + lane];
+      }
+      float xv[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) xv[j] = v[cc * D + j];
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int j = 0; j < D; ++j) y[r] = fmaf(m[r * D + j], xv[j], y[r]);
+    }
+    done = c + 1;
+    __syncthreads();  // every warp is done with this stage
+    if (threadIdx.x == 0 && c + 2 < nch) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(c + 2);
+    }
+  }
+  if (!ok) {
+    // flag, then wait (bounded) for this CTA's copies still in flight
+    if (threadIdx.x == 0) {
+      atomicExch(&a.ctrl->done, kBarrierTimeout);
+      const int issued = min(nch, done + 2);
+      for (int c = done; c < issued; ++c) amg_mbar_wait(bar0 + 8u * (uint32_t)(c & 1), (uint32_t)((c >> 1) & 1));
+    }
+    __syncthreads();
+    return;
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c) ys[w][c][lane] = y[c];
+  __syncthreads();
+  double dot = 0.0;
+  if (w == 0) {
+    const int64_t i = s * 32 + lane;
+    if (i < n_rows) {
+      const float sc = H ? *a.s16inv : 1.f;  // a power of two: exact
+      float yt[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        float t = ys[0][c][lane];
+#pragma unroll
+        for (int u = 1; u < kSellW; ++u) t += ys[u][c][lane];
+        yt[c] = H ? t * sc : t;
+      }
+      dot += op_epilogue<D, MODE>(a, i, yt);
+    }
+  }
+  if constexpr (op_has_dot<MODE>()) {
+    if (w == 0) {
+      const double t = warp_sum(dot);
+      if (lane == 0) a.partial[blockIdx.x] = t;
+    }
+  }
+}
+
 // Level 0 of a scalar field (heat): a slot holds one 4-byte value, so a
 // 32-row slice is only a few KB and the shared-slot CTA of k_sell_op spends
 // more on its CTA and its shared-memory sum than on streaming.  Here each warp
@@ -1263,6 +1438,9 @@ void launch_sell(int64_t n, const int64_t* sell_base, const int32_t* sell_col, c
   if constexpr (D == 1)
     k_sell_op1<MODE, H><<<(unsigned)((ns + kSell1W - 1) / kSell1W), kSell1W * 32, 0, st>>>(n, ns, sell_base, sell_col,
                                                                                           sell_val, a);
+  else if (g_amg_tma)
+    k_sell_op_tma<D, MODE, H><<<(unsigned)ns, kSellW * 32, 2 * tma0_stage<D, H>(), st>>>(n, sell_base, sell_col,
+                                                                                        sell_val, a);
   else
     k_sell_op<D, MODE, H><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, sell_base, sell_col, sell_val, a);
 }
@@ -3381,6 +3559,7 @@ int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const
 }
 
 void fem_amg_set_half_smoother(int enable) { g_amg_half = enable ? 1 : 0; }
+void fem_amg_set_level0_tma(int enable) { g_amg_tma = enable ? 1 : 0; }
 
 void fem_amg_set_fused_cycle(int enable) { g_amg_fused = enable ? 1 : 0; }
 
