@@ -316,14 +316,23 @@ def test_amg_fused_coarse_cycle_matches_per_level_kernels(cuda, half_smoother, k
     assert all(abs(a - b) <= 1 for a, b in zip(its[0], its[1])), its
 
 
-@pytest.mark.parametrize("kind", ["elastic", "planar"])
+@pytest.mark.parametrize("kind", ["elastic", "planar", "heat"])
 def test_amg_level0_bulk_copies_match_direct_loads(cuda, half_smoother, kind):
-    """Level-0 block SpMVs with each slice streamed into shared memory by bulk
+    """Level-0 SpMVs with each slice streamed into shared memory by bulk
     copies (fem_amg_set_level0_tma) against direct loads: the same sums in
-    the same order, so the solutions are bitwise identical."""
+    the same order, so the solutions are bitwise identical (3x3 and 2x2
+    blocks, and scalar rows)."""
     lib = half_smoother
     if kind == "elastic":
         m, _, _ = cube_problem(16)
+    elif kind == "heat":
+        from torchfem_gb300 import SolidHeat
+        from torchfem_gb300.materials import IsotropicConductivity3D
+
+        nodes, el = jittered_cube(24)
+        m = SolidHeat(nodes.to(cuda), el.to(cuda), IsotropicConductivity3D(1.0))
+        m.constraints[(nodes[:, 0] == 0.0).to(cuda)] = True
+        m.heat_flux[:] = 1.0 / len(nodes)
     else:
         nodes, el = mesh.rect_quad(41, 21, 2.0, 1.0)
         m = Planar(nodes.to(cuda), el.to(cuda), IsotropicElasticityPlaneStress(1000.0, 0.3))

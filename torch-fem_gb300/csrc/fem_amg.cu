@@ -1429,16 +1429,134 @@ __global__ void __launch_bounds__(kSell1W * 32) k_sell_op1(int64_t n_rows, int64
   }
 }
 
+// The scalar kernel with each warp's slice staged by bulk copies: lane 0
+// copies the slice's values and columns (contiguous, slot-major) into the
+// warp's part of shared memory with two cp.async.bulk on one mbarrier, then
+// the warp reads them from there; the same sums in the same order as
+// k_sell_op1.  Slices longer than kSell1Max slot-rows load directly.  The
+// wait is bounded: on a timeout the warp flags kBarrierTimeout, waits once
+// more (bounded) for its copy and returns.
+constexpr int kSell1Max = 32;
+
+template <bool H>
+__host__ __device__ constexpr int sell1_vb() { return H ? 64 : 128; }  // value bytes per slot-row
+template <bool H>
+__host__ __device__ constexpr int sell1_smem() { return kSell1W * kSell1Max * (sell1_vb<H>() + 128); }
+
+template <int MODE, bool H>
+__global__ void __launch_bounds__(kSell1W * 32) k_sell_op1_tma(int64_t n_rows, int64_t n_slices,
+                                                               const int64_t* __restrict__ sell_base,
+                                                               const int32_t* __restrict__ col,
+                                                               const float* __restrict__ sval, OpArgs a) {
+  constexpr int VB = sell1_vb<H>();
+  extern __shared__ __align__(128) unsigned char ring[];
+  __shared__ __align__(8) uint64_t bars[kSell1W];
+  if (amg_idle(a.ctrl)) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t s = (int64_t)blockIdx.x * kSell1W + w;
+  if (s >= n_slices) return;
+  const float* __restrict__ v = op_operand<MODE>(a);
+  const uint64_t pol = l2_policy(false);
+  const int64_t b0 = sell_base[s];
+  const int len = (int)((sell_base[s + 1] - b0) >> 5);
+  float y = 0.f;
+  if (len <= kSell1Max) {
+    unsigned char* wbuf = ring + (size_t)w * kSell1Max * (VB + 128);
+    const uint32_t bar = amg_smem_u32(&bars[w]), dst = amg_smem_u32(wbuf);
+    if (lane == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      if (len > 0) {
+        const uint32_t vb = (uint32_t)(len * VB), cb = (uint32_t)(len * 128);
+        const void* vsrc = H ? (const void*)(a.sv16 + b0) : (const void*)(sval + b0);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(vb + cb) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+            "%4;" ::"r"(dst),
+            "l"(vsrc), "r"(vb), "r"(bar), "l"(pol)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+            "%4;" ::"r"(dst + (uint32_t)(kSell1Max * VB)),
+            "l"(col + b0), "r"(cb), "r"(bar), "l"(pol)
+            : "memory");
+      }
+    }
+    __syncwarp();
+    const bool got = len == 0 || amg_mbar_wait(bar, 0);
+    if (!__all_sync(0xffffffffu, got)) {
+      if (lane == 0) {
+        atomicExch(&a.ctrl->done, kBarrierTimeout);
+        amg_mbar_wait(bar, 0);
+      }
+      __syncwarp();
+      return;
+    }
+    const int32_t* cs = reinterpret_cast<const int32_t*>(wbuf + kSell1Max * VB);
+    int k = 0;
+    for (; k + 4 <= len; k += 4) {
+      float m[4], xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int kk = k + u;
+        m[u] = H ? __half2float(reinterpret_cast<const __half*>(wbuf)[kk * 32 + lane])
+                 : reinterpret_cast<const float*>(wbuf)[kk * 32 + lane];
+        xv[u] = v[cs[kk * 32 + lane]];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) y = fmaf(m[u], xv[u], y);
+    }
+    for (; k < len; ++k) {
+      const float m = H ? __half2float(reinterpret_cast<const __half*>(wbuf)[k * 32 + lane])
+                        : reinterpret_cast<const float*>(wbuf)[k * 32 + lane];
+      y = fmaf(m, v[cs[k * 32 + lane]], y);
+    }
+  } else {
+    const int32_t* cp = col + b0 + lane;
+    const float* vp = sval + b0 + lane;
+    const __half* hp = H ? a.sv16 + b0 : nullptr;
+    int32_t cc[kSell1U];
+    float mv[kSell1U];
+    sell1_batch<H>(cp, vp, hp, 0, len, lane, pol, cc, mv);
+    for (int k = 0; k < len; k += kSell1U) {
+      int32_t cn[kSell1U];
+      float mn[kSell1U];
+      sell1_batch<H>(cp, vp, hp, k + kSell1U, len, lane, pol, cn, mn);
+#pragma unroll
+      for (int u = 0; u < kSell1U; ++u)
+        if (k + u < len) y = fmaf(mv[u], v[cc[u]], y);
+#pragma unroll
+      for (int u = 0; u < kSell1U; ++u) {
+        cc[u] = cn[u];
+        mv[u] = mn[u];
+      }
+    }
+  }
+  double dot = 0.0;
+  const int64_t i = s * 32 + lane;
+  if (i < n_rows) {
+    const float yt[1] = {H ? y * *a.s16inv : y};  // a power of two: exact
+    dot = op_epilogue<1, MODE>(a, i, yt);
+  }
+  if constexpr (op_has_dot<MODE>()) {
+    const double t = warp_sum(dot);
+    if (lane == 0) a.partial[s] = t;
+  }
+}
+
 // One level-0 pass: the shared-slot kernel for 2×2 / 3×3 blocks, the
 // warp-per-slice kernel for scalar rows.
 template <int D, int MODE, bool H>
 void launch_sell(int64_t n, const int64_t* sell_base, const int32_t* sell_col, const float* sell_val,
                  const OpArgs& a, cudaStream_t st) {
   const int64_t ns = (n + 31) / 32;
-  if constexpr (D == 1)
-    k_sell_op1<MODE, H><<<(unsigned)((ns + kSell1W - 1) / kSell1W), kSell1W * 32, 0, st>>>(n, ns, sell_base, sell_col,
-                                                                                          sell_val, a);
-  else if (g_amg_tma)
+  if constexpr (D == 1) {
+    const unsigned g = (unsigned)((ns + kSell1W - 1) / kSell1W);
+    if (g_amg_tma)
+      k_sell_op1_tma<MODE, H><<<g, kSell1W * 32, sell1_smem<H>(), st>>>(n, ns, sell_base, sell_col, sell_val, a);
+    else
+      k_sell_op1<MODE, H><<<g, kSell1W * 32, 0, st>>>(n, ns, sell_base, sell_col, sell_val, a);
+  } else if (g_amg_tma)
     k_sell_op_tma<D, MODE, H><<<(unsigned)ns, kSellW * 32, 2 * tma0_stage<D, H>(), st>>>(n, sell_base, sell_col,
                                                                                         sell_val, a);
   else
