@@ -1925,13 +1925,27 @@ struct CycArgs {
 // it publishes the CTA's writes), relaxed polling with a short sleep, one
 // acquire fence.  A wait that runs out sets the error flag and the CG's
 // done code; returns false on every thread once any CTA's wait ran out.
-__device__ __forceinline__ bool cyc_barrier(CycBarrier* b, AmgCtrl* c) {
+// Grid barrier of the fused cycle.  The counter only grows (it is zeroed
+// once per solve), so every barrier of a launch has a known target: the
+// first one learns the launch's base from the value its atomic returns, the
+// later ones arrive with a fire-and-forget release reduction (no round trip)
+// and poll for base + (j + 1) x grid.  `next` (thread 0's copy) carries the
+// target of the next barrier.  The wait is bounded (kCycSpin cycles); a
+// timeout flags the barrier and the solve.
+__device__ __forceinline__ bool cyc_barrier(CycBarrier* b, AmgCtrl* c, unsigned long long& next) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long old;
-    asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(old) : "l"(&b->seq) : "memory");
-    const unsigned long long target = (old / gridDim.x + 1) * gridDim.x;
+    unsigned long long target;
+    if (next == 0ull) {
+      unsigned long long old;
+      asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(old) : "l"(&b->seq) : "memory");
+      target = (old / gridDim.x + 1) * gridDim.x;
+    } else {
+      asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(&b->seq) : "memory");
+      target = next;
+    }
+    next = target + gridDim.x;
     const long long t0 = clock64();
     int good = 1;
     while (true) {
@@ -1948,7 +1962,7 @@ __device__ __forceinline__ bool cyc_barrier(CycBarrier* b, AmgCtrl* c) {
         good = 0;
         break;
       }
-      __nanosleep(64);
+      __nanosleep(32);
     }
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
     ok = good;
@@ -2267,6 +2281,7 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
   AmgCtrl* c = a.ctrl;
   CycBarrier* bar = a.bar;
   if (amg_idle(c)) return;
+  unsigned long long next = 0;  // target of the next grid barrier (thread 0)
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * kCycT + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * kCycT) >> 5;
@@ -2297,25 +2312,25 @@ __global__ void __launch_bounds__(kCycT) k_coarse_cycle(CycArgs a) {
         else cyc_restrict<K, K>(F, C, I, lane);
       }
     }
-    if (!cyc_barrier(bar, c)) return;
+    if (!cyc_barrier(bar, c, next)) return;
     cyc_level_pass<K, kOpS1>(C, lane, warp, n_warps, pol, part);
-    if (!cyc_barrier(bar, c)) return;
+    if (!cyc_barrier(bar, c, next)) return;
     cyc_level_pass<K, kOpS2>(C, lane, warp, n_warps, pol, part);
-    if (!cyc_barrier(bar, c)) return;
+    if (!cyc_barrier(bar, c, next)) return;
   }
   // up: prolongate, then the level's post-smoothing; level 0 continues in
   // the next launch
   for (int l = last - 1; l >= 0; --l) {
-    if (!cyc_barrier(bar, c)) return;
+    if (!cyc_barrier(bar, c, next)) return;
     const CycLevel& F = a.L[l];
     if (l == 0) {
       cyc_prolong<B0, K>(F, a.L[1].xb, F.x, tid, n_threads);
       break;
     }
     cyc_prolong<K, K>(F, a.L[l + 1].xb, F.x, tid, n_threads);
-    if (!cyc_barrier(bar, c)) return;
+    if (!cyc_barrier(bar, c, next)) return;
     cyc_level_pass<K, kOpS3>(F, lane, warp, n_warps, pol, part);
-    if (!cyc_barrier(bar, c)) return;
+    if (!cyc_barrier(bar, c, next)) return;
     cyc_level_pass<K, kOpS4>(F, lane, warp, n_warps, pol, part);
   }
 }
