@@ -3384,6 +3384,10 @@ bool launch_coarse_fused(fem_amg* h, cudaStream_t st) {
       return false;
     }
     h->cyc_blocks = std::min(occ, kCycPerSm) * sm_count();
+    // small hierarchies: no more CTAs than level 1 has rows for their warps
+    // (each grid barrier waits for every CTA)
+    const int64_t need = (h->L[1].n + kCycT / 32 - 1) / (kCycT / 32);
+    h->cyc_blocks = (int)std::max<int64_t>(std::min<int64_t>(need, h->cyc_blocks), std::min(32, h->cyc_blocks));
   }
   CycArgs ca{};
   ca.n_levels = h->n_levels;
