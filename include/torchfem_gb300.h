@@ -546,6 +546,18 @@ int fem_amg_create(const fem_blocks* blocks, const double* coords, const uint8_t
  * unchanged until the next setup. */
 int fem_amg_setup(fem_amg* amg, const fem_matrix* A32, void* stream);
 
+/* Keeps the preconditioner of the last fem_amg_setup and makes A32 (a matrix
+ * of the same sliced layout, e.g. the next Newton tangent) the operator of
+ * the following fem_amg_pcg calls: CG's q = A p and the FP64 refinement use
+ * A32, the V-cycle stays the one built for the setup matrix (its FP16
+ * smoothing copy, block-Jacobi inverse, Chebyshev bounds and coarse
+ * operators), a fixed symmetric positive definite operator, so CG converges
+ * to the solution of the new system.  Saves the numeric setup between
+ * tangents that change little.  Needs the FP16 smoothing copy
+ * (fem_amg_set_half_smoother(1)); FEM_INVALID otherwise.  No counterpart in
+ * the reference, which rebuilds its preconditioner per solve. */
+int fem_amg_rebind(fem_amg* amg, const fem_matrix* A32);
+
 /* Precision of the level-0 smoothing passes for the setups that follow
  * (process-wide; default 1).  1: the four Chebyshev passes of every V-cycle
  * read an FP16 copy of the level-0 matrix, scaled by a power of two and

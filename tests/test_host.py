@@ -172,7 +172,7 @@ def test_default_multigrid_falls_back_to_block_jacobi():
             self.calls = []
             self.d = d
 
-        def build_system(self, mesh, mat, con_mask, precision, keep_refs=(), precond="jacobi"):
+        def build_system(self, mesh, mat, con_mask, precision, keep_refs=(), precond="jacobi", amg_reuse=False):
             self.calls.append(precond)
             if precond == "amg":
                 raise _lib.FemError(_lib.FEM_BOUNDS, "fem_amg_create: a row exceeds its size limit")

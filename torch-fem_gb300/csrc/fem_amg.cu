@@ -2731,7 +2731,9 @@ struct fem_amg {
   const int64_t* sell_base = nullptr;
   const int32_t* sell_col = nullptr;
   const float* sell_val = nullptr;
-  const float* dinv0 = nullptr;
+  const float* dinv0 = nullptr;  // the hierarchy's own copy of the setup matrix's block-Jacobi inverse
+  float* dinv0_own = nullptr;
+  int64_t dinv0_len = 0;
   // FP16 smoothing copy of the level-0 matrix (allocated at the first setup)
   __half* sv16 = nullptr;
   int64_t sv16_len = 0;
@@ -3238,7 +3240,24 @@ int setup_impl(fem_amg* h, const fem_matrix* A, cudaStream_t st) {
   h->sell_base = A->row_ptr;
   h->sell_col = A->col;
   h->sell_val = static_cast<const float*>(A->val);
-  h->dinv0 = static_cast<const float*>(A->precond);
+  {
+    // the V-cycle keeps its own copy of the block-Jacobi inverse, so a later
+    // fem_amg_rebind to another matrix leaves the preconditioner unchanged
+    const int64_t len = h->L[0].n * B0 * B0;
+    if (len != h->dinv0_len) {
+      if (h->dinv0_own) {
+        cudaFree(h->dinv0_own);
+        h->mem.erase(std::remove(h->mem.begin(), h->mem.end(), (void*)h->dinv0_own), h->mem.end());
+        h->dinv0_own = nullptr;
+        h->dinv0_len = 0;
+      }
+      h->dinv0_own = h->alloc<float>(len, st);
+      if (!h->dinv0_own) return check_cuda("AMG block-Jacobi copy");
+      h->dinv0_len = len;
+    }
+    cudaMemcpyAsync(h->dinv0_own, A->precond, sizeof(float) * len, cudaMemcpyDeviceToDevice, st);
+    h->dinv0 = h->dinv0_own;
+  }
   cudaMemsetAsync(h->status, 0, sizeof(int32_t), st);
   {
     // the FP16 smoothing copy, sized from the sliced layout at the first setup
@@ -3662,6 +3681,21 @@ int fem_amg_setup(fem_amg* h, const fem_matrix* A, void* stream) {
   return h->dim == 3 ? setup_impl<3, 6>(h, A, st) : h->dim == 2 ? setup_impl<2, 3>(h, A, st) : setup_impl<1, 1>(h, A, st);
 }
 
+int fem_amg_rebind(fem_amg* h, const fem_matrix* A) {
+  if (!h || !h->ready || !A || A->format != FEM_FMT_SELL_F32 || A->block != h->dim || A->row_ptr != h->sell_base ||
+      A->col != h->sell_col) {
+    set_last_error("fem_amg_rebind: needs a set-up hierarchy and an FP32 sliced matrix of the same layout");
+    return FEM_INVALID;
+  }
+  if (!g_amg_half || !h->sv16) {
+    set_last_error("fem_amg_rebind: the V-cycle would smooth on the new matrix with the old bounds; it needs the "
+                   "FP16 smoothing copy");
+    return FEM_INVALID;
+  }
+  h->sell_val = static_cast<const float*>(A->val);
+  return FEM_OK;
+}
+
 size_t fem_amg_pcg_workspace_bytes(const fem_amg* h, const fem_operator64* op) {
   if (!h) return 0;
   if (!op) return 256;
@@ -3677,8 +3711,8 @@ int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const
     set_last_error("fem_amg_pcg: the hierarchy has no numeric setup (call fem_amg_setup)");
     return FEM_INVALID;
   }
-  if (!A || A->row_ptr != h->sell_base || A->val != h->sell_val || A->precond != h->dinv0) {
-    set_last_error("fem_amg_pcg: the matrix differs from the one of the last fem_amg_setup");
+  if (!A || A->row_ptr != h->sell_base || A->val != h->sell_val) {
+    set_last_error("fem_amg_pcg: the matrix differs from the one of the last fem_amg_setup or fem_amg_rebind");
     return FEM_INVALID;
   }
   if (ws_bytes < fem_amg_pcg_workspace_bytes(h, op) || (op && !ws)) {

@@ -80,6 +80,7 @@ class LinearSystem:
         self._op_refs = None
         self.amg: AmgHierarchy | None = None
         self.amg_ws: Tensor | None = None
+        self.amg_fresh = True  # False: solved with an earlier matrix's multigrid setup
         LinearSystem._tokens += 1
         self.token = LinearSystem._tokens
 
@@ -107,6 +108,14 @@ class AmgHierarchy:
     def setup(self, sysm: LinearSystem, stream: int) -> None:
         check(self.lib.fem_amg_setup(self.handle, C.byref(sysm.matrix), stream), "fem_amg_setup")
         self.current = sysm.token
+        sysm.amg_fresh = True
+
+    def rebind(self, sysm: LinearSystem) -> None:
+        """Solve sysm's matrix with the preconditioner of the last setup
+        (fem_amg_rebind)."""
+        check(self.lib.fem_amg_rebind(self.handle, C.byref(sysm.matrix)), "fem_amg_rebind")
+        self.current = sysm.token
+        sysm.amg_fresh = False
 
     def levels(self) -> list[_lib.FemAmgLevel]:
         out = []
@@ -461,9 +470,11 @@ class DeviceMesh:
         return h
 
     def build_system(self, mesh, mat, con_mask: Tensor, precision: str, keep_refs=(),
-                     precond: str = "jacobi") -> LinearSystem:
+                     precond: str = "jacobi", amg_reuse: bool = False) -> LinearSystem:
         """Element stiffness, assembly and preconditioner for one tangent.
-        precond "amg" adds the multigrid hierarchy to a mixed system."""
+        precond "amg" adds the multigrid hierarchy to a mixed system;
+        amg_reuse keeps the hierarchy's last numeric setup as the
+        preconditioner of the new matrix (fem_amg_rebind)."""
         sysm = LinearSystem(self, precision)
         L, st = self.lib, self.stream
         if precision == "fp64":
@@ -499,7 +510,10 @@ class DeviceMesh:
             ws_bytes = L.fem_pcg_mixed_workspace_bytes(C.byref(sysm.matrix), C.byref(sysm.op))
             if precond == "amg":
                 sysm.amg = self.amg_hierarchy(con_mask)
-                sysm.amg.setup(sysm, st)
+                if amg_reuse and sysm.amg.current != 0:
+                    sysm.amg.rebind(sysm)
+                else:
+                    sysm.amg.setup(sysm, st)
                 sysm.amg_ws = self._ws(L.fem_amg_pcg_workspace_bytes(sysm.amg.handle, C.byref(sysm.op)))
         else:
             raise ValueError(f"unknown precision {precision!r}")

@@ -22,12 +22,26 @@ from .sparse import SolveContext
 
 
 class NLContext(SolveContext):
-    """SolveContext plus the material kind and its local-Newton settings."""
+    """SolveContext plus the material kind and its local-Newton settings.
+
+    Multigrid reuse: the Newton corrections of a mixed-precision solve keep the
+    multigrid setup of an earlier tangent (fem_amg_rebind) while their CG
+    needs at most AMG_LAG_GROWTH times the iterations of the first correction
+    after the last setup (plus two); a correction that needs more triggers a
+    new setup for the next tangent.  CG always runs on the current tangent,
+    so the Newton iterates are those of a solve with a fresh setup up to the
+    inner tolerance.  Adjoint solves always set up afresh."""
+
+    AMG_LAG = True
+    AMG_LAG_GROWTH = 1.5
 
     def __init__(self, *args, kind: str, local_tol: float = 1e-5, local_max_iter: int = 10,
                  nlgeom: bool = False, **kw):
         super().__init__(*args, **kw)
         self.kind = kind
+        self.amg_lag = NLContext.AMG_LAG
+        self._lag_ref: int | None = None  # CG iterations of the first correction after a setup
+        self._lag_last: int | None = None  # CG iterations of the last correction
         self.local_tol = local_tol
         self.local_max_iter = local_max_iter
         self.nlgeom = nlgeom
@@ -52,12 +66,27 @@ class NLContext(SolveContext):
             outs = (sig, hg, state)
         return fe, tangent, outs
 
-    def tangent_system(self, tangent, thickness):
+    def tangent_system(self, tangent, thickness, lag: bool = False):
+        """The system of this tangent; lag=True (a Newton correction) may keep
+        the last multigrid setup as its preconditioner."""
         mesh = self.dm.make_mesh(thickness)
         mat = _lib.FemMaterial(_lib.FEM_MAT_TANGENT_IP, tangent.data_ptr())
-        self.system = self.build_system(mesh, mat, keep_refs=(tangent, thickness, mesh, mat))
+        reuse = (lag and self.amg_lag and self._lag_ref is not None and self._lag_last is not None
+                 and self._lag_last <= NLContext.AMG_LAG_GROWTH * self._lag_ref + 2)
+        self.system = self.build_system(mesh, mat, keep_refs=(tangent, thickness, mesh, mat), amg_reuse=reuse)
         self.system_key = None
         return self.system
+
+    def correction(self, res):
+        """A Newton correction on the current system, with the bookkeeping of
+        the multigrid reuse."""
+        dx = self.solve(res, inner=True)
+        if self.system is not None and self.system.amg is not None:
+            its = self.system.stats.iterations
+            if self.system.amg_fresh:
+                self._lag_ref = its
+            self._lag_last = its
+        return dx
 
 
 class NewtonNonlinear(torch.autograd.Function):
@@ -84,8 +113,8 @@ class NewtonNonlinear(torch.autograd.Function):
                 break
             if res_norm != res_norm or res_norm in (float("inf"), float("-inf")):
                 break
-            sc.tangent_system(tangent, thickness)
-            du = du - sc.solve(res, inner=True)
+            sc.tangent_system(tangent, thickness, lag=True)
+            du = du - sc.correction(res)
         if not converged:
             raise RuntimeError("Newton-Raphson iteration did not converge.")
         ctx.sc = sc

@@ -74,7 +74,7 @@ class SolveContext:
         mat = _lib.FemMaterial(self.mat_kind, mat_data.data_ptr())
         return mesh, mat
 
-    def build_system(self, mesh, mat, keep_refs) -> LinearSystem:
+    def build_system(self, mesh, mat, keep_refs, amg_reuse: bool = False) -> LinearSystem:
         """The device system of one tangent with this context's preconditioner.
         A multigrid hierarchy that cannot be built for this mesh (a row over its
         size caps, a coarsening that stalls, a singular coarse block) falls back
@@ -85,7 +85,7 @@ class SolveContext:
         precond = self.precond if self.precision == "mixed" else "jacobi"
         try:
             return self.dm.build_system(mesh, mat, self.con_mask, self.precision, keep_refs=keep_refs,
-                                        precond=precond)
+                                        precond=precond, amg_reuse=amg_reuse and precond == "amg")
         except (_lib.FemError, ValueError) as err:
             if precond != "amg" or self.precond_explicit:
                 raise
