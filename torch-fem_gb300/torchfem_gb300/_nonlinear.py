@@ -24,16 +24,20 @@ from .sparse import SolveContext
 class NLContext(SolveContext):
     """SolveContext plus the material kind and its local-Newton settings.
 
-    Multigrid reuse: the Newton corrections of a mixed-precision solve keep the
-    multigrid setup of an earlier tangent (fem_amg_rebind) while their CG
-    needs at most AMG_LAG_GROWTH times the iterations of the first correction
-    after the last setup (plus two); a correction that needs more triggers a
-    new setup for the next tangent.  CG always runs on the current tangent,
-    so the Newton iterates are those of a solve with a fresh setup up to the
-    inner tolerance.  Adjoint solves always set up afresh."""
+    Multigrid reuse (AMG_LAG): the Newton corrections of a mixed-precision
+    solve keep the multigrid setup of an earlier tangent (fem_amg_rebind)
+    while their CG needs at most AMG_LAG_GROWTH times the iterations of the
+    first correction after the last setup (plus two); a correction that needs
+    more triggers a new setup for the next tangent.  CG always runs on the
+    current tangent, so the Newton iterates are those of a solve with a fresh
+    setup up to the inner tolerance.  Adjoint solves always set up afresh.
+    Measured on the two nonlinear configurations (setup per correction
+    against reuse): the J2 plate 8.5 -> 7.4 s, the Neo-Hookean box 1.68 ->
+    1.61 s; with a growth limit of 1.5 instead of 1.1 the plate took 9.1 s,
+    the stale setups costing more CG iterations than they saved."""
 
     AMG_LAG = True
-    AMG_LAG_GROWTH = 1.5
+    AMG_LAG_GROWTH = 1.1
 
     def __init__(self, *args, kind: str, local_tol: float = 1e-5, local_max_iter: int = 10,
                  nlgeom: bool = False, **kw):
