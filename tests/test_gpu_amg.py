@@ -357,8 +357,10 @@ def test_amg_rebind_keeps_the_preconditioner_and_solves_the_new_matrix(cuda, hal
 
     m, nodes, el = cube_problem(12)
     dm = m.device_mesh
-    con = m.constraints.reshape(-1).to(torch.uint8).to(dm.device).contiguous()
-    b = torch.where(con.bool(), torch.zeros_like(m.forces.reshape(-1)), m.forces.reshape(-1)).to(dm.device)
+    con_cpu = m.constraints.reshape(-1).cpu()
+    con = con_cpu.to(torch.uint8).to(dm.device).contiguous()
+    f = m.forces.reshape(-1).cpu()
+    b = torch.where(con_cpu, torch.zeros_like(f), f).to(dm.device)
 
     def system(scale, reuse):
         E = torch.full((len(el),), 1000.0, dtype=torch.float64)
