@@ -741,6 +741,8 @@ def main():
                     help="FP64 replacement threshold of the multigrid CG (default: the library's)")
     ap.add_argument("--smoother", choices=["fp16", "fp32"], default="fp16",
                     help="level-0 smoothing passes of the multigrid V-cycle: FP16 copy or the FP32 matrix")
+    ap.add_argument("--pdl", type=int, choices=[0, 1], default=None,
+                    help="programmatic dependent launch in the multigrid CG iteration (default: the library's)")
     ap.add_argument("--level0", choices=["ldg", "tma"], default="tma",
                     help="level-0 block SpMVs of the multigrid CG: direct loads, or slices streamed by bulk copies")
     ap.add_argument("--residual", choices=["auto", "copy", "elements"], default="auto",
@@ -762,6 +764,8 @@ def main():
 
         _lib.load().fem_amg_set_half_smoother(1 if args.smoother == "fp16" else 0)
         _lib.load().fem_amg_set_level0_tma(1 if args.level0 == "tma" else 0)
+        if args.pdl is not None:
+            _lib.load().fem_amg_set_pdl(args.pdl)
         LinearSystem.RESIDUAL_COPY = {"auto": None, "copy": True, "elements": False}[args.residual]
         if args.amg_delta is not None:
             SolveContext.AMG_DELTA = args.amg_delta

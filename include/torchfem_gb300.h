@@ -588,6 +588,13 @@ void fem_amg_set_fused_cycle(int enable);
  * always use the warp-per-slice kernel.  No counterpart in the reference. */
 void fem_amg_set_level0_tma(int enable);
 
+/* Programmatic dependent launch for the CG iteration's chain of kernels
+ * (level-0 SpMVs, dot finishers, CG update; process-wide; default 1): each
+ * launch may be scheduled while its predecessor drains and waits on the
+ * device for the predecessor's completion.  Same work and results.  No
+ * counterpart in the reference. */
+void fem_amg_set_pdl(int enable);
+
 /* CG preconditioned by one V-cycle (Chebyshev smoothing) on the matrix of
  * the last fem_amg_setup, from x = 0.  With op != NULL: FP64 residual
  * replacement as in fem_pcg_mixed (threshold delta), stopping at

@@ -348,6 +348,32 @@ def test_amg_level0_bulk_copies_match_direct_loads(cuda, half_smoother, kind):
     assert torch.equal(out[1], out[0])
 
 
+@pytest.mark.parametrize("kind", ["elastic", "heat"])
+def test_amg_programmatic_dependent_launch_is_bitwise_neutral(cuda, half_smoother, kind):
+    """The CG iteration's kernels launched with programmatic dependent launch
+    (fem_amg_set_pdl) do the same work in the same order: bitwise the same
+    solution as ordinary launches."""
+    lib = half_smoother
+    if kind == "elastic":
+        m, _, _ = cube_problem(16)
+    else:
+        from torchfem_gb300 import SolidHeat
+        from torchfem_gb300.materials import IsotropicConductivity3D
+
+        nodes, el = jittered_cube(24)
+        m = SolidHeat(nodes.to(cuda), el.to(cuda), IsotropicConductivity3D(1.0))
+        m.constraints[(nodes[:, 0] == 0.0).to(cuda)] = True
+        m.heat_flux[:] = 1.0 / len(nodes)
+    out = {}
+    try:
+        for pdl in (0, 1):
+            lib.fem_amg_set_pdl(pdl)
+            out[pdl] = m.solve(stol=1e-12, precision="mixed", preconditioner="amg")[0].clone()
+    finally:
+        lib.fem_amg_set_pdl(1)
+    assert torch.equal(out[1], out[0])
+
+
 def test_amg_rebind_keeps_the_preconditioner_and_solves_the_new_matrix(cuda, half_smoother):
     """fem_amg_rebind: the hierarchy set up for one stiffness preconditions a
     changed one (a stiffer half of the cube); CG on the new matrix with FP64

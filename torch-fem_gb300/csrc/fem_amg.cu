@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "fem_common.cuh"
@@ -45,6 +46,7 @@ extern int g_timing;  // fem_set_timing
 int g_amg_half = 1;   // FP16 smoothing copy of the level-0 matrix (fem_amg_set_half_smoother)
 int g_amg_fused = 1;  // coarse levels as one cooperative launch per V-cycle (fem_amg_set_fused_cycle)
 int g_amg_tma = 1;    // level-0 slices streamed by bulk copies (fem_amg_set_level0_tma)
+int g_amg_pdl = 1;    // programmatic dependent launch in the CG iteration (fem_amg_set_pdl)
 int sell_apply64(const fem_matrix* A32, const double* sval64, const double* x, double* y, cudaStream_t st);
 size_t scan_workspace_bytes(int64_t n);
 int scan_exclusive(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t st);
@@ -127,6 +129,16 @@ struct AmgCtrl {
 
 __device__ __forceinline__ bool amg_idle(const AmgCtrl* c) {
   return (*(volatile const int*)&c->done) != 0 || (*(volatile const int*)&c->replace) != 0;
+}
+
+// Programmatic dependent launch on the CG iteration's chain of kernels: each
+// waits for its predecessor's completion (and memory) before reading
+// anything, then lets its own successor be scheduled early, so a launch's
+// set-up overlaps the predecessor's tail.  Both are no-ops for a kernel
+// launched without the attribute.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 template <int B>
@@ -1122,6 +1134,7 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op(int64_t n_rows, const i
                                                          const float* __restrict__ sval, OpArgs a) {
   constexpr int DD = D * D;
   __shared__ float ys[kSellW][D][32];
+  pdl_enter();
   if (amg_idle(a.ctrl)) return;
   const float* __restrict__ v = op_operand<MODE>(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1244,6 +1257,7 @@ __global__ void __launch_bounds__(kSellW * 32) k_sell_op_tma(int64_t n_rows, con
   extern __shared__ __align__(128) unsigned char ring[];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ float ys[kSellW][D][32];
+  pdl_enter();
   if (amg_idle(a.ctrl)) return;
   const float* __restrict__ v = op_operand<MODE>(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1389,6 +1403,7 @@ __global__ void __launch_bounds__(kSell1W * 32) k_sell_op1(int64_t n_rows, int64
                                                            const int64_t* __restrict__ sell_base,
                                                            const int32_t* __restrict__ col,
                                                            const float* __restrict__ sval, OpArgs a) {
+  pdl_enter();
   if (amg_idle(a.ctrl)) return;
   const int lane = threadIdx.x & 31;
   const int64_t s = (int64_t)blockIdx.x * kSell1W + (threadIdx.x >> 5);
@@ -1451,6 +1466,7 @@ __global__ void __launch_bounds__(kSell1W * 32) k_sell_op1_tma(int64_t n_rows, i
   constexpr int VB = sell1_vb<H>();
   extern __shared__ __align__(128) unsigned char ring[];
   __shared__ __align__(8) uint64_t bars[kSell1W];
+  pdl_enter();
   if (amg_idle(a.ctrl)) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t s = (int64_t)blockIdx.x * kSell1W + w;
@@ -1544,6 +1560,28 @@ __global__ void __launch_bounds__(kSell1W * 32) k_sell_op1_tma(int64_t n_rows, i
   }
 }
 
+// A launch of the CG iteration's kernel chain: with g_amg_pdl, through
+// cudaLaunchKernelEx with programmatic stream serialization (the kernel's
+// pdl_enter waits for its predecessor).
+template <typename... Ex, typename... Act>
+void launch_chain(dim3 g, dim3 b, size_t smem, cudaStream_t st, void (*k)(Ex...), Act&&... args) {
+  if (!g_amg_pdl) {
+    k<<<g, b, smem, st>>>(std::forward<Act>(args)...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = g;
+  cfg.blockDim = b;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, std::forward<Act>(args)...);
+}
+
 // One level-0 pass: the shared-slot kernel for 2×2 / 3×3 blocks, the
 // warp-per-slice kernel for scalar rows.
 template <int D, int MODE, bool H>
@@ -1553,14 +1591,16 @@ void launch_sell(int64_t n, const int64_t* sell_base, const int32_t* sell_col, c
   if constexpr (D == 1) {
     const unsigned g = (unsigned)((ns + kSell1W - 1) / kSell1W);
     if (g_amg_tma)
-      k_sell_op1_tma<MODE, H><<<g, kSell1W * 32, sell1_smem<H>(), st>>>(n, ns, sell_base, sell_col, sell_val, a);
+      launch_chain(g, kSell1W * 32, sell1_smem<H>(), st, k_sell_op1_tma<MODE, H>, n, ns, sell_base, sell_col,
+                   sell_val, a);
     else
-      k_sell_op1<MODE, H><<<g, kSell1W * 32, 0, st>>>(n, ns, sell_base, sell_col, sell_val, a);
-  } else if (g_amg_tma)
-    k_sell_op_tma<D, MODE, H><<<(unsigned)ns, kSellW * 32, 2 * tma0_stage<D, H>(), st>>>(n, sell_base, sell_col,
-                                                                                        sell_val, a);
-  else
-    k_sell_op<D, MODE, H><<<(unsigned)ns, kSellW * 32, 0, st>>>(n, sell_base, sell_col, sell_val, a);
+      launch_chain(g, kSell1W * 32, 0, st, k_sell_op1<MODE, H>, n, ns, sell_base, sell_col, sell_val, a);
+  } else if (g_amg_tma) {
+    launch_chain((unsigned)ns, kSellW * 32, 2 * tma0_stage<D, H>(), st, k_sell_op_tma<D, MODE, H>, n, sell_base,
+                 sell_col, sell_val, a);
+  } else {
+    launch_chain((unsigned)ns, kSellW * 32, 0, st, k_sell_op<D, MODE, H>, n, sell_base, sell_col, sell_val, a);
+  }
 }
 
 // The dot product of a level-0 pass that ends in one: the per-slice shares
@@ -1569,6 +1609,7 @@ void launch_sell(int64_t n, const int64_t* sell_base, const int32_t* sell_col, c
 template <int MODE>
 __global__ void __launch_bounds__(1024) k_dot_finish(int64_t n, OpArgs a) {
   __shared__ double red[32];
+  pdl_enter();
   if (amg_idle(a.ctrl)) return;
   double s = 0.0;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(a.partial + i);
@@ -2429,6 +2470,7 @@ __global__ void __launch_bounds__(256) k_cg_update(int64_t n_nod, float* __restr
                                                    float* __restrict__ d, float* __restrict__ mx,
                                                    double* __restrict__ partial, AmgCtrl* ctrl) {
   __shared__ double red[32];
+  pdl_enter();
   if (amg_idle(ctrl)) return;
   const float alpha = (float)ctrl->alpha;
   double rr = 0.0;
@@ -3164,7 +3206,7 @@ void launch_op(fem_amg* h, int l, const OpArgs& a, cudaStream_t st) {
     else
       launch_sell<B0, MODE, false>(L.n, h->sell_base, h->sell_col, h->sell_val, a, st);
     if constexpr (op_has_dot<MODE>()) {
-      k_dot_finish<MODE><<<1, 1024, 0, st>>>(ns, a);
+      launch_chain(1, 1024, 0, st, k_dot_finish<MODE>, ns, a);
       note_launch();
     }
     if (timed) cudaEventRecord(h->ev[2 * h->ev_used++ + 1], st);
@@ -3469,9 +3511,8 @@ void launch_iteration(fem_amg* h, cudaStream_t st) {
   a.partial = h->partial;
   a.ctrl = h->ctrl;
   launch_op<B0, K, kOpQc>(h, 0, a, st);
-  k_cg_update<B0><<<capped(grid_for(h->L[0].n, kT), 8), kT, 0, st>>>(h->L[0].n, h->xlo, h->rcg, h->p, h->q, h->dinv0,
-                                                                      h->L[0].theta_inv, h->L[0].d, h->L[0].x,
-                                                                      h->partial, h->ctrl);
+  launch_chain(capped(grid_for(h->L[0].n, kT), 8), kT, 0, st, k_cg_update<B0>, h->L[0].n, h->xlo, h->rcg, h->p,
+               h->q, h->dinv0, h->L[0].theta_inv, h->L[0].d, h->L[0].x, h->partial, h->ctrl);
   note_launch();
 }
 
@@ -3731,6 +3772,7 @@ int fem_amg_pcg(fem_amg* h, const fem_matrix* A, const fem_operator64* op, const
 
 void fem_amg_set_half_smoother(int enable) { g_amg_half = enable ? 1 : 0; }
 void fem_amg_set_level0_tma(int enable) { g_amg_tma = enable ? 1 : 0; }
+void fem_amg_set_pdl(int enable) { g_amg_pdl = enable ? 1 : 0; }
 
 void fem_amg_set_fused_cycle(int enable) { g_amg_fused = enable ? 1 : 0; }
 

@@ -246,6 +246,7 @@ _SIGNATURES = {
     "fem_amg_set_fused_cycle": (None, [C.c_int]),
     "fem_amg_set_level0_tma": (None, [C.c_int]),
     "fem_amg_rebind": (C.c_int, [vp, _P(FemMatrix)]),
+    "fem_amg_set_pdl": (None, [C.c_int]),
     "fem_set_cg_path": (None, [C.c_int]),
     "fem_get_cg_path": (C.c_int, []),
     "fem_pcg_workspace_bytes": (C.c_size_t, [_P(FemMatrix)]),
