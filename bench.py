@@ -554,7 +554,7 @@ CONFIG_METRIC = "config {k}: solve+grad s per 1M DOF, mixed precision (FP32 mult
 
 
 def config_workload(k: int, device):
-    """The BASELINE configurations 3, 4 and 5 as (model, parameter, step):
+    """The benchmark configurations 3, 4 and 5 as (model, parameter, step):
     step(precision, precond) runs the configuration's solve and the gradient
     of its loss and returns (primary field, gradient).
       3: SIMP cantilever, Quad1 400 x 200, compliance f.u, dL/drho;
