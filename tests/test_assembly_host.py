@@ -150,3 +150,32 @@ def test_coupled_pattern_matches_scipy(seed):
     assert np.allclose(got, ref, rtol=1e-14, atol=1e-14)
     # an explicit diagonal for every retained DOF
     assert len(diag_map) == n and np.all(ccol[diag_map] == np.arange(n))
+
+
+def test_csr_sums_duplicates_and_keeps_empty_rows():
+    rows = np.array([2, 0, 2, 2], dtype=np.int64)
+    cols = np.array([1, 3, 1, 0], dtype=np.int64)
+    vals = np.array([1.0, 2.0, 3.0, 4.0])
+    ptr_, col, val = _csr(rows, cols, vals, 4)
+    assert ptr_.tolist() == [0, 1, 1, 3, 3]
+    assert col.tolist() == [3, 0, 1]
+    assert val.tolist() == [2.0, 4.0, 4.0]
+
+
+def test_coupled_pattern_of_an_uncoupled_point_has_only_its_diagonal():
+    """A reference point that no coupling touches keeps an explicit (zero)
+    diagonal row, as Assembly._stiffness adds one for every retained DOF."""
+    a, _, n_a, _ = _two_blocks()
+    point = ReferencePoint([0.5, 0.5, 3.0])
+    asm = Assembly([a, point])
+    rows, cols, vals, retained = asm._build_T()
+    n = len(retained)
+    T = _csr(rows, cols, vals, asm.n_dofs)
+    M = sp.eye(a.n_dofs, format="csr") * 2.0
+    M.sort_indices()
+    patterns = [(0, M.indptr.astype(np.int64), M.indices.astype(np.int64))]
+    rptr, ccol, cptr, src, coef, fix, diag_map = coupled_pattern(T, patterns, n, np.zeros(n, dtype=bool))
+    for i in range(a.n_dofs, n):
+        assert rptr[i + 1] - rptr[i] == 1 and ccol[rptr[i]] == i
+        e = rptr[i]
+        assert np.all(coef[cptr[e]:cptr[e + 1]] == 0.0)
