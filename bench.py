@@ -550,6 +550,180 @@ def run_heat(args):
     print(json.dumps(line))
 
 
+ASSEMBLY_METRIC = "assembly solve+grad s per 1M DOF (coupled parts, FP64 Jacobi CG on T^T K T)"
+
+
+def assembly_workload(n: int, device):
+    """Two jittered n^3 Hexa1 cubes tied face to face at x = 1 (interfaces
+    unjittered, so the tied nodes coincide), the first clamped at x = 0, and
+    a reference point at x = 2.5 driving the far face x = 2 with a moment
+    about x and a pull along z.  Returns the assembly, its first part, the
+    per-element Young's moduli of that part and the point."""
+    from torchfem_gb300 import Assembly, ReferencePoint, Solid
+    from torchfem_gb300.materials import IsotropicElasticity3D
+
+    nodes, el = cube_nodes(n)
+    nodes_b = nodes.clone()
+    nodes_b[:, 0] += 1.0
+    E0 = 1000.0 * (1.0 + 0.1 * torch.randn(len(el), generator=torch.Generator().manual_seed(2), dtype=torch.float64))
+    a = Solid(nodes.to(device), el.to(device), IsotropicElasticity3D(E0.to(device), 0.3))
+    b = Solid(nodes_b.to(device), el.to(device), IsotropicElasticity3D(1000.0, 0.3))
+    a.constraints[(nodes[:, 0] == 0.0).to(device)] = True
+    point = ReferencePoint([2.5, 0.5, 0.5])
+    point.forces[0, 3] = 1.0
+    point.forces[0, 2] = 1.0
+    asm = Assembly([a, b, point])
+    asm.coupling(b, nodes_b[:, 0] == 1.0, a, nodes[:, 0] == 1.0)
+    asm.coupling(b, nodes_b[:, 0] == 2.0, point)
+    return asm, a, E0.to(device), point
+
+
+def assembly_step(asm, a, E0, point, stol):
+    from torchfem_gb300.materials import IsotropicElasticity3D
+
+    E = E0.detach().requires_grad_(True)
+    a.material = IsotropicElasticity3D(E, 0.3)
+    u, f, _, _, _ = asm.solve(stol=stol, differentiable_parameters=E)
+    w = torch.inner(point.forces.ravel().to(u[2].dtype), u[2].ravel())
+    (g,) = torch.autograd.grad(w, E)
+    return u, g
+
+
+def _assembly_port_step(n: int):
+    """The assembly oracle's coupled solve (numpy assembly, scipy Jacobi CG to
+    1e-10) of the workload at size n: (seconds, CG seconds, DOF, CG iterations)."""
+    from oracle import assembly_oracle as A
+    from oracle import fem_oracle as O
+
+    nodes, el = (t.numpy() for t in cube_nodes(n))
+    nodes_b = nodes.copy()
+    nodes_b[:, 0] += 1.0
+    E0 = 1000.0 * (1.0 + 0.1 * torch.randn(len(el), generator=torch.Generator().manual_seed(2),
+                                           dtype=torch.float64).numpy())
+    t0 = time.perf_counter()
+    a = A.ModelPart(O.LinearModel(nodes, el, O.elastic_c("3d", E0, 0.3, len(el))), 3)
+    b = A.ModelPart(O.LinearModel(nodes_b, el, O.elastic_c("3d", 1000.0, 0.3, len(el))), 3)
+    a.constraints[nodes[:, 0] == 0.0] = True
+    point = A.PointPart([2.5, 0.5, 0.5])
+    point.forces[0, 3] = 1.0
+    point.forces[0, 2] = 1.0
+    asm = A.AssemblyOracle([a, b, point])
+    asm.coupling(1, nodes_b[:, 0] == 1.0, 0, nodes[:, 0] == 1.0)
+    asm.coupling(1, nodes_b[:, 0] == 2.0, 2)
+    tc = time.perf_counter()
+    asm.solve(method="cg", rtol=1e-10)
+    t_cg = time.perf_counter() - tc
+    its = asm.cg_iterations
+    # the adjoint: one more solve of the same symmetric system
+    t = time.perf_counter() - t0 + t_cg
+    return t, 2 * t_cg, asm.n_dofs, 2 * its
+
+
+def assembly_cpu_baseline(n_sample: int, n_target: int):
+    """The oracle's coupled solve plus an adjoint solve on two sizes,
+    extrapolated to the workload as cpu_baseline does."""
+    n_small = max(4, (2 * n_sample) // 3)
+    t_s, cg_s, dofs_s, it_s = _assembly_port_step(n_small)
+    t_l, cg_l, dofs_l, it_l = _assembly_port_step(n_sample)
+    alpha = math.log(it_l / it_s) / math.log(n_sample / n_small) if it_s > 0 and it_l > 0 else 1.0
+    dofs_t = 2 * 3 * (n_target + 1) ** 3 + 6
+    it_t = it_l * (n_target / n_sample) ** alpha
+    t_t = (t_l - cg_l) * (dofs_t / dofs_l) + cg_l * (dofs_t / dofs_l) * (it_t / it_l)
+    return {"value": t_t / (dofs_t / 1e6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"assembly oracle (numpy part matrices, T^T K T, scipy Jacobi-CG to 1e-10, solve + an "
+                      f"adjoint solve of the same system) on the {n_small}^3 and {n_sample}^3 pairs ({dofs_s} and "
+                      f"{dofs_l} DOF: {t_s:.2f} s and {t_l:.2f} s), extrapolated to {n_target}^3 ({dofs_t} DOF) "
+                      f"with iterations ~ n^{alpha:.2f}",
+            "samples": {"n": [n_small, n_sample], "seconds": [t_s, t_l], "cg_iterations": [it_s, it_l]}}
+
+
+def run_assembly(args):
+    """The assembly workload at n = --assembly-n: --warmup untimed and --steps
+    timed coupled solves with the gradient, FP64 Jacobi CG on T^T K T (CUDA
+    events); beside it the same box as one monolithic mesh in FP64."""
+    from torchfem_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    lib = _lib.load()
+    n = args.assembly_n
+    t0 = time.perf_counter()
+    asm, a, E0, point = assembly_workload(n, dev)
+    assembly_step(asm, a, E0, point, args.stol)
+    torch.cuda.synchronize()
+    first_ms = (time.perf_counter() - t0) * 1e3
+    for _ in range(max(args.warmup, 0)):
+        assembly_step(asm, a, E0, point, args.stol)
+    stream = torch.cuda.current_stream(dev)
+    lib.fem_set_timing(1)
+    launches0 = lib.fem_launch_count()
+    spmv_ms = spmv_n = 0
+    iters = []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            u, g = assembly_step(asm, a, E0, point, args.stol)
+            st = asm.last_solve
+            iters.append(st.iterations)
+            spmv_ms += st.spmv_ms
+            spmv_n += st.spmv_timed
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    lib.fem_set_timing(0)
+    launches = lib.fem_launch_count() - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    st = asm.last_solve
+    n_dofs = asm.n_dofs
+    peak, peak_kind = measured_peak_hbm()
+    nr = st.n
+    sb = st.nnz * 12 + (nr + 1) * 8 + 13 * 8 * nr  # FP64 CSR values + columns, row pointers, vector streams
+    unit_s = spmv_ms / spmv_n / 1e3 if spmv_n else None
+    achieved = sb / unit_s / 1e9 if unit_s else None
+    # the same box as one mesh, FP64 Jacobi CG
+    from torchfem_gb300 import Solid, mesh
+    from torchfem_gb300.materials import IsotropicElasticity3D
+
+    nodes, el = mesh.cube_hexa(2 * n + 1, n + 1, n + 1, 2.0, 1.0, 1.0)
+    mono = Solid(nodes.to(dev), el.to(dev), IsotropicElasticity3D(1000.0, 0.3))
+    mono.constraints[(nodes[:, 0] == 0.0).to(dev)] = True
+    mono.forces[(nodes[:, 0] == 2.0).to(dev), 2] = 1.0 / int((nodes[:, 0] == 2.0).sum())
+    fm = mono.forces.detach().clone().requires_grad_(True)
+
+    def mono_step():
+        mono.forces = fm
+        uu, _, _, _, _ = mono.solve(stol=args.stol, differentiable_parameters=fm)
+        torch.autograd.grad(uu.sum(), fm)
+
+    mono_step()
+    torch.cuda.synchronize()
+    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    m0.record(stream)
+    mono_step()
+    m1.record(stream)
+    torch.cuda.synchronize()
+    mono_ms = m0.elapsed_time(m1)
+    line = {
+        "metric": ASSEMBLY_METRIC, "value": ms / 1e3 / (n_dofs / 1e6), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered cubes)",
+        "config": {"workload": f"assembly: two {n}^3 Hexa1 cubes tied at an interface, a reference point on the "
+                               f"far face (moment + pull), work and d/dE of the first cube",
+                   "dofs": n_dofs, "retained_dofs": nr, "coupled_nnz": st.nnz, "stol": args.stol},
+        "cg_iterations": iters, "gpu_launches": launches,
+        "setup_excluded_ms": {"models_pattern_and_first_solve": first_ms},
+        "roofline": {"bound": "hbm", "kernel": "persistent FP64 Jacobi-CG kernel on T^T K T (one iteration)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None, "algorithmic_bytes": sb,
+                     "avg_unit_us": unit_s * 1e6 if unit_s else None, "peak_source": peak_kind},
+        "monolithic_fp64": {"ms_per_step": mono_ms, "dofs": 3 * len(nodes),
+                            "note": "the same 2 x 1 x 1 box as one unjittered mesh, FP64 Jacobi CG, solve + adjoint"},
+        "clocks": clocks.summary(),
+        "cpu_baseline": assembly_cpu_baseline(args.assembly_cpu_n, n),
+    }
+    print(json.dumps(line))
+
+
 CONFIG_METRIC = "config {k}: solve+grad s per 1M DOF, mixed precision (FP32 multigrid CG + FP64 refinement) vs plain FP64"
 
 
@@ -735,7 +909,7 @@ def main():
     ap.add_argument("--cg-path", choices=["persistent", "persistent-regs", "kernels"], default="persistent")
     ap.add_argument("--precond", choices=["amg", "jacobi"], default="amg",
                     help="preconditioner of the mixed-precision headline")
-    ap.add_argument("--workload", choices=["elastic", "heat", "thermal", "config3", "config4", "config5"],
+    ap.add_argument("--workload", choices=["elastic", "heat", "thermal", "config3", "config4", "config5", "assembly"],
                     default="elastic")
     ap.add_argument("--amg-delta", type=float, default=None,
                     help="FP64 replacement threshold of the multigrid CG (default: the library's)")
@@ -751,6 +925,8 @@ def main():
     ap.add_argument("--thermal-n", type=int, default=1024, help="N of the thermal slab (N x N/2 x 1 elements)")
     ap.add_argument("--heat-n", type=int, default=100, help="elements per cube edge of the heat workload")
     ap.add_argument("--heat-cpu-n", type=int, default=30, help="cube size of the heat CPU baseline sample")
+    ap.add_argument("--assembly-n", type=int, default=40, help="elements per cube edge of the assembly workload")
+    ap.add_argument("--assembly-cpu-n", type=int, default=12, help="cube size of the assembly CPU baseline sample")
     args = ap.parse_args()
     torch.set_default_dtype(torch.float64)
     if args.impl == "reference":
@@ -774,6 +950,9 @@ def main():
         return
     if args.workload == "heat":
         run_heat(args)
+        return
+    if args.workload == "assembly":
+        run_assembly(args)
         return
     if args.workload == "thermal":
         run_thermal(args)

@@ -334,3 +334,52 @@ def test_modal_oracle(golden):
     assert _heat_rel(modes * sign[:, None, None], g["modes"]) < 1e-10
     assert _heat_rel(gE, g["g_E"]) < 1e-12
     assert _heat_rel(gr, g["g_rho"]) < 1e-12
+
+
+def test_assembly_oracle(golden):
+    """The assembly oracle (oracle/assembly_oracle.py) against the reference's
+    own coupled solves: a cube turned by a 3D reference point, a Quad1 plate
+    turned by a 2D point, a conducting cube held by a thermal point."""
+    from oracle import assembly_oracle as A
+    from oracle import heat_oracle as H
+
+    g = golden("assembly_cases.npz")
+
+    def rel(a, b):
+        return float(np.abs(np.asarray(a) - b).max() / max(np.abs(b).max(), 1e-300))
+
+    nodes, el = O.cube_hexa(3, 3, 3)
+    solid = A.ModelPart(O.LinearModel(nodes, el, O.elastic_c("3d", 1000.0, 0.3, len(el))), 3)
+    solid.constraints[nodes[:, 2] == 0.0] = True
+    point = A.PointPart([0.5, 0.5, 2.0])
+    point.forces[0, 3] = 50.0
+    point.forces[0, 1] = 7.0
+    asm = A.AssemblyOracle([solid, point])
+    asm.coupling(0, nodes[:, 2] == nodes[:, 2].max(), 1)
+    u, f = asm.solve()
+    assert rel(u[0], g["rp_u0"]) < 1e-10 and rel(u[1], g["rp_u1"]) < 1e-10
+    assert rel(f[0], g["rp_f0"]) < 1e-10 and rel(f[1], g["rp_f1"]) < 1e-10
+
+    nodes, el = O.rect_quad(5, 5)
+    plate = A.ModelPart(O.LinearModel(nodes, el, O.elastic_c("plane_stress", 1000.0, 0.3, len(el))), 2)
+    plate.constraints[nodes[:, 1] == 0.0] = True
+    p2 = A.PointPart([0.5, 1.5])
+    p2.forces[0, 2] = 20.0
+    p2.forces[0, 0] = 3.0
+    asm = A.AssemblyOracle([plate, p2])
+    asm.coupling(0, nodes[:, 1] == 1.0, 1)
+    u, f = asm.solve(method="cg")
+    assert rel(u[0], g["planar_u0"]) < 1e-9 and rel(u[1], g["planar_u1"]) < 1e-9
+    assert rel(f[1], g["planar_f1"]) < 1e-9
+
+    nodes, el = O.cube_hexa(4, 4, 4)
+    heat = A.ModelPart(H.HeatModel(nodes, el, np.eye(3)), 1)
+    heat.constraints[nodes[:, 2] == 0.0] = True
+    heat.forces[nodes[:, 0] == 0.0, 0] = 0.1
+    hp = A.PointPart([0.5, 0.5, 1.5], heat=True)
+    hp.forces[0, 0] = 4.0
+    asm = A.AssemblyOracle([heat, hp])
+    asm.coupling(0, nodes[:, 2] == 1.0, 1)
+    T, q = asm.solve()
+    assert rel(T[0], g["heat_T0"]) < 1e-10 and rel(T[1], g["heat_T1"]) < 1e-10
+    assert rel(q[0], g["heat_q0"]) < 1e-10 and rel(q[1], g["heat_q1"]) < 1e-10

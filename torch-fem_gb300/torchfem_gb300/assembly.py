@@ -272,65 +272,95 @@ def coupled_pattern(T, patterns, n: int, con: np.ndarray):
     return rptr, cols.astype(np.int32), cptr, src, coef, fix, diag_map
 
 
-class _AssemblyContext:
-    """What one Assembly.solve shares between its Newton steps and backward."""
+class _CoupledPattern:
+    """What a solve needs that depends only on the couplings and the parts'
+    patterns: the map T on the device, the pattern of K_r = T^T K T and its
+    per-entry contribution lists.  Built once and kept by the Assembly for
+    later solves while neither changes; the condensation flags are kept per
+    constraint set."""
 
-    def __init__(self, asm: "Assembly", T_rows, T_cols, T_vals, retained: Tensor, con: Tensor, device,
-                 slots: list[_PartSlot], stol: float, max_iter: int, rtol: float, atol: float, linear: str):
-        self.asm = asm
+    def __init__(self, T_rows, T_cols, T_vals, n_all: int, n: int, slots: list[_PartSlot], device):
+        self.n_all, self.n = n_all, n
         self.device = device
-        self.lib = _lib.load()
-        self.slots = slots
-        self.n_all = asm.n_dofs
-        self.n = int(len(retained))
-        self.stol, self.max_iter, self.rtol, self.atol = stol, max_iter, rtol, atol
-        self.linear = linear
-        self.T = _CsrPair(T_rows, T_cols, T_vals, (self.n_all, self.n), device)
-        con_bool = torch.zeros(self.n, dtype=torch.bool)
-        con_bool[con] = True
-        self.con_bool = con_bool.to(device)
-        self._symbolic(T_rows, T_cols, T_vals, con_bool.numpy())
-        self.iterations: list[int] = []
-        self.newton_iterations: list[int] = []
-        self.verbose = False
-        self.values_ready = False
-
-    # ------------------------------------------------------------ pattern --
-    def _symbolic(self, T_rows, T_cols, T_vals, con):
-        """Pattern of K_r = T^T K T and each entry's contribution list."""
+        self.T = _CsrPair(T_rows, T_cols, T_vals, (n_all, n), device)
         patterns = []
         voff = 0
-        self.part_vals: list[tuple[_PartSlot, int, int]] = []
-        for s in self.slots:
+        self.part_vals: list[tuple[int, int, int]] = []  # (slot index, value offset, values)
+        for j, s in enumerate(slots):
             if s.kind == "point":
                 continue
             rp = s.dm.row_ptr.cpu().numpy().astype(np.int64)
             cl = s.dm.col.cpu().numpy().astype(np.int64)
             patterns.append((s.offset, rp, cl))
-            self.part_vals.append((s, voff, int(rp[-1])))
+            self.part_vals.append((j, voff, int(rp[-1])))
             voff += int(rp[-1])
         self.n_kval = voff
-        T = _csr(T_rows, T_cols, T_vals, self.n_all)
-        rptr, cols, cptr, src, coef, fix, diag_map = coupled_pattern(T, patterns, self.n, con)
-        nnz = len(cols)
-        n = self.n
-        dev = self.device
+        T = _csr(T_rows, T_cols, T_vals, n_all)
+        rptr, cols, cptr, src, coef, _, diag_map = coupled_pattern(T, patterns, n, np.zeros(n, dtype=bool))
+        self.nnz = len(cols)
+        self.rows_host = np.repeat(np.arange(n, dtype=np.int32), np.diff(rptr))
+        self.cols_host = cols
+        self.row_ptr = torch.as_tensor(rptr).to(device)
+        self.col = torch.as_tensor(cols.astype(np.int32)).to(device)
+        self.cptr = torch.as_tensor(cptr).to(device)
+        self.src = torch.as_tensor(src).to(device)
+        self.coef = torch.as_tensor(coef).to(device)
+        self.diag_map = torch.as_tensor(diag_map).to(device)
+        self._fix: dict[bytes, Tensor] = {}
+
+    def fix_for(self, con: np.ndarray) -> Tensor:
+        """Condensation flags of K_r for these constrained retained DOFs."""
+        key = np.packbits(con).tobytes()
+        f = self._fix.get(key)
+        if f is None:
+            r, c = self.rows_host, self.cols_host
+            fix = np.zeros(self.nnz, dtype=np.uint8)
+            fix[con[r] | con[c]] = 1
+            fix[(r == c) & con[r]] = 2
+            f = torch.as_tensor(fix).to(self.device)
+            self._fix = {key: f}
+        return f
+
+
+class _AssemblyContext:
+    """What one Assembly.solve shares between its Newton steps and backward."""
+
+    def __init__(self, asm: "Assembly", pattern: _CoupledPattern, con: Tensor, device, slots: list[_PartSlot],
+                 stol: float, max_iter: int, rtol: float, atol: float, linear: str):
+        self.asm = asm
+        self.device = device
+        self.lib = _lib.load()
+        self.slots = slots
+        self.pattern = pattern
+        self.n_all = asm.n_dofs
+        self.n = pattern.n
+        self.stol, self.max_iter, self.rtol, self.atol = stol, max_iter, rtol, atol
+        self.linear = linear
+        self.T = pattern.T
+        con_bool = torch.zeros(self.n, dtype=torch.bool)
+        con_bool[con] = True
+        self.con_bool = con_bool.to(device)
+        self.fix = pattern.fix_for(con_bool.numpy())
+        self.part_vals = [(slots[j], voff, nnz) for j, voff, nnz in pattern.part_vals]
+        self.n_kval = pattern.n_kval
+        n, nnz = self.n, pattern.nnz
         self.nnz = nnz
-        self.row_ptr = torch.as_tensor(rptr).to(dev)
-        self.col = torch.as_tensor(cols.astype(np.int32)).to(dev)
-        self.cptr = torch.as_tensor(cptr).to(dev)
-        self.src = torch.as_tensor(src).to(dev)
-        self.coef = torch.as_tensor(coef).to(dev)
-        self.fix = torch.as_tensor(fix).to(dev)
-        self.diag_map = torch.as_tensor(diag_map).to(dev)
-        self.val = torch.empty(nnz, dtype=torch.float64, device=dev)
-        self.precond = torch.empty(n, dtype=torch.float64, device=dev)
-        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.row_ptr, self.col = pattern.row_ptr, pattern.col
+        self.cptr, self.src, self.coef, self.diag_map = pattern.cptr, pattern.src, pattern.coef, pattern.diag_map
+        self.val = torch.empty(nnz, dtype=torch.float64, device=device)
+        self.precond = torch.empty(n, dtype=torch.float64, device=device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=device)
         self.matrix = _lib.FemMatrix(_lib.FEM_FMT_CSR_F64, 1, n, n, ptr(self.row_ptr), ptr(self.col),
                                      ptr(self.val), ptr(self.precond))
         self.ws = torch.empty(max(int(self.lib.fem_pcg_workspace_bytes(C.byref(self.matrix))), 256),
-                              dtype=torch.uint8, device=dev)
+                              dtype=torch.uint8, device=device)
         self.mr_ws = None
+        self.iterations: list[int] = []
+        self.newton_iterations: list[int] = []
+        self.spmv_ms = 0.0  # CUDA-event time of the timed CG iterations (fem_set_timing)
+        self.spmv_timed = 0
+        self.verbose = False
+        self.values_ready = False
 
     # ------------------------------------------------------------- values --
     def assemble(self):
@@ -370,6 +400,8 @@ class _AssemblyContext:
             raise RuntimeError(f"CG failed with exit code {info.iterations}")
         check(rc, "assembly linear solve")
         self.iterations.append(int(info.iterations))
+        self.spmv_ms += float(info.spmv_ms)
+        self.spmv_timed += int(info.spmv_timed)
         return x
 
     # ----------------------------------------------------------- residual --
@@ -479,6 +511,8 @@ class Assembly:
         self._rows: list[tuple[Tensor, Tensor, Tensor]] = [(EMPTY, EMPTY, torch.empty(0, dtype=torch.float64))]
         self._links: list = []
         self.last_solve: _AssemblyContext | None = None
+        self._version = 0  # bumped by every coupling: the cached pattern is then rebuilt
+        self._pattern: tuple | None = None  # (key, _CoupledPattern)
 
     def __repr__(self) -> str:
         return f"<torch-fem assembly ({len(self.parts)} parts, {self.n_dofs} dofs)>"
@@ -507,6 +541,7 @@ class Assembly:
         distance = torch.cdist(x_sec, x_pri_all[primary_nodes])
         primary_nodes = primary_nodes[distance.argmin(dim=1)]
         self._links.append(((secondary, secondary_nodes), (primary, primary_nodes)))
+        self._version += 1
         secondary_base = self._at[id(secondary)] + secondary_nodes * n_sec
         primary_base = self._at[id(primary)] + primary_nodes * n_pri
         ones = torch.ones(len(secondary_nodes), dtype=torch.float64)
@@ -589,7 +624,10 @@ class Assembly:
         slots = [_PartSlot(p, off, dev) for p, off in zip(self.parts, self.offsets)]
         for s in slots:
             s.setup(track, max_iter, rtol, atol, stol)
-        actx = _AssemblyContext(self, T_rows, T_cols, T_vals, retained, con, dev, slots, stol, max_iter, rtol, atol,
+        key = (self._version, tuple(id(s.dm) if s.kind != "point" else None for s in slots))
+        if self._pattern is None or self._pattern[0] != key:
+            self._pattern = (key, _CoupledPattern(T_rows, T_cols, T_vals, self.n_dofs, len(retained), slots, dev))
+        actx = _AssemblyContext(self, self._pattern[1], con, dev, slots, stol, max_iter, rtol, atol,
                                 "minres" if method == "minres" else "cg")
         actx.verbose = verbose
         self.last_solve = actx
