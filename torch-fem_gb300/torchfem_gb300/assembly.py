@@ -236,22 +236,27 @@ def coupled_pattern(T, patterns, n: int, con: np.ndarray):
     k = np.concatenate(ks) if ks else np.zeros(0, np.int64)
     l_ = np.concatenate(ls) if ls else np.zeros(0, np.int64)
     q = np.concatenate(qs) if qs else np.zeros(0, np.int64)
-    ck = tp[k + 1] - tp[k]
-    cl_ = tp[l_ + 1] - tp[l_]
-    sizes = ck * cl_
-    keep = sizes > 0
-    k, l_, q, cl_, sizes = k[keep], l_[keep], q[keep], cl_[keep], sizes[keep]
+    tk, tl = tp[k], tp[l_]
+    ck = tp[k + 1] - tk
+    cl_ = tp[l_ + 1] - tl
+    # most rows of T are a retained DOF's single unit entry: those pairs map
+    # to one entry directly; only pairs touching coupled rows are expanded
+    one = (ck == 1) & (cl_ == 1)
+    i1, j1 = tc[tk[one]].astype(np.int64), tc[tl[one]].astype(np.int64)
+    c1, s1 = tv[tk[one]] * tv[tl[one]], q[one]
+    many = ~one & (ck > 0) & (cl_ > 0)
+    tk, tl, q, cl_, sizes = tk[many], tl[many], q[many], cl_[many], (ck * (tp[l_ + 1] - tp[l_]))[many]
     total = int(sizes.sum())
-    grp = np.repeat(np.arange(len(k)), sizes)
+    grp = np.repeat(np.arange(len(tk)), sizes)
     start = np.repeat(np.cumsum(sizes) - sizes, sizes)
     pos = np.arange(total, dtype=np.int64) - start
-    a_i = tp[k][grp] + pos // cl_[grp]
-    b_i = tp[l_][grp] + pos % cl_[grp]
+    a_i = tk[grp] + pos // cl_[grp]
+    b_i = tl[grp] + pos % cl_[grp]
     diag = np.arange(n, dtype=np.int64)
-    i_out = np.concatenate([tc[a_i].astype(np.int64), diag])
-    j_out = np.concatenate([tc[b_i].astype(np.int64), diag])
-    coef = np.concatenate([tv[a_i] * tv[b_i], np.zeros(n)])  # the explicit zero diagonal adds nothing
-    src = np.concatenate([q[grp], np.zeros(n, dtype=np.int64)])
+    i_out = np.concatenate([i1, tc[a_i].astype(np.int64), diag])
+    j_out = np.concatenate([j1, tc[b_i].astype(np.int64), diag])
+    coef = np.concatenate([c1, tv[a_i] * tv[b_i], np.zeros(n)])  # the explicit zero diagonal adds nothing
+    src = np.concatenate([s1, q[grp], np.zeros(n, dtype=np.int64)])
     key = i_out * n + j_out
     order = np.lexsort((src, key))
     key, coef, src = key[order], coef[order], src[order]
