@@ -363,3 +363,37 @@ def test_state_dependent_parts_are_refused(cuda):
     plate = Planar(nodes, elements, mat)
     with pytest.raises(NotImplementedError, match="constant tangent"):
         Assembly([plate]).solve()
+
+
+def test_long_point_rows_vs_oracle(cuda):
+    """Two tied jittered 12^3 cubes and a point driving the far 13 x 13-node
+    face: each point row of T^T K T holds every DOF of the face's two node
+    layers (about a thousand entries), past what the persistent CG gives one
+    lane group, so those rows take the CTA-wide reduction.  Displacements and
+    forces of all three parts match the oracle's direct solve."""
+    import bench
+    from oracle import assembly_oracle as A
+    from oracle import fem_oracle as O
+
+    n = 12
+    asm, a, E0, point = bench.assembly_workload(n, cuda)
+    u, f, _, _, _ = asm.solve(stol=STOL)
+    rp = asm.last_solve.pattern.row_ptr.cpu().numpy()
+    assert np.diff(rp).max() > 512
+    nodes, el = (t.numpy() for t in bench.cube_nodes(n))
+    nodes_b = nodes.copy()
+    nodes_b[:, 0] += 1.0
+    E_np = E0.cpu().numpy()
+    pa = A.ModelPart(O.LinearModel(nodes, el, O.elastic_c("3d", E_np, 0.3, len(el))), 3)
+    pb = A.ModelPart(O.LinearModel(nodes_b, el, O.elastic_c("3d", 1000.0, 0.3, len(el))), 3)
+    pa.constraints[nodes[:, 0] == 0.0] = True
+    pp = A.PointPart([2.5, 0.5, 0.5])
+    pp.forces[0, 3] = 1.0
+    pp.forces[0, 2] = 1.0
+    oracle = A.AssemblyOracle([pa, pb, pp])
+    oracle.coupling(1, nodes_b[:, 0] == 1.0, 0, nodes[:, 0] == 1.0)
+    oracle.coupling(1, nodes_b[:, 0] == 2.0, 2)
+    ou, of = oracle.solve()
+    for k in range(3):
+        assert rel(u[k], ou[k]) < RTOL, k
+        assert rel(f[k], of[k]) < RTOL, k

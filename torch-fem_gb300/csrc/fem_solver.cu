@@ -697,6 +697,14 @@ __global__ void k_copy_cast(int64_t n, const float* __restrict__ in, double* __r
 // order, so all CTAs take identical decisions and results are deterministic.
 // The matrix is streamed with L2 evict_first; the CG vectors stay in L2.
 constexpr int kCsrTpr = 8;  // lanes per scalar CSR row
+// CSR rows longer than kLongRow entries (a reference point's rows in a coupled
+// system hold every DOF next to its coupled face) are reduced by the whole CTA
+// after the short rows, in one fixed order; a group of kCsrTpr lanes would take
+// one row that long serially while every other CTA waits at the next barrier.
+// A CTA lists its first kLongMax long rows at launch; later ones stay with the
+// lane groups.
+constexpr int kLongRow = 512;
+constexpr int kLongMax = 32;
 #ifndef TFG_PTHREADS
 #define TFG_PTHREADS 512
 #endif
@@ -1116,6 +1124,40 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
       }
     }
   }
+  // long CSR rows of this CTA, ascending (warp ballots read in warp order);
+  // rows from long_cut on are left to the lane groups
+  __shared__ int64_t long_rows[kLongMax];
+  __shared__ unsigned long_mask[kPThreads / 32];
+  __shared__ double long_sum[kPThreads / 32];
+  __shared__ int n_long;
+  __shared__ int64_t long_cut;
+  if constexpr (G == 1) {
+    if (threadIdx.x == 0) {
+      n_long = 0;
+      long_cut = row_hi;
+    }
+    __syncthreads();
+    for (int64_t b = row_lo; b < row_hi; b += blockDim.x) {
+      const int64_t row = b + threadIdx.x;
+      const bool lg = row < row_hi && P.row_ptr[row + 1] - P.row_ptr[row] > kLongRow;
+      const unsigned m = __ballot_sync(0xffffffffu, lg);
+      if (lane == 0) long_mask[warp] = m;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int w = 0; w < NW; ++w) {
+          unsigned mm = long_mask[w];
+          while (mm) {
+            const int64_t rw = b + w * 32 + (__ffs(mm) - 1);
+            mm &= mm - 1;
+            if (long_cut != row_hi) break;
+            if (n_long < kLongMax) long_rows[n_long++] = rw;
+            else long_cut = rw;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
   double rz = c->rz;        // thread 0 keeps the CG scalars
   double alpha_d = 0.0;
   long long iters = c->iters;
@@ -1145,18 +1187,43 @@ __global__ void __launch_bounds__(kPThreads, MODE == 1 ? 1 : 2) k_pcg_persistent
       for (int64_t row0 = row_lo; row0 < row_hi; row0 += n_groups) {
         const int64_t row = row0 + gid;
         double sacc = 0.0;
+        bool own = false;
         if (row < row_hi) {
           const int64_t rs = P.row_ptr[row], re = P.row_ptr[row + 1];
+          own = re - rs <= kLongRow || row >= long_cut;
+          if (own) {
 #pragma unroll 4
-          for (int64_t j = rs + sub; j < re; j += TPR)
-            sacc += ld_l2(val + j, stream) * (double)p[ld_l2(P.col + j, stream)];
+            for (int64_t j = rs + sub; j < re; j += TPR)
+              sacc += ld_l2(val + j, stream) * (double)p[ld_l2(P.col + j, stream)];
+          }
         }
 #pragma unroll
         for (int o = TPR / 2; o > 0; o >>= 1) sacc += __shfl_down_sync(0xffffffffu, sacc, o, TPR);
-        if (sub == 0 && row < row_hi) {
+        if (sub == 0 && own) {
           q[row] = (VT)sacc;
           pq[0].fma(p[row], (VT)sacc);
         }
+      }
+      // the listed long rows: all threads, warp trees, then warp sums in order
+      const int nl = n_long;
+      for (int i = 0; i < nl; ++i) {
+        const int64_t row = long_rows[i];
+        const int64_t rs = P.row_ptr[row], re = P.row_ptr[row + 1];
+        double s = 0.0;
+#pragma unroll 4
+        for (int64_t j = rs + threadIdx.x; j < re; j += blockDim.x)
+          s += ld_l2(val + j, stream) * (double)p[ld_l2(P.col + j, stream)];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) long_sum[warp] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double t = 0.0;
+          for (int w = 0; w < NW; ++w) t += long_sum[w];
+          q[row] = (VT)t;
+          pq[0].fma(p[row], (VT)t);
+        }
+        __syncthreads();
       }
     } else if constexpr (MODE == 1 && G == 3) {
       // TMA ring per warp: whole slices per warp, no cross-warp reduction.
