@@ -49,3 +49,22 @@ def test_heat_and_assembly_baselines_use_the_same_rule(monkeypatch):
                                                                   12: (3.0, 1.6, 13188, 600)}[n])
     a = bench.assembly_cpu_baseline(12, 40)
     assert a["value"] > 0 and a["samples"]["n"] == [8, 12]
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """`--impl reference` prints one line whose value and step time are the
+    mean of the timed runs' extrapolations (warm-up runs dropped)."""
+    import json
+
+    samples = {16: (2.0, 1.0, 3 * 17**3, 500), 24: (6.0, 4.0, 3 * 25**3, 750)}
+    monkeypatch.setattr(bench, "_port_step", lambda n: samples[n])
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    args = SimpleNamespace(gpus=1, steps=2, warmup=3, cpu_n=24, n=70)
+    bench.run_reference(args)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    ref = bench.cpu_baseline(24, 70)
+    assert line["impl"] == "reference" and line["higher_is_better"] is False
+    assert line["value"] == pytest.approx(ref["value"])
+    assert line["ms_per_step"] == pytest.approx(1e3 * ref["samples"]["predicted_seconds"])
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["kind"] == "port"
