@@ -7,11 +7,11 @@
 //
 // The sparsity of K_r and, for each of its entries, the list of part-matrix
 // entries that sum into it (with the product of the two T coefficients) are
-// fixed by the couplings and the part patterns: the host builds them once per
-// solve.  Every Newton iteration then forms the values with one kernel here,
-// a thread per entry summing its contributions in a fixed order, and the
-// residual T^T (F_int - F_ext) and the expansion u = T q are rectangular CSR
-// products by the second kernel.
+// fixed by the couplings and the part patterns: the host builds them once and
+// keeps them while the couplings and parts do not change.  Every solve then
+// forms the values with one kernel here, a thread per entry summing its
+// contributions in a fixed order, and the residual T^T (F_int - F_ext) and the
+// expansion u = T q are rectangular CSR products by the second kernel.
 #include "fem_common.cuh"
 
 namespace tfg {
