@@ -150,6 +150,10 @@ def test_coupled_pattern_matches_scipy(seed):
     assert np.allclose(got, ref, rtol=1e-14, atol=1e-14)
     # an explicit diagonal for every retained DOF
     assert len(diag_map) == n and np.all(ccol[diag_map] == np.arange(n))
+    # columns ascend within each row, and each entry's contributions are in
+    # source order (the fixed summation order of the GPU values)
+    assert all(np.all(np.diff(ccol[rptr[i]:rptr[i + 1]]) > 0) for i in range(n))
+    assert all(np.all(np.diff(src[cptr[e]:cptr[e + 1]]) >= 0) for e in range(len(ccol)))
 
 
 def test_csr_sums_duplicates_and_keeps_empty_rows():

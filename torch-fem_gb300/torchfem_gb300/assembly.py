@@ -225,27 +225,47 @@ def coupled_pattern(T, patterns, n: int, con: np.ndarray):
     flags (1 zero, 2 unit diagonal) and the diagonal positions.
     """
     tp, tc, tv = T
-    ks, ls, qs = [], [], []
+    n_all = len(tp) - 1
+    cnt = np.diff(tp)
+    head = tp[:-1]
+    # most rows of T are one unit entry (a retained DOF, or a DOF tied to one
+    # primary DOF): per DOF, that entry's column and coefficient; a pair of
+    # such rows maps one part entry to one entry of K_r directly
+    single = cnt == 1
+    tgt = np.zeros(n_all, dtype=np.int64)
+    cf = np.zeros(n_all)
+    tgt[single] = tc[head[single]]
+    cf[single] = tv[head[single]]
+    key1, c1, s1, ks, ls, qs = [], [], [], [], [], []
     voff = 0
     for offset, rp, cl in patterns:
-        nnz = int(rp[-1])
-        ks.append(np.repeat(np.arange(len(rp) - 1, dtype=np.int64), np.diff(rp)) + offset)
-        ls.append(cl + offset)
-        qs.append(np.arange(nnz, dtype=np.int64) + voff)
-        voff += nnz
-    k = np.concatenate(ks) if ks else np.zeros(0, np.int64)
-    l_ = np.concatenate(ls) if ls else np.zeros(0, np.int64)
-    q = np.concatenate(qs) if qs else np.zeros(0, np.int64)
-    tk, tl = tp[k], tp[l_]
-    ck = tp[k + 1] - tk
-    cl_ = tp[l_ + 1] - tl
-    # most rows of T are a retained DOF's single unit entry: those pairs map
-    # to one entry directly; only pairs touching coupled rows are expanded
-    one = (ck == 1) & (cl_ == 1)
-    i1, j1 = tc[tk[one]].astype(np.int64), tc[tl[one]].astype(np.int64)
-    c1, s1 = tv[tk[one]] * tv[tl[one]], q[one]
-    many = ~one & (ck > 0) & (cl_ > 0)
-    tk, tl, q, cl_, sizes = tk[many], tl[many], q[many], cl_[many], (ck * (tp[l_ + 1] - tp[l_]))[many]
+        m = np.diff(rp)
+        d = np.arange(offset, offset + len(m), dtype=np.int64)
+        col = cl + offset
+        one = np.repeat(single[d], m) & single[col]
+        row = np.repeat(d, m)
+        io = np.flatnonzero(one)
+        ko, lo = row[io], col[io]
+        key1.append(tgt[ko] * n + tgt[lo])
+        c1.append(cf[ko] * cf[lo])
+        s1.append(io + voff)
+        # the other pairs touch a row with several entries (a reference
+        # point's rigid map): expanded below
+        rest = np.flatnonzero(~one)
+        kr, lr = row[rest], col[rest]
+        keep = (cnt[kr] > 0) & (cnt[lr] > 0)
+        ks.append(kr[keep])
+        ls.append(lr[keep])
+        qs.append(rest[keep] + voff)
+        voff += int(rp[-1])
+
+    def cat(xs, dt):
+        return np.concatenate(xs) if xs else np.zeros(0, dt)
+
+    key1, c1, s1 = cat(key1, np.int64), cat(c1, np.float64), cat(s1, np.int64)
+    k, l_, q = cat(ks, np.int64), cat(ls, np.int64), cat(qs, np.int64)
+    tk, tl, cl_ = head[k], head[l_], cnt[l_]
+    sizes = cnt[k] * cl_
     total = int(sizes.sum())
     grp = np.repeat(np.arange(len(tk)), sizes)
     start = np.repeat(np.cumsum(sizes) - sizes, sizes)
@@ -253,27 +273,25 @@ def coupled_pattern(T, patterns, n: int, con: np.ndarray):
     a_i = tk[grp] + pos // cl_[grp]
     b_i = tl[grp] + pos % cl_[grp]
     diag = np.arange(n, dtype=np.int64)
-    i_out = np.concatenate([i1, tc[a_i].astype(np.int64), diag])
-    j_out = np.concatenate([j1, tc[b_i].astype(np.int64), diag])
+    key = np.concatenate([key1, tc[a_i].astype(np.int64) * n + tc[b_i], diag * (n + 1)])
     coef = np.concatenate([c1, tv[a_i] * tv[b_i], np.zeros(n)])  # the explicit zero diagonal adds nothing
     src = np.concatenate([s1, q[grp], np.zeros(n, dtype=np.int64)])
-    key = i_out * n + j_out
     order = np.lexsort((src, key))
     key, coef, src = key[order], coef[order], src[order]
-    first = np.r_[True, key[1:] != key[:-1]] if len(key) else np.zeros(0, bool)
-    ukey = key[first]
-    cptr = np.zeros(len(ukey) + 1, dtype=np.int64)
-    cptr[1:] = np.cumsum(np.diff(np.r_[np.nonzero(first)[0], len(key)]))
-    rows = ukey // n
-    cols = ukey % n
+    first = np.empty(len(key), dtype=bool)
+    if len(key):
+        first[0] = True
+        np.not_equal(key[1:], key[:-1], out=first[1:])
+    starts = np.flatnonzero(first)
+    cptr = np.append(starts, len(key)).astype(np.int64)
+    rows, cols = np.divmod(key[starts], n)
     rptr = np.zeros(n + 1, dtype=np.int64)
-    np.add.at(rptr, rows + 1, 1)
-    rptr = np.cumsum(rptr)
-    fix = np.zeros(len(ukey), dtype=np.uint8)
-    fix[con[rows] | con[cols]] = 1
-    on_diag = rows == cols
-    fix[on_diag & con[rows]] = 2
-    diag_map = np.nonzero(on_diag)[0].astype(np.int64)
+    np.cumsum(np.bincount(rows, minlength=n), out=rptr[1:])
+    fix = np.zeros(len(starts), dtype=np.uint8)
+    if con.any():
+        fix[con[rows] | con[cols]] = 1
+        fix[(rows == cols) & con[rows]] = 2
+    diag_map = np.flatnonzero(rows == cols).astype(np.int64)
     return rptr, cols.astype(np.int32), cptr, src, coef, fix, diag_map
 
 
