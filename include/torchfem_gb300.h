@@ -677,7 +677,7 @@ int fem_csr_spmm(const fem_matrix* A, int nvec, const double* X, double* Y, void
  * assembly.py:378-650): the coupling map T [n_dofs x n_retained] eliminates
  * the secondary DOFs, u = T q, and the solved system is
  * K_r = T^T blockdiag(K_parts) T with the Dirichlet condensation of
- * Assembly._stiffness (assembly.py:293-330).  The host builds the pattern of
+ * Assembly._stiffness (assembly.py:295-334).  The host builds the pattern of
  * K_r and, per entry, the contributing part-matrix entries once per solve.
  *
  * Values of K_r: out[e] = sum_{c in [ptr[e], ptr[e+1])} coef[c] * kval[src[c]]
@@ -691,7 +691,7 @@ int fem_coupled_values(int64_t n_out, const int64_t* ptr, const int64_t* src, co
 
 /* y = A x for a rectangular FP64 CSR matrix [n_rows x any] with int64 row
  * pointers and int32 columns: u = T q and T^T (F_int - F_ext) of an assembly
- * (the _mv products of assembly.py:24-26). */
+ * (the _mv products of assembly.py:23-25). */
 int fem_csr_apply(int64_t n_rows, const int64_t* row_ptr, const int32_t* col, const double* val,
                   const double* x, double* y, void* stream);
 

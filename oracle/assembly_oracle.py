@@ -5,12 +5,12 @@ to pin the GPU library's assemblies and by `bench.py`'s CPU baseline of the
 assembly workload.  The product (`torch-fem_gb300/`) never imports it.
 
 Restated reference code (paths relative to the torch-fem repository):
-  coupling rows        src/torchfem/assembly.py:181-268 (nearest primary node,
+  coupling rows        src/torchfem/assembly.py:180-257 (nearest primary node,
                        u_s = u_p + theta_p x (x_s - x_p), theta_s = theta_p)
-  elimination map T    src/torchfem/assembly.py:270-307
-  reduced stiffness    src/torchfem/assembly.py:309-350 (T^T K T, explicit
+  elimination map T    src/torchfem/assembly.py:258-294
+  reduced stiffness    src/torchfem/assembly.py:295-334 (T^T K T, explicit
                        diagonal, Dirichlet condensation)
-  solve                src/torchfem/assembly.py:378-577, one linear load step:
+  solve                src/torchfem/assembly.py:378-608, one linear load step:
                        res = T^T (F_int(T q) - F_ext), q -= K_r^-1 res, and
                        the retained DOFs' forces T^T F_int
 
@@ -27,7 +27,7 @@ import scipy.sparse.linalg as spla
 
 class PointPart:
     """A reference point: rigid-body DOFs (3 + 3 in 3D, 2 + 1 in 2D) or one
-    temperature (heat), no stiffness (assembly.py:38-107)."""
+    temperature (heat), no stiffness (assembly.py:39-106)."""
 
     def __init__(self, position, heat: bool = False):
         self.nodes = np.asarray(position, dtype=np.float64).reshape(1, -1)

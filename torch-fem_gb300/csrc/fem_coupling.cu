@@ -3,7 +3,7 @@
 // matrices; a coupling map T [n_dofs x n_retained] eliminates the secondary
 // DOFs (u = T q), so the solved system is the Galerkin product
 //   K_r = T^T blockdiag(K_parts) T
-// with the Dirichlet condensation of Assembly._stiffness (assembly.py:293-330).
+// with the Dirichlet condensation of Assembly._stiffness (assembly.py:295-334).
 //
 // The sparsity of K_r and, for each of its entries, the list of part-matrix
 // entries that sum into it (with the product of the two T coefficients) are

@@ -9,8 +9,9 @@ The compute runs on the GPU:
   matrices and the deterministic CSR assembly), unconstrained;
 * the reduced matrix K_r = T^T blockdiag(K_parts) T is formed by
   `fem_coupled_values` from per-entry contribution lists that the host builds
-  once per solve (the pattern of K_r depends on the couplings and the part
-  patterns only), with the Dirichlet condensation of Assembly._stiffness;
+  once and keeps while the couplings and parts do not change (the pattern of
+  K_r depends on them only), with the Dirichlet condensation of
+  Assembly._stiffness;
 * u = T q and T^T (F_int - F_ext) are `fem_csr_apply` products;
 * the linear solves are the FP64 Jacobi CG (or MINRES) of the single models.
 
@@ -43,7 +44,7 @@ K = 5  # differentiable inputs per part of a Newton node: u_prev, flux_prev, de0
 
 
 class ReferencePoint:
-    """A free node with rigid-body DOFs and no stiffness (assembly.py:38-77):
+    """A free node with rigid-body DOFs and no stiffness (assembly.py:39-73):
     three translations and three rotations in 3D, two and one in 2D."""
 
     n_nod = 1
@@ -67,7 +68,7 @@ class ReferencePoint:
 
 
 class ReferencePointHeat:
-    """A free node with one temperature and no capacity (assembly.py:80-107)."""
+    """A free node with one temperature and no capacity (assembly.py:76-106)."""
 
     n_nod = 1
     n_dof_per_node = 1
@@ -505,7 +506,7 @@ class _AssemblyNewton(torch.autograd.Function):
 
 
 class Assembly:
-    """Several models coupled by kinematic constraints (assembly.py:110-650).
+    """Several models coupled by kinematic constraints (assembly.py:113-650).
 
     Parts keep their own nodes, elements, materials and boundary conditions;
     their DOFs are stacked in the order given, and `coupling(...)` ties
@@ -543,7 +544,7 @@ class Assembly:
     def coupling(self, secondary: Part, mask: Tensor, primary: Part, primary_mask: Tensor | None = None,
                  dofs: Iterable[int] | None = None):
         """Couples nodes of `secondary` to the nearest nodes of `primary`
-        (assembly.py:181-257)."""
+        (assembly.py:180-247)."""
         if id(secondary) not in self._at or id(primary) not in self._at:
             raise ValueError("Both parts must belong to this assembly.")
         n_sec = secondary.n_dof_per_node
@@ -579,7 +580,7 @@ class Assembly:
                     self._rows.append((secondary_base + dof, rot, skew[:, dof, axis]))
 
     def _skew(self, r: Tensor) -> Tensor:
-        """Columns of the theta x r operator (assembly.py:259-268)."""
+        """Columns of the theta x r operator (assembly.py:248-257)."""
         r = torch.cat([r, torch.zeros(len(r), 3 - self.dim, dtype=r.dtype)], dim=1)
         eye = torch.eye(3, dtype=r.dtype).expand(len(r), 3, 3)
         cross = torch.linalg.cross(eye, r[:, None, :].expand(-1, 3, -1), dim=-1)
@@ -587,7 +588,7 @@ class Assembly:
 
     def _build_T(self):
         """Rows, columns and values of the map u = T q, and the retained DOFs
-        (assembly.py:270-307), with the reference's checks."""
+        (assembly.py:258-294), with the reference's checks."""
         eliminated = torch.cat(self._eliminated)
         if len(torch.unique(eliminated)) != len(eliminated):
             raise ValueError("A DOF is eliminated by more than one constraint.")
@@ -611,7 +612,7 @@ class Assembly:
               return_intermediate: bool = False, aggregate_integration_points: bool = True,
               differentiable_parameters: Tensor | Iterable[Tensor] | None = None):
         """Quasi-static solve of the coupled parts by load increments
-        (assembly.py:378-577).  Same arguments and results as the reference:
+        (assembly.py:378-608).  Same arguments and results as the reference:
         lists with one entry per part of (u, f, flux, grad, state).  The
         linear solves run on the GPU in FP64 ("cg"/None: Jacobi CG,
         "minres": Jacobi MINRES)."""
