@@ -53,7 +53,7 @@ class Planar(PlanarGeometry, Mechanics):
 
 
 class PlanarHeat(PlanarGeometry, Heat):
-    """Planar heat conduction model: one temperature per node (planar.py:325-340)."""
+    """Planar heat conduction model: one temperature per node (planar.py:325-339)."""
 
     def __repr__(self) -> str:
         return f"<torch-fem planar heat ({self.n_nod} nodes, {self.n_elem} {self.etype.__name__} elements)>"
